@@ -1,0 +1,186 @@
+// Test infrastructure only: a C entry layer over the UNMODIFIED reference
+// CompiledKernel + PortableRuntime sources, compiled by oracle/ref_build.sh
+// into oracle/_ref/libwvref.so.  It is used to generate golden fixtures and
+// to pin the numpy oracle; the shipped GPU path never links or loads it.
+//
+// Reference interfaces driven here:
+//   WVTransformConstantStratificationKernel::create / nonlinearFlux /
+//     transformUVWEtaToWaveVortex / transformUVEtaToWaveVortex /
+//     transformWaveVortexToUVWEta
+//     (CompiledKernel/include/WaveVortexKernel/WVTransformConstantStratificationKernel.hpp:47-110)
+//   WVConstantStratificationIntegrationSystem::create / evaluateRightHandSide
+//     (PortableRuntime/include/WaveVortexRuntime/WVConstantStratificationIntegrationSystem.hpp:40-66)
+//   WVFixedStepRK4::step (PortableRuntime/src/WVRungeKutta.cpp:335-462)
+//   WVReferenceFFTEngine, the exact direct DFT/DCT-I/DST-I engine
+//     (CompiledKernel/adapters/reference/WVReferenceFFTEngine.cpp:47-107)
+
+#include "WVReferenceFFTEngine.hpp"
+#include "WaveVortexKernel/WVTransformConstantStratificationKernel.hpp"
+#include "WaveVortexRuntime/WVConstantStratificationIntegrationSystem.hpp"
+#include "WaveVortexRuntime/WVExtensionCatalog.hpp"
+#include "WaveVortexRuntime/WVForcingContracts.hpp"
+#include "WaveVortexRuntime/WVRungeKutta.hpp"
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <string>
+
+using namespace wavevortex;
+using namespace wavevortex::runtime;
+
+namespace {
+
+struct RefHandle {
+    std::unique_ptr<WVTransformConstantStratificationKernel> kernel;
+    std::unique_ptr<WVConstantStratificationIntegrationSystem> system;
+    std::unique_ptr<WVFixedStepRK4> rk4;
+    std::string message;
+};
+
+WVTransformConstantStratificationConfiguration makeConfiguration(const std::uint64_t* sizes, const double* values, const std::uint8_t* flags) {
+    WVTransformConstantStratificationConfiguration c;
+    c.Nx = sizes[0]; c.Ny = sizes[1]; c.Nz = sizes[2]; c.Nj = sizes[3];
+    c.Lx = values[0]; c.Ly = values[1]; c.Lz = values[2]; c.N0 = values[3];
+    c.rho0 = values[4]; c.g = values[5]; c.planetaryRadius = values[6];
+    c.rotationRate = values[7]; c.latitude = values[8];
+    c.isHydrostatic = flags[0] != 0; c.shouldAntialias = flags[1] != 0;
+    return c;
+}
+
+WVFrozenForcingEntry forcingEntry(const char* type, const char* name, WVForcingStage stage, std::uint8_t priority) {
+    WVFrozenForcingEntry e;
+    e.typeIdentifier = type;
+    e.name = name;
+    e.stage = stage;
+    e.priority = priority;
+    e.sourceGroupPath = "oracle";
+    e.configuration = {"wave-vortex-forcing-configuration-v1", 1, {}};
+    return e;
+}
+
+int fail(RefHandle* h, const WVKernelStatus& status) {
+    if (h) h->message = status.message;
+    return static_cast<int>(status.code);
+}
+
+WVComplexConstView cview(const double* p, WVShape2D s) { return {reinterpret_cast<const WVComplex64*>(p), s}; }
+WVComplexView mview(double* p, WVShape2D s) { return {reinterpret_cast<WVComplex64*>(p), s}; }
+
+} // namespace
+
+extern "C" {
+
+// schedule: 0 = {nonlinear advection}; 1 = {nonlinear advection, adaptive damping}
+int wvref_create(const std::uint64_t* sizes, const double* values, const std::uint8_t* flags, int schedule, void** out) {
+    auto h = std::make_unique<RefHandle>();
+    const auto c = makeConfiguration(sizes, values, flags);
+    auto status = WVTransformConstantStratificationKernel::create(c, std::make_unique<WVReferenceFFTEngine>(), h->kernel);
+    if (!status) { *out = nullptr; return static_cast<int>(status.code); }
+    WVFrozenForcingSchedule frozen;
+    frozen.entries.push_back(forcingEntry("WVNonlinearAdvection", "nonlinear", WVForcingStage::spatial, 127));
+    if (schedule == 1) frozen.entries.push_back(forcingEntry("WVAdaptiveDamping", "adaptive", WVForcingStage::spectral, 100));
+    std::shared_ptr<const WVExtensionCatalog> catalog;
+    status = makeBuiltInExtensionCatalog(catalog);
+    if (!status) { *out = nullptr; return static_cast<int>(status.code); }
+    status = WVConstantStratificationIntegrationSystem::create(c, frozen, catalog, std::make_unique<WVReferenceFFTEngine>(), h->system);
+    if (!status) { *out = nullptr; return static_cast<int>(status.code); }
+    h->rk4 = std::make_unique<WVFixedStepRK4>(*h->system);
+    *out = h.release();
+    return 0;
+}
+
+void wvref_destroy(void* handle) { delete static_cast<RefHandle*>(handle); }
+
+const char* wvref_message(void* handle) { return handle ? static_cast<RefHandle*>(handle)->message.c_str() : ""; }
+
+// out: Nkl, NxHalf, M
+void wvref_sizes(void* handle, std::uint64_t* out) {
+    const auto& d = static_cast<RefHandle*>(handle)->kernel->descriptor();
+    out[0] = d.Nkl();
+    out[1] = d.halfSpectrumMappings().NxHalf;
+    out[2] = d.spectralShape().elementCount();
+}
+
+// Descriptor arrays for ordering / coefficient checks.
+// modes: [Nkl] kMode, lMode; omega, fWaveScale, ApmDScaled, A0FromVorticity, A0FromBuoyancy, NA0Field, ApmNProjection [M];
+// storage rows + conj flags [Nkl].
+void wvref_descriptor(void* handle, std::int64_t* kMode, std::int64_t* lMode, double* omega, double* fWaveScale,
+                      double* A0FromVorticity, double* A0FromBuoyancy, double* NA0Field, double* ApmNProjection,
+                      double* UApField, double* WApField, std::uint64_t* storageRows, std::uint8_t* conjugated) {
+    const auto& d = static_cast<RefHandle*>(handle)->kernel->descriptor();
+    const auto& m = d.verticalModes();
+    for (std::size_t i = 0; i < d.Nkl(); ++i) {
+        kMode[i] = d.fourierModes()[i].kMode;
+        lMode[i] = d.fourierModes()[i].lMode;
+        storageRows[i] = d.halfSpectrumMappings().storageRowsByWVIndex[i];
+        conjugated[i] = d.halfSpectrumMappings().conjugatesStoredValueByWVIndex[i];
+    }
+    const auto M = d.spectralShape().elementCount();
+    std::memcpy(omega, m.omega.data(), M * sizeof(double));
+    std::memcpy(fWaveScale, m.fWaveScale.data(), M * sizeof(double));
+    std::memcpy(A0FromVorticity, m.A0FromVorticity.data(), M * sizeof(double));
+    std::memcpy(A0FromBuoyancy, m.A0FromBuoyancy.data(), M * sizeof(double));
+    std::memcpy(NA0Field, m.NA0Field.data(), M * sizeof(double));
+    std::memcpy(ApmNProjection, m.ApmNProjection.data(), M * sizeof(double));
+    std::memcpy(UApField, m.UApField.data(), M * 2 * sizeof(double));
+    std::memcpy(WApField, m.WApField.data(), M * 2 * sizeof(double));
+}
+
+int wvref_flux(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,
+               double* Fp, double* Fm, double* F0) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVState state{t, t0, {cview(Ap, s), cview(Am, s), cview(A0, s)}};
+    WVFlux flux{mview(Fp, s), mview(Fm, s), mview(F0, s)};
+    const auto status = h->kernel->nonlinearFlux(state, flux);
+    return status ? 0 : fail(h, status);
+}
+
+// Full scheduled right-hand side (nonlinear advection, plus adaptive damping when created with schedule 1).
+int wvref_rhs(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,
+              double* Fp, double* Fm, double* F0) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVIntegrationState state{{t, t0, {cview(Ap, s), cview(Am, s), cview(A0, s)}}, nullptr, 0};
+    WVIntegrationFlux flux{{mview(Fp, s), mview(Fm, s), mview(F0, s)}, nullptr, 0};
+    const auto status = h->system->evaluateRightHandSide(state, flux);
+    return status ? 0 : fail(h, status);
+}
+
+int wvref_forward(void* handle, const double* fields, double t, double t0, double* Ap, double* Am, double* A0) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    const auto s = h->kernel->descriptor().spectralShape();
+    const std::size_t channels = c.isHydrostatic ? 3 : 4;
+    WVRealFieldBundleConstView view{fields, {c.Nx, c.Ny, c.Nz, channels}};
+    WVMutableCoefficients out{mview(Ap, s), mview(Am, s), mview(A0, s)};
+    const auto status = c.isHydrostatic ? h->kernel->transformUVEtaToWaveVortex(view, t, t0, out)
+                                        : h->kernel->transformUVWEtaToWaveVortex(view, t, t0, out);
+    return status ? 0 : fail(h, status);
+}
+
+int wvref_inverse(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0, double* fields) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVState state{t, t0, {cview(Ap, s), cview(Am, s), cview(A0, s)}};
+    WVRealFieldBundleView view{fields, {c.Nx, c.Ny, c.Nz, 4}};
+    const auto status = h->kernel->transformWaveVortexToUVWEta(state, view);
+    return status ? 0 : fail(h, status);
+}
+
+// Fixed-step RK4 through the reference integrator; state updated in place, *t advanced.
+int wvref_rk4(void* handle, double* Ap, double* Am, double* A0, double* t, double t0, double dt, int steps) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVMutableIntegrationState state{{*t, t0, {mview(Ap, s), mview(Am, s), mview(A0, s)}}, nullptr, 0};
+    for (int i = 0; i < steps; ++i) {
+        const auto status = h->rk4->step(state, dt);
+        if (!status) return fail(h, status);
+    }
+    *t = state.waveVortex.t;
+    return 0;
+}
+
+} // extern "C"

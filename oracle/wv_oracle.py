@@ -1,0 +1,795 @@
+"""CPU oracle for the constant-stratification spectral time step.
+
+TEST INFRASTRUCTURE ONLY.  This module restates, in numpy/scipy, the reference
+algorithm of WaveVortexModel's compiled kernel so that tests, the smoke check
+and the CPU baseline of the benchmark can check the GPU path against it.  The
+shipped GPU library never imports or calls this file.
+
+Parity of this restatement is pinned against golden fixtures produced by the
+reference's own C++ sources (CompiledKernel + PortableRuntime + the exact
+direct-DFT engine), see tests/golden/make_golden.py and
+tests/test_oracle_golden.py.
+
+Storage conventions follow the reference:
+  * coefficient arrays are column-major [Nj, Nkl] complex (j fastest); here a
+    numpy array of shape (Nkl, Nj) complex128 in C order has the same memory.
+  * spatial fields are column-major [Nx, Ny, Nz, ch] (x fastest); here shape
+    (ch, Nz, Ny, Nx) in C order.
+
+Citations are to files of the reference project.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+try:  # scipy gives multi-threaded FFTs; numpy is the fallback.
+    import scipy.fft as _sfft
+
+    def _rfft2(x, workers):
+        return _sfft.rfft2(x, axes=(-2, -1), workers=workers)
+
+    def _irfft2(x, s, workers):
+        return _sfft.irfft2(x, s=s, axes=(-2, -1), norm="forward", workers=workers)
+
+    def _dct1(x, axis):
+        return _sfft.dct(x, type=1, axis=axis)
+
+    def _dst1(x, axis):
+        return _sfft.dst(x, type=1, axis=axis)
+
+except ImportError:  # pragma: no cover
+    _sfft = None
+
+    def _rfft2(x, workers):
+        return np.fft.rfft2(x, axes=(-2, -1))
+
+    def _irfft2(x, s, workers):
+        return np.fft.irfft2(x, s=s, axes=(-2, -1), norm="forward")
+
+    def _dct1(x, axis):
+        x = np.moveaxis(x, axis, -1)
+        n = x.shape[-1]
+        k = np.arange(n)
+        C = 2.0 * np.cos(np.pi * np.outer(k, k) / (n - 1))
+        C[:, 0] = 1.0
+        C[:, -1] = (-1.0) ** k
+        return np.moveaxis(x @ C.T, -1, axis)
+
+    def _dst1(x, axis):
+        x = np.moveaxis(x, axis, -1)
+        n = x.shape[-1]
+        k = np.arange(1, n + 1)
+        S = 2.0 * np.sin(np.pi * np.outer(k, k) / (n + 1))
+        return np.moveaxis(x @ S.T, -1, axis)
+
+
+PI = 3.141592653589793238462643383279502884
+# WVKernelTypes.cpp:13-16: the F/G normalization uses 9.81 regardless of g.
+MODAL_NORMALIZATION_GRAVITY = 9.81
+CONTRACT_VERSION = 4  # WVKernelTypes.hpp:11
+
+
+@dataclass
+class Config:
+    """WVTransformConstantStratificationConfiguration (WVKernelTypes.hpp:129-146)."""
+
+    Nx: int
+    Ny: int
+    Nz: int
+    Nj: int
+    Lx: float
+    Ly: float
+    Lz: float
+    N0: float = 5.2e-3
+    rho0: float = 1025.0
+    g: float = 9.81
+    planetaryRadius: float = 6.371e6
+    rotationRate: float = 7.2921e-5
+    latitude: float = 33.0
+    isHydrostatic: bool = False
+    shouldAntialias: bool = True
+    contractVersion: int = CONTRACT_VERSION
+
+
+def default_nj(Nz: int) -> int:
+    """Nj = floor(2(Nz-1)/3) (WVGeometryDoublyPeriodicStratifiedConstant.m:61-68)."""
+    return (2 * (Nz - 1)) // 3
+
+
+class OracleError(ValueError):
+    def __init__(self, code, message):
+        super().__init__(message)
+        self.code = code
+
+
+# WVKernelStatusCode (WVKernelTypes.hpp:22-35)
+SUCCESS, INVALID_CONFIGURATION, INVALID_SHAPE, INVALID_POINTER, OVERLAPPING, SIZE_OVERFLOW, \
+    ALLOCATION_FAILURE, FFT_PLAN_FAILURE, FFT_EXECUTION_FAILURE, NUMERICAL_FAILURE, UNSUPPORTED, \
+    REENTRANT = range(12)
+
+
+def _dft_modes(n):
+    """dftModes (WVKernelTypes.cpp:38-45)."""
+    pos = (n + 1) // 2
+    return list(range(pos)) + [-v for v in range(n // 2, 0, -1)]
+
+
+def _dft_index(mode, n):
+    return mode if mode >= 0 else n + mode
+
+
+@dataclass
+class Descriptor:
+    """Immutable descriptor (WVTransformConstantStratificationDescriptor::create,
+    WVKernelTypes.cpp:119-330)."""
+
+    c: Config
+    kMode: np.ndarray = None
+    lMode: np.ndarray = None
+    k: np.ndarray = None
+    l: np.ndarray = None
+    Kh: np.ndarray = None
+    cosAlpha: np.ndarray = None
+    sinAlpha: np.ndarray = None
+    f: float = 0.0
+    z: np.ndarray = None
+    m: np.ndarray = None
+    h0: np.ndarray = None
+    Fg: np.ndarray = None
+    Gg: np.ndarray = None
+    gWaveScale: np.ndarray = None
+    inertialScale: np.ndarray = None
+    apmWProjectionPrefactor: np.ndarray = None
+    hpm: np.ndarray = None
+    arrays: dict = field(default_factory=dict)
+    NxHalf: int = 0
+    storageRow: np.ndarray = None
+    conjugated: np.ndarray = None
+    completionRows: np.ndarray = None
+    completionSources: np.ndarray = None
+    selfConjugateRows: np.ndarray = None
+
+    @property
+    def Nkl(self):
+        return len(self.kMode)
+
+    @property
+    def M(self):
+        return self.Nkl * self.c.Nj
+
+
+def build_descriptor(c: Config) -> Descriptor:
+    if c.contractVersion != CONTRACT_VERSION:
+        raise OracleError(INVALID_CONFIGURATION, "Unsupported kernel contract version.")
+    if c.Nx < 2 or c.Ny < 2 or c.Nz < 3 or c.Nj < 1 or c.Nj > c.Nz - 1:
+        raise OracleError(INVALID_CONFIGURATION,
+                          "Nx and Ny must be at least 2, Nz at least 3, and Nj must lie in [1,Nz-1].")
+    for v in (c.Lx, c.Ly, c.Lz, c.N0, c.rho0, c.g, c.planetaryRadius, c.rotationRate):
+        if not (math.isfinite(v) and v > 0.0):
+            raise OracleError(INVALID_CONFIGURATION,
+                              "Physical lengths and constants must be finite and positive, and latitude must lie in [-90,90].")
+    if not math.isfinite(c.latitude) or abs(c.latitude) > 90.0:
+        raise OracleError(INVALID_CONFIGURATION,
+                          "Physical lengths and constants must be finite and positive, and latitude must lie in [-90,90].")
+    d = Descriptor(c=c)
+    Nx, Ny, Nz, Nj = c.Nx, c.Ny, c.Nz, c.Nj
+    kModes = _dft_modes(Nx)
+    lModes = _dft_modes(Ny)
+    maxAbsK = 2.0 * PI * (float(Nx // 2) / c.Lx)
+    K, L = [], []
+    # WVKernelTypes.cpp:143-158: l outer, k inner; primary, non-Nyquist, inside 2/3 disk.
+    for lm in lModes:
+        for km in kModes:
+            kSelf = km == 0 or (Nx % 2 == 0 and km == -(Nx // 2))
+            lSelf = lm == 0 or (Ny % 2 == 0 and lm == -(Ny // 2))
+            primary = lm > 0 or (lSelf and (km > 0 or kSelf))
+            nyq = (Nx % 2 == 0 and km == -(Nx // 2)) or (Ny % 2 == 0 and lm == -(Ny // 2))
+            if not primary or nyq:
+                continue
+            K.append(km)
+            L.append(lm)
+    K = np.array(K, dtype=np.int64)
+    L = np.array(L, dtype=np.int64)
+    k = 2.0 * PI * (K.astype(np.float64) / c.Lx)
+    l = 2.0 * PI * (L.astype(np.float64) / c.Ly)
+    # radialMagnitude: sqrt(k*k + l*l) with no fused multiply-add (WVKernelTypes.cpp:22-29)
+    Kh = np.sqrt(k * k + l * l)
+    if c.shouldAntialias:
+        keep = ~(Kh > 2.0 * maxAbsK / 3.0)
+        K, L, k, l, Kh = K[keep], L[keep], k[keep], l[keep], Kh[keep]
+    order = np.lexsort((L, K, Kh))  # sort by (Kh, kMode, lMode) (WVKernelTypes.cpp:159-166)
+    K, L, k, l, Kh = K[order], L[order], k[order], l[order], Kh[order]
+    d.kMode, d.lMode, d.k, d.l, d.Kh = K, L, k, l, Kh
+    with np.errstate(divide="ignore", invalid="ignore"):
+        d.cosAlpha = np.where(Kh == 0.0, 0.0, k / Kh)
+        d.sinAlpha = np.where(Kh == 0.0, 0.0, l / Kh)
+
+    f = 2.0 * c.rotationRate * math.sin(c.latitude * PI / 180.0)
+    d.f = f
+    dz = c.Lz / float(Nz - 1)
+    d.z = dz * np.arange(Nz, dtype=np.float64) - c.Lz
+    jj = np.arange(Nj, dtype=np.float64)
+    m = jj * PI / c.Lz
+    d.m = m
+    h0 = np.empty(Nj)
+    h0[0] = c.Lz
+    h0[1:] = c.N0 * c.N0 / (c.g * m[1:] * m[1:])
+    d.h0 = h0
+    N02 = c.N0 * c.N0
+    f2 = f * f
+    if not c.isHydrostatic and N02 <= f2:
+        raise OracleError(INVALID_CONFIGURATION,
+                          "Nonhydrostatic constant stratification requires N0 squared greater than f squared.")
+    sign = np.where(np.arange(Nj) % 2 == 0, 1.0, -1.0)
+    root = math.sqrt(2.0 * MODAL_NORMALIZATION_GRAVITY / (c.Lz * N02))
+    rootw = math.sqrt(2.0 * MODAL_NORMALIZATION_GRAVITY / (c.Lz * (N02 - f2))) if N02 != f2 else float("inf")
+    Fg = sign * h0 * m * root
+    Fg[0] = 2.0
+    Gg = sign * root
+    Gg[0] = 1.0
+    if c.isHydrostatic:
+        Gw_v = Gg.copy()
+    else:
+        Gw_v = sign * rootw
+        Gw_v[0] = Gg[0]
+    Gwg_v = Gg / Gw_v
+    d.Fg, d.Gg = Fg, Gg
+    d.gWaveScale = Gg / Gwg_v
+
+    # Per-coefficient arrays (WVKernelTypes.cpp:214-284), shape (Nkl, Nj).
+    KhC = Kh[:, None]
+    Kh2 = KhC * KhC
+    full = (len(Kh), Nj)
+    M_ = m[None, :]
+    signC = sign[None, :]
+    jC = np.arange(Nj)[None, :]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if c.isHydrostatic:
+            hpm = np.broadcast_to(N02 / (c.g * M_ * M_), full).copy()
+        else:
+            hpm = (N02 - f2) / (c.g * (M_ * M_ + Kh2))
+        hpm[:, 0] = 1.0
+        FgC = Fg[None, :]
+        GgC = Gg[None, :]
+        if c.isHydrostatic:
+            Fw = np.broadcast_to(FgC, full).copy()
+            Gw = np.broadcast_to(GgC, full).copy()
+        else:
+            Fw = signC * hpm * M_ * rootw
+            Gw = np.broadcast_to(signC * rootw, full).copy()
+            Fw[:, 0] = 2.0
+            Gw[:, 0] = 1.0
+        omega = np.sqrt(c.g * hpm * Kh2 + f2)
+        Fwg = FgC / Fw
+        Gwg = GgC / Gw
+        fWaveScale = FgC / Fwg
+        inertialScale = (0.5 * Fwg / FgC)[0]
+        prefactor = sign * math.sqrt(c.g * c.Lz / (2.0 * (N02 - f2))) if N02 != f2 else sign * float("inf")
+        ApmDScaled = np.broadcast_to((m / 2.0) * prefactor, full).copy()
+        isWave = (KhC > 0.0) & (jC > 0)
+        isInertial = np.broadcast_to(KhC == 0.0, full)
+        isGeo = np.broadcast_to(KhC > 0.0, full)
+        isMDA = (KhC == 0.0) & (jC > 0)
+        cosA = d.cosAlpha[:, None]
+        sinA = d.sinAlpha[:, None]
+        kC = k[:, None]
+        lC = l[:, None]
+        z0 = np.zeros(full)
+        gws = d.gWaveScale[None, :]
+        UAp_r = np.where(isWave, cosA * fWaveScale, np.where(isInertial, fWaveScale, 0.0))
+        UAp_i = np.where(isWave, (-(f / omega) * sinA) * fWaveScale, 0.0)
+        VAp_r = np.where(isWave, sinA * fWaveScale, 0.0)
+        VAp_i = np.where(isWave, ((f / omega) * cosA) * fWaveScale, np.where(isInertial, fWaveScale, 0.0))
+        WAp_i = np.where(isWave, (-KhC * hpm) * gws, 0.0)
+        NAp = np.where(isWave, (-KhC * hpm / omega) * gws, 0.0)
+        deltaScale = h0[None, :] * Gwg / FgC
+        ApmD_i = np.where(isWave, (-1.0 / (2.0 * KhC * hpm)) * deltaScale, 0.0)
+        ApmN = np.where(isWave, (-omega / (2.0 * KhC * hpm)) * Gwg / GgC, 0.0)
+        Lr2Inverse = np.where(jC == 0, 0.0, f2 / (c.g * h0[None, :]))
+        denom = Kh2 + Lr2Inverse
+        UA0_i = np.where(isGeo, (lC / denom) * FgC, 0.0)
+        VA0_i = np.where(isGeo, (-kC / denom) * FgC, 0.0)
+        NA0 = np.where(isGeo, np.where(jC == 0, 0.0, -(f / c.g) / denom) * GgC, np.where(isMDA, GgC, 0.0))
+        A0FromVorticity = np.where(isGeo, 1.0 / FgC, np.where(isMDA, (f2 / (2.0 * h0[None, :])) / FgC, 0.0))
+        A0FromBuoyancy = np.where(isGeo, np.where(jC == 0, 0.0, (-f / h0[None, :]) / GgC),
+                                  np.where(isMDA, 1.0 / GgC, 0.0))
+    d.hpm = hpm
+    d.inertialScale = inertialScale
+    d.apmWProjectionPrefactor = prefactor
+    d.arrays = dict(
+        omega=omega, fWaveScale=fWaveScale,
+        UAp=UAp_r + 1j * UAp_i, VAp=VAp_r + 1j * VAp_i, WAp=z0 + 1j * WAp_i, NAp=NAp,
+        UA0=z0 + 1j * UA0_i, VA0=z0 + 1j * VA0_i, NA0=NA0,
+        A0FromVorticity=A0FromVorticity, A0FromBuoyancy=A0FromBuoyancy,
+        ApmD=z0 + 1j * ApmD_i, ApmN=ApmN, ApmDScaled=ApmDScaled,
+    )
+
+    # Half-spectrum mappings (WVKernelTypes.cpp:286-321)
+    NxHalf = Nx // 2 + 1
+    d.NxHalf = NxHalf
+    conj = K < 0
+    kk = np.where(conj, -K, K)
+    ll = np.where(conj, -L, L)
+    ll_idx = np.where(ll >= 0, ll, Ny + ll)
+    d.storageRow = (kk + NxHalf * ll_idx).astype(np.int64)
+    d.conjugated = conj
+    represented = np.zeros(NxHalf * Ny, dtype=bool)
+    represented[d.storageRow] = True
+    comp_rows, comp_src, self_rows = [], [], []
+    for iL in range(Ny):
+        lm = iL if iL <= Ny // 2 else iL - Ny
+        dest = NxHalf * _dft_index(lm, Ny)
+        src = NxHalf * _dft_index(-lm, Ny)
+        if not represented[dest] and represented[src]:
+            comp_rows.append(dest)
+            comp_src.append(src)
+        if lm == 0 or (Ny % 2 == 0 and abs(lm) == Ny // 2):
+            if represented[dest]:
+                self_rows.append(dest)
+    d.completionRows = np.array(comp_rows[::-1], dtype=np.int64)
+    d.completionSources = np.array(comp_src[::-1], dtype=np.int64)
+    d.selfConjugateRows = np.array(self_rows, dtype=np.int64)
+    return d
+
+
+# ---------------------------------------------------------------------------
+# Vertical transforms with the reference's plan semantics
+# (verticalSpecification, WVTransformConstantStratificationKernel.cpp:161-174;
+#  REDFT00/RODFT00 definitions, adapters/reference/WVReferenceFFTEngine.cpp:88-107)
+
+
+def _dct_inplace_complex(x, axis=-1):
+    return _dct1(x.real, axis) + 1j * _dct1(x.imag, axis)
+
+
+def _dst_positions(x):
+    """DST-I over storage positions 1..Nz-2 along the last axis; positions 0 and
+    Nz-1 pass through unchanged (in-place plan offset by one)."""
+    y = x.copy()
+    inner = x[..., 1:-1]
+    y[..., 1:-1] = _dst1(inner.real, -1) + 1j * _dst1(inner.imag, -1)
+    return y
+
+
+def _columns_to_half(desc, cols):
+    """Scatter per-WV-mode z columns (ch, Nkl, Nz) into the half spectrum
+    (ch, Nz, Ny, NxHalf); conjugate where the mode is stored conjugated, then
+    Hermitian completion and self-conjugate rows (completeHermitianBoundaries,
+    WVTransformConstantStratificationKernel.cpp:433-438)."""
+    c = desc.c
+    nch = cols.shape[0]
+    half = np.zeros((nch, c.Ny * desc.NxHalf, c.Nz), dtype=np.complex128)
+    vals = np.where(desc.conjugated[None, :, None], np.conj(cols), cols)
+    half[:, desc.storageRow, :] = vals
+    if len(desc.completionRows):
+        half[:, desc.completionRows, :] = np.conj(half[:, desc.completionSources, :])
+    if len(desc.selfConjugateRows):
+        half[:, desc.selfConjugateRows, :] = half[:, desc.selfConjugateRows, :].real
+    return half
+
+
+def _half_rows_to_spatial(desc, half_rows):
+    """c2r (unnormalized, FFTW semantics) of half spectra stored by row
+    (ch, rows, Nz) -> fields (ch, Nz, Ny, Nx)."""
+    c = desc.c
+    nch = half_rows.shape[0]
+    h = half_rows.reshape(nch, c.Ny, desc.NxHalf, c.Nz).transpose(0, 3, 1, 2)
+    return _irfft2(h, (c.Ny, c.Nx), -1)
+
+
+def _spatial_to_half_rows(desc, fields):
+    """r2c (unnormalized) of fields (ch, Nz, Ny, Nx) -> (ch, rows, Nz)."""
+    c = desc.c
+    h = _rfft2(fields, -1)  # (ch, Nz, Ny, NxHalf)
+    nch = fields.shape[0]
+    return h.transpose(0, 2, 3, 1).reshape(nch, c.Ny * desc.NxHalf, c.Nz)
+
+
+def _gather_columns(desc, half_rows):
+    """Read the stored value of every WV mode (storedValue<Conjugated>,
+    WVTransformConstantStratificationKernel.cpp:211-216): (ch, Nkl, Nz)."""
+    v = half_rows[:, desc.storageRow, :]
+    return np.where(desc.conjugated[None, :, None], np.conj(v), v)
+
+
+def _pad_z(desc, coef):
+    """(…, Nkl, Nj) -> (…, Nkl, Nz) with zeros for j >= Nj."""
+    c = desc.c
+    out = np.zeros(coef.shape[:-1] + (c.Nz,), dtype=np.complex128)
+    out[..., : c.Nj] = coef
+    return out
+
+
+def _forward_dct_columns(desc, cols):
+    """DCT-I then normalizeForwardDCT (kernel.cpp:176-183); returns (…, Nkl, Nj)."""
+    c = desc.c
+    y = _dct_inplace_complex(cols, -1) * (1.0 / float(c.Nz - 1))
+    y[..., c.Nz - 1] *= 0.5
+    return y[..., : c.Nj]
+
+
+def _forward_dst_columns(desc, cols):
+    """DST-I then normalizeForwardDST (kernel.cpp:185-193)."""
+    c = desc.c
+    y = _dst_positions(cols)
+    y = y * (1.0 / float(c.Nz - 1))
+    y[..., 0] = 0.0
+    y[..., c.Nz - 1] = 0.0
+    return y[..., : c.Nj]
+
+
+# ---------------------------------------------------------------------------
+# Coefficient algebra (WVCoefficientFormulas.hpp)
+
+
+def phase(desc, t, t0):
+    el = t - t0
+    return np.cos(desc.arrays["omega"] * el) + 1j * np.sin(desc.arrays["omega"] * el)
+
+
+def _field_values(desc, Ap, Am, A0, p):
+    """coefficientValueForField<0..3> (WVCoefficientFormulas.hpp:27-33) on
+    evolved coefficients (evolveWaveVortexCoefficients :23-25)."""
+    a = desc.arrays
+    Ape = Ap * p
+    Ame = Am * np.conj(p)
+    u = a["UAp"] * Ape + np.conj(a["UAp"]) * Ame + a["UA0"] * A0
+    v = a["VAp"] * Ape + np.conj(a["VAp"]) * Ame + a["VA0"] * A0
+    w = a["WAp"] * Ape + a["WAp"] * Ame
+    n = Ape * a["NAp"] + Ame * (-a["NAp"]) + A0 * a["NA0"]
+    return u, v, w, n
+
+
+def _inverse_columns_cos(desc, coef):
+    return _dct_inplace_complex(_pad_z(desc, coef), -1)
+
+
+def _inverse_columns_sin(desc, coef):
+    return _dst_positions(_pad_z(desc, coef))
+
+
+def inverse_uvweta(desc, Ap, Am, A0, t, t0):
+    """transformWaveVortexToUVWEta (kernel.cpp:745-776): returns (4, Nz, Ny, Nx)."""
+    c = desc.c
+    p = phase(desc, t, t0)
+    u, v, w, n = _field_values(desc, Ap, Am, A0, p)
+    u = u * 0.5
+    v = v * 0.5
+    w = w * 0.5
+    n = n * 0.5
+    w[:, 0] = 0.0
+    n[:, 0] = 0.0
+    if c.Nj == c.Nz:  # j + 1 == Nz endpoint (never reached since Nj <= Nz-1)
+        w[:, -1] = 0.0
+        n[:, -1] = 0.0
+    cols = np.stack([_inverse_columns_cos(desc, u), _inverse_columns_cos(desc, v),
+                     _inverse_columns_sin(desc, w), _inverse_columns_sin(desc, n)])
+    half = _columns_to_half(desc, cols)
+    return _half_rows_to_spatial(desc, half)
+
+
+def velocity_fields(desc, Ap, Am, A0, t, t0):
+    """transformWaveVortexToUVWImpl (kernel.cpp:778-805): (3, Nz, Ny, Nx)."""
+    p = phase(desc, t, t0)
+    u, v, w, _ = _field_values(desc, Ap, Am, A0, p)
+    u = u * 0.5
+    v = v * 0.5
+    w = w * 0.5
+    w[:, 0] = 0.0
+    cols = np.stack([_inverse_columns_cos(desc, u), _inverse_columns_cos(desc, v), _inverse_columns_sin(desc, w)])
+    return _half_rows_to_spatial(desc, _columns_to_half(desc, cols))
+
+
+def derivative_fields(desc, Ap, Am, A0, t, t0, target):
+    """transformToSpatialDomainWithDerivativesFromStateImpl (kernel.cpp:907-945)
+    with normalizedDerivativeSpectrum (WVCoefficientFormulas.hpp:42-58):
+    returns (3, Nz, Ny, Nx) = d/dx, d/dy, d/dz of field `target`."""
+    p = phase(desc, t, t0)
+    val = _field_values(desc, Ap, Am, A0, p)[target]
+    # Column values are taken in the WV (unconjugated) frame: derivative factors
+    # i*k, i*l use the mode's own wavenumbers; conjugated storage then conjugates.
+    kC = desc.k[:, None]
+    lC = desc.l[:, None]
+    mC = desc.m[None, :]
+    cosine = target < 2
+    x = val * (1j * kC)
+    y = val * (1j * lC)
+    zz = val * (-mC if cosine else mC)
+    if cosine:
+        x = x * 0.5
+        y = y * 0.5
+        zz = zz * 0.5
+        zz[:, 0] = 0.0
+        cols = np.stack([_inverse_columns_cos(desc, x), _inverse_columns_cos(desc, y), _inverse_columns_sin(desc, zz)])
+    else:
+        x = x * 0.5
+        y = y * 0.5
+        x[:, 0] = 0.0
+        y[:, 0] = 0.0
+        zz = zz * 0.5
+        cols = np.stack([_inverse_columns_sin(desc, x), _inverse_columns_sin(desc, y), _inverse_columns_cos(desc, zz)])
+    return _half_rows_to_spatial(desc, _columns_to_half(desc, cols))
+
+
+def _project_target(desc, S, target, p, Fp, Fm, F0):
+    """projectSingleFluxTargetImpl + projectFluxTargetMode
+    (kernel.cpp:947-990, 396-431). Accumulates in place."""
+    c = desc.c
+    a = desc.arrays
+    half = _spatial_to_half_rows(desc, S[None])
+    cols = _gather_columns(desc, half)[0]  # (Nkl, Nz)
+    if target < 2:
+        coef = _forward_dct_columns(desc, cols)
+    else:
+        coef = _forward_dst_columns(desc, cols)
+    value = coef * (1.0 / float(c.Nx * c.Ny))
+    kC = desc.k[:, None]
+    lC = desc.l[:, None]
+    if target == 0:
+        A0c = value * (1j * (-lC)) * a["A0FromVorticity"]
+    elif target == 1:
+        A0c = value * (1j * kC) * a["A0FromVorticity"]
+    elif target == 3:
+        A0c = value * a["A0FromBuoyancy"]
+    else:
+        A0c = np.zeros_like(value)
+    buoyV = (value if target == 3 else 0.0) - A0c * a["NA0"]
+    buoy = buoyV * a["ApmN"]
+    if c.isHydrostatic:
+        if target == 0:
+            wave = value * (1j * kC) * a["ApmD"]
+        elif target == 1:
+            wave = value * (1j * lC) * a["ApmD"]
+        else:
+            wave = np.zeros_like(value)
+    else:
+        if target == 0:
+            wave = value * (desc.cosAlpha[:, None] * a["ApmDScaled"])
+        elif target == 1:
+            wave = value * (desc.sinAlpha[:, None] * a["ApmDScaled"])
+        elif target == 2:
+            wave = value * (1j * ((desc.Kh[:, None] / 2.0) * desc.apmWProjectionPrefactor[None, :]))
+        else:
+            wave = np.zeros_like(value)
+    cp = wave + buoy
+    cm = wave - buoy
+    # inertial override for WV index 0 (inertialCoefficientPair<Target>, WVCoefficientFormulas.hpp:101-107)
+    sc = desc.inertialScale
+    if target == 0:
+        cp[0] = value[0] * sc
+    elif target == 1:
+        cp[0] = value[0] * (-1j) * sc
+    else:
+        cp[0] = 0.0
+    cm[0] = np.conj(cp[0])
+    Fp += cp * np.conj(p)
+    Fm += cm * p
+    F0 += A0c
+
+
+def nonlinear_flux(desc, Ap, Am, A0, t, t0):
+    """nonlinearFluxImpl (kernel.cpp:1173-1244): returns (Fp, Fm, F0)."""
+    c = desc.c
+    p = phase(desc, t, t0)
+    U, V, W = velocity_fields(desc, Ap, Am, A0, t, t0)
+    Fp = np.zeros_like(Ap)
+    Fm = np.zeros_like(Ap)
+    F0 = np.zeros_like(Ap)
+    targets = (0, 1, 3) if c.isHydrostatic else (0, 1, 2, 3)
+    for q in targets:
+        dx, dy, dz = derivative_fields(desc, Ap, Am, A0, t, t0, q)
+        S = -(U * dx + V * dy + W * dz)
+        _project_target(desc, S, q, p, Fp, Fm, F0)
+    return Fp, Fm, F0
+
+
+def forward(desc, fields, t, t0):
+    """transformUVWEtaToWaveVortexImpl / transformUVEtaToWaveVortexImpl
+    (kernel.cpp:651-684, 597-635) with projectNonhydrostaticMode /
+    projectHydrostaticMode (:335-370, :299-333). fields: (ch, Nz, Ny, Nx)."""
+    c = desc.c
+    a = desc.arrays
+    half = _spatial_to_half_rows(desc, fields)
+    cols = _gather_columns(desc, half)
+    hs = 1.0 / float(c.Nx * c.Ny)
+    kC = desc.k[:, None]
+    lC = desc.l[:, None]
+    if c.isHydrostatic:
+        U = _forward_dct_columns(desc, cols[0]) * hs
+        V = _forward_dct_columns(desc, cols[1]) * hs
+        N = _forward_dst_columns(desc, cols[2]) * hs
+        W = None
+    else:
+        U = _forward_dct_columns(desc, cols[0]) * hs
+        V = _forward_dct_columns(desc, cols[1]) * hs
+        W = _forward_dst_columns(desc, cols[2]) * hs
+        N = _forward_dst_columns(desc, cols[3]) * hs
+    A0 = (V * (1j * kC) - U * (1j * lC)) * a["A0FromVorticity"] + N * a["A0FromBuoyancy"]
+    buoy = (N - A0 * a["NA0"]) * a["ApmN"]
+    if c.isHydrostatic:
+        div = U * (1j * kC) + V * (1j * lC)
+        wave = a["ApmD"] * div
+    else:
+        delta = (U * desc.cosAlpha[:, None] + V * desc.sinAlpha[:, None]) * a["ApmDScaled"]
+        wbar = (1j * ((desc.Kh[:, None] / 2.0) * desc.apmWProjectionPrefactor[None, :])) * W
+        wave = delta + wbar
+    Ap = wave + buoy
+    Am = wave - buoy
+    Ap[0] = (U[0] - V[0] * 1j) * desc.inertialScale
+    Am[0] = np.conj(Ap[0])
+    p = phase(desc, t, t0)
+    return Ap * np.conj(p), Am * p, A0
+
+
+# ---------------------------------------------------------------------------
+# Forcing: adaptive damping (PortableRuntime/src/WVForcingEngine.cpp:30-38, 352-381, 710-726)
+
+
+def _vanishing_filter(value, cutoff, maximum):
+    value = abs(value)
+    if value < cutoff:
+        return 0.0
+    if value > maximum:
+        return 1.0
+    if maximum == cutoff:
+        return 1.0 if value >= maximum else 0.0
+    ratio = (value - maximum) / (value - cutoff)
+    return math.exp(-(ratio * ratio))
+
+
+def adaptive_damping_operator(desc):
+    c = desc.c
+    f2 = desc.f * desc.f
+    if not f2 > 0.0:
+        raise OracleError(UNSUPPORTED, "Adaptive damping requires nonzero Coriolis frequency.")
+    maxComp = float(np.max(np.maximum(np.abs(desc.k), np.abs(desc.l))))
+    if not maxComp > 0.0:
+        raise OracleError(INVALID_CONFIGURATION, "Adaptive damping requires resolved horizontal wavenumbers.")
+    effRes = PI / maxComp
+    dklMin = min(2.0 * PI / c.Lx, 2.0 * PI / c.Ly)
+    klCut = dklMin * (maxComp / dklMin) ** 0.75
+    jMax = float(c.Nj - 1)
+    jCut = jMax ** 0.75 if c.Nj > 2 else 0.0
+    prefXY = effRes / (PI * PI)
+    refLr2 = c.g * desc.h0[-1] / f2
+    prefZ = (PI * PI * refLr2 / (effRes * effRes)) * prefXY
+    damp = np.empty((desc.Nkl, c.Nj))
+    for i in range(desc.Nkl):
+        Qkl = _vanishing_filter(desc.Kh[i], klCut, maxComp)
+        for j in range(c.Nj):
+            Qj = _vanishing_filter(float(j), jCut, jMax) if c.Nj > 2 else 1.0
+            Lr2inv = 0.0 if j == 0 else f2 / (c.g * desc.h0[j])
+            damp[i, j] = -prefXY * Qkl * desc.Kh[i] * desc.Kh[i] - prefZ * Qj * Lr2inv
+    return damp
+
+
+def rhs(desc, Ap, Am, A0, t, t0, damping=None):
+    """Scheduled RHS: nonlinear advection, then (optionally) adaptive damping
+    using max sqrt(u^2+v^2) of the physical velocity."""
+    Fp, Fm, F0 = nonlinear_flux(desc, Ap, Am, A0, t, t0)
+    if damping is not None:
+        fields = inverse_uvweta(desc, Ap, Am, A0, t, t0)
+        speed = float(np.max(np.sqrt(fields[0] * fields[0] + fields[1] * fields[1])))
+        s = speed * damping
+        Fp = Fp + Ap * s
+        Fm = Fm + Am * s
+        F0 = F0 + A0 * s
+    return Fp, Fm, F0
+
+
+def rk4_step(desc, Ap, Am, A0, t, t0, h, damping=None):
+    """WVFixedStepRK4::step (PortableRuntime/src/WVRungeKutta.cpp:335-462)."""
+    y = (Ap, Am, A0)
+    k = rhs(desc, *y, t, t0, damping)
+    wsum = [x.copy() for x in k]
+    stage = [y[i] + (0.5 * h) * k[i] for i in range(3)]
+    k = rhs(desc, *stage, t + 0.5 * h, t0, damping)
+    wsum = [wsum[i] + 2.0 * k[i] for i in range(3)]
+    stage = [y[i] + (0.5 * h) * k[i] for i in range(3)]
+    k = rhs(desc, *stage, t + 0.5 * h, t0, damping)
+    wsum = [wsum[i] + 2.0 * k[i] for i in range(3)]
+    stage = [y[i] + h * k[i] for i in range(3)]
+    k = rhs(desc, *stage, t + h, t0, damping)
+    wsum = [wsum[i] + 1.0 * k[i] for i in range(3)]
+    out = [y[i] + (h / 6.0) * wsum[i] for i in range(3)]
+    return out[0], out[1], out[2], t + h
+
+
+def rk4(desc, Ap, Am, A0, t, t0, h, steps, damping=None):
+    for _ in range(steps):
+        Ap, Am, A0, t = rk4_step(desc, Ap, Am, A0, t, t0, h, damping)
+    return Ap, Am, A0, t
+
+
+# ---------------------------------------------------------------------------
+# Energy flux diagnostic (@WVTransform/energyFluxFromNonlinearFlux.m:37-44 with
+# total-energy factors of the flow components)
+
+
+def energy_factors(desc):
+    c = desc.c
+    Kh = desc.Kh[:, None]
+    j = np.arange(c.Nj)[None, :]
+    hpm = desc.hpm
+    Apm = np.where((Kh > 0) & (j > 0), 2.0 * hpm, 0.0)
+    Apm = np.where((Kh == 0) & (j > 0), hpm, Apm)
+    Apm = np.where((Kh == 0) & (j == 0), c.Lz, Apm)
+    f2 = desc.f * desc.f
+    K2 = Kh * Kh
+    with np.errstate(divide="ignore", invalid="ignore"):
+        Lr2inv = np.where(j == 0, 0.0, f2 / (c.g * desc.h0[None, :]))
+        geo_j = (K2 * desc.h0[None, :] + f2 / c.g) / ((K2 + Lr2inv) ** 2)
+        geo_0 = c.Lz / K2
+    A0f = np.where((Kh > 0) & (j > 0), geo_j, 0.0)
+    A0f = np.where((Kh > 0) & (j == 0), geo_0, A0f)
+    A0f = np.where((Kh == 0) & (j > 0), c.g / 2.0, A0f)
+    return Apm, A0f
+
+
+def energy_flux(desc, Ap, Am, A0, Fp, Fm, F0):
+    Apm_f, A0_f = energy_factors(desc)
+    Ep = 2.0 * Apm_f * np.real(Fp * np.conj(Ap))
+    Em = 2.0 * Apm_f * np.real(Fm * np.conj(Am))
+    E0 = 2.0 * A0_f * np.real(F0 * np.conj(A0))
+    return Ep, Em, E0
+
+
+# ---------------------------------------------------------------------------
+# Synthetic states
+
+
+def random_state(desc, seed, scale=1e-3):
+    """Seeded arbitrary complex coefficients (not necessarily representable)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shape = (desc.Nkl, desc.c.Nj)
+    out = []
+    for _ in range(3):
+        out.append(scale * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    return tuple(out)
+
+
+def spectrum_state(desc, seed, urms=0.1, t0=0.0):
+    """Seeded state with uniform random phases and Gaussian amplitudes shaped by
+    the isotropic spectrum (Kh^2 + (j*pi/Lz)^2)^(-3/4) in amplitude (energy
+    ~ (Kh^2+m^2)^(-3/2)), made representable by one inverse->forward round trip
+    and scaled to the requested rms velocity."""
+    c = desc.c
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shape = (desc.Nkl, c.Nj)
+    K2 = desc.Kh[:, None] ** 2 + (np.arange(c.Nj)[None, :] * PI / c.Lz) ** 2
+    with np.errstate(divide="ignore"):
+        env = np.where(K2 > 0, K2 ** (-0.75), 0.0)
+    comps = []
+    for _ in range(3):
+        amp = rng.standard_normal(shape) * env
+        ph = rng.uniform(0.0, 2.0 * PI, shape)
+        comps.append(amp * np.exp(1j * ph))
+    Ap, Am, A0 = comps
+    fields = inverse_uvweta(desc, Ap, Am, A0, t0, t0)
+    Ap, Am, A0 = forward(desc, fields[[0, 1, 3]] if c.isHydrostatic else fields, t0, t0)
+    fields = inverse_uvweta(desc, Ap, Am, A0, t0, t0)
+    rms = math.sqrt(float(np.mean(fields[0] ** 2 + fields[1] ** 2 + fields[2] ** 2)))
+    s = urms / rms if rms > 0 else 1.0
+    return Ap * s, Am * s, A0 * s
+
+
+def cfl_time_step(desc, Ap, Am, A0, t0=0.0, cfl=0.5):
+    """Fixed-step dt per WVModelFixedTimeStepMethods.timeStepForCFL
+    (Integrators/WVModelFixedTimeStepMethods.m:50-95): cfl times the minimum of
+    dx_eff/max|u_h|, (3/2)dz/max|w| (levels above the bottom) and the period
+    of the fastest resolved wave (j >= 1)."""
+    c = desc.c
+    fields = inverse_uvweta(desc, Ap, Am, A0, t0, t0)
+    U = float(np.max(np.sqrt(fields[0] ** 2 + fields[1] ** 2)))
+    dx = PI / float(np.max(np.maximum(np.abs(desc.k), np.abs(desc.l))))
+    dz = c.Lz / (c.Nz - 1)
+    Wm = float(np.max(np.abs(fields[2][1:])))
+    advective = cfl * dx / U if U > 0 else float("inf")
+    if Wm > 0:
+        advective = min(advective, cfl * (1.5 * dz) / Wm)
+    omax = float(np.max(np.abs(desc.arrays["omega"][:, 1:]))) if c.Nj > 1 else 0.0
+    oscillatory = cfl * 2.0 * PI / omax if omax > 0 else float("inf")
+    return min(advective, oscillatory)

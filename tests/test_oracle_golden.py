@@ -1,0 +1,91 @@
+"""Pins the numpy oracle against golden vectors produced by the reference's own
+C++ kernel (CompiledKernel + PortableRuntime, exact direct-DFT engine)."""
+import numpy as np
+import pytest
+
+import wv_oracle as O
+from _cases import FP64_REL_TOL, config_from_case, golden_cases, load_golden, rel_err
+
+CASES = golden_cases()
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def case(request):
+    name = request.param
+    cf = CASES[name]
+    desc = O.build_descriptor(config_from_case(cf))
+    return name, cf, desc, load_golden(name)
+
+
+def test_descriptor_ordering_and_arrays_bitwise(case):
+    name, cf, d, g = case
+    assert np.array_equal(d.kMode, g["desc_kMode"])
+    assert np.array_equal(d.lMode, g["desc_lMode"])
+    assert np.array_equal(d.storageRow, g["desc_storageRow"])
+    assert np.array_equal(d.conjugated, g["desc_conjugated"])
+    # Mode-set construction restates WVKernelTypes.cpp:119-330 operation for operation.
+    assert np.array_equal(d.arrays["omega"].ravel(), g["desc_omega"])
+    assert np.array_equal(d.arrays["fWaveScale"].ravel(), g["desc_fWaveScale"])
+    assert np.array_equal(d.arrays["UAp"].ravel(), g["desc_UApField"])
+    assert np.array_equal(d.arrays["WAp"].ravel(), g["desc_WApField"])
+    assert np.array_equal(d.arrays["A0FromVorticity"].ravel(), g["desc_A0FromVorticity"])
+    assert np.array_equal(d.arrays["A0FromBuoyancy"].ravel(), g["desc_A0FromBuoyancy"])
+    assert np.array_equal(d.arrays["NA0"].ravel(), g["desc_NA0Field"])
+    assert np.array_equal(d.arrays["ApmN"].ravel(), g["desc_ApmNProjection"])
+
+
+def test_nonlinear_flux(case):
+    name, cf, d, g = case
+    F = O.nonlinear_flux(d, g["Ap"], g["Am"], g["A0"], float(g["t"]), float(g["t0"]))
+    for got, key in zip(F, ("Fp", "Fm", "F0")):
+        assert rel_err(got, g[key]) <= FP64_REL_TOL, key
+
+
+def test_scheduled_rhs(case):
+    name, cf, d, g = case
+    damp = O.adaptive_damping_operator(d) if cf["damping"] else None
+    R = O.rhs(d, g["Ap"], g["Am"], g["A0"], float(g["t"]), float(g["t0"]), damp)
+    for got, key in zip(R, ("Rp", "Rm", "R0")):
+        assert rel_err(got, g[key]) <= FP64_REL_TOL, key
+
+
+def test_forward_transform(case):
+    name, cf, d, g = case
+    B = O.forward(d, g["fields"], float(g["t"]), float(g["t0"]))
+    for got, key in zip(B, ("Bp", "Bm", "B0")):
+        assert rel_err(got, g[key]) <= FP64_REL_TOL, key
+
+
+def test_inverse_transform(case):
+    name, cf, d, g = case
+    inv = O.inverse_uvweta(d, g["Ap"], g["Am"], g["A0"], float(g["t"]), float(g["t0"]))
+    assert rel_err(inv, g["inverse"]) <= FP64_REL_TOL
+
+
+def test_fixed_rk4(case):
+    name, cf, d, g = case
+    damp = O.adaptive_damping_operator(d) if cf["damping"] else None
+    K = O.rk4(d, g["rk_Ap"], g["rk_Am"], g["rk_A0"], float(g["rk_t"]), float(g["rk_t0"]), float(g["rk_dt"]),
+              int(g["rk_steps"]), damp)
+    for got, key in zip(K[:3], ("Kp", "Km", "K0")):
+        assert rel_err(got, g[key]) <= FP64_REL_TOL, key
+    assert K[3] == float(g["rk_tout"])
+
+
+def test_zero_state_gives_exactly_zero_flux():
+    """TestWVKernelContract.cpp:395-414: zero state -> bit-exact zero flux."""
+    cf = CASES["odd_15x13x9"]
+    d = O.build_descriptor(config_from_case(cf))
+    z = np.zeros((d.Nkl, d.c.Nj), np.complex128)
+    F = O.nonlinear_flux(d, z, z, z, 3.0, 1.0)
+    for x in F:
+        assert np.all(x == 0)
+
+
+def test_invalid_configuration_rejected():
+    cf = dict(CASES["odd_15x13x9"])
+    c = config_from_case(cf)
+    c.Nj = c.Nz
+    with pytest.raises(O.OracleError) as e:
+        O.build_descriptor(c)
+    assert e.value.code == O.INVALID_CONFIGURATION
