@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark: fixed-step RK4 steps/s of the constant-stratification spectral
+step (wave-vortex transforms + nonlinear flux + RK4) at 256x256x129.
+
+Workload (one "step" = one WVFixedStepRK4 step = 4 nonlinear fluxes + stage
+arithmetic): Lx = Ly = 800 km, Lz = 4000 m, N0 = 5.2e-3 1/s, latitude 33,
+nonhydrostatic, 2/3 antialiasing; seeded synthetic state (uniform random
+phases, Gaussian amplitudes shaped by (Kh^2 + m^2)^(-3/4), representable via
+one inverse/forward round trip, 0.1 m/s rms velocity); dt = 0.5 x the CFL limit.
+
+  value : device-timed RK4 steps/s, state resident in HBM (CUDA events on the
+          launching stream, L2 flushed between steps)
+  e2e   : the same through the host-pointer C ABI (wv_rk4_steps), state copied
+          host->device and back every step, wall-clock timed
+  --impl reference : the CPU oracle restatement of the reference algorithm
+          (numpy/scipy, all host threads), on the same workload
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "wave-vortex-model_gb300")
+if PKG not in sys.path:
+    sys.path.insert(0, PKG)
+
+GRID = dict(Nx=256, Ny=256, Nz=129, Nj=85, Lx=800e3, Ly=800e3, Lz=4000.0, N0=5.2e-3, latitude=33.0)
+METRIC = "RK4 steps/s 256x256x129 (fixed-step RK4 of the nonlinear wave-vortex flux)"
+UNIT = "RK4 steps/s"
+SEED = 1
+URMS = 0.1
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), reasons=sorted(reasons), samples=len(sm))
+        return out
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def configuration(wvgpu):
+    return wvgpu.Configuration(Nx=GRID["Nx"], Ny=GRID["Ny"], Nz=GRID["Nz"], Nj=GRID["Nj"], Lx=GRID["Lx"], Ly=GRID["Ly"],
+                               Lz=GRID["Lz"], N0=GRID["N0"], latitude=GRID["latitude"])
+
+
+def stage_bytes(sizes, nt, s):
+    """Algorithmic HBM bytes per launch of each flux stage under this layout
+    (s = bytes per complex of the xy working type), as in the design notes:
+      vertical inverse: read Ap,Am,A0 (+omega) and write (4+nt) z-grid channels of the active rows
+      y inverse:        read (4+nt) channels of active rows, write (4+2nt) channels x Ny x kx columns
+      x products:       read (4+2nt) channels x Ny x kx, write nt channels x Ny x kx
+      y forward:        read nt x Ny x kx, write nt channels of the active rows
+      vertical forward: read nt channels of active rows and Ap,Am,A0 (+omega), write Fp,Fm,F0"""
+    M, P, KX = sizes["M"], sizes["active_rows"], sizes["kx_columns"]
+    Ny, Nz = GRID["Ny"], GRID["Nz"]
+    col = Nz * P * s
+    grid = Nz * Ny * KX * s
+    return {
+        "vertical_inverse": 3 * 16 * M + 8 * M + (4 + nt) * col,
+        "y_inverse": (4 + nt) * col + (4 + 2 * nt) * grid,
+        "x_products": (4 + 2 * nt) * grid + nt * grid,
+        "y_forward": nt * grid + nt * col,
+        "vertical_forward": nt * col + 3 * 16 * M + 8 * M + 3 * 16 * M,
+    }
+
+
+def fp64_peak_tflops(torch):
+    """FP64 throughput of this GPU, measured with a float64 GEMM (cuBLAS)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def traffic_from_profile(stage):
+    """Per-launch DRAM bytes of a stage from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            parts = line.split()
+            if len(parts) >= 3 and not line.startswith("#") and parts[0] == stage and parts[1] == "fp64":
+                return float(parts[2])
+    return None
+
+
+def cpu_baseline_oracle(state, dt):
+    """One RK4 step of the CPU oracle (numpy/scipy restatement of the reference)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import wv_oracle as O
+    c = O.Config(Nx=GRID["Nx"], Ny=GRID["Ny"], Nz=GRID["Nz"], Nj=GRID["Nj"], Lx=GRID["Lx"], Ly=GRID["Ly"], Lz=GRID["Lz"],
+                 N0=GRID["N0"], latitude=GRID["latitude"])
+    d = O.build_descriptor(c)
+    Ap, Am, A0 = state
+    O.rk4_step(d, Ap, Am, A0, 0.0, 0.0, dt)  # warm (FFT plans, page-in)
+    t = time.perf_counter()
+    O.rk4_step(d, Ap, Am, A0, 0.0, 0.0, dt)
+    el = time.perf_counter() - t
+    return {"value": 1.0 / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "1 RK4 step (4 nonlinear fluxes) of the 256x256x129 state with the numpy/scipy oracle "
+                      "(scipy.fft workers=-1); seconds per step %.2f" % el}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import wvgpu
+    from wvgpu import build
+    build.build()
+    cfg = configuration(wvgpu)
+    k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision=args.precision)
+    state = wvgpu.synthetic_state(k, seed=SEED + rank * 0, urms=URMS)
+    dt = wvgpu.cfl_time_step(k, *state)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+    stream = torch.cuda.current_stream()
+    t, t0 = 0.0, 0.0
+    for _ in range(args.warmup):
+        _, _, _, t = k.rk4(*dev, t, t0, dt, 1)
+    torch.cuda.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    launches0 = k.metrics()["kernel_launches"]
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    total_ms = 0.0
+    barrier()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _, _, _, t = k.rk4(*dev, t, t0, dt, 1)
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+    barrier()
+    launches = k.metrics()["kernel_launches"] - launches0
+    t_s = total_ms / 1e3
+    if world > 1:
+        tt = torch.tensor([t_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_s = float(tt.item())
+    value = world * args.steps / t_s
+
+    # per-stage device times (instrumented pass, not part of the timed region)
+    k.setStageInstrumentation(True)
+    _, _, _, _ = k.rk4(*dev, t, t0, dt, 1)
+    torch.cuda.synchronize()
+    st = k.stage_times()
+    k.setStageInstrumentation(False)
+    names = ["vertical_inverse", "y_inverse", "x_products", "y_forward", "vertical_forward"]
+    per_launch = {n: st[n + "_ms"] / max(st["fluxes"], 1) for n in names}
+    dominant = max(per_launch, key=per_launch.get)
+    s = 16 if args.precision == "fp64" else 8
+    nt = 4
+    sbytes = stage_bytes(k.sizes, nt, s)
+    peaks, peak_kind = measured_peaks()
+    achieved = sbytes[dominant] / (per_launch[dominant] * 1e-3) / 1e9
+    traffic = traffic_from_profile(dominant)
+    flux_ms = sum(per_launch.values())
+    M, P = k.sizes["M"], k.sizes["active_rows"]
+    hr = P * GRID["Nz"]
+    b_flux = 104 * M + 24 * s * hr
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": sbytes[dominant], "avg_launch_ms": per_launch[dominant],
+                "stage_ms_per_flux": per_launch,
+                "flux": {"algorithmic_bytes": b_flux, "ms": flux_ms,
+                         "achieved_gbs": b_flux / (flux_ms * 1e-3) / 1e9,
+                         "frac": b_flux / (flux_ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}}
+    if args.precision == "fp64":
+        try:
+            roofline["fp64_gemm_peak_tflops_measured"] = fp64_peak_tflops(torch)
+        except Exception:  # pragma: no cover
+            roofline["fp64_gemm_peak_tflops_measured"] = None
+
+    # end to end through the host-pointer C ABI, pinned host buffers
+    host = [torch.empty(a.shape, dtype=torch.complex128, pin_memory=True).numpy() for a in state]
+    for hbuf, a in zip(host, state):
+        hbuf[...] = a
+    te = 0.0
+    k.rk4(*host, te, t0, dt, 1)  # warm the host path
+    barrier()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        Ap, Am, A0, te = k.rk4(*host, te, t0, dt, 1)
+        host[0][...], host[1][...], host[2][...] = Ap, Am, A0
+    e2e_s = time.perf_counter() - w0
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    coeff_bytes = 3 * M * 16
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32 xy/vertical + f64 phases/projection/RK4",
+        "data": "synthetic", "config": {
+            "workload": "fixed-step RK4, nonlinear advection, 256x256x129, 800 km x 800 km x 4 km, N0 5.2e-3, lat 33, "
+                        "0.1 m/s rms seeded spectrum state, dt = 0.5 x CFL",
+            "grid": [GRID["Nx"], GRID["Ny"], GRID["Nz"]], "Nj": GRID["Nj"], "Nkl": k.sizes["Nkl"], "dt_s": dt,
+            "precision": args.precision, "parallelism": f"replicas x{world}",
+            "l2": "flushed between timed steps (256 MB write)"},
+        "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": coeff_bytes,
+                "d2h_bytes_per_step": coeff_bytes},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_oracle(state, dt)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    k.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import wv_oracle as O
+    c = O.Config(Nx=GRID["Nx"], Ny=GRID["Ny"], Nz=GRID["Nz"], Nj=GRID["Nj"], Lx=GRID["Lx"], Ly=GRID["Ly"], Lz=GRID["Lz"],
+                 N0=GRID["N0"], latitude=GRID["latitude"])
+    d = O.build_descriptor(c)
+    Ap, Am, A0 = O.spectrum_state(d, seed=SEED, urms=URMS)
+    dt = O.cfl_time_step(d, Ap, Am, A0)
+    t, t0 = 0.0, 0.0
+    for _ in range(min(args.warmup, 1)):
+        Ap, Am, A0, t = O.rk4_step(d, Ap, Am, A0, t, t0, dt)
+    budget = 150.0
+    done, el = 0, 0.0
+    w0 = time.perf_counter()
+    while done < args.steps:
+        Ap, Am, A0, t = O.rk4_step(d, Ap, Am, A0, t, t0, dt)
+        done += 1
+        el = time.perf_counter() - w0
+        if el > budget:
+            break
+    value = done / el
+    sample = (f"{done} of {args.steps} RK4 steps of the 256x256x129 state (4 nonlinear fluxes each) with the "
+              f"numpy/scipy restatement of the reference kernel, {min(args.warmup, 1)} warm-up step; "
+              f"capped at {budget:.0f} s")
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * el / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "impl": "reference",
+           "config": {"workload": "fixed-step RK4, nonlinear advection, 256x256x129 (CPU oracle of the reference kernel)",
+                      "grid": [GRID["Nx"], GRID["Ny"], GRID["Nz"]], "dt_s": dt, "parallelism": "host threads"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

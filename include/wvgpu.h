@@ -1,0 +1,195 @@
+/*
+ * wvgpu.h — C ABI of the GB300 (sm_103a) constant-stratification spectral
+ * time step of WaveVortexModel: wave-vortex transforms, the nonlinear flux
+ * with 2/3 antialiasing, adaptive damping and fixed-step RK4.
+ *
+ * Plain pointers and sizes only.  Coefficient arrays are column-major
+ * [Nj, Nkl] complex doubles stored as interleaved (re, im) pairs (the
+ * reference's WVComplex64 layout, CompiledKernel/include/WaveVortexKernel/
+ * WVKernelTypes.hpp:13-20); spatial field bundles are column-major
+ * [Nx, Ny, Nz, Nfield] doubles (x fastest).
+ *
+ * Each entry point names the reference interface it replaces.  Host-pointer
+ * entries copy through the handle's device buffers (the drop-in path for the
+ * MATLAB gateway and PortableRuntime); *_device entries take device pointers
+ * and a cudaStream_t passed as void* (the path for torch / CUDA callers).
+ */
+#ifndef WVGPU_H
+#define WVGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WV_CONTRACT_VERSION 4u /* WVKernelContractVersion, WVKernelTypes.hpp:11 */
+
+/* Numerically identical to wavevortex::WVKernelStatusCode (WVKernelTypes.hpp:22-35). */
+enum {
+    WV_SUCCESS = 0,
+    WV_INVALID_CONFIGURATION = 1,
+    WV_INVALID_SHAPE = 2,
+    WV_INVALID_POINTER = 3,
+    WV_OVERLAPPING_ARRAYS = 4,
+    WV_SIZE_OVERFLOW = 5,
+    WV_ALLOCATION_FAILURE = 6,
+    WV_FFT_PLAN_FAILURE = 7,
+    WV_FFT_EXECUTION_FAILURE = 8,
+    WV_NUMERICAL_FAILURE = 9,
+    WV_UNSUPPORTED_OPERATION = 10,
+    WV_REENTRANT_EXECUTION = 11
+};
+
+/* WVTransformConstantStratificationConfiguration (WVKernelTypes.hpp:129-146). */
+typedef struct wv_config {
+    uint32_t contract_version;
+    uint64_t Nx, Ny, Nz, Nj;
+    double Lx, Ly, Lz;
+    double N0, rho0, g;
+    double planetary_radius, rotation_rate, latitude;
+    uint8_t is_hydrostatic;
+    uint8_t should_antialias;
+} wv_config;
+
+/* Arithmetic of a handle.  FP64: the plain drop-in, every stage in double.
+ * MIXED: FP32 xy transforms and quadratic products, FP64 phases, projections,
+ * flux accumulation and RK4 stage accumulation. */
+enum { WV_PRECISION_FP64 = 0, WV_PRECISION_MIXED = 1 };
+
+/* Forcing schedule of the right-hand side (WVFrozenForcingSchedule entries
+ * WVNonlinearAdvection and WVAdaptiveDamping, PortableRuntime/src/WVForcingEngine.cpp). */
+#define WV_FORCING_NONLINEAR_ADVECTION 1u
+#define WV_FORCING_ADAPTIVE_DAMPING 2u
+
+typedef struct wv_handle wv_handle;
+
+/* Sizes derived from a configuration (no GPU needed). */
+typedef struct wv_sizes {
+    uint64_t Nx, Ny, Nz, Nj, Nkl, NxHalf;
+    uint64_t M;              /* Nj * Nkl coefficients per component */
+    uint64_t active_rows;    /* half-spectrum rows holding data (retained + Hermitian completion) */
+    uint64_t kx_columns;     /* kx columns 0..kx_columns-1 that hold data */
+    uint64_t device_bytes;   /* device memory a handle of this configuration allocates (FP64) */
+} wv_sizes;
+
+/* Counters of a handle (subset of WVKernelMetrics, WVTransformConstantStratificationKernel.hpp:12-45). */
+typedef struct wv_metrics {
+    uint64_t nonlinear_flux_calls;
+    uint64_t rhs_evaluations;
+    uint64_t forward_calls;
+    uint64_t inverse_calls;
+    uint64_t rk4_steps;
+    uint64_t kernel_launches;
+    uint64_t device_bytes;
+    double last_max_horizontal_speed;
+} wv_metrics;
+
+/* ---- configuration and descriptor (host only, no GPU) ---------------------------- */
+
+/* Validates a configuration and reports its sizes.
+ * Replaces WVTransformConstantStratificationDescriptor::create validation
+ * (CompiledKernel/src/WVKernelTypes.cpp:119-133,196-201) and the MEX "estimate"
+ * command (CompiledKernel/adapters/native-fftw/wv_compiled_backend_mex.cpp:225-245). */
+int wv_describe(const wv_config* config, wv_sizes* sizes, char* message, size_t message_capacity);
+
+/* Mode set of the descriptor in canonical WV order (WVKernelTypes.cpp:143-166,286-307):
+ * kMode/lMode [Nkl] and omega [Nj,Nkl] (any pointer may be NULL). */
+int wv_describe_modes(const wv_config* config, int64_t* kMode, int64_t* lMode, double* omega,
+                      uint64_t* storage_rows, uint8_t* conjugated);
+
+/* ---- handle lifetime -------------------------------------------------------------- */
+
+/* Replaces WVTransformConstantStratificationKernel::create
+ * (CompiledKernel/include/WaveVortexKernel/WVTransformConstantStratificationKernel.hpp:47)
+ * and the MEX "create" command (wv_compiled_backend_mex.cpp:247-260).  Builds the
+ * descriptor on the host in FP64, uploads it once, and allocates the device arena
+ * on the current CUDA device. */
+int wv_create(const wv_config* config, int precision, wv_handle** handle);
+
+/* Replaces the MEX "delete" command (wv_compiled_backend_mex.cpp:276-281). */
+void wv_destroy(wv_handle* handle);
+
+/* Message of the last failing call on this handle (WVKernelStatus::message). */
+const char* wv_last_message(const wv_handle* handle);
+
+int wv_get_sizes(const wv_handle* handle, wv_sizes* sizes);
+int wv_get_metrics(const wv_handle* handle, wv_metrics* metrics);
+
+/* Forcing schedule for wv_evaluate_rhs / wv_rk4_*: a bitwise OR of WV_FORCING_*.
+ * Default: WV_FORCING_NONLINEAR_ADVECTION (defaultNonlinearAdvectionSchedule,
+ * PortableRuntime/src/WVForcingContracts.cpp:118-132). */
+int wv_set_forcing(wv_handle* handle, uint32_t forcing_flags);
+
+/* Per-stage device time of the nonlinear flux, summed over instrumented fluxes
+ * (the GPU counterpart of WVKernelMetrics' stage seconds,
+ * WVTransformConstantStratificationKernel.hpp:31-44). */
+typedef struct wv_stage_times {
+    double vertical_inverse_ms;   /* phase, field spectra, vertical inverse contraction */
+    double y_inverse_ms;          /* inverse FFTs along y */
+    double x_products_ms;         /* c2r along x, quadratic products, r2c along x */
+    double y_forward_ms;          /* forward FFTs along y */
+    double vertical_forward_ms;   /* vertical forward contraction and projection */
+    uint64_t fluxes;
+} wv_stage_times;
+
+/* setStageInstrumentation (kernel.cpp:570-581): when enabled, each flux records
+ * CUDA events between its five stages on its stream and waits for them, adding
+ * the elapsed device time to the handle's stage times (reset on enable). */
+int wv_set_stage_instrumentation(wv_handle* handle, int enabled);
+int wv_get_stage_times(const wv_handle* handle, wv_stage_times* times);
+
+/* ---- operators (host pointers) ------------------------------------------------------ */
+
+/* WVTransformConstantStratificationKernel::nonlinearFlux (kernel.cpp:1140-1146).
+ * Ap, Am, A0 in; Fp, Fm, F0 out; all [Nj, Nkl] complex. */
+int wv_nonlinear_flux(wv_handle* handle, double t, double t0,
+                      const double* Ap, const double* Am, const double* A0,
+                      double* Fp, double* Fm, double* F0);
+
+/* WVIntegrationSystem::evaluateRightHandSide with the handle's forcing schedule
+ * (PortableRuntime/src/WVConstantStratificationIntegrationSystem.cpp:295-330); the
+ * MEX "nonlinearFlux" command (wv_compiled_backend_mex.cpp:318-331). */
+int wv_evaluate_rhs(wv_handle* handle, double t, double t0,
+                    const double* Ap, const double* Am, const double* A0,
+                    double* Fp, double* Fm, double* F0);
+
+/* transformUVWEtaToWaveVortex (nonhydrostatic, 4 fields u,v,w,eta) or
+ * transformUVEtaToWaveVortex (hydrostatic, 3 fields u,v,eta) (kernel.cpp:583-684);
+ * MEX "forward" (wv_compiled_backend_mex.cpp:285-296). */
+int wv_forward(wv_handle* handle, const double* fields, double t, double t0,
+               double* Ap, double* Am, double* A0);
+
+/* transformWaveVortexToUVWEta (kernel.cpp:686-694,745-776): fields [Nx,Ny,Nz,4];
+ * MEX "inverse" (wv_compiled_backend_mex.cpp:297-306). */
+int wv_inverse(wv_handle* handle, double t, double t0,
+               const double* Ap, const double* Am, const double* A0, double* fields);
+
+/* WVFixedStepRK4::step applied n_steps times (PortableRuntime/src/WVRungeKutta.cpp:335-462)
+ * on the handle's forcing schedule.  State updated in place; *t advanced by n_steps*dt. */
+int wv_rk4_steps(wv_handle* handle, double* Ap, double* Am, double* A0,
+                 double* t, double t0, double dt, int n_steps);
+
+/* ---- operators (device pointers, stream passed as cudaStream_t cast to void*) ------- */
+
+int wv_nonlinear_flux_device(wv_handle* handle, double t, double t0,
+                             const double* Ap, const double* Am, const double* A0,
+                             double* Fp, double* Fm, double* F0, void* stream);
+int wv_evaluate_rhs_device(wv_handle* handle, double t, double t0,
+                           const double* Ap, const double* Am, const double* A0,
+                           double* Fp, double* Fm, double* F0, void* stream);
+int wv_forward_device(wv_handle* handle, const double* fields, double t, double t0,
+                      double* Ap, double* Am, double* A0, void* stream);
+int wv_inverse_device(wv_handle* handle, double t, double t0,
+                      const double* Ap, const double* Am, const double* A0, double* fields, void* stream);
+/* Runs n_steps RK4 steps on device-resident state; the time is kept on the host
+ * (t in/out) exactly as WVFixedStepRK4 advances it (t <- t + dt per step). */
+int wv_rk4_steps_device(wv_handle* handle, double* Ap, double* Am, double* A0,
+                        double* t, double t0, double dt, int n_steps, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WVGPU_H */

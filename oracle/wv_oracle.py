@@ -793,3 +793,68 @@ def cfl_time_step(desc, Ap, Am, A0, t0=0.0, cfl=0.5):
     omax = float(np.max(np.abs(desc.arrays["omega"][:, 1:]))) if c.Nj > 1 else 0.0
     oscillatory = cfl * 2.0 * PI / omax if omax > 0 else float("inf")
     return min(advective, oscillatory)
+
+
+# ---------------------------------------------------------------------------
+# Second summation order for the vertical transforms (noise-floor estimate).
+# Exact dense DCT-I / DST-I matrices with integer argument reduction.  Two
+# valid FP64 evaluations of the same flux differ by the computation's own
+# rounding noise; tests use that difference as the floor of attainable parity.
+
+import contextlib
+
+
+def _cospi(a, b):
+    r = np.mod(a, 2 * b)
+    return np.cos(PI * r / b)
+
+
+def _sinpi(a, b):
+    r = np.mod(a, 2 * b)
+    out = np.sin(PI * r / b)
+    out[(r == 0) | (r == b)] = 0.0
+    return out
+
+
+def _dct1_dense(x, axis):
+    x = np.moveaxis(x, axis, -1)
+    n = x.shape[-1]
+    k = np.arange(n)
+    C = 2.0 * _cospi(np.outer(k, k), n - 1)
+    C[:, 0] = 1.0
+    C[:, -1] = (-1.0) ** k
+    return np.moveaxis(x @ C.T, -1, axis)
+
+
+def _dst1_dense(x, axis):
+    x = np.moveaxis(x, axis, -1)
+    n = x.shape[-1]
+    k = np.arange(1, n + 1)
+    S = 2.0 * _sinpi(np.outer(k, k), n + 1)
+    return np.moveaxis(x @ S.T, -1, axis)
+
+
+@contextlib.contextmanager
+def dense_vertical():
+    """Evaluate the vertical transforms as exact dense matrix products instead
+    of FFT-based DCT-I/DST-I (same mathematics, different rounding)."""
+    global _dct1, _dst1
+    saved = (_dct1, _dst1)
+    _dct1, _dst1 = _dct1_dense, _dst1_dense
+    try:
+        yield
+    finally:
+        _dct1, _dst1 = saved
+
+
+def noise_floor(fn, *args, **kwargs):
+    """(result, floor): result of fn with FFT-based vertical transforms and the
+    per-output relative difference (max|diff|/max|ref|) to the dense ordering."""
+    ref = fn(*args, **kwargs)
+    with dense_vertical():
+        alt = fn(*args, **kwargs)
+    floors = []
+    for a, b in zip(alt, ref):
+        den = float(np.max(np.abs(b)))
+        floors.append(float(np.max(np.abs(a - b))) / den if den > 0 else 0.0)
+    return ref, floors

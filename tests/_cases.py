@@ -37,3 +37,10 @@ def rel_err(a, b):
     den = float(np.max(np.abs(b))) if b.size else 0.0
     num = float(np.max(np.abs(a - b))) if b.size else 0.0
     return num / den if den > 0 else num
+
+
+def parity_tolerance(floor):
+    """Parity gate for states where the FP64 noise floor of the computation
+    (two valid orderings of the oracle) exceeds the reference's 1e-12 gate:
+    within 3x that measured floor, never looser than needed."""
+    return max(FP64_REL_TOL, 3.0 * floor)

@@ -1,0 +1,719 @@
+// C ABI of the GB300 constant-stratification spectral step (include/wvgpu.h).
+//
+// A handle owns: the FP64 descriptor and layout plan (built on the host,
+// uploaded once), the device scratch arena of the flux pipeline, device
+// mirrors for the host-pointer entry points and the RK4 workspace.  Caller
+// buffers are never retained.  Calls on one handle are not reentrant
+// (ExecutionGuard, CompiledKernel/src/WVTransformConstantStratificationKernel.cpp:76-84).
+#include "wvgpu.h"
+#include "wv_descriptor.hpp"
+#include "wv_kernels.cuh"
+#include "wv_plan.hpp"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using wvgpu::Descriptor;
+using wvgpu::Plan;
+using wvgpu::Status;
+namespace dev = wvgpu::dev;
+
+struct wv_handle {
+    Descriptor desc;
+    Plan plan;
+    int precision = WV_PRECISION_FP64;
+    uint32_t forcing = WV_FORCING_NONLINEAR_ADVECTION;
+    std::string message;
+    std::atomic<bool> busy{false};
+    wv_metrics metrics{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocations;
+    size_t deviceBytes = 0;
+    dev::DescDev dd{};
+    // pipeline scratch (typed by precision)
+    void* zspec = nullptr;
+    void* yspec = nullptr;
+    void* pspec = nullptr;
+    void* fspec = nullptr;
+    unsigned long long* maxSpeed = nullptr;
+    // host-entry mirrors and RK4 workspace, [3][M] complex each
+    double* state = nullptr;
+    double* flux = nullptr;
+    double* stage = nullptr;
+    double* kbuf = nullptr;
+    double* acc = nullptr;
+    double* fields = nullptr;  // [4][R] doubles
+    bool hasDamping = false;
+    bool instrument = false;
+    cudaEvent_t ev[6] = {};
+    wv_stage_times stages{};
+};
+
+namespace {
+
+struct Guard {
+    std::atomic<bool>& flag;
+    bool entered;
+    explicit Guard(std::atomic<bool>& f) : flag(f), entered(!f.exchange(true)) {}
+    ~Guard() { if (entered) flag.store(false); }
+};
+
+int fail(wv_handle* h, int code, const std::string& message) {
+    if (h) h->message = message;
+    return code;
+}
+
+int cuda_fail(wv_handle* h, cudaError_t e, const char* where) {
+    const int code = e == cudaErrorMemoryAllocation ? WV_ALLOCATION_FAILURE : WV_FFT_EXECUTION_FAILURE;
+    return fail(h, code, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename V>
+cudaError_t upload(wv_handle* h, const std::vector<V>& host, const V** out) {
+    void* p = nullptr;
+    const size_t bytes = std::max<size_t>(host.size() * sizeof(V), 16);
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return e;
+    h->allocations.push_back(p);
+    h->deviceBytes += bytes;
+    if (!host.empty()) e = cudaMemcpy(p, host.data(), host.size() * sizeof(V), cudaMemcpyHostToDevice);
+    *out = static_cast<const V*>(p);
+    return e;
+}
+
+cudaError_t alloc(wv_handle* h, size_t bytes, void** out) {
+    void* p = nullptr;
+    bytes = std::max<size_t>(bytes, 16);
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return e;
+    h->allocations.push_back(p);
+    h->deviceBytes += bytes;
+    *out = p;
+    return cudaMemset(p, 0, bytes);
+}
+
+std::vector<double> interleave(const std::vector<wvgpu::cdouble>& v) {
+    std::vector<double> out(2 * v.size());
+    for (size_t i = 0; i < v.size(); ++i) { out[2 * i] = v[i].real(); out[2 * i + 1] = v[i].imag(); }
+    return out;
+}
+
+template <typename T>
+std::vector<T> cast(const std::vector<double>& v) { return std::vector<T>(v.begin(), v.end()); }
+
+size_t elem_size(int precision) { return precision == WV_PRECISION_FP64 ? sizeof(double) : sizeof(float); }
+
+// Scratch element counts (complex) of the flux pipeline.
+struct ScratchSizes { size_t z, y, p, f; };
+ScratchSizes scratch_sizes(const Plan& p) {
+    const size_t nt = p.targets.count;
+    ScratchSizes s;
+    s.z = (4 + nt) * p.Nz * p.positions;
+    s.y = p.Nz * (4 + 2 * nt) * p.Ny * p.kxColumns;
+    s.p = p.Nz * 4 * p.Ny * p.kxColumns;
+    s.f = 4 * p.Nz * p.positions;
+    return s;
+}
+
+bool overlaps(const void* a, size_t an, const void* b, size_t bn) {
+    if (!a || !b || !an || !bn) return false;
+    const auto x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return x < y + bn && y < x + an;
+}
+
+// ---- kernel launch helpers --------------------------------------------------------
+
+template <typename T>
+size_t smem_vinv(const Plan& p) { return 4 * p.Nj * dev::kVinvModes * sizeof(dev::cx<T>); }
+template <typename T>
+size_t smem_y(const Plan& p) { return (p.Ny + 2 * dev::kYG * p.Ny) * sizeof(dev::cx<T>); }
+inline size_t x_len(const Plan& p) { return p.Nx % 2 == 0 ? p.Nx / 2 : p.Nx; }
+template <typename T>
+size_t smem_xflux(const Plan& p) {
+    const size_t nt = p.targets.count, L = x_len(p);
+    return (L + p.Nx + (4 + 2 * nt) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (3 + 3 * nt) * p.Nx * sizeof(T);
+}
+template <typename T>
+size_t smem_xc2r(const Plan& p, int nch) { return (x_len(p) + p.Nx + nch * p.kxColumns + 8 * x_len(p)) * sizeof(dev::cx<T>); }
+template <typename T>
+size_t smem_xr2c(const Plan& p) { return (x_len(p) + p.Nx + 8 * x_len(p)) * sizeof(dev::cx<T>) + 4 * p.Nx * sizeof(T); }
+template <typename T>
+size_t smem_vfwd(const Plan& p, int nch) { return nch * p.zHalf * dev::kVfwdModes * sizeof(dev::cx2t<T>); }
+
+template <typename T>
+cudaError_t set_smem_limits(const Plan& p) {
+    cudaError_t e;
+#define WV_SET(kernel, bytes)                                                                                   \
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)); \
+    if (e != cudaSuccess) return e;
+    WV_SET((dev::k_vinv<T, true>), smem_vinv<T>(p));
+    WV_SET((dev::k_vinv<T, false>), smem_vinv<T>(p));
+    WV_SET((dev::k_yinv<T>), smem_y<T>(p));
+    WV_SET((dev::k_yfwd<T>), smem_y<T>(p));
+    WV_SET((dev::k_xflux<T>), smem_xflux<T>(p));
+    WV_SET((dev::k_xc2r_fields<T>), smem_xc2r<T>(p, 4));
+    WV_SET((dev::k_xr2c_fields<T>), smem_xr2c<T>(p));
+    WV_SET((dev::k_vfwd<T, true>), smem_vfwd<T>(p, 4));
+    WV_SET((dev::k_vfwd<T, false>), smem_vfwd<T>(p, 4));
+#undef WV_SET
+    return cudaSuccess;
+}
+
+inline unsigned cdiv(size_t a, size_t b) { return static_cast<unsigned>((a + b - 1) / b); }
+
+// One nonlinear flux (+ adaptive damping when requested) on device buffers.
+template <typename T>
+cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                        double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    const double elapsed = t - t0;
+    auto* z = static_cast<dev::cx<T>*>(h->zspec);
+    auto* y = static_cast<dev::cx<T>*>(h->yspec);
+    auto* ps = static_cast<dev::cx<T>*>(h->pspec);
+    auto* f = static_cast<dev::cx<T>*>(h->fspec);
+    const int nt = p.targets.count;
+    const bool inst = h->instrument;
+    if (inst) cudaEventRecord(h->ev[0], s);
+    dev::k_vinv<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, h->maxSpeed);
+    if (inst) cudaEventRecord(h->ev[1], s);
+    dev::YInvMap map{};
+    map.nOut = 4 + 2 * nt;
+    for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
+    for (int t2 = 0; t2 < nt; ++t2) {
+        map.src[4 + t2] = p.targets.q[t2]; map.mulL[4 + t2] = 1;            // q_y = i l q
+        map.src[4 + nt + t2] = 4 + t2;     map.mulL[4 + nt + t2] = 0;        // q_z
+    }
+    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(d, map, z, 4 + nt, y);
+    if (inst) cudaEventRecord(h->ev[2], s);
+    dev::k_xflux<T><<<dim3(p.Ny, p.Nz), 256, smem_xflux<T>(p), s>>>(d, y, ps, h->maxSpeed);
+    if (inst) cudaEventRecord(h->ev[3], s);
+    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nt), 256, smem_y<T>(p), s>>>(d, ps, nt, f);
+    if (inst) cudaEventRecord(h->ev[4], s);
+    dev::k_vfwd<T, true><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nt), s>>>(
+        d, f, nt, elapsed, Ap, Am, A0, h->maxSpeed, damping ? 1 : 0, Fp, Fm, F0);
+    h->metrics.kernel_launches += 5;
+    cudaError_t e = cudaGetLastError();
+    if (inst && e == cudaSuccess) {
+        cudaEventRecord(h->ev[5], s);
+        e = cudaEventSynchronize(h->ev[5]);
+        float ms[5] = {};
+        for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]);
+        h->stages.vertical_inverse_ms += ms[0];
+        h->stages.y_inverse_ms += ms[1];
+        h->stages.x_products_ms += ms[2];
+        h->stages.y_forward_ms += ms[3];
+        h->stages.vertical_forward_ms += ms[4];
+        h->stages.fluxes += 1;
+    }
+    return e;
+}
+
+template <typename T>
+cudaError_t launch_inverse(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                           double* fields, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    auto* z = static_cast<dev::cx<T>*>(h->zspec);
+    auto* y = static_cast<dev::cx<T>*>(h->yspec);
+    dev::k_vinv<T, false><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, t - t0, z, nullptr);
+    dev::YInvMap map{};
+    map.nOut = 4;
+    for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
+    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(d, map, z, 4, y);
+    dev::k_xc2r_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xc2r<T>(p, 4), s>>>(d, y, 4, fields);
+    h->metrics.kernel_launches += 3;
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_forward(wv_handle* h, const double* fields, double t, double t0, double* Ap, double* Am, double* A0,
+                           cudaStream_t s) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    const int nch = h->desc.c.is_hydrostatic ? 3 : 4;
+    auto* ps = static_cast<dev::cx<T>*>(h->pspec);
+    auto* f = static_cast<dev::cx<T>*>(h->fspec);
+    dev::k_xr2c_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xr2c<T>(p), s>>>(d, fields, nch, ps);
+    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nch), 256, smem_y<T>(p), s>>>(d, ps, nch, f);
+    dev::k_vfwd<T, false><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nch), s>>>(
+        d, f, nch, t - t0, nullptr, nullptr, nullptr, nullptr, 0, Ap, Am, A0);
+    h->metrics.kernel_launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t flux_any(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
+                     double* Fm, double* F0, bool damping, cudaStream_t s) {
+    return h->precision == WV_PRECISION_FP64 ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s)
+                                             : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s);
+}
+
+// Scheduled RHS on contiguous [3][M] complex state/flux buffers.
+cudaError_t rhs_contiguous(wv_handle* h, double t, double t0, const double* y, double* k, cudaStream_t s) {
+    const size_t M2 = 2 * h->plan.M;
+    const bool damping = (h->forcing & WV_FORCING_ADAPTIVE_DAMPING) != 0;
+    if (!(h->forcing & WV_FORCING_NONLINEAR_ADVECTION)) {
+        // damping only is not a configuration the reference's default schedules produce
+        return cudaErrorNotSupported;
+    }
+    return flux_any(h, t, t0, y, y + M2, y + 2 * M2, k, k + M2, k + 2 * M2, damping, s);
+}
+
+// WVFixedStepRK4::step (PortableRuntime/src/WVRungeKutta.cpp:335-462) on the
+// contiguous device state h->state.
+cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t s) {
+    const size_t n = 6 * h->plan.M;
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
+    cudaError_t e;
+    e = rhs_contiguous(h, t, t0, h->state, h->kbuf, s); if (e != cudaSuccess) return e;
+    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, h->state, 0.5 * dt, h->stage, 1, n);
+    e = rhs_contiguous(h, t + 0.5 * dt, t0, h->stage, h->kbuf, s); if (e != cudaSuccess) return e;
+    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, h->state, 0.5 * dt, h->stage, 0, n);
+    e = rhs_contiguous(h, t + 0.5 * dt, t0, h->stage, h->kbuf, s); if (e != cudaSuccess) return e;
+    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, h->state, dt, h->stage, 0, n);
+    e = rhs_contiguous(h, t + dt, t0, h->stage, h->kbuf, s); if (e != cudaSuccess) return e;
+    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, nullptr, 0.0, nullptr, 0, n);
+    dev::k_affine<<<grid, 256, 0, s>>>(h->state, h->acc, dt / 6.0, h->state, n);
+    h->metrics.kernel_launches += 5;
+    h->metrics.rk4_steps += 1;
+    h->metrics.rhs_evaluations += 4;
+    return cudaGetLastError();
+}
+
+int check_times(wv_handle* h, double t, double t0) {
+    if (!std::isfinite(t) || !std::isfinite(t0)) return fail(h, WV_INVALID_CONFIGURATION, "State times must be finite.");
+    return WV_SUCCESS;
+}
+
+int check_state_flux(wv_handle* h, const double* Ap, const double* Am, const double* A0, double* Fp, double* Fm, double* F0) {
+    const char* names[] = {"Ap", "Am", "A0", "Fp", "Fm", "F0"};
+    const void* ptrs[] = {Ap, Am, A0, Fp, Fm, F0};
+    for (int i = 0; i < 6; ++i)
+        if (!ptrs[i]) return fail(h, WV_INVALID_POINTER, std::string(names[i]) + " has a null data pointer.");
+    const size_t bytes = h->plan.M * 16;
+    const void* outs[] = {Fp, Fm, F0};
+    const void* ins[] = {Ap, Am, A0};
+    for (int i = 0; i < 3; ++i) {
+        for (int j = i + 1; j < 3; ++j)
+            if (overlaps(outs[i], bytes, outs[j], bytes)) return fail(h, WV_OVERLAPPING_ARRAYS, "Flux outputs must not overlap.");
+        for (const void* in : ins)
+            if (overlaps(outs[i], bytes, in, bytes)) return fail(h, WV_OVERLAPPING_ARRAYS, "Flux outputs must not overlap state inputs.");
+    }
+    return WV_SUCCESS;
+}
+
+int finish(wv_handle* h, cudaError_t e, const char* where) {
+    if (e != cudaSuccess) return cuda_fail(h, e, where);
+    return WV_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wv_describe(const wv_config* config, wv_sizes* sizes, char* message, size_t cap) {
+    auto msg = [&](const std::string& m) {
+        if (message && cap) { std::strncpy(message, m.c_str(), cap - 1); message[cap - 1] = 0; }
+    };
+    if (!config) { msg("Configuration pointer is null."); return WV_INVALID_POINTER; }
+    Descriptor d;
+    Status st = wvgpu::build_descriptor(*config, d);
+    if (!st) { msg(st.message); return st.code; }
+    Plan p;
+    st = wvgpu::build_plan(d, p);
+    if (!st) { msg(st.message); return st.code; }
+    if (sizes) {
+        sizes->Nx = p.Nx; sizes->Ny = p.Ny; sizes->Nz = p.Nz; sizes->Nj = p.Nj; sizes->Nkl = p.Nkl; sizes->NxHalf = p.NxHalf;
+        sizes->M = p.M; sizes->active_rows = p.positions; sizes->kx_columns = p.kxColumns;
+        const auto s = scratch_sizes(p);
+        const size_t R = p.Nx * p.Ny * p.Nz;
+        sizes->device_bytes = (s.z + s.y + s.p + s.f) * 16 + 5 * 6 * p.M * sizeof(double) + 4 * R * sizeof(double) +
+                              20 * p.M * sizeof(double);
+    }
+    msg("");
+    return WV_SUCCESS;
+}
+
+int wv_describe_modes(const wv_config* config, int64_t* kMode, int64_t* lMode, double* omega, uint64_t* rows, uint8_t* conj) {
+    if (!config) return WV_INVALID_POINTER;
+    Descriptor d;
+    Status st = wvgpu::build_descriptor(*config, d);
+    if (!st) return st.code;
+    if (kMode) std::memcpy(kMode, d.kMode.data(), d.Nkl * sizeof(int64_t));
+    if (lMode) std::memcpy(lMode, d.lMode.data(), d.Nkl * sizeof(int64_t));
+    if (omega) std::memcpy(omega, d.omega.data(), d.M * sizeof(double));
+    if (rows) std::memcpy(rows, d.storageRow.data(), d.Nkl * sizeof(uint64_t));
+    if (conj) std::memcpy(conj, d.conjugated.data(), d.Nkl);
+    return WV_SUCCESS;
+}
+
+void wv_destroy(wv_handle* h) {
+    if (!h) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(h->device);
+    if (h->stream) { cudaStreamSynchronize(h->stream); cudaStreamDestroy(h->stream); }
+    for (auto& ev : h->ev) if (ev) cudaEventDestroy(ev);
+    for (void* p : h->allocations) cudaFree(p);
+    cudaSetDevice(prev);
+    delete h;
+}
+
+int wv_create(const wv_config* config, int precision, wv_handle** out) {
+    if (!out) return WV_INVALID_POINTER;
+    *out = nullptr;
+    if (!config) return WV_INVALID_POINTER;
+    if (precision != WV_PRECISION_FP64 && precision != WV_PRECISION_MIXED) return WV_INVALID_CONFIGURATION;
+    wv_handle* h = new (std::nothrow) wv_handle();
+    if (!h) return WV_ALLOCATION_FAILURE;
+    h->precision = precision;
+    Status st = wvgpu::build_descriptor(*config, h->desc);
+    if (st) st = wvgpu::build_plan(h->desc, h->plan);
+    if (!st) { const int code = st.code; delete h; return code; }
+    const Descriptor& d = h->desc;
+    const Plan& p = h->plan;
+    cudaGetDevice(&h->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    std::vector<double> damping;
+    if (e == cudaSuccess) {
+        Status ds = wvgpu::adaptive_damping_operator(d, damping);
+        h->hasDamping = static_cast<bool>(ds);
+        if (!ds) damping.assign(d.M, 0.0);
+    }
+    auto& dd = h->dd;
+    dd.Nx = p.Nx; dd.Ny = p.Ny; dd.Nz = p.Nz; dd.Nj = p.Nj; dd.Nkl = p.Nkl; dd.NxHalf = p.NxHalf; dd.M = p.M;
+    dd.positions = p.positions; dd.kxColumns = p.kxColumns; dd.zHalf = p.zHalf;
+    dd.nt = p.targets.count;
+    for (int i = 0; i < 4; ++i) dd.tq[i] = p.targets.q[i];
+    dd.hydrostatic = d.c.is_hydrostatic ? 1 : 0;
+    dd.xEven = p.Nx % 2 == 0 ? 1 : 0;
+    dd.xLen = static_cast<int>(x_len(p));
+    dd.fx.N = p.fx.N; dd.fx.nstages = p.fx.nstages; dd.fy.N = p.fy.N; dd.fy.nstages = p.fy.nstages;
+    for (int i = 0; i < dev::kMaxStages; ++i) { dd.fx.radix[i] = p.fx.radix[i]; dd.fy.radix[i] = p.fy.radix[i]; }
+    std::vector<int32_t> posKy(p.posKy), colStart(p.colStart), modeWV(p.modeWV), modePos(p.modePos), modeComp(p.modeCompPos);
+    std::vector<double> inertial(d.inertialScale), apmw(d.apmWProjectionPrefactor);
+#define WV_UP(vec, field)                                            \
+    if (e == cudaSuccess) {                                          \
+        e = upload(h, vec, &dd.field);                               \
+    }
+    WV_UP(d.omega, omega);
+    std::vector<double> UAp = interleave(d.UAp), VAp = interleave(d.VAp), WAp = interleave(d.WAp), UA0 = interleave(d.UA0),
+                        VA0 = interleave(d.VA0), ApmD = interleave(d.ApmD);
+    WV_UP(UAp, UAp); WV_UP(VAp, VAp); WV_UP(WAp, WAp); WV_UP(d.NAp, NAp); WV_UP(UA0, UA0); WV_UP(VA0, VA0); WV_UP(d.NA0, NA0);
+    WV_UP(d.A0FromVorticity, A0FromVorticity); WV_UP(d.A0FromBuoyancy, A0FromBuoyancy); WV_UP(d.ApmN, ApmN);
+    WV_UP(d.ApmDScaled, ApmDScaled); WV_UP(ApmD, ApmD); WV_UP(damping, damping);
+    WV_UP(d.k, k); WV_UP(d.l, l); WV_UP(d.Kh, Kh); WV_UP(d.cosAlpha, cosAlpha); WV_UP(d.sinAlpha, sinAlpha);
+    WV_UP(inertial, inertialScale); WV_UP(apmw, apmWPrefactor);
+    WV_UP(posKy, posKy); WV_UP(colStart, colStart); WV_UP(modeWV, modeWV); WV_UP(modePos, modePos); WV_UP(modeComp, modeCompPos);
+    WV_UP(p.modeFlags, modeFlags);
+    WV_UP(p.rowK, rowK); WV_UP(p.rowL, rowL);
+#undef WV_UP
+    auto upT = [&](const std::vector<double>& v, const void** dst) {
+        if (e != cudaSuccess) return;
+        if (precision == WV_PRECISION_FP64) {
+            const double* q = nullptr; e = upload(h, v, &q); *dst = q;
+        } else {
+            const std::vector<float> f = cast<float>(v);
+            const float* q = nullptr; e = upload(h, f, &q); *dst = q;
+        }
+    };
+    upT(p.Ccos, &dd.Ccos); upT(p.Csin, &dd.Csin); upT(p.CcosM, &dd.CcosM); upT(p.CsinM, &dd.CsinM);
+    upT(p.Fcos, &dd.Fcos); upT(p.Fsin, &dd.Fsin); upT(p.twx, &dd.twx); upT(p.twxN, &dd.twxN); upT(p.twy, &dd.twy);
+    const auto ss = scratch_sizes(p);
+    const size_t cb = 2 * elem_size(precision);
+    const size_t R = p.Nx * p.Ny * p.Nz;
+    if (e == cudaSuccess) e = alloc(h, ss.z * cb, &h->zspec);
+    if (e == cudaSuccess) e = alloc(h, ss.y * cb, &h->yspec);
+    if (e == cudaSuccess) e = alloc(h, ss.p * cb, &h->pspec);
+    if (e == cudaSuccess) e = alloc(h, ss.f * cb, &h->fspec);
+    void* tmp = nullptr;
+    if (e == cudaSuccess) { e = alloc(h, sizeof(unsigned long long), &tmp); h->maxSpeed = static_cast<unsigned long long*>(tmp); }
+    const size_t stateBytes = 6 * p.M * sizeof(double);
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->state = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->flux = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->stage = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->kbuf = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->acc = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, 4 * R * sizeof(double), &tmp); h->fields = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) e = precision == WV_PRECISION_FP64 ? set_smem_limits<double>(p) : set_smem_limits<float>(p);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        const int code = e == cudaErrorMemoryAllocation ? WV_ALLOCATION_FAILURE : WV_FFT_PLAN_FAILURE;
+        wv_destroy(h);
+        return code;
+    }
+    h->metrics.device_bytes = h->deviceBytes;
+    *out = h;
+    return WV_SUCCESS;
+}
+
+const char* wv_last_message(const wv_handle* h) { return h ? h->message.c_str() : "null handle"; }
+
+int wv_get_sizes(const wv_handle* h, wv_sizes* s) {
+    if (!h || !s) return WV_INVALID_POINTER;
+    const Plan& p = h->plan;
+    s->Nx = p.Nx; s->Ny = p.Ny; s->Nz = p.Nz; s->Nj = p.Nj; s->Nkl = p.Nkl; s->NxHalf = p.NxHalf; s->M = p.M;
+    s->active_rows = p.positions; s->kx_columns = p.kxColumns; s->device_bytes = h->deviceBytes;
+    return WV_SUCCESS;
+}
+
+int wv_get_metrics(const wv_handle* h, wv_metrics* m) {
+    if (!h || !m) return WV_INVALID_POINTER;
+    *m = h->metrics;
+    return WV_SUCCESS;
+}
+
+int wv_set_stage_instrumentation(wv_handle* h, int enabled) {
+    if (!h) return WV_INVALID_POINTER;
+    if (enabled) {
+        cudaSetDevice(h->device);
+        for (auto& ev : h->ev) {
+            if (!ev) {
+                const cudaError_t e = cudaEventCreate(&ev);
+                if (e != cudaSuccess) return cuda_fail(h, e, "stage instrumentation");
+            }
+        }
+        h->stages = wv_stage_times{};
+    }
+    h->instrument = enabled != 0;
+    return WV_SUCCESS;
+}
+
+int wv_get_stage_times(const wv_handle* h, wv_stage_times* t) {
+    if (!h || !t) return WV_INVALID_POINTER;
+    *t = h->stages;
+    return WV_SUCCESS;
+}
+
+int wv_set_forcing(wv_handle* h, uint32_t flags) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!(flags & WV_FORCING_NONLINEAR_ADVECTION) || (flags & ~3u))
+        return fail(h, WV_UNSUPPORTED_OPERATION, "Supported schedules: nonlinear advection, optionally with adaptive damping.");
+    if ((flags & WV_FORCING_ADAPTIVE_DAMPING) && !h->hasDamping)
+        return fail(h, WV_UNSUPPORTED_OPERATION, "Adaptive damping requires nonzero Coriolis frequency.");
+    h->forcing = flags;
+    return WV_SUCCESS;
+}
+
+// ---- device-pointer entries --------------------------------------------------------
+
+int wv_nonlinear_flux_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                             double* Fp, double* Fm, double* F0, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const cudaError_t e = flux_any(h, t, t0, Ap, Am, A0, Fp, Fm, F0, false, static_cast<cudaStream_t>(stream));
+    h->metrics.nonlinear_flux_calls++;
+    return finish(h, e, "nonlinear flux");
+}
+
+int wv_evaluate_rhs_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                           double* Fp, double* Fm, double* F0, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const bool damping = (h->forcing & WV_FORCING_ADAPTIVE_DAMPING) != 0;
+    const cudaError_t e = flux_any(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, static_cast<cudaStream_t>(stream));
+    h->metrics.rhs_evaluations++;
+    return finish(h, e, "right-hand side");
+}
+
+int wv_inverse_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* fields,
+                      void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Inverse transform received a null pointer.");
+    const size_t fb = 4 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
+    for (const void* in : {static_cast<const void*>(Ap), static_cast<const void*>(Am), static_cast<const void*>(A0)})
+        if (overlaps(fields, fb, in, cb)) return fail(h, WV_OVERLAPPING_ARRAYS, "Inverse spatial output must not overlap coefficient inputs.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64
+                              ? launch_inverse<double>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream))
+                              : launch_inverse<float>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream));
+    h->metrics.inverse_calls++;
+    return finish(h, e, "inverse transform");
+}
+
+int wv_forward_device(wv_handle* h, const double* fields, double t, double t0, double* Ap, double* Am, double* A0, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Forward transform received a null pointer.");
+    const int nch = h->desc.c.is_hydrostatic ? 3 : 4;
+    const size_t fb = nch * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
+    const void* outs[] = {Ap, Am, A0};
+    for (int i = 0; i < 3; ++i) {
+        if (overlaps(outs[i], cb, fields, fb)) return fail(h, WV_OVERLAPPING_ARRAYS, "Forward coefficient outputs must not overlap the spatial input.");
+        for (int j = i + 1; j < 3; ++j)
+            if (overlaps(outs[i], cb, outs[j], cb)) return fail(h, WV_OVERLAPPING_ARRAYS, "Forward coefficient outputs must not overlap each other.");
+    }
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64
+                              ? launch_forward<double>(h, fields, t, t0, Ap, Am, A0, static_cast<cudaStream_t>(stream))
+                              : launch_forward<float>(h, fields, t, t0, Ap, Am, A0, static_cast<cudaStream_t>(stream));
+    h->metrics.forward_calls++;
+    return finish(h, e, "forward transform");
+}
+
+int wv_rk4_steps_device(wv_handle* h, double* Ap, double* Am, double* A0, double* t, double t0, double dt, int n, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!Ap || !Am || !A0 || !t) return fail(h, WV_INVALID_POINTER, "RK4 received a null pointer.");
+    int rc = check_times(h, *t, t0); if (rc) return rc;
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
+    if (n < 0) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step count must be nonnegative.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "RK4 stepping is not reentrant.");
+    cudaSetDevice(h->device);
+    auto s = static_cast<cudaStream_t>(stream);
+    const size_t cb = h->plan.M * 16;
+    cudaError_t e = cudaSuccess;
+    const double* src[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, src[c], cb, cudaMemcpyDeviceToDevice, s);
+    double tt = *t;
+    for (int i = 0; i < n && e == cudaSuccess; ++i) {
+        e = rk4_step(h, tt, t0, dt, s);
+        tt = tt + dt;
+    }
+    double* dst[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(dst[c], reinterpret_cast<char*>(h->state) + c * cb, cb, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "RK4");
+    *t = tt;
+    return WV_SUCCESS;
+}
+
+// ---- host-pointer entries ------------------------------------------------------------
+
+static int host_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
+                     double* Fm, double* F0, bool scheduled) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16;
+    auto s = h->stream;
+    cudaError_t e = cudaSuccess;
+    const double* in[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, in[c], cb, cudaMemcpyHostToDevice, s);
+    const size_t M2 = 2 * h->plan.M;
+    const bool damping = scheduled && (h->forcing & WV_FORCING_ADAPTIVE_DAMPING);
+    if (e == cudaSuccess)
+        e = flux_any(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->flux, h->flux + M2, h->flux + 2 * M2, damping, s);
+    double* out[] = {Fp, Fm, F0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(out[c], reinterpret_cast<char*>(h->flux) + c * cb, cb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (scheduled) h->metrics.rhs_evaluations++; else h->metrics.nonlinear_flux_calls++;
+    return finish(h, e, scheduled ? "right-hand side" : "nonlinear flux");
+}
+
+int wv_nonlinear_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
+                      double* Fm, double* F0) {
+    return host_flux(h, t, t0, Ap, Am, A0, Fp, Fm, F0, false);
+}
+
+int wv_evaluate_rhs(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
+                    double* Fm, double* F0) {
+    return host_flux(h, t, t0, Ap, Am, A0, Fp, Fm, F0, true);
+}
+
+int wv_inverse(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* fields) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Inverse transform received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16, M2 = 2 * h->plan.M;
+    const size_t fb = 4 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double);
+    auto s = h->stream;
+    cudaError_t e = cudaSuccess;
+    const double* in[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, in[c], cb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64
+                ? launch_inverse<double>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s)
+                : launch_inverse<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fields, h->fields, fb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    h->metrics.inverse_calls++;
+    return finish(h, e, "inverse transform");
+}
+
+int wv_forward(wv_handle* h, const double* fields, double t, double t0, double* Ap, double* Am, double* A0) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Forward transform received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const int nch = h->desc.c.is_hydrostatic ? 3 : 4;
+    const size_t cb = h->plan.M * 16, M2 = 2 * h->plan.M;
+    const size_t fb = nch * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double);
+    auto s = h->stream;
+    cudaError_t e = cudaMemcpyAsync(h->fields, fields, fb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64
+                ? launch_forward<double>(h, h->fields, t, t0, h->flux, h->flux + M2, h->flux + 2 * M2, s)
+                : launch_forward<float>(h, h->fields, t, t0, h->flux, h->flux + M2, h->flux + 2 * M2, s);
+    double* out[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(out[c], reinterpret_cast<char*>(h->flux) + c * cb, cb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    h->metrics.forward_calls++;
+    return finish(h, e, "forward transform");
+}
+
+int wv_rk4_steps(wv_handle* h, double* Ap, double* Am, double* A0, double* t, double t0, double dt, int n) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!Ap || !Am || !A0 || !t) return fail(h, WV_INVALID_POINTER, "RK4 received a null pointer.");
+    int rc = check_times(h, *t, t0); if (rc) return rc;
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
+    if (n < 0) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step count must be nonnegative.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "RK4 stepping is not reentrant.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16;
+    auto s = h->stream;
+    cudaError_t e = cudaSuccess;
+    const double* in[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, in[c], cb, cudaMemcpyHostToDevice, s);
+    double tt = *t;
+    for (int i = 0; i < n && e == cudaSuccess; ++i) {
+        e = rk4_step(h, tt, t0, dt, s);
+        tt = tt + dt;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // A failed step leaves the caller's state untouched (TestWVForcingAndRK4.cpp:316-319).
+    double* out[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(out[c], reinterpret_cast<char*>(h->state) + c * cb, cb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "RK4");
+    *t = tt;
+    return WV_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,831 @@
+// CUDA kernels of the constant-stratification spectral step (sm_103a).
+//
+// Pipeline of one nonlinear flux (nonlinearFluxImpl, kernel.cpp:1173-1244),
+// restructured for the GPU:
+//   vinv   : per retained (k,l) column: phase, evolved coefficients, field
+//            spectra (coefficientValueForField), then the vertical inverse
+//            DCT-I/DST-I as a folded dense contraction -> zspec[ch][z][pos]
+//   yinv   : per (z, kx): inverse FFT along y of each channel (and of i*l*q)
+//            -> yspec[z][ch][y][kx]
+//   xflux  : per (z, y) row: c2r along x of U,V,W and every derivative,
+//            quadratic products S_q = -(u q_x + v q_y + w q_z), max |u_h|,
+//            r2c of S_q along x -> pspec[z][q][y][kx]
+//   yfwd   : per (z, kx): forward FFT along y, gathered to active rows -> fspec
+//   vfwd   : per column: forward DCT-I/DST-I contraction, projection onto
+//            Ap/Am/A0 (projectFluxTargetMode, kernel.cpp:396-431), phase,
+//            adaptive damping, written as Fp/Fm/F0.
+// T is the working type of the xy stage (double for FP64 handles, float for
+// MIXED); phases, projections and accumulations are always double.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace wvgpu {
+namespace dev {
+
+template <typename T> struct cxt;
+template <> struct cxt<double> { using type = double2; };
+template <> struct cxt<float> { using type = float2; };
+template <typename T> using cx = typename cxt<T>::type;
+
+template <typename T> __device__ __forceinline__ cx<T> mk(T a, T b) { cx<T> r; r.x = a; r.y = b; return r; }
+template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) { return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+template <typename T> __device__ __forceinline__ cx<T> cconj(cx<T> a) { return mk<T>(a.x, -a.y); }
+template <typename T> __device__ __forceinline__ cx<T> cscale(cx<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+// multiply by +i (INV) or -i (forward) : used by radix-4 butterflies
+template <bool INV, typename T> __device__ __forceinline__ cx<T> mul_mi(cx<T> a) { return INV ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x); }
+
+// Exact complex arithmetic of the reference (no contraction), double only.
+struct zd { double re, im; };
+__device__ __forceinline__ zd zmul(zd a, zd b) {
+    return {__dsub_rn(__dmul_rn(a.re, b.re), __dmul_rn(a.im, b.im)), __dadd_rn(__dmul_rn(a.re, b.im), __dmul_rn(a.im, b.re))};
+}
+__device__ __forceinline__ zd zadd(zd a, zd b) { return {__dadd_rn(a.re, b.re), __dadd_rn(a.im, b.im)}; }
+__device__ __forceinline__ zd zsub(zd a, zd b) { return {__dsub_rn(a.re, b.re), __dsub_rn(a.im, b.im)}; }
+__device__ __forceinline__ zd zscale(zd a, double s) { return {__dmul_rn(a.re, s), __dmul_rn(a.im, s)}; }
+__device__ __forceinline__ zd zconj(zd a) { return {a.re, -a.im}; }
+__device__ __forceinline__ zd zload(const double* p) { const double2 v = *reinterpret_cast<const double2*>(p); return {v.x, v.y}; }
+__device__ __forceinline__ void zstore(double* p, zd v) { *reinterpret_cast<double2*>(p) = make_double2(v.re, v.im); }
+
+constexpr int kMaxStages = 24;
+
+struct FFTDev {
+    int N;
+    int nstages;
+    int radix[kMaxStages];
+};
+
+// ---------------------------------------------------------------------------
+// Shared-memory Stockham FFT over `lines` lines of length N (leading dim ld).
+// Forward uses exp(-2 pi i k/N), inverse the conjugate; both unnormalized.
+
+template <typename T, bool INV>
+__device__ __forceinline__ cx<T> twid(const cx<T>* tw, int idx) {
+    cx<T> w = tw[idx];
+    return INV ? cconj<T>(w) : w;
+}
+
+template <typename T, bool INV>
+__device__ void fft_stage(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst, int N, int R, int Ns, int lines, int ld,
+                          const cx<T>* __restrict__ tw) {
+    const int nb = N / R;
+    const int tstride = N / (Ns * R);
+    if (R == 4) {
+        for (int it = threadIdx.x; it < lines * nb; it += blockDim.x) {
+            const int line = it / nb, j = it - line * nb;
+            const cx<T>* in = src + line * ld;
+            cx<T>* out = dst + line * ld;
+            const int k = j % Ns;
+            const int ts = k * tstride;
+            cx<T> v0 = in[j], v1 = in[j + nb], v2 = in[j + 2 * nb], v3 = in[j + 3 * nb];
+            if (ts) {
+                v1 = cmul<T>(v1, twid<T, INV>(tw, ts));
+                v2 = cmul<T>(v2, twid<T, INV>(tw, 2 * ts));
+                v3 = cmul<T>(v3, twid<T, INV>(tw, 3 * ts));
+            }
+            const cx<T> a = cadd<T>(v0, v2), b = csub<T>(v0, v2), c = cadd<T>(v1, v3), d = mul_mi<INV, T>(csub<T>(v1, v3));
+            const int o = (j / Ns) * Ns * 4 + k;
+            out[o] = cadd<T>(a, c);
+            out[o + Ns] = cadd<T>(b, d);
+            out[o + 2 * Ns] = csub<T>(a, c);
+            out[o + 3 * Ns] = csub<T>(b, d);
+        }
+    } else if (R == 2) {
+        for (int it = threadIdx.x; it < lines * nb; it += blockDim.x) {
+            const int line = it / nb, j = it - line * nb;
+            const cx<T>* in = src + line * ld;
+            cx<T>* out = dst + line * ld;
+            const int k = j % Ns;
+            const int ts = k * tstride;
+            cx<T> v0 = in[j], v1 = in[j + nb];
+            if (ts) v1 = cmul<T>(v1, twid<T, INV>(tw, ts));
+            const int o = (j / Ns) * Ns * 2 + k;
+            out[o] = cadd<T>(v0, v1);
+            out[o + Ns] = csub<T>(v0, v1);
+        }
+    } else if (R == 3) {
+        const T s3 = INV ? T(0.86602540378443864676) : T(-0.86602540378443864676);
+        for (int it = threadIdx.x; it < lines * nb; it += blockDim.x) {
+            const int line = it / nb, j = it - line * nb;
+            const cx<T>* in = src + line * ld;
+            cx<T>* out = dst + line * ld;
+            const int k = j % Ns;
+            const int ts = k * tstride;
+            cx<T> v0 = in[j], v1 = in[j + nb], v2 = in[j + 2 * nb];
+            if (ts) {
+                v1 = cmul<T>(v1, twid<T, INV>(tw, ts));
+                v2 = cmul<T>(v2, twid<T, INV>(tw, 2 * ts));
+            }
+            const cx<T> t1 = cadd<T>(v1, v2);
+            const cx<T> t2 = mk<T>(v0.x - T(0.5) * t1.x, v0.y - T(0.5) * t1.y);
+            const cx<T> dlt = csub<T>(v1, v2);
+            const cx<T> t3 = mk<T>(-s3 * dlt.y, s3 * dlt.x);  // i * s3 * (v1 - v2)
+            const int o = (j / Ns) * Ns * 3 + k;
+            out[o] = cadd<T>(v0, t1);
+            out[o + Ns] = cadd<T>(t2, t3);
+            out[o + 2 * Ns] = csub<T>(t2, t3);
+        }
+    } else {
+        // Generic radix: one output per work item, O(R) dot product.
+        for (int it = threadIdx.x; it < lines * N; it += blockDim.x) {
+            const int line = it / N, rem = it - line * N;
+            const int j = rem % nb, r = rem / nb;
+            const cx<T>* in = src + line * ld;
+            cx<T>* out = dst + line * ld;
+            const int k = j % Ns;
+            const int step = (k * tstride + r * nb) % N;
+            cx<T> acc = mk<T>(T(0), T(0));
+            int e = 0;
+            for (int m = 0; m < R; ++m) {
+                acc = cadd<T>(acc, cmul<T>(in[j + m * nb], twid<T, INV>(tw, e)));
+                e += step;
+                if (e >= N) e -= N;
+            }
+            out[(j / Ns) * Ns * R + k + r * Ns] = acc;
+        }
+    }
+}
+
+// Runs all stages; returns the buffer holding the result (a or b).
+template <typename T, bool INV>
+__device__ cx<T>* fft_lines(cx<T>* a, cx<T>* b, const FFTDev& f, int lines, int ld, const cx<T>* tw) {
+    int Ns = 1;
+    for (int s = 0; s < f.nstages; ++s) {
+        fft_stage<T, INV>(a, b, f.N, f.radix[s], Ns, lines, ld, tw);
+        __syncthreads();
+        Ns *= f.radix[s];
+        cx<T>* t = a; a = b; b = t;
+    }
+    return a;
+}
+
+// ---------------------------------------------------------------------------
+// Parameters shared by the kernels of one handle.
+
+struct DescDev {
+    int Nx, Ny, Nz, Nj, Nkl, NxHalf, M;
+    int positions, kxColumns, zHalf;
+    int nt;          // number of flux targets
+    int tq[4];       // target ids (0=u,1=v,2=w,3=eta)
+    int hydrostatic;
+    // descriptor arrays [M] (j fastest)
+    const double* omega;
+    const double* UAp;   // complex interleaved
+    const double* VAp;
+    const double* WAp;
+    const double* NAp;
+    const double* UA0;
+    const double* VA0;
+    const double* NA0;
+    const double* A0FromVorticity;
+    const double* A0FromBuoyancy;
+    const double* ApmN;
+    const double* ApmDScaled;
+    const double* ApmD;  // complex (hydrostatic projection)
+    const double* damping;  // [M] adaptive damping operator (or null)
+    // per WV mode [Nkl]
+    const double* k;
+    const double* l;
+    const double* Kh;
+    const double* cosAlpha;
+    const double* sinAlpha;
+    // per j [Nj]
+    const double* inertialScale;
+    const double* apmWPrefactor;
+    // plan
+    const int* posKy;       // [positions]
+    const int* colStart;    // [kxColumns+1]
+    const int* modeWV;      // [Nkl] in position order
+    const int* modePos;
+    const int* modeCompPos;
+    const unsigned char* modeFlags;
+    const double* rowK;     // [kxColumns]
+    const double* rowL;     // [Ny]
+    const void* Ccos;       // T[zHalf][Nj]
+    const void* Csin;
+    const void* CcosM;
+    const void* CsinM;
+    const void* Fcos;       // T[Nj][zHalf]
+    const void* Fsin;
+    const void* twx;        // cx<T>[xLen]: twiddles of the x line FFT (length Nx/2 for even Nx, else Nx)
+    const void* twxN;       // cx<T>[Nx]: exp(-2 pi i k/Nx) for the real-FFT split/merge
+    const void* twy;        // cx<T>[Ny]
+    int xEven;              // Nx even: real rows go through half-length complex FFTs
+    int xLen;               // Nx/2 (even) or Nx (odd)
+    FFTDev fx, fy;          // fx factors xLen
+};
+
+// ---------------------------------------------------------------------------
+// vinv: evolved field spectra + vertical inverse contraction.
+//   mode FIELDS: channels U, V, W, N (transformWaveVortexToUVWEta)
+//   mode FLUX:   channels U, V, W, N, then d/dz of each flux target.
+// Column values are in the stored frame: conjugated for kMode < 0 storage,
+// imaginary part cleared on self-conjugate rows (kernel.cpp:211-291,433-438).
+
+constexpr int kVinvModes = 8;
+
+template <typename T, bool FLUX>
+__global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restrict__ Ap, const double* __restrict__ Am,
+                                             const double* __restrict__ A0, double elapsed, cx<T>* __restrict__ zspec,
+                                             unsigned long long* __restrict__ maxSpeedBits) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // fld[f][j][mode], f = u, v, w, eta (stored frame), working precision T
+    cx<T>* fld = reinterpret_cast<cx<T>*>(smem_raw);
+    const int Nj = d.Nj;
+    const int m0 = blockIdx.x * kVinvModes;
+    const int nm = min(kVinvModes, d.Nkl - m0);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && maxSpeedBits) *maxSpeedBits = 0ull;
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it / Nj, j = it - mi * Nj;
+        const int mode = m0 + mi;
+        const int w = d.modeWV[mode];
+        const unsigned char flags = d.modeFlags[mode];
+        const int idx = j + Nj * w;
+        double s, c;
+        sincos(d.omega[idx] * elapsed, &s, &c);
+        const zd p{c, s};
+        // evolveWaveVortexCoefficients + coefficientValueForField<0..3> (WVCoefficientFormulas.hpp:23-33)
+        const zd ap = zmul(zload(Ap + 2 * idx), p);
+        const zd am = zmul(zload(Am + 2 * idx), zconj(p));
+        const zd a0 = zload(A0 + 2 * idx);
+        const zd uap = zload(d.UAp + 2 * idx), vap = zload(d.VAp + 2 * idx), wap = zload(d.WAp + 2 * idx);
+        const zd ua0 = zload(d.UA0 + 2 * idx), va0 = zload(d.VA0 + 2 * idx);
+        const double nap = d.NAp[idx], na0 = d.NA0[idx];
+        zd u = zadd(zadd(zmul(uap, ap), zmul(zconj(uap), am)), zmul(ua0, a0));
+        zd v = zadd(zadd(zmul(vap, ap), zmul(zconj(vap), am)), zmul(va0, a0));
+        zd ww = zadd(zmul(wap, ap), zmul(wap, am));
+        zd n = zadd(zadd(zscale(ap, nap), zscale(am, -nap)), zscale(a0, na0));
+        if (flags & 1) { u = zconj(u); v = zconj(v); ww = zconj(ww); n = zconj(n); }
+        if (flags & 2) { u.im = 0.0; v.im = 0.0; ww.im = 0.0; n.im = 0.0; }
+        fld[(0 * Nj + j) * kVinvModes + mi] = mk<T>(T(u.re), T(u.im));
+        fld[(1 * Nj + j) * kVinvModes + mi] = mk<T>(T(v.re), T(v.im));
+        fld[(2 * Nj + j) * kVinvModes + mi] = mk<T>(T(ww.re), T(ww.im));
+        fld[(3 * Nj + j) * kVinvModes + mi] = mk<T>(T(n.re), T(n.im));
+    }
+    __syncthreads();
+    const int Zh = d.zHalf, Nz = d.Nz, P = d.positions;
+    const T* Cc = reinterpret_cast<const T*>(d.Ccos);
+    const T* Cs = reinterpret_cast<const T*>(d.Csin);
+    const T* Ccm = reinterpret_cast<const T*>(d.CcosM);
+    const T* Csm = reinterpret_cast<const T*>(d.CsinM);
+    // channel layout: 0 U(cos u) 1 V(cos v) 2 W(sin w) 3 N(sin eta) then d/dz per flux target
+    for (int it = threadIdx.x; it < nm * Zh; it += blockDim.x) {
+        const int n = it / nm;
+        const int mm = it - n * nm;
+        const int mode = m0 + mm;
+        // E (even j) and O (odd j) partial sums; channels U V W N Uz Vz Wz Nz
+        T E[8][2], O[8][2];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) { E[a][0] = T(0); E[a][1] = T(0); O[a][0] = T(0); O[a][1] = T(0); }
+        const T* cc = Cc + n * Nj;
+        const T* cs = Cs + n * Nj;
+        const T* ccm = Ccm + n * Nj;
+        const T* csm = Csm + n * Nj;
+        auto accum = [&](T (&A)[8][2], int j) {
+            const cx<T> u = fld[(0 * Nj + j) * kVinvModes + mm];
+            const cx<T> v = fld[(1 * Nj + j) * kVinvModes + mm];
+            const cx<T> w = fld[(2 * Nj + j) * kVinvModes + mm];
+            const cx<T> e = fld[(3 * Nj + j) * kVinvModes + mm];
+            const T a = cc[j], b = cs[j];
+            A[0][0] += a * u.x; A[0][1] += a * u.y;
+            A[1][0] += a * v.x; A[1][1] += a * v.y;
+            A[2][0] += b * w.x; A[2][1] += b * w.y;
+            A[3][0] += b * e.x; A[3][1] += b * e.y;
+            if (FLUX) {
+                const T am = ccm[j], bm = csm[j];
+                A[4][0] += bm * u.x; A[4][1] += bm * u.y;
+                A[5][0] += bm * v.x; A[5][1] += bm * v.y;
+                A[6][0] += am * w.x; A[6][1] += am * w.y;
+                A[7][0] += am * e.x; A[7][1] += am * e.y;
+            }
+        };
+        int j = 0;
+        for (; j + 1 < Nj; j += 2) { accum(E, j); accum(O, j + 1); }
+        if (j < Nj) accum(E, j);
+        const int pos = d.modePos[mode];
+        const int cpos = d.modeCompPos[mode];
+        const int n2 = Nz - 1 - n;
+        auto put = [&](int ch, const T* Ec, const T* Oc, bool sine) {
+            // cos family: out[n] = E+O, out[Nz-1-n] = E-O ; sin family: out[Nz-1-n] = O-E
+            cx<T>* base = zspec + (size_t)ch * Nz * P;
+            const cx<T> lo = mk<T>(Ec[0] + Oc[0], Ec[1] + Oc[1]);
+            base[(size_t)n * P + pos] = lo;
+            if (cpos >= 0) base[(size_t)n * P + cpos] = mk<T>(lo.x, -lo.y);
+            if (n2 != n) {
+                const cx<T> hi = sine ? mk<T>(Oc[0] - Ec[0], Oc[1] - Ec[1]) : mk<T>(Ec[0] - Oc[0], Ec[1] - Oc[1]);
+                base[(size_t)n2 * P + pos] = hi;
+                if (cpos >= 0) base[(size_t)n2 * P + cpos] = mk<T>(hi.x, -hi.y);
+            }
+        };
+        put(0, E[0], O[0], false);
+        put(1, E[1], O[1], false);
+        put(2, E[2], O[2], true);
+        put(3, E[3], O[3], true);
+        if (FLUX) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                if (t < d.nt) {
+                    const int q = d.tq[t];
+                    if (q == 0) put(4 + t, E[4], O[4], true);
+                    else if (q == 1) put(4 + t, E[5], O[5], true);
+                    else if (q == 2) put(4 + t, E[6], O[6], false);
+                    else put(4 + t, E[7], O[7], false);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// yinv: inverse FFT along y for kx columns [kx0, kx0+G) of plane z.
+// Output channel oc reads input channel src[oc]; if mulL[oc], multiplies by i*l.
+
+constexpr int kYG = 4;
+
+struct YInvMap {
+    int nOut;
+    int src[16];
+    int mulL[16];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_yinv(DescDev d, YInvMap map, const cx<T>* __restrict__ zspec, int nInCh,
+                                             cx<T>* __restrict__ yspec) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Ny = d.Ny, Nz = d.Nz, P = d.positions, KX = d.kxColumns;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* bufA = tw + Ny;
+    cx<T>* bufB = bufA + kYG * Ny;
+    const int kx0 = blockIdx.x * kYG;
+    const int z = blockIdx.y;
+    const int g = min(kYG, KX - kx0);
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
+    for (int i = threadIdx.x; i < Ny; i += blockDim.x) tw[i] = twg[i];
+    (void)nInCh;
+    for (int oc = 0; oc < map.nOut; ++oc) {
+        for (int i = threadIdx.x; i < kYG * Ny; i += blockDim.x) bufA[i] = mk<T>(T(0), T(0));
+        __syncthreads();
+        const cx<T>* in = zspec + ((size_t)map.src[oc] * Nz + z) * P;
+        const int pBeg = d.colStart[kx0], pEnd = d.colStart[kx0 + g];
+        for (int p = pBeg + threadIdx.x; p < pEnd; p += blockDim.x) {
+            // column of p
+            int gi = 0;
+            while (gi + 1 < g && p >= d.colStart[kx0 + gi + 1]) ++gi;
+            const int ky = d.posKy[p];
+            cx<T> v = in[p];
+            if (map.mulL[oc]) {
+                const T l = T(d.rowL[ky]);
+                v = mk<T>(-l * v.y, l * v.x);
+            }
+            bufA[gi * Ny + ky] = v;
+        }
+        __syncthreads();
+        cx<T>* res = fft_lines<T, true>(bufA, bufB, d.fy, g, Ny, tw);
+        cx<T>* out = yspec + (((size_t)z * map.nOut + oc) * Ny) * KX;
+        for (int i = threadIdx.x; i < g * Ny; i += blockDim.x) {
+            const int y = i / g, gi = i - y * g;
+            out[(size_t)y * KX + kx0 + gi] = res[gi * Ny + y];
+        }
+        __syncthreads();
+        if (res != bufA) {
+            // keep bufA/bufB roles fixed for the next channel
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Real transforms along x, one real row per complex line.  For even Nx a row
+// of Nx reals is one complex line of Nx/2 (the standard split of even and odd
+// samples), so each row's rounding stays relative to its own magnitude.
+
+// Half-spectrum value at 0 <= k <= Nx/2 (zero for k >= KX), optionally times
+// i*k_row; imaginary parts at k = 0 and k = Nx/2 are dropped (c2r semantics).
+template <typename T>
+__device__ __forceinline__ cx<T> half_at(const cx<T>* h, int k, int KX, int Nx, const double* rowK, bool useK) {
+    if (k >= KX) return mk<T>(T(0), T(0));
+    cx<T> v = h[k];
+    if (k == 0 || 2 * k == Nx) v.y = T(0);
+    if (useK) {
+        const T kk = T(rowK[k]);
+        v = mk<T>(-kk * v.y, kk * v.x);
+    }
+    return v;
+}
+
+// Entry k of the complex line whose inverse FFT yields the real row.
+template <typename T>
+__device__ __forceinline__ cx<T> c2r_line_entry(const DescDev& d, const cx<T>* h, int k, bool useK, const cx<T>* twN) {
+    const int Nx = d.Nx, KX = d.kxColumns;
+    if (d.xEven) {
+        const int M = Nx >> 1;
+        const cx<T> a = half_at<T>(h, k, KX, Nx, d.rowK, useK);
+        const cx<T> b = cconj<T>(half_at<T>(h, M - k, KX, Nx, d.rowK, useK));
+        const cx<T> e = cadd<T>(a, b);
+        const cx<T> o = cmul<T>(csub<T>(a, b), cconj<T>(twN[k]));  // * exp(+2 pi i k/Nx)
+        return mk<T>(e.x - o.y, e.y + o.x);                        // e + i o
+    }
+    if (2 * k <= Nx) return half_at<T>(h, k, KX, Nx, d.rowK, useK);
+    return cconj<T>(half_at<T>(h, Nx - k, KX, Nx, d.rowK, useK));
+}
+
+// Real sample x of the row from the inverse-transformed line.
+template <typename T>
+__device__ __forceinline__ T c2r_sample(const DescDev& d, const cx<T>* line, int x) {
+    if (d.xEven) { const cx<T> v = line[x >> 1]; return (x & 1) ? v.y : v.x; }
+    return line[x].x;
+}
+
+// Entry n of the complex line whose forward FFT gives the row's spectrum.
+template <typename T>
+__device__ __forceinline__ cx<T> r2c_line_entry(const DescDev& d, const T* row, int n) {
+    if (d.xEven) return mk<T>(row[2 * n], row[2 * n + 1]);
+    return mk<T>(row[n], T(0));
+}
+
+// Spectrum value at k < KX from the forward-transformed line.
+template <typename T>
+__device__ __forceinline__ cx<T> r2c_value(const DescDev& d, const cx<T>* line, int k, const cx<T>* twN) {
+    if (d.xEven) {
+        const int M = d.Nx >> 1;
+        const cx<T> zk = line[k % M];
+        const cx<T> zn = cconj<T>(line[(M - (k % M)) % M]);
+        const cx<T> e = mk<T>(T(0.5) * (zk.x + zn.x), T(0.5) * (zk.y + zn.y));
+        const cx<T> df = csub<T>(zk, zn);
+        const cx<T> o = mk<T>(T(0.5) * df.y, T(-0.5) * df.x);  // (zk - zn) / (2i)
+        return cadd<T>(e, cmul<T>(twN[k], o));
+    }
+    return line[k];
+}
+
+// ---------------------------------------------------------------------------
+// xflux: one CTA per (y, z) row.
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
+                                              unsigned long long* __restrict__ maxSpeedBits) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nx = d.Nx, Ny = d.Ny, KX = d.kxColumns, nt = d.nt, L = d.xLen;
+    const int nIn = 4 + 2 * nt;          // U V W N, q_y..., q_z...
+    const int nReal = 3 + 3 * nt;        // U V W, then (q_x, q_y, q_z) per target
+    const int y = blockIdx.x, z = blockIdx.y;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);  // [L]
+    cx<T>* twN = tw + L;                              // [Nx]
+    cx<T>* spec = twN + Nx;                           // [nIn][KX]
+    cx<T>* bufA = spec + nIn * KX;                    // [8][L]
+    cx<T>* bufB = bufA + 8 * L;
+    T* phys = reinterpret_cast<T*>(bufB + 8 * L);    // [nReal][Nx]
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
+    const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = twg[i];
+    for (int i = threadIdx.x; i < Nx; i += blockDim.x) twN[i] = twgN[i];
+    for (int i = threadIdx.x; i < nIn * KX; i += blockDim.x) {
+        const int c = i / KX, k = i - c * KX;
+        spec[i] = yspec[(((size_t)z * nIn + c) * Ny + y) * KX + k];
+    }
+    __syncthreads();
+    // real row r -> (input channel, times i*k)
+    auto rowSrc = [&](int r, int& ch, bool& useK) {
+        if (r < 3) { ch = r; useK = false; return; }
+        const int t = (r - 3) / 3, kind = (r - 3) % 3;
+        const int q = d.tq[t];
+        if (kind == 0) { ch = q; useK = true; }          // q_x = i k q   (q indexes U,V,W,N)
+        else if (kind == 1) { ch = 4 + t; useK = false; } // q_y
+        else { ch = 4 + nt + t; useK = false; }           // q_z
+    };
+    for (int rb = 0; rb < nReal; rb += 8) {
+        const int nr = min(8, nReal - rb);
+        for (int i = threadIdx.x; i < nr * L; i += blockDim.x) {
+            const int li = i / L, k = i - li * L;
+            int ch; bool useK;
+            rowSrc(rb + li, ch, useK);
+            bufA[li * L + k] = c2r_line_entry<T>(d, spec + ch * KX, k, useK, twN);
+        }
+        __syncthreads();
+        cx<T>* res = fft_lines<T, true>(bufA, bufB, d.fx, nr, L, tw);
+        for (int i = threadIdx.x; i < nr * Nx; i += blockDim.x) {
+            const int li = i / Nx, x = i - li * Nx;
+            phys[(rb + li) * Nx + x] = c2r_sample<T>(d, res + li * L, x);
+        }
+        __syncthreads();
+    }
+    // quadratic products S_q = -(u q_x + v q_y + w q_z) and max horizontal speed
+    T* S = reinterpret_cast<T*>(bufA);  // [nt][Nx] reals (bufA holds 16 L >= 4 Nx reals)
+    double vmax = 0.0;
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+        const T U = phys[0 * Nx + x], V = phys[1 * Nx + x], W = phys[2 * Nx + x];
+        for (int t = 0; t < nt; ++t) {
+            const T qx = phys[(3 + 3 * t) * Nx + x], qy = phys[(4 + 3 * t) * Nx + x], qz = phys[(5 + 3 * t) * Nx + x];
+            S[t * Nx + x] = -(U * qx + V * qy + W * qz);
+        }
+        const double sp = sqrt(double(U) * double(U) + double(V) * double(V));
+        vmax = fmax(vmax, sp);
+    }
+    for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmax(m, red[i]);
+        if (maxSpeedBits) atomicMax(maxSpeedBits, (unsigned long long)__double_as_longlong(m));
+    }
+    // forward real transform of each S_q
+    for (int i = threadIdx.x; i < nt * L; i += blockDim.x) {
+        const int t = i / L, n = i - t * L;
+        bufB[t * L + n] = r2c_line_entry<T>(d, S + t * Nx, n);
+    }
+    __syncthreads();
+    cx<T>* scratch = reinterpret_cast<cx<T>*>(phys);  // nReal*Nx reals >= 2*nt*L reals
+    cx<T>* res = fft_lines<T, false>(bufB, scratch, d.fx, nt, L, tw);
+    for (int i = threadIdx.x; i < nt * KX; i += blockDim.x) {
+        const int t = i / KX, k = i - t * KX;
+        pspec[(((size_t)z * nt + t) * Ny + y) * KX + k] = r2c_value<T>(d, res + t * L, k, twN);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// xc2r_fields: c2r of nch channel spectra to the real rows of a field bundle
+// fields[ch][z][y][x] (x fastest) -- transformWaveVortexToUVWEta output.
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_xc2r_fields(DescDev d, const cx<T>* __restrict__ yspec, int nch,
+                                                    double* __restrict__ fields) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nx = d.Nx, Ny = d.Ny, Nz = d.Nz, KX = d.kxColumns, L = d.xLen;
+    const int y = blockIdx.x, z = blockIdx.y;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* twN = tw + L;
+    cx<T>* spec = twN + Nx;
+    cx<T>* bufA = spec + nch * KX;
+    cx<T>* bufB = bufA + 4 * L;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
+    const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = twg[i];
+    for (int i = threadIdx.x; i < Nx; i += blockDim.x) twN[i] = twgN[i];
+    for (int i = threadIdx.x; i < nch * KX; i += blockDim.x) {
+        const int c = i / KX, k = i - c * KX;
+        spec[i] = yspec[(((size_t)z * nch + c) * Ny + y) * KX + k];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nch * L; i += blockDim.x) {
+        const int li = i / L, k = i - li * L;
+        bufA[li * L + k] = c2r_line_entry<T>(d, spec + li * KX, k, false, twN);
+    }
+    __syncthreads();
+    cx<T>* res = fft_lines<T, true>(bufA, bufB, d.fx, nch, L, tw);
+    const size_t R = (size_t)Nx * Ny * Nz;
+    for (int i = threadIdx.x; i < nch * Nx; i += blockDim.x) {
+        const int li = i / Nx, x = i - li * Nx;
+        fields[(size_t)li * R + ((size_t)z * Ny + y) * Nx + x] = double(c2r_sample<T>(d, res + li * L, x));
+    }
+}
+
+// xr2c_fields: r2c along x of field rows -> pspec[z][ch][y][kx] (kx < KX).
+template <typename T>
+__global__ void __launch_bounds__(256) k_xr2c_fields(DescDev d, const double* __restrict__ fields, int nch,
+                                                    cx<T>* __restrict__ pspec) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nx = d.Nx, Ny = d.Ny, Nz = d.Nz, KX = d.kxColumns, L = d.xLen;
+    const int y = blockIdx.x, z = blockIdx.y;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* twN = tw + L;
+    cx<T>* bufA = twN + Nx;
+    cx<T>* bufB = bufA + 4 * L;
+    T* row = reinterpret_cast<T*>(bufB + 4 * L);  // [nch][Nx]
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
+    const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = twg[i];
+    for (int i = threadIdx.x; i < Nx; i += blockDim.x) twN[i] = twgN[i];
+    const size_t R = (size_t)Nx * Ny * Nz;
+    for (int i = threadIdx.x; i < nch * Nx; i += blockDim.x) {
+        const int c = i / Nx, x = i - c * Nx;
+        row[c * Nx + x] = T(fields[(size_t)c * R + ((size_t)z * Ny + y) * Nx + x]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nch * L; i += blockDim.x) {
+        const int c = i / L, n = i - c * L;
+        bufA[c * L + n] = r2c_line_entry<T>(d, row + c * Nx, n);
+    }
+    __syncthreads();
+    cx<T>* res = fft_lines<T, false>(bufA, bufB, d.fx, nch, L, tw);
+    for (int i = threadIdx.x; i < nch * KX; i += blockDim.x) {
+        const int t = i / KX, k = i - t * KX;
+        pspec[(((size_t)z * nch + t) * Ny + y) * KX + k] = r2c_value<T>(d, res + t * L, k, twN);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// yfwd: forward FFT along y for kx columns [kx0, kx0+G) of plane z, channel c;
+// gathered to the active rows: fspec[c][z][pos].
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_yfwd(DescDev d, const cx<T>* __restrict__ pspec, int nch, cx<T>* __restrict__ fspec) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Ny = d.Ny, Nz = d.Nz, P = d.positions, KX = d.kxColumns;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* bufA = tw + Ny;
+    cx<T>* bufB = bufA + kYG * Ny;
+    const int kx0 = blockIdx.x * kYG;
+    const int z = blockIdx.y;
+    const int c = blockIdx.z;
+    const int g = min(kYG, KX - kx0);
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
+    for (int i = threadIdx.x; i < Ny; i += blockDim.x) tw[i] = twg[i];
+    const cx<T>* in = pspec + (((size_t)z * nch + c) * Ny) * KX;
+    for (int i = threadIdx.x; i < g * Ny; i += blockDim.x) {
+        const int y = i / g, gi = i - y * g;
+        bufA[gi * Ny + y] = in[(size_t)y * KX + kx0 + gi];
+    }
+    __syncthreads();
+    cx<T>* res = fft_lines<T, false>(bufA, bufB, d.fy, g, Ny, tw);
+    cx<T>* out = fspec + ((size_t)c * Nz + z) * P;
+    const int pBeg = d.colStart[kx0], pEnd = d.colStart[kx0 + g];
+    for (int p = pBeg + threadIdx.x; p < pEnd; p += blockDim.x) {
+        int gi = 0;
+        while (gi + 1 < g && p >= d.colStart[kx0 + gi + 1]) ++gi;
+        out[p] = res[gi * Ny + d.posKy[p]];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// vfwd: forward vertical contraction and projection.
+//  FLUX:  accumulates the nonlinear flux of every target (projectFluxTargetMode)
+//         and, when damping != null, adds A * (maxSpeed * damping).
+//  !FLUX: forward transform (projectNonhydrostaticMode / projectHydrostaticMode).
+
+constexpr int kVfwdModes = 8;
+
+template <typename T>
+struct cx2t { cx<T> p, q; };
+
+template <typename T, bool FLUX>
+__global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict__ fspec, int nch, double elapsed,
+                                             const double* __restrict__ Ap, const double* __restrict__ Am,
+                                             const double* __restrict__ A0, const unsigned long long* __restrict__ maxSpeedBits,
+                                             int applyDamping, double* __restrict__ Fp, double* __restrict__ Fm,
+                                             double* __restrict__ F0) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nj = d.Nj, Nz = d.Nz, Zh = d.zHalf, P = d.positions;
+    const int m0 = blockIdx.x * kVfwdModes;
+    const int nm = min(kVfwdModes, d.Nkl - m0);
+    // folded columns pq[c][n][mode] = (S_n + S_{Nz-1-n}, S_n - S_{Nz-1-n})
+    cx2t<T>* pq = reinterpret_cast<cx2t<T>*>(smem_raw);
+    for (int it = threadIdx.x; it < nch * Zh * nm; it += blockDim.x) {
+        const int mm = it % nm;
+        const int rest = it / nm;
+        const int n = rest % Zh, c = rest / Zh;
+        const int pos = d.modePos[m0 + mm];
+        const cx<T>* col = fspec + (size_t)c * Nz * P + pos;
+        const cx<T> a = col[(size_t)n * P];
+        const int n2 = Nz - 1 - n;
+        cx2t<T> v;
+        if (n2 == n) {
+            v.p = a; v.q = a;
+        } else {
+            const cx<T> b = col[(size_t)n2 * P];
+            v.p = cadd<T>(a, b); v.q = csub<T>(a, b);
+        }
+        pq[(c * Zh + n) * kVfwdModes + mm] = v;
+    }
+    __syncthreads();
+    double maxSpeed = 0.0;
+    if (FLUX && applyDamping) maxSpeed = __longlong_as_double((long long)*maxSpeedBits);
+    const T* Fc = reinterpret_cast<const T*>(d.Fcos);
+    const T* Fs = reinterpret_cast<const T*>(d.Fsin);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mm = it % nm, j = it / nm;
+        const int mode = m0 + mm;
+        const int w = d.modeWV[mode];
+        const bool conj = d.modeFlags[mode] & 1;
+        const int idx = j + Nj * w;
+        const bool evenJ = (j & 1) == 0;
+        const T* fc = Fc + (size_t)j * Zh;
+        const T* fs = Fs + (size_t)j * Zh;
+        // forward vertical transform of each channel
+        zd val[4] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c >= nch) break;
+            int q;
+            if (FLUX) q = d.tq[c];
+            else q = (d.hydrostatic && c == 2) ? 3 : c;
+            const bool cosine = q < 2;
+            const T* F = cosine ? fc : fs;
+            const bool useP = cosine ? evenJ : !evenJ;
+            T re = T(0), im = T(0);
+            const cx2t<T>* col = pq + (size_t)c * Zh * kVfwdModes + mm;
+            for (int n = 0; n < Zh; ++n) {
+                const cx2t<T> v = col[n * kVfwdModes];
+                const T f = F[n];
+                const cx<T> s = useP ? v.p : v.q;
+                re += f * s.x;
+                im += f * s.y;
+            }
+            zd z{double(re), double(im)};
+            if (conj) z = zconj(z);
+            val[c] = z;
+        }
+    const double k = d.k[w], l = d.l[w];
+        double s, cph;
+        sincos(d.omega[idx] * elapsed, &s, &cph);
+        const zd p{cph, s};
+        if (FLUX) {
+            zd fp{0.0, 0.0}, fm{0.0, 0.0}, f0{0.0, 0.0};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (c >= nch) break;
+                const int q = d.tq[c];
+                const zd value = val[c];
+                zd A0c{0.0, 0.0};
+                if (q == 0) A0c = zscale(zmul(value, zd{0.0, -l}), d.A0FromVorticity[idx]);
+                if (q == 1) A0c = zscale(zmul(value, zd{0.0, k}), d.A0FromVorticity[idx]);
+                if (q == 3) A0c = zscale(value, d.A0FromBuoyancy[idx]);
+                const zd bv = zsub(q == 3 ? value : zd{0.0, 0.0}, zscale(A0c, d.NA0[idx]));
+                const zd buoy = zscale(bv, d.ApmN[idx]);
+                zd wave{0.0, 0.0};
+                if (d.hydrostatic) {
+                    const zd apmd = zload(d.ApmD + 2 * idx);
+                    if (q == 0) wave = zmul(zmul(value, zd{0.0, k}), apmd);
+                    if (q == 1) wave = zmul(zmul(value, zd{0.0, l}), apmd);
+                } else {
+                    if (q == 0) wave = zscale(value, __dmul_rn(d.cosAlpha[w], d.ApmDScaled[idx]));
+                    if (q == 1) wave = zscale(value, __dmul_rn(d.sinAlpha[w], d.ApmDScaled[idx]));
+                    if (q == 2) wave = zmul(value, zd{0.0, __dmul_rn(d.Kh[w] / 2.0, d.apmWPrefactor[j])});
+                }
+                zd cp = zadd(wave, buoy), cm = zsub(wave, buoy);
+                if (w == 0) {
+                    const double sc = d.inertialScale[j];
+                    cp = zd{0.0, 0.0};
+                    if (q == 0) cp = zscale(value, sc);
+                    if (q == 1) cp = zscale(zmul(value, zd{0.0, -1.0}), sc);
+                    cm = zconj(cp);
+                }
+                fp = zadd(fp, zmul(cp, zconj(p)));
+                fm = zadd(fm, zmul(cm, p));
+                f0 = zadd(f0, A0c);
+            }
+            if (applyDamping) {
+                const double sd = __dmul_rn(maxSpeed, d.damping[idx]);
+                fp = zadd(fp, zscale(zload(Ap + 2 * idx), sd));
+                fm = zadd(fm, zscale(zload(Am + 2 * idx), sd));
+                f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sd));
+            }
+            zstore(Fp + 2 * idx, fp);
+            zstore(Fm + 2 * idx, fm);
+            zstore(F0 + 2 * idx, f0);
+        } else {
+            const zd U = val[0], V = val[1];
+            const zd W = d.hydrostatic ? zd{0.0, 0.0} : val[2];
+            const zd N = d.hydrostatic ? val[2] : val[3];
+            const zd vort = zsub(zmul(V, zd{0.0, k}), zmul(U, zd{0.0, l}));
+            const zd a0 = zadd(zscale(vort, d.A0FromVorticity[idx]), zscale(N, d.A0FromBuoyancy[idx]));
+            zd cp, cm;
+            if (w == 0) {
+                cp = zscale(zsub(U, zmul(V, zd{0.0, 1.0})), d.inertialScale[j]);
+                cm = zconj(cp);
+            } else {
+                const zd buoy = zscale(zsub(N, zscale(a0, d.NA0[idx])), d.ApmN[idx]);
+                zd wave;
+                if (d.hydrostatic) {
+                    const zd div = zadd(zmul(U, zd{0.0, k}), zmul(V, zd{0.0, l}));
+                    wave = zmul(zload(d.ApmD + 2 * idx), div);
+                } else {
+                    const zd delta = zscale(zadd(zscale(U, d.cosAlpha[w]), zscale(V, d.sinAlpha[w])), d.ApmDScaled[idx]);
+                    const zd wbar = zmul(zd{0.0, __dmul_rn(d.Kh[w] / 2.0, d.apmWPrefactor[j])}, W);
+                    wave = zadd(delta, wbar);
+                }
+                cp = zadd(wave, buoy);
+                cm = zsub(wave, buoy);
+            }
+            zstore(Fp + 2 * idx, zmul(cp, zconj(p)));
+            zstore(Fm + 2 * idx, zmul(cm, p));
+            zstore(F0 + 2 * idx, a0);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// RK4 stage arithmetic on 3*M complex (6*M doubles), written without
+// contraction like IntegrationBuffer::setAffine / addScaled
+// (PortableRuntime/src/WVRungeKutta.cpp:140-176).
+
+// out = base + scale * inc
+__global__ void k_affine(const double* __restrict__ base, const double* __restrict__ inc, double scale, double* __restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __dadd_rn(base[i], __dmul_rn(scale, inc[i]));
+}
+// acc = acc + scale * inc ; stage = base + cs * inc   (both from the same k)
+__global__ void k_accumulate_and_stage(double* __restrict__ acc, const double* __restrict__ inc, double scale,
+                                       const double* __restrict__ base, double cs, double* __restrict__ stage, int first, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double k = inc[i];
+        acc[i] = first ? k : __dadd_rn(acc[i], __dmul_rn(scale, k));
+        if (stage) stage[i] = __dadd_rn(base[i], __dmul_rn(cs, k));
+    }
+}
+
+}  // namespace dev
+}  // namespace wvgpu

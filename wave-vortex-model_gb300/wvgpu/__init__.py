@@ -1,0 +1,417 @@
+"""Python host binding of the GB300 constant-stratification spectral step.
+
+Mirrors the reference's kernel interface
+(CompiledKernel/include/WaveVortexKernel/WVTransformConstantStratificationKernel.hpp:47-110)
+on top of the C ABI in include/wvgpu.h: same operation names, same argument
+meaning, and failures raised with the reference's status codes and messages.
+
+Coefficient arrays are complex128 of shape (Nkl, Nj) -- the same memory as
+the reference's column-major [Nj, Nkl] WVComplex64 arrays; field bundles are
+float64 of shape (nfield, Nz, Ny, Nx) -- the same memory as [Nx, Ny, Nz, nfield].
+numpy arrays go through the host-pointer entry points; CUDA torch tensors
+through the device-pointer entry points on the current torch stream.
+
+There is no CPU fallback: if libwvgpu.so is missing or no GPU is present,
+operations raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libwvgpu.so")
+
+CONTRACT_VERSION = 4
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+FORCING_NONLINEAR_ADVECTION = 1
+FORCING_ADAPTIVE_DAMPING = 2
+
+# WVKernelStatusCode (CompiledKernel/include/WaveVortexKernel/WVKernelTypes.hpp:22-35)
+STATUS_NAMES = ["success", "invalidConfiguration", "invalidShape", "invalidPointer", "overlappingArrays", "sizeOverflow",
+                "allocationFailure", "fftPlanFailure", "fftExecutionFailure", "numericalFailure", "unsupportedOperation",
+                "reentrantExecution"]
+
+# MATLAB error identifiers of the gateway (wv_compiled_backend_mex.cpp:61-77)
+_IDENTIFIERS = {1: "WaveVortexModel:CompiledKernelInvalidConfiguration", 2: "WaveVortexModel:CompiledKernelShape",
+                3: "WaveVortexModel:CompiledKernelOwnership", 4: "WaveVortexModel:CompiledKernelOwnership",
+                5: "WaveVortexModel:CompiledKernelSizeOverflow", 6: "WaveVortexModel:CompiledKernelAllocation",
+                7: "WaveVortexModel:CompiledKernelPlan", 8: "WaveVortexModel:CompiledKernelExecution",
+                9: "WaveVortexModel:CompiledKernelNumericalFailure", 10: "WaveVortexModel:CompiledKernelUnsupportedOperation",
+                11: "WaveVortexModel:CompiledKernelReentrantExecution"}
+
+
+class WVKernelError(RuntimeError):
+    def __init__(self, code, message):
+        self.code = int(code)
+        self.status = STATUS_NAMES[self.code] if 0 <= self.code < len(STATUS_NAMES) else "unknown"
+        self.identifier = _IDENTIFIERS.get(self.code, "WaveVortexModel:CompiledKernelFailure")
+        super().__init__(f"{self.identifier}: {message}")
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [("contract_version", ctypes.c_uint32), ("Nx", ctypes.c_uint64), ("Ny", ctypes.c_uint64),
+                ("Nz", ctypes.c_uint64), ("Nj", ctypes.c_uint64), ("Lx", ctypes.c_double), ("Ly", ctypes.c_double),
+                ("Lz", ctypes.c_double), ("N0", ctypes.c_double), ("rho0", ctypes.c_double), ("g", ctypes.c_double),
+                ("planetary_radius", ctypes.c_double), ("rotation_rate", ctypes.c_double), ("latitude", ctypes.c_double),
+                ("is_hydrostatic", ctypes.c_uint8), ("should_antialias", ctypes.c_uint8)]
+
+
+class _Sizes(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("Nx", "Ny", "Nz", "Nj", "Nkl", "NxHalf", "M", "active_rows", "kx_columns",
+                                               "device_bytes")]
+
+
+class _StageTimes(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("vertical_inverse_ms", "y_inverse_ms", "x_products_ms", "y_forward_ms",
+                                               "vertical_forward_ms")] + [("fluxes", ctypes.c_uint64)]
+
+
+class _Metrics(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("nonlinear_flux_calls", "rhs_evaluations", "forward_calls", "inverse_calls",
+                                               "rk4_steps", "kernel_launches", "device_bytes")] + \
+               [("last_max_horizontal_speed", ctypes.c_double)]
+
+
+@dataclass
+class Configuration:
+    """WVTransformConstantStratificationConfiguration (WVKernelTypes.hpp:129-146)."""
+
+    Nx: int
+    Ny: int
+    Nz: int
+    Nj: int
+    Lx: float
+    Ly: float
+    Lz: float
+    N0: float = 5.2e-3
+    rho0: float = 1025.0
+    g: float = 9.81
+    planetaryRadius: float = 6.371e6
+    rotationRate: float = 7.2921e-5
+    latitude: float = 33.0
+    isHydrostatic: bool = False
+    shouldAntialias: bool = True
+    contractVersion: int = CONTRACT_VERSION
+
+    def _c(self):
+        return _Config(self.contractVersion, self.Nx, self.Ny, self.Nz, self.Nj, self.Lx, self.Ly, self.Lz, self.N0,
+                       self.rho0, self.g, self.planetaryRadius, self.rotationRate, self.latitude,
+                       int(bool(self.isHydrostatic)), int(bool(self.shouldAntialias)))
+
+
+_lib = None
+
+
+def library_path():
+    return LIB_PATH
+
+
+def load_library():
+    """Loads libwvgpu.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libwvgpu.so not found at {LIB_PATH}; build it with wvgpu.build.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    D = ctypes.c_double
+    lib.wv_describe.argtypes = [ctypes.POINTER(_Config), ctypes.POINTER(_Sizes), ctypes.c_char_p, ctypes.c_size_t]
+    lib.wv_describe_modes.argtypes = [ctypes.POINTER(_Config), P, P, P, P, P]
+    lib.wv_create.argtypes = [ctypes.POINTER(_Config), ctypes.c_int, ctypes.POINTER(P)]
+    lib.wv_destroy.argtypes = [P]
+    lib.wv_destroy.restype = None
+    lib.wv_last_message.argtypes = [P]
+    lib.wv_last_message.restype = ctypes.c_char_p
+    lib.wv_get_sizes.argtypes = [P, ctypes.POINTER(_Sizes)]
+    lib.wv_get_metrics.argtypes = [P, ctypes.POINTER(_Metrics)]
+    lib.wv_set_forcing.argtypes = [P, ctypes.c_uint32]
+    lib.wv_set_stage_instrumentation.argtypes = [P, ctypes.c_int]
+    lib.wv_get_stage_times.argtypes = [P, ctypes.POINTER(_StageTimes)]
+    for name in ("wv_nonlinear_flux", "wv_evaluate_rhs"):
+        getattr(lib, name).argtypes = [P, D, D, P, P, P, P, P, P]
+    for name in ("wv_nonlinear_flux_device", "wv_evaluate_rhs_device"):
+        getattr(lib, name).argtypes = [P, D, D, P, P, P, P, P, P, P]
+    lib.wv_forward.argtypes = [P, P, D, D, P, P, P]
+    lib.wv_forward_device.argtypes = [P, P, D, D, P, P, P, P]
+    lib.wv_inverse.argtypes = [P, D, D, P, P, P, P]
+    lib.wv_inverse_device.argtypes = [P, D, D, P, P, P, P, P]
+    lib.wv_rk4_steps.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int]
+    lib.wv_rk4_steps_device.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int, P]
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    """Names of the C entry points this binding expects (declared in include/wvgpu.h)."""
+    return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
+            "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
+            "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
+            "wv_inverse_device", "wv_rk4_steps_device"]
+
+
+def describe(configuration: Configuration):
+    """Validates a configuration on the host and returns its sizes (no GPU needed)."""
+    lib = load_library()
+    s = _Sizes()
+    buf = ctypes.create_string_buffer(512)
+    rc = lib.wv_describe(ctypes.byref(configuration._c()), ctypes.byref(s), buf, 512)
+    if rc != 0:
+        raise WVKernelError(rc, buf.value.decode())
+    return {n: int(getattr(s, n)) for n, _ in _Sizes._fields_}
+
+
+def describe_modes(configuration: Configuration):
+    """Canonical WV mode order and dispersion relation built on the host."""
+    lib = load_library()
+    s = describe(configuration)
+    Nkl, M = s["Nkl"], s["M"]
+    kMode = np.zeros(Nkl, np.int64)
+    lMode = np.zeros(Nkl, np.int64)
+    omega = np.zeros(M)
+    rows = np.zeros(Nkl, np.uint64)
+    conj = np.zeros(Nkl, np.uint8)
+    rc = lib.wv_describe_modes(ctypes.byref(configuration._c()), kMode.ctypes.data, lMode.ctypes.data, omega.ctypes.data,
+                               rows.ctypes.data, conj.ctypes.data)
+    if rc != 0:
+        raise WVKernelError(rc, "descriptor construction failed")
+    return dict(kMode=kMode, lMode=lMode, omega=omega.reshape(Nkl, s["Nj"]), storageRow=rows.astype(np.int64),
+                conjugated=conj.astype(bool))
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+class WVTransformConstantStratificationKernel:
+    """GPU kernel handle with the reference kernel's operations."""
+
+    def __init__(self, configuration: Configuration, precision: str = "fp64"):
+        lib = load_library()
+        self.configuration = configuration
+        self.precision = precision
+        p = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED}[precision]
+        h = ctypes.c_void_p()
+        rc = lib.wv_create(ctypes.byref(configuration._c()), p, ctypes.byref(h))
+        if rc != 0:
+            msg = "GPU kernel creation failed"
+            try:
+                describe(configuration)
+            except WVKernelError as e:
+                raise e
+            raise WVKernelError(rc, msg)
+        self._h = h
+        self._lib = lib
+        s = _Sizes()
+        lib.wv_get_sizes(h, ctypes.byref(s))
+        self.sizes = {n: int(getattr(s, n)) for n, _ in _Sizes._fields_}
+        self.Nkl = self.sizes["Nkl"]
+        self.Nj = configuration.Nj
+        self.spectral_shape = (self.Nkl, self.Nj)
+        self.spatial_shape = (configuration.Nz, configuration.Ny, configuration.Nx)
+
+    @classmethod
+    def create(cls, configuration: Configuration, precision: str = "fp64"):
+        return cls(configuration, precision)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.wv_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WVKernelError(rc, self._lib.wv_last_message(self._h).decode())
+
+    # -- helpers --------------------------------------------------------------------
+    def _host_coeff(self, a, name):
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        if a.shape != self.spectral_shape:
+            raise WVKernelError(2, f"{name} must have shape [Nj,Nkl].")
+        return a
+
+    def _dev_coeff(self, a, name):
+        import torch
+        if a.dtype != torch.complex128 or tuple(a.shape) != self.spectral_shape or not a.is_contiguous():
+            raise WVKernelError(2, f"{name} must be a contiguous complex128 [Nj,Nkl] tensor.")
+        return a
+
+    @staticmethod
+    def _stream():
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    # -- operations ----------------------------------------------------------------------
+    def set_forcing(self, nonlinear=True, adaptive_damping=False):
+        flags = (FORCING_NONLINEAR_ADVECTION if nonlinear else 0) | (FORCING_ADAPTIVE_DAMPING if adaptive_damping else 0)
+        self._check(self._lib.wv_set_forcing(self._h, flags))
+
+    def nonlinearFlux(self, t, t0, Ap, Am, A0, out=None, scheduled=False):
+        """nonlinearFlux (kernel.cpp:1140-1146); with scheduled=True the forcing
+        schedule's right-hand side (WVIntegrationSystem::evaluateRightHandSide)."""
+        if _is_torch(Ap):
+            import torch
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            F = out if out is not None else tuple(torch.empty_like(Ap) for _ in range(3))
+            fn = self._lib.wv_evaluate_rhs_device if scheduled else self._lib.wv_nonlinear_flux_device
+            self._check(fn(self._h, float(t), float(t0), Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(), F[0].data_ptr(),
+                           F[1].data_ptr(), F[2].data_ptr(), self._stream()))
+            return F
+        Ap, Am, A0 = (self._host_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        F = out if out is not None else tuple(np.empty(self.spectral_shape, np.complex128) for _ in range(3))
+        fn = self._lib.wv_evaluate_rhs if scheduled else self._lib.wv_nonlinear_flux
+        self._check(fn(self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data, F[0].ctypes.data,
+                       F[1].ctypes.data, F[2].ctypes.data))
+        return F
+
+    def evaluateRightHandSide(self, t, t0, Ap, Am, A0, out=None):
+        return self.nonlinearFlux(t, t0, Ap, Am, A0, out=out, scheduled=True)
+
+    def transformWaveVortexToUVWEta(self, t, t0, Ap, Am, A0, out=None):
+        """transformWaveVortexToUVWEta (kernel.cpp:686-694): fields (4, Nz, Ny, Nx)."""
+        shape = (4,) + self.spatial_shape
+        if _is_torch(Ap):
+            import torch
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            f = out if out is not None else torch.empty(shape, dtype=torch.float64, device=Ap.device)
+            self._check(self._lib.wv_inverse_device(self._h, float(t), float(t0), Ap.data_ptr(), Am.data_ptr(),
+                                                    A0.data_ptr(), f.data_ptr(), self._stream()))
+            return f
+        Ap, Am, A0 = (self._host_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        f = out if out is not None else np.empty(shape, np.float64)
+        self._check(self._lib.wv_inverse(self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data,
+                                         f.ctypes.data))
+        return f
+
+    def _forward(self, fields, t, t0, nch):
+        shape = (nch,) + self.spatial_shape
+        if _is_torch(fields):
+            import torch
+            if tuple(fields.shape) != shape or fields.dtype != torch.float64 or not fields.is_contiguous():
+                raise WVKernelError(2, "Fields must have shape [Nx,Ny,Nz,Nfield].")
+            A = tuple(torch.empty(self.spectral_shape, dtype=torch.complex128, device=fields.device) for _ in range(3))
+            self._check(self._lib.wv_forward_device(self._h, fields.data_ptr(), float(t), float(t0), A[0].data_ptr(),
+                                                    A[1].data_ptr(), A[2].data_ptr(), self._stream()))
+            return A
+        fields = np.ascontiguousarray(fields, dtype=np.float64)
+        if fields.shape != shape:
+            raise WVKernelError(2, "Fields must have shape [Nx,Ny,Nz,Nfield].")
+        A = tuple(np.empty(self.spectral_shape, np.complex128) for _ in range(3))
+        self._check(self._lib.wv_forward(self._h, fields.ctypes.data, float(t), float(t0), A[0].ctypes.data,
+                                         A[1].ctypes.data, A[2].ctypes.data))
+        return A
+
+    def transformUVWEtaToWaveVortex(self, fields, t, t0):
+        """transformUVWEtaToWaveVortex (kernel.cpp:637-684), nonhydrostatic handles."""
+        if self.configuration.isHydrostatic:
+            raise WVKernelError(1, "transformUVWEtaToWaveVortex requires a nonhydrostatic kernel.")
+        return self._forward(fields, t, t0, 4)
+
+    def transformUVEtaToWaveVortex(self, fields, t, t0):
+        """transformUVEtaToWaveVortex (kernel.cpp:583-635), hydrostatic handles."""
+        if not self.configuration.isHydrostatic:
+            raise WVKernelError(1, "transformUVEtaToWaveVortex requires a hydrostatic kernel.")
+        return self._forward(fields, t, t0, 3)
+
+    def rk4(self, Ap, Am, A0, t, t0, dt, steps):
+        """WVFixedStepRK4::step x steps (PortableRuntime/src/WVRungeKutta.cpp:335-462).
+        numpy inputs are copied; torch CUDA inputs are advanced in place.
+        Returns (Ap, Am, A0, t)."""
+        tt = ctypes.c_double(float(t))
+        if _is_torch(Ap):
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            self._check(self._lib.wv_rk4_steps_device(self._h, Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(), ctypes.byref(tt),
+                                                      float(t0), float(dt), int(steps), self._stream()))
+            return Ap, Am, A0, tt.value
+        Ap, Am, A0 = (self._host_coeff(a, n).copy() for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        self._check(self._lib.wv_rk4_steps(self._h, Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data, ctypes.byref(tt),
+                                           float(t0), float(dt), int(steps)))
+        return Ap, Am, A0, tt.value
+
+    def setStageInstrumentation(self, enabled):
+        """setStageInstrumentation (kernel.cpp:570-581): per-stage device times."""
+        self._check(self._lib.wv_set_stage_instrumentation(self._h, int(bool(enabled))))
+
+    def stage_times(self):
+        t = _StageTimes()
+        self._check(self._lib.wv_get_stage_times(self._h, ctypes.byref(t)))
+        return {n: getattr(t, n) for n, _ in _StageTimes._fields_}
+
+    def metrics(self):
+        m = _Metrics()
+        self._check(self._lib.wv_get_metrics(self._h, ctypes.byref(m)))
+        return {n: getattr(m, n) for n, _ in _Metrics._fields_}
+
+
+# ---------------------------------------------------------------------------
+# Synthetic states and time step through the GPU transforms (no CPU oracle).
+
+PI = 3.141592653589793238462643383279502884
+
+
+def spectral_wavenumbers(kernel):
+    """Kh [Nkl] and m [Nj] of a kernel's canonical mode order."""
+    c = kernel.configuration
+    modes = describe_modes(c)
+    k = 2.0 * PI * (modes["kMode"].astype(np.float64) / c.Lx)
+    l = 2.0 * PI * (modes["lMode"].astype(np.float64) / c.Ly)
+    return np.sqrt(k * k + l * l), np.arange(c.Nj) * PI / c.Lz, modes
+
+
+def synthetic_state(kernel, seed, urms=0.1, t0=0.0):
+    """Seeded state: uniform random phases, Gaussian amplitudes shaped by the
+    isotropic spectrum (Kh^2 + m^2)^(-3/4) in amplitude (energy ~ (Kh^2+m^2)^-1.5),
+    made representable by one inverse -> forward round trip on the GPU and
+    scaled to the requested rms velocity (u, v, w)."""
+    c = kernel.configuration
+    Kh, m, _ = spectral_wavenumbers(kernel)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shape = kernel.spectral_shape
+    K2 = Kh[:, None] ** 2 + m[None, :] ** 2
+    with np.errstate(divide="ignore"):
+        env = np.where(K2 > 0, K2 ** (-0.75), 0.0)
+    comps = []
+    for _ in range(3):
+        amp = rng.standard_normal(shape) * env
+        ph = rng.uniform(0.0, 2.0 * PI, shape)
+        comps.append(amp * np.exp(1j * ph))
+    f = kernel.transformWaveVortexToUVWEta(t0, t0, *comps)
+    fwd = f[[0, 1, 3]] if c.isHydrostatic else f
+    A = kernel.transformUVEtaToWaveVortex(fwd, t0, t0) if c.isHydrostatic else kernel.transformUVWEtaToWaveVortex(fwd, t0, t0)
+    f = kernel.transformWaveVortexToUVWEta(t0, t0, *A)
+    rms = math.sqrt(float(np.mean(f[0] ** 2 + f[1] ** 2 + f[2] ** 2)))
+    s = urms / rms if rms > 0 else 1.0
+    return tuple(a * s for a in A)
+
+
+def cfl_time_step(kernel, Ap, Am, A0, t0=0.0, cfl=0.5):
+    """WVModelFixedTimeStepMethods.timeStepForCFL
+    (Integrators/WVModelFixedTimeStepMethods.m:50-95): cfl times the minimum of
+    dx_eff/max|u_h|, (3/2)dz/max|w| above the bottom and the fastest wave period."""
+    c = kernel.configuration
+    Kh, m, modes = spectral_wavenumbers(kernel)
+    f = kernel.transformWaveVortexToUVWEta(t0, t0, Ap, Am, A0)
+    U = float(np.max(np.sqrt(f[0] ** 2 + f[1] ** 2)))
+    kk = np.abs(2.0 * PI * (modes["kMode"] / c.Lx))
+    ll = np.abs(2.0 * PI * (modes["lMode"] / c.Ly))
+    dx = PI / float(np.max(np.maximum(kk, ll)))
+    dz = c.Lz / (c.Nz - 1)
+    Wm = float(np.max(np.abs(f[2][1:])))
+    advective = cfl * dx / U if U > 0 else float("inf")
+    if Wm > 0:
+        advective = min(advective, cfl * (1.5 * dz) / Wm)
+    omax = float(np.max(np.abs(modes["omega"][:, 1:]))) if c.Nj > 1 else 0.0
+    oscillatory = cfl * 2.0 * PI / omax if omax > 0 else float("inf")
+    return min(advective, oscillatory)
