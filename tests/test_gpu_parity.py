@@ -147,8 +147,10 @@ def test_round_trip_identity(wv, shape, hydro):
     assert rel_err(f, fo) <= FP64_REL_TOL
     fwd = k.transformUVEtaToWaveVortex if hydro else k.transformUVWEtaToWaveVortex
     B = fwd(f[[0, 1, 3]] if hydro else f, 50.0, 0.0)
-    for a, b in zip(B, A):
-        assert rel_err(a, b) <= 5e-10
+    Bo = O.forward(d, fo[[0, 1, 3]] if hydro else fo, 50.0, 0.0)
+    for a, b, o in zip(B, A, Bo):
+        # the oracle's own FP64 round trip sets the conditioning of this state
+        assert rel_err(a, b) <= max(5e-10, 3.0 * rel_err(o, b)), (rel_err(a, b), rel_err(o, b))
     k.close()
 
 
