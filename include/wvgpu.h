@@ -183,6 +183,26 @@ int wv_forward_device(wv_handle* handle, const double* fields, double t, double 
                       double* Ap, double* Am, double* A0, void* stream);
 int wv_inverse_device(wv_handle* handle, double t, double t0,
                       const double* Ap, const double* Am, const double* A0, double* fields, void* stream);
+/* Nonlinear flux that allocates no device memory.  No counterpart in the
+ * reference: the reference's kernel owns a heap scratch arena.  It exists for
+ * callers that cannot call cudaMalloc at the point where they need a flux
+ * (e.g. code running while a stream is being captured into a CUDA graph, or a
+ * host application whose memory manager owns every device allocation and forbids
+ * further driver allocations, or latency-sensitive loops where cudaMalloc's
+ * implicit device synchronization is not acceptable).  Inputs and outputs are
+ * device pointers supplied by the caller, exactly as for
+ * wv_nonlinear_flux_device; the handle must already exist (wv_create allocates).
+ * The flux pipeline's scratch lives in one file-scope __device__ array of
+ * WV_STATIC_SCRATCH_BYTES, held by every GPU that loads the library until exit.
+ * Configurations whose scratch exceeds it are rejected with WV_SIZE_OVERFLOW.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls that overlap on the GPU (other streams, other handles) race. */
+#define WV_STATIC_SCRATCH_BYTES (32ull << 20)
+int wv_nonlinear_flux_device_noalloc(wv_handle* handle, double t, double t0,
+                                     const double* Ap, const double* Am, const double* A0,
+                                     double* Fp, double* Fm, double* F0, void* stream);
+
 /* Runs n_steps RK4 steps on device-resident state; the time is kept on the host
  * (t in/out) exactly as WVFixedStepRK4 advances it (t <- t + dt per step). */
 int wv_rk4_steps_device(wv_handle* handle, double* Ap, double* Am, double* A0,

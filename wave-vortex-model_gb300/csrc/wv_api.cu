@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -312,6 +313,78 @@ int check_state_flux(wv_handle* h, const double* Ap, const double* Am, const dou
 int finish(wv_handle* h, cudaError_t e, const char* where) {
     if (e != cudaSuccess) return cuda_fail(h, e, where);
     return WV_SUCCESS;
+}
+
+// ---- static scratch for callers that cannot allocate ------------------------------
+//
+// One file-scope device array holds the flux pipeline's scratch for
+// wv_nonlinear_flux_device_noalloc.  Every GPU that loads this library keeps
+// WV_STATIC_SCRATCH_BYTES resident until the process exits.  In host code the
+// array's name is only a host-side stand-in; its device address is looked up
+// once per device with cudaGetSymbolAddress, with that device current.
+
+constexpr size_t kStaticScratchBytes = WV_STATIC_SCRATCH_BYTES;
+__device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_scratch_mutex;
+void* g_static_scratch_address[kMaxDevices] = {};
+
+// Device address of g_static_scratch on `device` (the current device).
+cudaError_t static_scratch_address(int device, void** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_static_scratch_mutex);
+    if (!g_static_scratch_address[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return e;
+        g_static_scratch_address[device] = p;
+    }
+    *out = g_static_scratch_address[device];
+    return cudaSuccess;
+}
+
+inline size_t round256(size_t n) { return (n + 255) / 256 * 256; }
+
+// Byte offsets of the four scratch buffers and the speed counter inside the
+// static array; returns the total size.
+size_t static_scratch_layout(const Plan& p, size_t complexBytes, size_t offs[5]) {
+    const auto ss = scratch_sizes(p);
+    const size_t sizes[5] = {ss.z * complexBytes, ss.y * complexBytes, ss.p * complexBytes, ss.f * complexBytes,
+                             sizeof(unsigned long long)};
+    size_t off = 0;
+    for (int i = 0; i < 5; ++i) { offs[i] = off; off += round256(sizes[i]); }
+    return off;
+}
+
+// The flux of launch_flux on caller-independent scratch pointers (no damping).
+template <typename T>
+cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                               double* Fp, double* Fm, double* F0, unsigned char* base, const size_t offs[5], cudaStream_t s) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    const double elapsed = t - t0;
+    auto* z = reinterpret_cast<dev::cx<T>*>(base + offs[0]);
+    auto* y = reinterpret_cast<dev::cx<T>*>(base + offs[1]);
+    auto* ps = reinterpret_cast<dev::cx<T>*>(base + offs[2]);
+    auto* f = reinterpret_cast<dev::cx<T>*>(base + offs[3]);
+    // k_vinv clears this counter (block 0) before k_xflux accumulates into it.
+    auto* speed = reinterpret_cast<unsigned long long*>(base + offs[4]);
+    const int nt = p.targets.count;
+    dev::k_vinv<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    dev::YInvMap map{};
+    map.nOut = 4 + 2 * nt;
+    for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
+    for (int t2 = 0; t2 < nt; ++t2) {
+        map.src[4 + t2] = p.targets.q[t2]; map.mulL[4 + t2] = 1;
+        map.src[4 + nt + t2] = 4 + t2;     map.mulL[4 + nt + t2] = 0;
+    }
+    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(d, map, z, 4 + nt, y);
+    dev::k_xflux<T><<<dim3(p.Ny, p.Nz), 256, smem_xflux<T>(p), s>>>(d, y, ps, speed);
+    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nt), 256, smem_y<T>(p), s>>>(d, ps, nt, f);
+    dev::k_vfwd<T, true><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nt), s>>>(
+        d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -714,6 +787,34 @@ int wv_rk4_steps(wv_handle* h, double* Ap, double* Am, double* A0, double* t, do
     if (e != cudaSuccess) return cuda_fail(h, e, "RK4");
     *t = tt;
     return WV_SUCCESS;
+}
+
+// Flux on the static scratch array: no cudaMalloc, cudaFree or allocating
+// library call.  See include/wvgpu.h for who needs it and its limits.
+int wv_nonlinear_flux_device_noalloc(wv_handle* h, double t, double t0, const double* Ap, const double* Am,
+                                     const double* A0, double* Fp, double* Fm, double* F0, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
+    size_t offs[5];
+    const size_t need = static_scratch_layout(h->plan, 2 * elem_size(h->precision), offs);
+    if (need > kStaticScratchBytes)
+        return fail(h, WV_SIZE_OVERFLOW, "This configuration needs " + std::to_string(need) +
+                                             " bytes of flux scratch; the static scratch array holds " +
+                                             std::to_string(kStaticScratchBytes) + " bytes.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaError_t e = cudaSetDevice(h->device);
+    void* base = nullptr;
+    if (e == cudaSuccess) e = static_scratch_address(h->device, &base);
+    if (e != cudaSuccess) return cuda_fail(h, e, "static scratch set-up");
+    auto s = static_cast<cudaStream_t>(stream);
+    e = h->precision == WV_PRECISION_FP64
+            ? launch_flux_static<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, static_cast<unsigned char*>(base), offs, s)
+            : launch_flux_static<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, static_cast<unsigned char*>(base), offs, s);
+    h->metrics.nonlinear_flux_calls++;
+    h->metrics.kernel_launches += 5;
+    return finish(h, e, "nonlinear flux (static scratch)");
 }
 
 }  // extern "C"

@@ -136,7 +136,7 @@ def load_library():
     lib.wv_get_stage_times.argtypes = [P, ctypes.POINTER(_StageTimes)]
     for name in ("wv_nonlinear_flux", "wv_evaluate_rhs"):
         getattr(lib, name).argtypes = [P, D, D, P, P, P, P, P, P]
-    for name in ("wv_nonlinear_flux_device", "wv_evaluate_rhs_device"):
+    for name in ("wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_nonlinear_flux_device_noalloc"):
         getattr(lib, name).argtypes = [P, D, D, P, P, P, P, P, P, P]
     lib.wv_forward.argtypes = [P, P, D, D, P, P, P]
     lib.wv_forward_device.argtypes = [P, P, D, D, P, P, P, P]
@@ -153,7 +153,7 @@ def exported_symbols():
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
-            "wv_inverse_device", "wv_rk4_steps_device"]
+            "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc"]
 
 
 def describe(configuration: Configuration):
