@@ -45,7 +45,6 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -167,7 +166,7 @@ def fp64_peak_tflops(torch):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def traffic_from_profile(stage):
+def traffic_from_profile(stage, precision="fp64"):
     """Per-launch DRAM bytes of a stage from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
@@ -175,7 +174,7 @@ def traffic_from_profile(stage):
     with open(path) as fh:
         for line in fh:
             parts = line.split()
-            if len(parts) >= 3 and not line.startswith("#") and parts[0] == stage and parts[1] == "fp64":
+            if len(parts) >= 3 and not line.startswith("#") and parts[0] == stage and parts[1] == precision:
                 return float(parts[2])
     return None
 
@@ -197,6 +196,60 @@ def cpu_baseline_oracle(state, dt):
                       "(scipy.fft workers=-1); seconds per step %.2f" % el}
 
 
+def _time_steps(k, dev, t, t0, dt, steps, warmup, stream, barrier, flush, torch):
+    """Device time (ms) of `steps` RK4 steps, one event pair per step, L2 flushed between."""
+    for _ in range(warmup):
+        _, _, _, t = k.rk4(*dev, t, t0, dt, 1)
+    barrier()
+    total = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, _, _, t = k.rk4(*dev, t, t0, dt, 1)
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    barrier()
+    return total, t
+
+
+def _stage_profile(k, dev, t, t0, dt, precision, torch):
+    k.setStageInstrumentation(True)
+    k.rk4(*dev, t, t0, dt, 1)
+    torch.cuda.synchronize()
+    st = k.stage_times()
+    k.setStageInstrumentation(False)
+    names = ["vertical_inverse", "y_inverse", "x_products", "y_forward", "vertical_forward"]
+    per_launch = {n: st[n + "_ms"] / max(st["fluxes"], 1) for n in names}
+    dominant = max(per_launch, key=per_launch.get)
+    s = 16 if precision == "fp64" else 8
+    sbytes = stage_bytes(k.sizes, 4, s)
+    peaks, peak_kind = measured_peaks()
+    achieved = sbytes[dominant] / (per_launch[dominant] * 1e-3) / 1e9
+    flux_ms = sum(per_launch.values())
+    M, P = k.sizes["M"], k.sizes["active_rows"]
+    b_flux = 104 * M + 24 * s * P * GRID["Nz"]
+    return {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "traffic": traffic_from_profile(dominant, precision),
+            "peak_source": peak_kind, "algorithmic_bytes_per_launch": sbytes[dominant],
+            "avg_launch_ms": per_launch[dominant], "stage_ms_per_flux": per_launch,
+            "flux": {"algorithmic_bytes": b_flux, "ms": flux_ms, "achieved_gbs": b_flux / (flux_ms * 1e-3) / 1e9,
+                     "frac": b_flux / (flux_ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}}
+
+
+def _field_error_after(kd, km, state, dt, steps, torch, np):
+    """Relative L2 error per field (u, v, w, eta) of the mixed form against FP64 after `steps` RK4 steps."""
+    d64 = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+    d32 = [x.clone() for x in d64]
+    _, _, _, t1 = kd.rk4(*d64, 0.0, 0.0, dt, steps)
+    km.rk4(*d32, 0.0, 0.0, dt, steps)
+    torch.cuda.synchronize()
+    f64 = kd.transformWaveVortexToUVWEta(t1, 0.0, *(x.cpu().numpy() for x in d64))
+    f32 = kd.transformWaveVortexToUVWEta(t1, 0.0, *(x.cpu().numpy() for x in d32))
+    return [float(np.linalg.norm(f32[i] - f64[i]) / np.linalg.norm(f64[i])) for i in range(4)]
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -210,74 +263,50 @@ def run_ours(args):
     from wvgpu import build
     build.build()
     cfg = configuration(wvgpu)
-    k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision=args.precision)
-    state = wvgpu.synthetic_state(k, seed=SEED + rank * 0, urms=URMS)
+    k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    state = wvgpu.synthetic_state(k, seed=SEED, urms=URMS)
     dt = wvgpu.cfl_time_step(k, *state)
-    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
     stream = torch.cuda.current_stream()
-    t, t0 = 0.0, 0.0
-    for _ in range(args.warmup):
-        _, _, _, t = k.rk4(*dev, t, t0, dt, 1)
-    torch.cuda.synchronize()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
-    launches0 = k.metrics()["kernel_launches"]
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
-    total_ms = 0.0
-    barrier()
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            _, _, _, t = k.rk4(*dev, t, t0, dt, 1)
-            e1.record(stream)
-            e1.synchronize()
-            total_ms += e0.elapsed_time(e1)
-    barrier()
-    launches = k.metrics()["kernel_launches"] - launches0
-    t_s = total_ms / 1e3
-    if world > 1:
-        tt = torch.tensor([t_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_s = float(tt.item())
-    value = world * args.steps / t_s
+    def max_over_ranks(x):
+        if world > 1:
+            tt = torch.tensor([x], device="cuda", dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            return float(tt.item())
+        return x
 
-    # per-stage device times (instrumented pass, not part of the timed region)
-    k.setStageInstrumentation(True)
-    _, _, _, _ = k.rk4(*dev, t, t0, dt, 1)
-    torch.cuda.synchronize()
-    st = k.stage_times()
-    k.setStageInstrumentation(False)
-    names = ["vertical_inverse", "y_inverse", "x_products", "y_forward", "vertical_forward"]
-    per_launch = {n: st[n + "_ms"] / max(st["fluxes"], 1) for n in names}
-    dominant = max(per_launch, key=per_launch.get)
-    s = 16 if args.precision == "fp64" else 8
-    nt = 4
-    sbytes = stage_bytes(k.sizes, nt, s)
-    peaks, peak_kind = measured_peaks()
-    achieved = sbytes[dominant] / (per_launch[dominant] * 1e-3) / 1e9
-    traffic = traffic_from_profile(dominant)
-    flux_ms = sum(per_launch.values())
-    M, P = k.sizes["M"], k.sizes["active_rows"]
-    hr = P * GRID["Nz"]
-    b_flux = 104 * M + 24 * s * hr
-    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": sbytes[dominant], "avg_launch_ms": per_launch[dominant],
-                "stage_ms_per_flux": per_launch,
-                "flux": {"algorithmic_bytes": b_flux, "ms": flux_ms,
-                         "achieved_gbs": b_flux / (flux_ms * 1e-3) / 1e9,
-                         "frac": b_flux / (flux_ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}}
-    if args.precision == "fp64":
-        try:
-            roofline["fp64_gemm_peak_tflops_measured"] = fp64_peak_tflops(torch)
-        except Exception:  # pragma: no cover
-            roofline["fp64_gemm_peak_tflops_measured"] = None
+    t0 = 0.0
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+    launches0 = k.metrics()["kernel_launches"]
+    with ClockSampler(local) as clocks:
+        total_ms, t = _time_steps(k, dev, 0.0, t0, dt, args.steps, args.warmup, stream, barrier, flush, torch)
+    launches = k.metrics()["kernel_launches"] - launches0 - 25 * args.warmup
+    t_s = max_over_ranks(total_ms / 1e3)
+    value = world * args.steps / t_s
+    roofline = _stage_profile(k, dev, t, t0, dt, "fp64", torch)
+    try:
+        roofline["fp64_gemm_peak_tflops_measured"] = fp64_peak_tflops(torch)
+    except Exception:  # pragma: no cover
+        roofline["fp64_gemm_peak_tflops_measured"] = None
+
+    # mixed-precision form on the same state
+    km = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="mixed")
+    devm = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+    mixed_ms, tm = _time_steps(km, devm, 0.0, t0, dt, args.steps, args.warmup, stream, barrier, flush, torch)
+    mixed_value = world * args.steps / max_over_ranks(mixed_ms / 1e3)
+    mixed = {"value": mixed_value, "unit": UNIT, "ms_per_step": mixed_ms / args.steps,
+             "speedup_vs_fp64": mixed_value / value,
+             "dtype": "f32 xy transforms, products and vertical contractions; f64 phases, projection, RK4",
+             "roofline": _stage_profile(km, devm, tm, t0, dt, "mixed", torch)}
+    if rank == 0:
+        mixed["rel_field_err_vs_fp64_after_100_steps"] = _field_error_after(k, km, state, dt, 100, torch, np)
+    km.close()
 
     # end to end through the host-pointer C ABI, pinned host buffers
     host = [torch.empty(a.shape, dtype=torch.complex128, pin_memory=True).numpy() for a in state]
@@ -290,26 +319,23 @@ def run_ours(args):
     for _ in range(args.steps):
         Ap, Am, A0, te = k.rk4(*host, te, t0, dt, 1)
         host[0][...], host[1][...], host[2][...] = Ap, Am, A0
-    e2e_s = time.perf_counter() - w0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(time.perf_counter() - w0)
+    M = k.sizes["M"]
     coeff_bytes = 3 * M * 16
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32 xy/vertical + f64 phases/projection/RK4",
-        "data": "synthetic", "config": {
+        "dtype": "f64", "data": "synthetic", "config": {
             "workload": "fixed-step RK4, nonlinear advection, 256x256x129, 800 km x 800 km x 4 km, N0 5.2e-3, lat 33, "
                         "0.1 m/s rms seeded spectrum state, dt = 0.5 x CFL",
             "grid": [GRID["Nx"], GRID["Ny"], GRID["Nz"]], "Nj": GRID["Nj"], "Nkl": k.sizes["Nkl"], "dt_s": dt,
-            "precision": args.precision, "parallelism": f"replicas x{world}",
-            "l2": "flushed between timed steps (256 MB write)"},
+            "precision": "fp64 (plain drop-in); the mixed form is reported under 'mixed'",
+            "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MB write)"},
         "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": coeff_bytes,
                 "d2h_bytes_per_step": coeff_bytes},
         "gpu_launches": launches,
         "roofline": roofline,
+        "mixed": mixed,
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

