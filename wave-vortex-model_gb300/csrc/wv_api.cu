@@ -9,6 +9,7 @@
 #include "wv_descriptor.hpp"
 #include "wv_kernels.cuh"
 #include "wv_plan.hpp"
+#include "wv_warpfft.cuh"
 
 #include <cuda_runtime.h>
 
@@ -169,6 +170,143 @@ cudaError_t set_smem_limits(const Plan& p) {
 
 inline unsigned cdiv(size_t a, size_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 
+// ---- warp-FFT dispatch -------------------------------------------------------------
+// y lines of Ny = 32*R and x rows of Nx = 64*R run on register-resident warp
+// FFTs; other lengths use the shared-memory Stockham kernels.
+
+template <typename T>
+inline int warp_ry(const Plan& p) {
+    // FP64 stays on the shared-memory radix-4 Stockham kernels: on the FP64 pipe
+    // the radix-2 shuffle stages (64-bit shuffles, the twiddle product evaluated
+    // in every lane) cost more than the smem round trips they replace.
+    if (sizeof(T) == 8 || p.Ny % 32 != 0) return 0;
+    const int r = static_cast<int>(p.Ny / 32);
+    return (r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8 || r == 16) ? r : 0;
+}
+template <typename T>
+inline int warp_rx(const Plan& p) {
+    if (sizeof(T) == 8 || p.Nx % 64 != 0) return 0;
+    const int r = static_cast<int>(p.Nx / 64);
+    const int rmax = sizeof(T) == 8 ? 4 : 8;  // register budget of the fused x row
+    return ((r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8) && r <= rmax) ? r : 0;
+}
+template <typename T>
+size_t smem_y_w(const Plan& p) { return (p.Ny + p.Ny * dev::kWG) * sizeof(dev::cx<T>); }
+template <typename T>
+size_t smem_xflux_w(const Plan& p) {
+    const size_t L = p.Nx / 2, nIn = 4 + 2 * p.targets.count;
+    return (3 * L + dev::kWG * (nIn * p.kxColumns + L)) * sizeof(dev::cx<T>);
+}
+template <typename T>
+size_t smem_xc2r_w(const Plan& p, int nch) {
+    const size_t L = p.Nx / 2;
+    return (3 * L + dev::kWG * (nch * p.kxColumns + L)) * sizeof(dev::cx<T>);
+}
+template <typename T>
+size_t smem_xr2c_w(const Plan& p) { const size_t L = p.Nx / 2; return (3 * L + dev::kWG * L) * sizeof(dev::cx<T>); }
+
+#define WV_RSWITCH_Y(R, BODY)                                             \
+    switch (R) {                                                          \
+        case 1: { constexpr int RR = 1; BODY; } break;                    \
+        case 2: { constexpr int RR = 2; BODY; } break;                    \
+        case 3: { constexpr int RR = 3; BODY; } break;                    \
+        case 4: { constexpr int RR = 4; BODY; } break;                    \
+        case 6: { constexpr int RR = 6; BODY; } break;                    \
+        case 8: { constexpr int RR = 8; BODY; } break;                    \
+        case 16: { constexpr int RR = 16; BODY; } break;                  \
+        default: break;                                                   \
+    }
+#define WV_RSWITCH_X(T, R, BODY)                                          \
+    switch (R) {                                                          \
+        case 1: { constexpr int RR = 1; BODY; } break;                    \
+        case 2: { constexpr int RR = 2; BODY; } break;                    \
+        case 3: { constexpr int RR = 3; BODY; } break;                    \
+        case 4: { constexpr int RR = 4; BODY; } break;                    \
+        case 6: { if constexpr (sizeof(T) == 4) { constexpr int RR = 6; BODY; } } break; \
+        case 8: { if constexpr (sizeof(T) == 4) { constexpr int RR = 8; BODY; } } break; \
+        default: break;                                                   \
+    }
+
+template <typename T>
+cudaError_t set_smem_limits_w(const Plan& p) {
+    cudaError_t e = cudaSuccess;
+    const int ry = warp_ry<T>(p), rx = warp_rx<T>(p);
+    WV_RSWITCH_Y(ry, {
+        e = cudaFuncSetAttribute(dev::k_yinv_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y_w<T>(p));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dev::k_yfwd_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y_w<T>(p));
+    });
+    if (e != cudaSuccess) return e;
+    WV_RSWITCH_X(T, rx, {
+        e = cudaFuncSetAttribute(dev::k_xflux_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_xflux_w<T>(p));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dev::k_xc2r_fields_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_xc2r_w<T>(p, 4));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dev::k_xr2c_fields_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_xr2c_w<T>(p));
+    });
+    return e;
+}
+
+template <typename T>
+void launch_yinv(wv_handle* h, const dev::YInvMap& map, const dev::cx<T>* z, dev::cx<T>* y, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const int ry = warp_ry<T>(p);
+    if (ry) {
+        const dim3 grid(cdiv(p.kxColumns, dev::kWG), p.Nz, map.nOut);
+        WV_RSWITCH_Y(ry, (dev::k_yinv_w<T, RR><<<grid, 256, smem_y_w<T>(p), s>>>(h->dd, map, z, y)));
+        return;
+    }
+    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(h->dd, map, z, 0, y);
+}
+
+template <typename T>
+void launch_yfwd(wv_handle* h, const dev::cx<T>* ps, int nch, dev::cx<T>* f, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const int ry = warp_ry<T>(p);
+    if (ry) {
+        const dim3 grid(cdiv(p.kxColumns, dev::kWG), p.Nz, nch);
+        WV_RSWITCH_Y(ry, (dev::k_yfwd_w<T, RR><<<grid, 256, smem_y_w<T>(p), s>>>(h->dd, ps, nch, f)));
+        return;
+    }
+    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nch), 256, smem_y<T>(p), s>>>(h->dd, ps, nch, f);
+}
+
+template <typename T>
+void launch_xflux(wv_handle* h, const dev::cx<T>* y, dev::cx<T>* ps, unsigned long long* speed, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const int rx = warp_rx<T>(p);
+    if (rx) {
+        const dim3 grid(cdiv(p.Ny, dev::kWG), p.Nz);
+        WV_RSWITCH_X(T, rx, (dev::k_xflux_w<T, RR><<<grid, 256, smem_xflux_w<T>(p), s>>>(h->dd, y, ps, speed)));
+        return;
+    }
+    dev::k_xflux<T><<<dim3(p.Ny, p.Nz), 256, smem_xflux<T>(p), s>>>(h->dd, y, ps, speed);
+}
+
+template <typename T>
+void launch_xc2r(wv_handle* h, const dev::cx<T>* y, double* fields, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const int rx = warp_rx<T>(p);
+    if (rx) {
+        const dim3 grid(cdiv(p.Ny, dev::kWG), p.Nz);
+        WV_RSWITCH_X(T, rx, (dev::k_xc2r_fields_w<T, RR><<<grid, 256, smem_xc2r_w<T>(p, 4), s>>>(h->dd, y, 4, fields)));
+        return;
+    }
+    dev::k_xc2r_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xc2r<T>(p, 4), s>>>(h->dd, y, 4, fields);
+}
+
+template <typename T>
+void launch_xr2c(wv_handle* h, const double* fields, int nch, dev::cx<T>* ps, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const int rx = warp_rx<T>(p);
+    if (rx) {
+        const dim3 grid(cdiv(p.Ny, dev::kWG), p.Nz);
+        WV_RSWITCH_X(T, rx, (dev::k_xr2c_fields_w<T, RR><<<grid, 256, smem_xr2c_w<T>(p), s>>>(h->dd, fields, nch, ps)));
+        return;
+    }
+    dev::k_xr2c_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xr2c<T>(p), s>>>(h->dd, fields, nch, ps);
+}
+
 // One nonlinear flux (+ adaptive damping when requested) on device buffers.
 template <typename T>
 cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
@@ -192,11 +330,11 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
         map.src[4 + t2] = p.targets.q[t2]; map.mulL[4 + t2] = 1;            // q_y = i l q
         map.src[4 + nt + t2] = 4 + t2;     map.mulL[4 + nt + t2] = 0;        // q_z
     }
-    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(d, map, z, 4 + nt, y);
+    launch_yinv<T>(h, map, z, y, s);
     if (inst) cudaEventRecord(h->ev[2], s);
-    dev::k_xflux<T><<<dim3(p.Ny, p.Nz), 256, smem_xflux<T>(p), s>>>(d, y, ps, h->maxSpeed);
+    launch_xflux<T>(h, y, ps, h->maxSpeed, s);
     if (inst) cudaEventRecord(h->ev[3], s);
-    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nt), 256, smem_y<T>(p), s>>>(d, ps, nt, f);
+    launch_yfwd<T>(h, ps, nt, f, s);
     if (inst) cudaEventRecord(h->ev[4], s);
     dev::k_vfwd<T, true><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nt), s>>>(
         d, f, nt, elapsed, Ap, Am, A0, h->maxSpeed, damping ? 1 : 0, Fp, Fm, F0);
@@ -228,8 +366,8 @@ cudaError_t launch_inverse(wv_handle* h, double t, double t0, const double* Ap, 
     dev::YInvMap map{};
     map.nOut = 4;
     for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
-    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(d, map, z, 4, y);
-    dev::k_xc2r_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xc2r<T>(p, 4), s>>>(d, y, 4, fields);
+    launch_yinv<T>(h, map, z, y, s);
+    launch_xc2r<T>(h, y, fields, s);
     h->metrics.kernel_launches += 3;
     return cudaGetLastError();
 }
@@ -242,8 +380,8 @@ cudaError_t launch_forward(wv_handle* h, const double* fields, double t, double 
     const int nch = h->desc.c.is_hydrostatic ? 3 : 4;
     auto* ps = static_cast<dev::cx<T>*>(h->pspec);
     auto* f = static_cast<dev::cx<T>*>(h->fspec);
-    dev::k_xr2c_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xr2c<T>(p), s>>>(d, fields, nch, ps);
-    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nch), 256, smem_y<T>(p), s>>>(d, ps, nch, f);
+    launch_xr2c<T>(h, fields, nch, ps, s);
+    launch_yfwd<T>(h, ps, nch, f, s);
     dev::k_vfwd<T, false><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nch), s>>>(
         d, f, nch, t - t0, nullptr, nullptr, nullptr, nullptr, 0, Ap, Am, A0);
     h->metrics.kernel_launches += 3;
@@ -379,9 +517,9 @@ cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* 
         map.src[4 + t2] = p.targets.q[t2]; map.mulL[4 + t2] = 1;
         map.src[4 + nt + t2] = 4 + t2;     map.mulL[4 + nt + t2] = 0;
     }
-    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(d, map, z, 4 + nt, y);
-    dev::k_xflux<T><<<dim3(p.Ny, p.Nz), 256, smem_xflux<T>(p), s>>>(d, y, ps, speed);
-    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nt), 256, smem_y<T>(p), s>>>(d, ps, nt, f);
+    launch_yinv<T>(h, map, z, y, s);
+    launch_xflux<T>(h, y, ps, speed, s);
+    launch_yfwd<T>(h, ps, nt, f, s);
     dev::k_vfwd<T, true><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nt), s>>>(
         d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
     return cudaGetLastError();
@@ -470,6 +608,7 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     dd.xLen = static_cast<int>(x_len(p));
     dd.fx.N = p.fx.N; dd.fx.nstages = p.fx.nstages; dd.fy.N = p.fy.N; dd.fy.nstages = p.fy.nstages;
     for (int i = 0; i < dev::kMaxStages; ++i) { dd.fx.radix[i] = p.fx.radix[i]; dd.fy.radix[i] = p.fy.radix[i]; }
+    std::vector<int32_t> ymap(p.ymap);
     std::vector<int32_t> posKy(p.posKy), colStart(p.colStart), modeWV(p.modeWV), modePos(p.modePos), modeComp(p.modeCompPos);
     std::vector<double> inertial(d.inertialScale), apmw(d.apmWProjectionPrefactor);
 #define WV_UP(vec, field)                                            \
@@ -484,7 +623,7 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     WV_UP(d.ApmDScaled, ApmDScaled); WV_UP(ApmD, ApmD); WV_UP(damping, damping);
     WV_UP(d.k, k); WV_UP(d.l, l); WV_UP(d.Kh, Kh); WV_UP(d.cosAlpha, cosAlpha); WV_UP(d.sinAlpha, sinAlpha);
     WV_UP(inertial, inertialScale); WV_UP(apmw, apmWPrefactor);
-    WV_UP(posKy, posKy); WV_UP(colStart, colStart); WV_UP(modeWV, modeWV); WV_UP(modePos, modePos); WV_UP(modeComp, modeCompPos);
+    WV_UP(posKy, posKy); WV_UP(colStart, colStart); WV_UP(ymap, ymap); WV_UP(modeWV, modeWV); WV_UP(modePos, modePos); WV_UP(modeComp, modeCompPos);
     WV_UP(p.modeFlags, modeFlags);
     WV_UP(p.rowK, rowK); WV_UP(p.rowL, rowL);
 #undef WV_UP
@@ -516,6 +655,7 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->acc = static_cast<double*>(tmp); }
     if (e == cudaSuccess) { e = alloc(h, 4 * R * sizeof(double), &tmp); h->fields = static_cast<double*>(tmp); }
     if (e == cudaSuccess) e = precision == WV_PRECISION_FP64 ? set_smem_limits<double>(p) : set_smem_limits<float>(p);
+    if (e == cudaSuccess) e = precision == WV_PRECISION_FP64 ? set_smem_limits_w<double>(p) : set_smem_limits_w<float>(p);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         const int code = e == cudaErrorMemoryAllocation ? WV_ALLOCATION_FAILURE : WV_FFT_PLAN_FAILURE;

@@ -198,6 +198,7 @@ struct DescDev {
     // plan
     const int* posKy;       // [positions]
     const int* colStart;    // [kxColumns+1]
+    const int* ymap;        // [kxColumns][Ny] position of (kx, ky) or -1
     const int* modeWV;      // [Nkl] in position order
     const int* modePos;
     const int* modeCompPos;

@@ -93,6 +93,8 @@ Status build_plan(const Descriptor& d, Plan& p) {
         else compPosOfMode[rows[i].compOf] = static_cast<int32_t>(i);
     }
     for (size_t k = 0; k < p.kxColumns; ++k) p.colStart[k + 1] += p.colStart[k];
+    p.ymap.assign(p.kxColumns * p.Ny, -1);
+    for (size_t i = 0; i < rows.size(); ++i) p.ymap[rows[i].kx * p.Ny + rows[i].ky] = static_cast<int32_t>(i);
     // Modes in position order.
     std::vector<int32_t> order(d.Nkl);
     std::iota(order.begin(), order.end(), 0);

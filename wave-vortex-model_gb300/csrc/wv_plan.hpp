@@ -44,6 +44,7 @@ struct Plan {
     // Active rows in (kx, ky) order.
     std::vector<int32_t> posKx, posKy;
     std::vector<int32_t> colStart;        // [kxColumns+1] positions of each kx column
+    std::vector<int32_t> ymap;            // [kxColumns][Ny] position of row (kx, ky), -1 if inactive
     // Modes (retained WV columns) in position order.
     std::vector<int32_t> modeWV;          // WV index
     std::vector<int32_t> modePos;         // position of its storage row

@@ -1,0 +1,376 @@
+// Register-resident warp FFTs and the y / x passes built on them.
+//
+// A line of N = 32*R complex values lives in one warp: lane t holds R values.
+// An R-point DFT in registers, a twiddle by exp(+-2 pi i t k/N) and five
+// shfl_xor butterfly stages across lanes give the N-point DFT with no shared
+// memory and no block barrier.  Two orderings:
+//   fft_P : input  x[t + 32 r] in register r of lane t (natural)
+//           output X[k1 + R*brev5(t)] in register k1 of lane t (lane bit-reversed)
+//   fft_Q : input in fft_P's output layout, output in natural layout
+// (fft_Q with sign s is the transpose of fft_P with sign s; the DFT matrix is
+// symmetric, so both compute the same transform.)  Inverse transforms of
+// spectra use fft_P; forward transforms of physical rows produced by fft_P use
+// fft_Q, so physical samples never leave registers.
+#pragma once
+
+#include "wv_kernels.cuh"
+
+namespace wvgpu {
+namespace dev {
+
+__host__ __device__ constexpr int brev_bits(int i, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+__host__ __device__ constexpr int ilog2c(int r) { return r <= 1 ? 0 : 1 + ilog2c(r >> 1); }
+
+template <typename T>
+__device__ __forceinline__ cx<T> shfl_xor_cx(cx<T> v, int m) {
+    return mk<T>(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// multiply by exp(sigma * i pi / 2): -i (forward) or +i (inverse)
+template <bool INV, typename T>
+__device__ __forceinline__ cx<T> rot90(cx<T> b) { return INV ? mk<T>(-b.y, b.x) : mk<T>(b.y, -b.x); }
+
+// In-register R-point DFT, natural order in and out.  tw: N-entry table of
+// exp(-2 pi i k/N) with R | N.
+template <typename T, int R, bool INV>
+__device__ __forceinline__ void small_dft(cx<T> (&v)[R], const cx<T>* tw, int N) {
+    if constexpr (R == 1) {
+        return;
+    } else if constexpr ((R & (R - 1)) == 0) {
+        constexpr int LOG = ilog2c(R);
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int j = brev_bits(i, LOG);
+            if (i < j) { const cx<T> t = v[i]; v[i] = v[j]; v[j] = t; }
+        }
+#pragma unroll
+        for (int len = 2; len <= R; len <<= 1) {
+#pragma unroll
+            for (int i = 0; i < R; i += len) {
+#pragma unroll
+                for (int j = 0; j < len / 2; ++j) {
+                    const cx<T> a = v[i + j];
+                    cx<T> b = v[i + j + len / 2];
+                    if (j != 0) {
+                        if (4 * j == len) b = rot90<INV, T>(b);
+                        else b = cmul<T>(b, twid<T, INV>(tw, j * (N / len)));
+                    }
+                    v[i + j] = cadd<T>(a, b);
+                    v[i + j + len / 2] = csub<T>(a, b);
+                }
+            }
+        }
+    } else {
+        cx<T> out[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            cx<T> acc = v[0];
+#pragma unroll
+            for (int r = 1; r < R; ++r) acc = cadd<T>(acc, cmul<T>(v[r], twid<T, INV>(tw, ((r * k) % R) * (N / R))));
+            out[k] = acc;
+        }
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = out[k];
+    }
+}
+
+template <typename T, int R, bool INV>
+__device__ __forceinline__ void fft_P(cx<T> (&v)[R], const cx<T>* tw, int lane) {
+    constexpr int N = 32 * R;
+    small_dft<T, R, INV>(v, tw, N);
+#pragma unroll
+    for (int k = 1; k < R; ++k) v[k] = cmul<T>(v[k], twid<T, INV>(tw, lane * k));
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const cx<T> w = twid<T, INV>(tw, (lane & (h - 1)) * (N / (2 * h)));
+        const bool bottom = (lane & h) != 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const cx<T> u = shfl_xor_cx<T>(v[r], h);
+            v[r] = bottom ? cmul<T>(csub<T>(u, v[r]), w) : cadd<T>(v[r], u);
+        }
+    }
+}
+
+template <typename T, int R, bool INV>
+__device__ __forceinline__ void fft_Q(cx<T> (&v)[R], const cx<T>* tw, int lane) {
+    constexpr int N = 32 * R;
+#pragma unroll
+    for (int h = 1; h <= 16; h <<= 1) {
+        const cx<T> w = twid<T, INV>(tw, (lane & (h - 1)) * (N / (2 * h)));
+        const bool bottom = (lane & h) != 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const cx<T> u = shfl_xor_cx<T>(v[r], h);
+            v[r] = bottom ? csub<T>(u, cmul<T>(w, v[r])) : cadd<T>(v[r], cmul<T>(w, u));
+        }
+    }
+#pragma unroll
+    for (int k = 1; k < R; ++k) v[k] = cmul<T>(v[k], twid<T, INV>(tw, lane * k));
+    small_dft<T, R, INV>(v, tw, N);
+}
+
+// Index of register k1 of lane t in fft_P's output.
+template <int R>
+__device__ __forceinline__ int p_index(int k1, int lane) { return k1 + R * brev_bits(lane, 5); }
+
+constexpr int kWG = 8;  // kx columns (y pass) or rows (x pass) per CTA: one per warp
+
+// ---------------------------------------------------------------------------
+// y inverse: CTA = (8 kx columns, plane z, output channel); warp = one column.
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_yinv_w(DescDev d, YInvMap map, const cx<T>* __restrict__ zspec,
+                                               cx<T>* __restrict__ yspec) {
+    constexpr int N = 32 * R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);   // [N]
+    cx<T>* tile = tw + N;                              // [N][kWG]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int kx0 = blockIdx.x * kWG, z = blockIdx.y, oc = blockIdx.z;
+    const int KX = d.kxColumns, P = d.positions, Nz = d.Nz;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
+    __syncthreads();
+    const int kx = kx0 + warp;
+    if (kx < KX) {
+        const cx<T>* in = zspec + ((size_t)map.src[oc] * Nz + z) * P;
+        const int* ym = d.ymap + (size_t)kx * N;
+        const bool mulL = map.mulL[oc] != 0;
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int y = lane + 32 * r;
+            const int pos = ym[y];
+            cx<T> val = pos >= 0 ? in[pos] : mk<T>(T(0), T(0));
+            if (mulL) {
+                const T l = T(d.rowL[y]);
+                val = mk<T>(-l * val.y, l * val.x);
+            }
+            v[r] = val;
+        }
+        fft_P<T, R, true>(v, tw, lane);
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) tile[p_index<R>(k1, lane) * kWG + warp] = v[k1];
+    }
+    __syncthreads();
+    const int g = min(kWG, KX - kx0);
+    cx<T>* out = yspec + (((size_t)z * map.nOut + oc) * N) * KX + kx0;
+    for (int i = threadIdx.x; i < N * kWG; i += blockDim.x) {
+        const int y = i / kWG, gi = i - y * kWG;
+        if (gi < g) out[(size_t)y * KX + gi] = tile[i];
+    }
+}
+
+// y forward: CTA = (8 kx columns, plane z, channel); gathered to active rows.
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_yfwd_w(DescDev d, const cx<T>* __restrict__ pspec, int nch,
+                                               cx<T>* __restrict__ fspec) {
+    constexpr int N = 32 * R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tile = tw + N;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int kx0 = blockIdx.x * kWG, z = blockIdx.y, c = blockIdx.z;
+    const int KX = d.kxColumns, P = d.positions, Nz = d.Nz;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
+    const int g = min(kWG, KX - kx0);
+    const cx<T>* in = pspec + (((size_t)z * nch + c) * N) * KX + kx0;
+    for (int i = threadIdx.x; i < N * kWG; i += blockDim.x) {
+        const int y = i / kWG, gi = i - y * kWG;
+        tile[i] = gi < g ? in[(size_t)y * KX + gi] : mk<T>(T(0), T(0));
+    }
+    __syncthreads();
+    const int kx = kx0 + warp;
+    if (kx >= KX) return;
+    cx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = tile[(lane + 32 * r) * kWG + warp];
+    fft_P<T, R, false>(v, tw, lane);
+    __syncwarp();
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) tile[p_index<R>(k1, lane) * kWG + warp] = v[k1];
+    __syncwarp();
+    cx<T>* out = fspec + ((size_t)c * Nz + z) * P;
+    const int pBeg = d.colStart[kx], pEnd = d.colStart[kx + 1];
+    for (int p = pBeg + lane; p < pEnd; p += 32) out[p] = tile[d.posKy[p] * kWG + warp];
+}
+
+// ---------------------------------------------------------------------------
+// x pass: one warp per (y, z) row, 8 rows per CTA.  Real rows of Nx = 64*R
+// samples are complex lines of L = 32*R (even/odd sample split); physical
+// samples 2n, 2n+1 with n = k1 + R*brev5(lane) stay in registers.
+
+template <typename T, int R>
+__device__ __forceinline__ void c2r_row(const DescDev& d, const cx<T>* h, bool useK, const cx<T>* twL, const cx<T>* twN,
+                                        int lane, cx<T> (&v)[R]) {
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = c2r_line_entry<T>(d, h, lane + 32 * q, useK, twN);
+    fft_P<T, R, true>(v, twL, lane);
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
+                                                unsigned long long* __restrict__ maxSpeedBits) {
+    constexpr int L = 32 * R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double warpMax[kWG];
+    __shared__ int warpsDone;
+    const int Ny = d.Ny, KX = d.kxColumns, nt = d.nt;
+    const int nIn = 4 + 2 * nt;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int z = blockIdx.y;
+    const int y = blockIdx.x * kWG + warp;
+    cx<T>* twL = reinterpret_cast<cx<T>*>(smem_raw);   // [L]
+    cx<T>* twN = twL + L;                               // [2L]
+    cx<T>* spec = twN + 2 * L + warp * (nIn * KX + L);  // per warp: [nIn][KX] spectra + [L] line
+    cx<T>* line = spec + nIn * KX;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
+    const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) twL[i] = twg[i];
+    for (int i = threadIdx.x; i < 2 * L; i += blockDim.x) twN[i] = twgN[i];
+    if (threadIdx.x == 0) warpsDone = 0;
+    __syncthreads();
+    if (y >= Ny) return;
+    for (int i = lane; i < nIn * KX; i += 32) {
+        const int c = i / KX, k = i - c * KX;
+        spec[i] = yspec[(((size_t)z * nIn + c) * Ny + y) * KX + k];
+    }
+    __syncwarp();
+    cx<T> U[R], V[R], W[R], S[4][R];
+    cx<T> v[R];
+    c2r_row<T, R>(d, spec + 0 * KX, false, twL, twN, lane, U);
+    c2r_row<T, R>(d, spec + 1 * KX, false, twL, twN, lane, V);
+    c2r_row<T, R>(d, spec + 2 * KX, false, twL, twN, lane, W);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        if (t >= nt) break;
+        const int q = d.tq[t];
+        c2r_row<T, R>(d, spec + q * KX, true, twL, twN, lane, v);            // q_x
+#pragma unroll
+        for (int k = 0; k < R; ++k) S[t][k] = mk<T>(U[k].x * v[k].x, U[k].y * v[k].y);
+        c2r_row<T, R>(d, spec + (4 + t) * KX, false, twL, twN, lane, v);     // q_y
+#pragma unroll
+        for (int k = 0; k < R; ++k) S[t][k] = mk<T>(S[t][k].x + V[k].x * v[k].x, S[t][k].y + V[k].y * v[k].y);
+        c2r_row<T, R>(d, spec + (4 + nt + t) * KX, false, twL, twN, lane, v);  // q_z
+#pragma unroll
+        for (int k = 0; k < R; ++k) S[t][k] = mk<T>(-(S[t][k].x + W[k].x * v[k].x), -(S[t][k].y + W[k].y * v[k].y));
+    }
+    double vmax = 0.0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        vmax = fmax(vmax, sqrt(double(U[k].x) * double(U[k].x) + double(V[k].x) * double(V[k].x)));
+        vmax = fmax(vmax, sqrt(double(U[k].y) * double(U[k].y) + double(V[k].y) * double(V[k].y)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    // one atomic per CTA: the rows of this CTA reduce through shared memory
+    if (lane == 0) {
+        warpMax[warp] = vmax;
+        __threadfence_block();
+        if (atomicAdd(&warpsDone, 1) == min(kWG, Ny - (int)blockIdx.x * kWG) - 1 && maxSpeedBits) {
+            double m = 0.0;
+            for (int i = 0; i < min(kWG, Ny - (int)blockIdx.x * kWG); ++i) m = fmax(m, warpMax[i]);
+            atomicMax(maxSpeedBits, (unsigned long long)__double_as_longlong(m));
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        if (t >= nt) break;
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = S[t][k];
+        fft_Q<T, R, false>(v, twL, lane);
+#pragma unroll
+        for (int qq = 0; qq < R; ++qq) line[lane + 32 * qq] = v[qq];
+        __syncwarp();
+        cx<T>* out = pspec + (((size_t)z * nt + t) * Ny + y) * KX;
+        for (int k = lane; k < KX; k += 32) out[k] = r2c_value<T>(d, line, k, twN);
+        __syncwarp();
+    }
+}
+
+// inverse fields: c2r of nch channels to fields[ch][z][y][x]
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_xc2r_fields_w(DescDev d, const cx<T>* __restrict__ yspec, int nch,
+                                                      double* __restrict__ fields) {
+    constexpr int L = 32 * R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Ny = d.Ny, Nz = d.Nz, KX = d.kxColumns, Nx = 2 * L;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int z = blockIdx.y;
+    const int y = blockIdx.x * kWG + warp;
+    cx<T>* twL = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* twN = twL + L;
+    cx<T>* spec = twN + 2 * L + warp * (nch * KX + L);
+    cx<T>* line = spec + nch * KX;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
+    const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) twL[i] = twg[i];
+    for (int i = threadIdx.x; i < 2 * L; i += blockDim.x) twN[i] = twgN[i];
+    __syncthreads();
+    if (y >= Ny) return;
+    for (int i = lane; i < nch * KX; i += 32) {
+        const int c = i / KX, k = i - c * KX;
+        spec[i] = yspec[(((size_t)z * nch + c) * Ny + y) * KX + k];
+    }
+    __syncwarp();
+    const size_t R3 = (size_t)Nx * Ny * Nz;
+    for (int c = 0; c < nch; ++c) {
+        cx<T> v[R];
+        c2r_row<T, R>(d, spec + c * KX, false, twL, twN, lane, v);
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) line[p_index<R>(k1, lane)] = v[k1];
+        __syncwarp();
+        double* out = fields + (size_t)c * R3 + ((size_t)z * Ny + y) * Nx;
+        const T* samples = reinterpret_cast<const T*>(line);
+        for (int x = lane; x < Nx; x += 32) out[x] = double(samples[x]);
+        __syncwarp();
+    }
+}
+
+// forward fields: r2c of field rows -> pspec[z][ch][y][kx]
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_xr2c_fields_w(DescDev d, const double* __restrict__ fields, int nch,
+                                                      cx<T>* __restrict__ pspec) {
+    constexpr int L = 32 * R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Ny = d.Ny, Nz = d.Nz, KX = d.kxColumns, Nx = 2 * L;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int z = blockIdx.y;
+    const int y = blockIdx.x * kWG + warp;
+    cx<T>* twL = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* twN = twL + L;
+    cx<T>* line = twN + 2 * L + warp * L;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
+    const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) twL[i] = twg[i];
+    for (int i = threadIdx.x; i < 2 * L; i += blockDim.x) twN[i] = twgN[i];
+    __syncthreads();
+    if (y >= Ny) return;
+    const size_t R3 = (size_t)Nx * Ny * Nz;
+    for (int c = 0; c < nch; ++c) {
+        const double* row = fields + (size_t)c * R3 + ((size_t)z * Ny + y) * Nx;
+        T* samples = reinterpret_cast<T*>(line);
+        for (int x = lane; x < Nx; x += 32) samples[x] = T(row[x]);
+        __syncwarp();
+        cx<T> v[R];
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) v[k1] = line[p_index<R>(k1, lane)];
+        __syncwarp();
+        fft_Q<T, R, false>(v, twL, lane);
+#pragma unroll
+        for (int qq = 0; qq < R; ++qq) line[lane + 32 * qq] = v[qq];
+        __syncwarp();
+        cx<T>* out = pspec + (((size_t)z * nch + c) * Ny + y) * KX;
+        for (int k = lane; k < KX; k += 32) out[k] = r2c_value<T>(d, line, k, twN);
+        __syncwarp();
+    }
+}
+
+}  // namespace dev
+}  // namespace wvgpu
