@@ -194,8 +194,8 @@ template <typename T>
 size_t smem_y_w(const Plan& p) { return (p.Ny + p.Ny * dev::kWG) * sizeof(dev::cx<T>); }
 template <typename T>
 size_t smem_xflux_w(const Plan& p) {
-    const size_t L = p.Nx / 2, nIn = 4 + 2 * p.targets.count;
-    return (3 * L + dev::kWG * (nIn * p.kxColumns + L)) * sizeof(dev::cx<T>);
+    const size_t L = p.Nx / 2;
+    return (3 * L + dev::kWG * L) * sizeof(dev::cx<T>);
 }
 template <typename T>
 size_t smem_xc2r_w(const Plan& p, int nch) {
@@ -627,6 +627,15 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     WV_UP(p.modeFlags, modeFlags);
     WV_UP(p.rowK, rowK); WV_UP(p.rowL, rowL);
 #undef WV_UP
+    if (precision == WV_PRECISION_MIXED) {
+        auto upf = [&](const std::vector<double>& v, const float** dst) {
+            if (e != cudaSuccess) return;
+            const std::vector<float> f = cast<float>(v);
+            e = upload(h, f, dst);
+        };
+        upf(UAp, &dd.fUAp); upf(VAp, &dd.fVAp); upf(WAp, &dd.fWAp); upf(d.NAp, &dd.fNAp);
+        upf(UA0, &dd.fUA0); upf(VA0, &dd.fVA0); upf(d.NA0, &dd.fNA0);
+    }
     auto upT = [&](const std::vector<double>& v, const void** dst) {
         if (e != cudaSuccess) return;
         if (precision == WV_PRECISION_FP64) {

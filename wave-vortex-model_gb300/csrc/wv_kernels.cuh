@@ -186,6 +186,14 @@ struct DescDev {
     const double* ApmDScaled;
     const double* ApmD;  // complex (hydrostatic projection)
     const double* damping;  // [M] adaptive damping operator (or null)
+    // FP32 copies of the field factors (MIXED handles only; complex interleaved)
+    const float* fUAp;
+    const float* fVAp;
+    const float* fWAp;
+    const float* fNAp;
+    const float* fUA0;
+    const float* fVA0;
+    const float* fNA0;
     // per WV mode [Nkl]
     const double* k;
     const double* l;
@@ -245,6 +253,38 @@ __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restric
         const int w = d.modeWV[mode];
         const unsigned char flags = d.modeFlags[mode];
         const int idx = j + Nj * w;
+        if constexpr (sizeof(T) == 4) {
+            // MIXED: phase angle in FP64 reduced to [-pi, pi], then FP32 phase and field spectra.
+            const double ang = d.omega[idx] * elapsed;
+            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+            float sf, cf;
+            sincosf(float(red), &sf, &cf);
+            const float2 ap0 = make_float2(float(Ap[2 * idx]), float(Ap[2 * idx + 1]));
+            const float2 am0 = make_float2(float(Am[2 * idx]), float(Am[2 * idx + 1]));
+            const float2 a0 = make_float2(float(A0[2 * idx]), float(A0[2 * idx + 1]));
+            const float2 ap = make_float2(ap0.x * cf - ap0.y * sf, ap0.x * sf + ap0.y * cf);
+            const float2 am = make_float2(am0.x * cf + am0.y * sf, am0.y * cf - am0.x * sf);
+            const float2 uap = *reinterpret_cast<const float2*>(d.fUAp + 2 * idx);
+            const float2 vap = *reinterpret_cast<const float2*>(d.fVAp + 2 * idx);
+            const float2 wap = *reinterpret_cast<const float2*>(d.fWAp + 2 * idx);
+            const float2 ua0 = *reinterpret_cast<const float2*>(d.fUA0 + 2 * idx);
+            const float2 va0 = *reinterpret_cast<const float2*>(d.fVA0 + 2 * idx);
+            const float nap = d.fNAp[idx], na0 = d.fNA0[idx];
+            auto cm2 = [](float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+            auto cj = [](float2 a) { return make_float2(a.x, -a.y); };
+            auto ca = [](float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); };
+            float2 u = ca(ca(cm2(uap, ap), cm2(cj(uap), am)), cm2(ua0, a0));
+            float2 v = ca(ca(cm2(vap, ap), cm2(cj(vap), am)), cm2(va0, a0));
+            float2 ww = ca(cm2(wap, ap), cm2(wap, am));
+            float2 n = make_float2(ap.x * nap - am.x * nap + a0.x * na0, ap.y * nap - am.y * nap + a0.y * na0);
+            if (flags & 1) { u = cj(u); v = cj(v); ww = cj(ww); n = cj(n); }
+            if (flags & 2) { u.y = 0.f; v.y = 0.f; ww.y = 0.f; n.y = 0.f; }
+            fld[(0 * Nj + j) * kVinvModes + mi] = mk<T>(u.x, u.y);
+            fld[(1 * Nj + j) * kVinvModes + mi] = mk<T>(v.x, v.y);
+            fld[(2 * Nj + j) * kVinvModes + mi] = mk<T>(ww.x, ww.y);
+            fld[(3 * Nj + j) * kVinvModes + mi] = mk<T>(n.x, n.y);
+            continue;
+        }
         double s, c;
         sincos(d.omega[idx] * elapsed, &s, &c);
         const zd p{c, s};
@@ -734,40 +774,51 @@ __global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict
         sincos(d.omega[idx] * elapsed, &s, &cph);
         const zd p{cph, s};
         if (FLUX) {
-            zd fp{0.0, 0.0}, fm{0.0, 0.0}, f0{0.0, 0.0};
+            // Contributions of every target are summed first and rotated to the
+            // reference time once: sum_q c_q conj(p) = (sum_q c_q) conj(p).
+            // Per-target formulas of projectFluxTargetMode (kernel.cpp:396-431);
+            // contraction into FMA is allowed here.
+            const double vort = d.A0FromVorticity[idx], buoyF = d.A0FromBuoyancy[idx];
+            const double na0 = d.NA0[idx], apmn = d.ApmN[idx];
+            double cpr = 0.0, cpi = 0.0, cmr = 0.0, cmi = 0.0, f0r = 0.0, f0i = 0.0;
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 if (c >= nch) break;
                 const int q = d.tq[c];
-                const zd value = val[c];
-                zd A0c{0.0, 0.0};
-                if (q == 0) A0c = zscale(zmul(value, zd{0.0, -l}), d.A0FromVorticity[idx]);
-                if (q == 1) A0c = zscale(zmul(value, zd{0.0, k}), d.A0FromVorticity[idx]);
-                if (q == 3) A0c = zscale(value, d.A0FromBuoyancy[idx]);
-                const zd bv = zsub(q == 3 ? value : zd{0.0, 0.0}, zscale(A0c, d.NA0[idx]));
-                const zd buoy = zscale(bv, d.ApmN[idx]);
-                zd wave{0.0, 0.0};
+                const zd v = val[c];
+                double ar = 0.0, ai = 0.0;  // A0 contribution
+                if (q == 0) { ar = (v.im * l) * vort; ai = (-v.re * l) * vort; }
+                if (q == 1) { ar = (-v.im * k) * vort; ai = (v.re * k) * vort; }
+                if (q == 3) { ar = v.re * buoyF; ai = v.im * buoyF; }
+                double br = -ar * na0, bi = -ai * na0;  // buoyancy value
+                if (q == 3) { br += v.re; bi += v.im; }
+                br *= apmn; bi *= apmn;
+                double wr = 0.0, wi = 0.0;  // wave contribution
                 if (d.hydrostatic) {
                     const zd apmd = zload(d.ApmD + 2 * idx);
-                    if (q == 0) wave = zmul(zmul(value, zd{0.0, k}), apmd);
-                    if (q == 1) wave = zmul(zmul(value, zd{0.0, l}), apmd);
+                    double xr = 0.0, xi = 0.0;  // value * i*(k or l)
+                    if (q == 0) { xr = -v.im * k; xi = v.re * k; }
+                    if (q == 1) { xr = -v.im * l; xi = v.re * l; }
+                    wr = xr * apmd.re - xi * apmd.im;
+                    wi = xr * apmd.im + xi * apmd.re;
                 } else {
-                    if (q == 0) wave = zscale(value, __dmul_rn(d.cosAlpha[w], d.ApmDScaled[idx]));
-                    if (q == 1) wave = zscale(value, __dmul_rn(d.sinAlpha[w], d.ApmDScaled[idx]));
-                    if (q == 2) wave = zmul(value, zd{0.0, __dmul_rn(d.Kh[w] / 2.0, d.apmWPrefactor[j])});
+                    if (q == 0) { const double sc = d.cosAlpha[w] * d.ApmDScaled[idx]; wr = v.re * sc; wi = v.im * sc; }
+                    if (q == 1) { const double sc = d.sinAlpha[w] * d.ApmDScaled[idx]; wr = v.re * sc; wi = v.im * sc; }
+                    if (q == 2) { const double sc = (d.Kh[w] / 2.0) * d.apmWPrefactor[j]; wr = -v.im * sc; wi = v.re * sc; }
                 }
-                zd cp = zadd(wave, buoy), cm = zsub(wave, buoy);
+                double pr = wr + br, pi = wi + bi, mr = wr - br, mi = wi - bi;
                 if (w == 0) {
                     const double sc = d.inertialScale[j];
-                    cp = zd{0.0, 0.0};
-                    if (q == 0) cp = zscale(value, sc);
-                    if (q == 1) cp = zscale(zmul(value, zd{0.0, -1.0}), sc);
-                    cm = zconj(cp);
+                    pr = 0.0; pi = 0.0;
+                    if (q == 0) { pr = v.re * sc; pi = v.im * sc; }
+                    if (q == 1) { pr = v.im * sc; pi = -v.re * sc; }
+                    mr = pr; mi = -pi;
                 }
-                fp = zadd(fp, zmul(cp, zconj(p)));
-                fm = zadd(fm, zmul(cm, p));
-                f0 = zadd(f0, A0c);
+                cpr += pr; cpi += pi; cmr += mr; cmi += mi; f0r += ar; f0i += ai;
             }
+            zd fp{cpr * p.re + cpi * p.im, cpi * p.re - cpr * p.im};   // (cp) * conj(p)
+            zd fm{cmr * p.re - cmi * p.im, cmr * p.im + cmi * p.re};   // (cm) * p
+            zd f0{f0r, f0i};
             if (applyDamping) {
                 const double sd = __dmul_rn(maxSpeed, d.damping[idx]);
                 fp = zadd(fp, zscale(zload(Ap + 2 * idx), sd));

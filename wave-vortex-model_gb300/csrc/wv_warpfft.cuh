@@ -215,7 +215,7 @@ __device__ __forceinline__ void c2r_row(const DescDev& d, const cx<T>* h, bool u
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(256) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
+__global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
                                                 unsigned long long* __restrict__ maxSpeedBits) {
     constexpr int L = 32 * R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -228,8 +228,7 @@ __global__ void __launch_bounds__(256) k_xflux_w(DescDev d, const cx<T>* __restr
     const int y = blockIdx.x * kWG + warp;
     cx<T>* twL = reinterpret_cast<cx<T>*>(smem_raw);   // [L]
     cx<T>* twN = twL + L;                               // [2L]
-    cx<T>* spec = twN + 2 * L + warp * (nIn * KX + L);  // per warp: [nIn][KX] spectra + [L] line
-    cx<T>* line = spec + nIn * KX;
+    cx<T>* line = twN + 2 * L + warp * L;               // per warp: [L]
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
     const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
     for (int i = threadIdx.x; i < L; i += blockDim.x) twL[i] = twg[i];
@@ -237,35 +236,43 @@ __global__ void __launch_bounds__(256) k_xflux_w(DescDev d, const cx<T>* __restr
     if (threadIdx.x == 0) warpsDone = 0;
     __syncthreads();
     if (y >= Ny) return;
-    for (int i = lane; i < nIn * KX; i += 32) {
-        const int c = i / KX, k = i - c * KX;
-        spec[i] = yspec[(((size_t)z * nIn + c) * Ny + y) * KX + k];
-    }
-    __syncwarp();
-    cx<T> U[R], V[R], W[R], S[4][R];
-    cx<T> v[R];
-    c2r_row<T, R>(d, spec + 0 * KX, false, twL, twN, lane, U);
-    c2r_row<T, R>(d, spec + 1 * KX, false, twL, twN, lane, V);
-    c2r_row<T, R>(d, spec + 2 * KX, false, twL, twN, lane, W);
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        if (t >= nt) break;
-        const int q = d.tq[t];
-        c2r_row<T, R>(d, spec + q * KX, true, twL, twN, lane, v);            // q_x
-#pragma unroll
-        for (int k = 0; k < R; ++k) S[t][k] = mk<T>(U[k].x * v[k].x, U[k].y * v[k].y);
-        c2r_row<T, R>(d, spec + (4 + t) * KX, false, twL, twN, lane, v);     // q_y
-#pragma unroll
-        for (int k = 0; k < R; ++k) S[t][k] = mk<T>(S[t][k].x + V[k].x * v[k].x, S[t][k].y + V[k].y * v[k].y);
-        c2r_row<T, R>(d, spec + (4 + nt + t) * KX, false, twL, twN, lane, v);  // q_z
-#pragma unroll
-        for (int k = 0; k < R; ++k) S[t][k] = mk<T>(-(S[t][k].x + W[k].x * v[k].x), -(S[t][k].y + W[k].y * v[k].y));
-    }
+    // spectra of this row: channel c at row + c*Ny*KX (read straight from L2/HBM, coalesced)
+    const cx<T>* row = yspec + (((size_t)z * nIn) * Ny + y) * KX;
+    const size_t cstride = (size_t)Ny * KX;
+    cx<T> U[R], V[R], W[R], v[R], S[R];
+    c2r_row<T, R>(d, row + 0 * cstride, false, twL, twN, lane, U);
+    c2r_row<T, R>(d, row + 1 * cstride, false, twL, twN, lane, V);
+    c2r_row<T, R>(d, row + 2 * cstride, false, twL, twN, lane, W);
     double vmax = 0.0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         vmax = fmax(vmax, sqrt(double(U[k].x) * double(U[k].x) + double(V[k].x) * double(V[k].x)));
         vmax = fmax(vmax, sqrt(double(U[k].y) * double(U[k].y) + double(V[k].y) * double(V[k].y)));
+    }
+#pragma unroll 1
+    for (int t = 0; t < nt; ++t) {
+        const int q = d.tq[t];
+        // S_q = -(u q_x + v q_y + w q_z), accumulated in that order
+#pragma unroll 1
+        for (int kind = 0; kind < 3; ++kind) {
+            const int ch = kind == 0 ? q : (kind == 1 ? 4 + t : 4 + nt + t);
+            c2r_row<T, R>(d, row + ch * cstride, kind == 0, twL, twN, lane, v);
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const cx<T> m = kind == 0 ? U[k] : (kind == 1 ? V[k] : W[k]);
+                const cx<T> p = mk<T>(m.x * v[k].x, m.y * v[k].y);
+                S[k] = kind == 0 ? p : mk<T>(S[k].x + p.x, S[k].y + p.y);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < R; ++k) S[k] = mk<T>(-S[k].x, -S[k].y);
+        fft_Q<T, R, false>(S, twL, lane);
+#pragma unroll
+        for (int qq = 0; qq < R; ++qq) line[lane + 32 * qq] = S[qq];
+        __syncwarp();
+        cx<T>* out = pspec + (((size_t)z * nt + t) * Ny + y) * KX;
+        for (int k = lane; k < KX; k += 32) out[k] = r2c_value<T>(d, line, k, twN);
+        __syncwarp();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
@@ -273,24 +280,12 @@ __global__ void __launch_bounds__(256) k_xflux_w(DescDev d, const cx<T>* __restr
     if (lane == 0) {
         warpMax[warp] = vmax;
         __threadfence_block();
-        if (atomicAdd(&warpsDone, 1) == min(kWG, Ny - (int)blockIdx.x * kWG) - 1 && maxSpeedBits) {
+        const int rows = min(kWG, Ny - (int)blockIdx.x * kWG);
+        if (atomicAdd(&warpsDone, 1) == rows - 1 && maxSpeedBits) {
             double m = 0.0;
-            for (int i = 0; i < min(kWG, Ny - (int)blockIdx.x * kWG); ++i) m = fmax(m, warpMax[i]);
+            for (int i = 0; i < rows; ++i) m = fmax(m, warpMax[i]);
             atomicMax(maxSpeedBits, (unsigned long long)__double_as_longlong(m));
         }
-    }
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        if (t >= nt) break;
-#pragma unroll
-        for (int k = 0; k < R; ++k) v[k] = S[t][k];
-        fft_Q<T, R, false>(v, twL, lane);
-#pragma unroll
-        for (int qq = 0; qq < R; ++qq) line[lane + 32 * qq] = v[qq];
-        __syncwarp();
-        cx<T>* out = pspec + (((size_t)z * nt + t) * Ny + y) * KX;
-        for (int k = lane; k < KX; k += 32) out[k] = r2c_value<T>(d, line, k, twN);
-        __syncwarp();
     }
 }
 
