@@ -858,3 +858,209 @@ def noise_floor(fn, *args, **kwargs):
         den = float(np.max(np.abs(b)))
         floors.append(float(np.max(np.abs(a - b))) / den if den > 0 else 0.0)
     return ref, floors
+
+
+# ---------------------------------------------------------------------------
+# Adjoint (vector-Jacobian products).  No counterpart in the reference; the
+# GPU adjoint is checked against this restatement, against central finite
+# differences (exact for the quadratic flux up to rounding) and by the
+# dot-product test.  Inner product on complex arrays: <a, b> = Re sum conj(a) b.
+
+
+def _inverse_matrices(desc):
+    """(Nz, Nj) real matrices of the inverse vertical transforms with the x0.5
+    coefficient-production scaling: value channels (cos, sin) and the
+    z-derivative channels (-m sin for cosine fields, +m cos for sine fields)."""
+    c = desc.c
+    z = np.arange(c.Nz)[:, None]
+    j = np.arange(c.Nj)[None, :]
+    L = c.Nz - 1
+    ccos = np.where(j == 0, 0.5, _cospi(j * z, L))
+    csin = np.where((j >= 1) & (z >= 1) & (z <= c.Nz - 2), _sinpi(j * z, L), 0.0)
+    m = desc.m[None, :]
+    return ccos, csin, -m * csin, m * ccos
+
+
+def _forward_matrices(desc):
+    """(Nj, Nz) forward vertical matrices (DCT-I / DST-I + normalization) times
+    the horizontal scale 1/(Nx Ny)."""
+    c = desc.c
+    n = np.arange(c.Nz)[None, :]
+    j = np.arange(c.Nj)[:, None]
+    L = c.Nz - 1
+    fc = np.where(n == 0, 1.0, np.where(n == c.Nz - 1, (-1.0) ** j, 2.0 * _cospi(j * n, L)))
+    fc = np.where(j == c.Nz - 1, 0.5 * fc, fc) / L
+    fs = np.where((j >= 1) & (n >= 1) & (n <= c.Nz - 2), 2.0 * _sinpi(j * n, L), 0.0) / L
+    hs = 1.0 / float(c.Nx * c.Ny)
+    return fc * hs, fs * hs
+
+
+def _rows_to_columns_adjoint(desc, half_rows):
+    """Adjoint of _columns_to_half for one channel: (rows, Nz) -> (Nkl, Nz) in
+    the WV frame (completion rows folded back conjugated, self-conjugate rows
+    real, conjugated storage undone)."""
+    h = half_rows.copy()
+    if len(desc.completionRows):
+        np.add.at(h, desc.completionSources, np.conj(h[desc.completionRows]))
+    if len(desc.selfConjugateRows):
+        h[desc.selfConjugateRows] = h[desc.selfConjugateRows].real
+    v = h[desc.storageRow]
+    return np.where(desc.conjugated[:, None], np.conj(v), v)
+
+
+def _c2r_adjoint(desc, fields):
+    """Adjoint of the unnormalized c2r (FFTW semantics): fields (ch, Nz, Ny, Nx)
+    -> half rows (ch, rows, Nz); interior kx carry weight 2."""
+    h = _spatial_to_half_rows(desc, fields)
+    c = desc.c
+    kx = np.arange(desc.NxHalf)
+    w = np.where((kx == 0) | (2 * kx == c.Nx), 1.0, 2.0)
+    wr = np.tile(w, c.Ny)  # row = kx + NxHalf*ky
+    return h * wr[None, :, None]
+
+
+def _r2c_adjoint(desc, half_rows):
+    """Adjoint of the unnormalized r2c: half rows (ch, rows, Nz) -> fields
+    Re sum_{kx<=Nx/2} H e^{+i...} (interior kx at weight 1/2 under c2r)."""
+    c = desc.c
+    kx = np.arange(desc.NxHalf)
+    w = np.where((kx == 0) | (2 * kx == c.Nx), 1.0, 0.5)
+    wr = np.tile(w, c.Ny)
+    return _half_rows_to_spatial(desc, half_rows * wr[None, :, None])
+
+
+def flux_vjp(desc, Ap, Am, A0, t, t0, Fpb, Fmb, F0b):
+    """Adjoint of nonlinear_flux: returns (Apb, Amb, A0b) with
+    <(Fpb, Fmb, F0b), dF> = <(Apb, Amb, A0b), dA> for every perturbation dA."""
+    c = desc.c
+    a = desc.arrays
+    p = phase(desc, t, t0)
+    targets = (0, 1, 3) if c.isHydrostatic else (0, 1, 2, 3)
+    ccos, csin, csinm, ccosm = _inverse_matrices(desc)
+    fcos, fsin = _forward_matrices(desc)
+    kC = desc.k[:, None]
+    lC = desc.l[:, None]
+    vort, buoyF, na0, apmn = a["A0FromVorticity"], a["A0FromBuoyancy"], a["NA0"], a["ApmN"]
+    cpb = Fpb * p
+    cmb = Fmb * np.conj(p)
+    a0b = F0b
+    # recomputed forward fields
+    U, V, W = velocity_fields(desc, Ap, Am, A0, t, t0)
+    fb = {f: np.zeros_like(Ap) for f in range(4)}  # field-value adjoints u, v, w, eta (WV frame, j space)
+    grad_U = np.zeros_like(U)
+    grad_V = np.zeros_like(V)
+    grad_W = np.zeros_like(W)
+    for q in targets:
+        # projection adjoint -> value bar (Nkl, Nj)
+        wave_b = cpb + cmb
+        buoy_b = cpb - cmb
+        bv_b = buoy_b * apmn
+        A0c_b = a0b - na0 * bv_b
+        vb = np.zeros_like(Ap)
+        if q == 3:
+            vb = vb + bv_b
+        if q == 0:
+            vb = vb + (1j * lC) * vort * A0c_b
+        elif q == 1:
+            vb = vb + (-1j * kC) * vort * A0c_b
+        elif q == 3:
+            vb = vb + buoyF * A0c_b
+        if c.isHydrostatic:
+            if q == 0:
+                vb = vb + (-1j * kC) * np.conj(a["ApmD"]) * wave_b
+            elif q == 1:
+                vb = vb + (-1j * lC) * np.conj(a["ApmD"]) * wave_b
+        else:
+            if q == 0:
+                vb = vb + (desc.cosAlpha[:, None] * a["ApmDScaled"]) * wave_b
+            elif q == 1:
+                vb = vb + (desc.sinAlpha[:, None] * a["ApmDScaled"]) * wave_b
+            elif q == 2:
+                sc = (desc.Kh[:, None] / 2.0) * desc.apmWProjectionPrefactor[None, :]
+                vb = vb + (-1j * sc) * wave_b
+        # inertial mode (WV index 0): contributions overridden
+        sc0 = desc.inertialScale
+        tot = cpb[0] + np.conj(cmb[0])
+        v0 = np.zeros(c.Nj, np.complex128)
+        if q == 0:
+            v0 = sc0 * tot
+        elif q == 1:
+            v0 = (1j * sc0) * tot
+        if q == 3:
+            v0 = v0 + buoyF[0] * a0b[0]
+        vb[0] = v0
+        # forward vertical adjoint: (Nkl, Nj) -> (Nkl, Nz)
+        F = fcos if q < 2 else fsin
+        col_b = vb @ F
+        # scatter to stored rows (conjugated storage), then adjoint of r2c -> S bar
+        half = np.zeros((1, c.Ny * desc.NxHalf, c.Nz), np.complex128)
+        half[0, desc.storageRow, :] = np.where(desc.conjugated[:, None], np.conj(col_b), col_b)
+        Sb = _r2c_adjoint(desc, half)[0]
+        # products adjoint with the recomputed forward derivative fields
+        dx, dy, dz = derivative_fields(desc, Ap, Am, A0, t, t0, q)
+        grad_U -= Sb * dx
+        grad_V -= Sb * dy
+        grad_W -= Sb * dz
+        gx, gy, gz = -Sb * U, -Sb * V, -Sb * W
+        hb = _c2r_adjoint(desc, np.stack([gx, gy, gz]))
+        cx_ = _rows_to_columns_adjoint(desc, hb[0])
+        cy_ = _rows_to_columns_adjoint(desc, hb[1])
+        cz_ = _rows_to_columns_adjoint(desc, hb[2])
+        Cv = ccos if q < 2 else csin
+        Cz = csinm if q < 2 else ccosm
+        fb[q] = fb[q] + (-1j * kC) * (cx_ @ Cv) + (-1j * lC) * (cy_ @ Cv) + cz_ @ Cz
+    # advecting velocity adjoints
+    hb = _c2r_adjoint(desc, np.stack([grad_U, grad_V, grad_W]))
+    fb[0] = fb[0] + _rows_to_columns_adjoint(desc, hb[0]) @ ccos
+    fb[1] = fb[1] + _rows_to_columns_adjoint(desc, hb[1]) @ ccos
+    fb[2] = fb[2] + _rows_to_columns_adjoint(desc, hb[2]) @ csin
+    return _assembly_adjoint(desc, fb[0], fb[1], fb[2], fb[3], p)
+
+
+def _assembly_adjoint(desc, ub, vb, wb, nb, p):
+    """Adjoint of _field_values (coefficientValueForField on evolved coefficients)."""
+    a = desc.arrays
+    Apeb = np.conj(a["UAp"]) * ub + np.conj(a["VAp"]) * vb + np.conj(a["WAp"]) * wb + a["NAp"] * nb
+    Ameb = a["UAp"] * ub + a["VAp"] * vb + np.conj(a["WAp"]) * wb - a["NAp"] * nb
+    A0b = np.conj(a["UA0"]) * ub + np.conj(a["VA0"]) * vb + a["NA0"] * nb
+    return Apeb * np.conj(p), Ameb * p, A0b
+
+
+def inverse_vjp(desc, t, t0, fields_bar):
+    """Adjoint of inverse_uvweta: fields_bar (4, Nz, Ny, Nx) -> (Apb, Amb, A0b)."""
+    ccos, csin, _, _ = _inverse_matrices(desc)
+    p = phase(desc, t, t0)
+    hb = _c2r_adjoint(desc, fields_bar)
+    ub = _rows_to_columns_adjoint(desc, hb[0]) @ ccos
+    vb = _rows_to_columns_adjoint(desc, hb[1]) @ ccos
+    wb = _rows_to_columns_adjoint(desc, hb[2]) @ csin
+    nb = _rows_to_columns_adjoint(desc, hb[3]) @ csin
+    return _assembly_adjoint(desc, ub, vb, wb, nb, p)
+
+
+def rk4_step_vjp(desc, Ap, Am, A0, t, t0, h, yb):
+    """Adjoint of rk4_step (no damping): given the cotangent of y_{n+1},
+    returns the cotangent of y_n.  Stage states are recomputed from y_n."""
+    y = (Ap, Am, A0)
+    k1 = nonlinear_flux(desc, *y, t, t0)
+    s2 = [y[i] + (0.5 * h) * k1[i] for i in range(3)]
+    k2 = nonlinear_flux(desc, *s2, t + 0.5 * h, t0)
+    s3 = [y[i] + (0.5 * h) * k2[i] for i in range(3)]
+    k3 = nonlinear_flux(desc, *s3, t + 0.5 * h, t0)
+    s4 = [y[i] + h * k3[i] for i in range(3)]
+    kb4 = [(h / 6.0) * x for x in yb]
+    kb3 = [(h / 3.0) * x for x in yb]
+    kb2 = [(h / 3.0) * x for x in yb]
+    kb1 = [(h / 6.0) * x for x in yb]
+    out = [x.copy() for x in yb]
+    sb = flux_vjp(desc, *s4, t + h, t0, *kb4)
+    out = [out[i] + sb[i] for i in range(3)]
+    kb3 = [kb3[i] + h * sb[i] for i in range(3)]
+    sb = flux_vjp(desc, *s3, t + 0.5 * h, t0, *kb3)
+    out = [out[i] + sb[i] for i in range(3)]
+    kb2 = [kb2[i] + (0.5 * h) * sb[i] for i in range(3)]
+    sb = flux_vjp(desc, *s2, t + 0.5 * h, t0, *kb2)
+    out = [out[i] + sb[i] for i in range(3)]
+    kb1 = [kb1[i] + (0.5 * h) * sb[i] for i in range(3)]
+    sb = flux_vjp(desc, *y, t, t0, *kb1)
+    return tuple(out[i] + sb[i] for i in range(3))
