@@ -183,6 +183,36 @@ int wv_forward_device(wv_handle* handle, const double* fields, double t, double 
                       double* Ap, double* Am, double* A0, void* stream);
 int wv_inverse_device(wv_handle* handle, double t, double t0,
                       const double* Ap, const double* Am, const double* A0, double* fields, void* stream);
+/* ---- adjoint (vector-Jacobian products) --------------------------------------------
+ * No counterpart in the reference.  For complex arrays the inner product is
+ * <a, b> = Re sum conj(a) b; a cotangent x_bar of an output x is mapped to the
+ * cotangent of the inputs such that <x_bar, dx> = <in_bar, d in> for every
+ * perturbation.  Device pointers, [Nj, Nkl] complex unless stated.  The first
+ * adjoint call on a handle allocates its adjoint workspace.  The nonlinear
+ * advection schedule only (adaptive damping's max|u_h| is not differentiable):
+ * handles with adaptive damping enabled return WV_UNSUPPORTED_OPERATION. */
+
+/* Flux VJP at state (Ap, Am, A0, t): (Fpb, Fmb, F0b) -> (Apb, Amb, A0b). */
+int wv_flux_vjp_device(wv_handle* handle, double t, double t0,
+                       const double* Ap, const double* Am, const double* A0,
+                       const double* Fpb, const double* Fmb, const double* F0b,
+                       double* Apb, double* Amb, double* A0b, void* stream);
+/* Inverse-transform VJP: fields_bar [Nx,Ny,Nz,4] -> (Apb, Amb, A0b). */
+int wv_inverse_vjp_device(wv_handle* handle, double t, double t0, const double* fields_bar,
+                          double* Apb, double* Amb, double* A0b, void* stream);
+/* One RK4 step's VJP at state (Ap, Am, A0, t): (Apb, Amb, A0b) hold the cotangent
+ * of the state after the step on entry and of the state before it on return.
+ * The stage states are recomputed. */
+int wv_rk4_step_vjp_device(wv_handle* handle, const double* Ap, const double* Am, const double* A0,
+                           double t, double t0, double dt, double* Apb, double* Amb, double* A0b, void* stream);
+/* Adjoint of n_steps RK4 steps from state (Ap, Am, A0, t): a forward pass keeps
+ * a checkpoint every checkpoint_every steps, each segment is recomputed from its
+ * checkpoint and stepped backward.  (Apb, Amb, A0b): cotangent at t + n_steps*dt
+ * on entry, at t on return. */
+int wv_rk4_adjoint_device(wv_handle* handle, const double* Ap, const double* Am, const double* A0,
+                          double t, double t0, double dt, int n_steps, int checkpoint_every,
+                          double* Apb, double* Amb, double* A0b, void* stream);
+
 /* Nonlinear flux that allocates no device memory.  No counterpart in the
  * reference: the reference's kernel owns a heap scratch arena.  It exists for
  * callers that cannot call cudaMalloc at the point where they need a flux

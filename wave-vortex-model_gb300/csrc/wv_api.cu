@@ -10,6 +10,7 @@
 #include "wv_kernels.cuh"
 #include "wv_plan.hpp"
 #include "wv_warpfft.cuh"
+#include "wv_adjoint.cuh"
 
 #include <cuda_runtime.h>
 
@@ -53,6 +54,19 @@ struct wv_handle {
     double* acc = nullptr;
     double* fields = nullptr;  // [4][R] doubles
     bool hasDamping = false;
+    // adjoint workspace (allocated on the first adjoint call)
+    bool adjointReady = false;
+    void* zadj = nullptr;   // [nt][z][pos]
+    void* yadj = nullptr;   // [z][nt][y][kx]
+    void* yout = nullptr;   // [z][4+2nt][y][kx]
+    void* fadj = nullptr;   // [4+2nt][z][pos]
+    double* st[4] = {};     // RK4 stage states (st[1..3]) for the step adjoint
+    double* kb = nullptr;
+    double* sb = nullptr;
+    double* ybacc = nullptr;
+    double* ybin = nullptr;
+    std::vector<double*> checkpoints;  // multi-step adjoint: saved states
+    std::vector<double*> segment;      // multi-step adjoint: states of one segment
     bool instrument = false;
     cudaEvent_t ev[6] = {};
     wv_stage_times stages{};
@@ -388,6 +402,126 @@ cudaError_t launch_forward(wv_handle* h, const double* fields, double t, double 
     return cudaGetLastError();
 }
 
+// ---- adjoint ------------------------------------------------------------------------
+
+template <typename T>
+size_t smem_vfwd_adj(const Plan& p) { return p.targets.count * p.Nj * dev::kVfwdModes * sizeof(dev::cx<T>); }
+template <typename T>
+size_t smem_xadj(const Plan& p) {
+    const size_t nt = p.targets.count, L = x_len(p), nIn = 4 + 2 * nt, nReal = 3 + 3 * nt;
+    return (L + p.Nx + (nIn + nt) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (2 * nReal + nt) * p.Nx * sizeof(T);
+}
+template <typename T>
+size_t smem_xr2c_adj(const Plan& p) { return (x_len(p) + p.Nx + 8 * x_len(p)) * sizeof(dev::cx<T>) + 4 * p.Nx * sizeof(T); }
+template <typename T>
+size_t smem_vinv_adj(const Plan& p, bool flux) {
+    return (flux ? 4 + p.targets.count : 4) * p.zHalf * dev::kVinvModes * sizeof(dev::cx2t<T>);
+}
+
+template <typename T>
+cudaError_t set_smem_limits_adj(const Plan& p) {
+    const size_t limit = 227 * 1024;
+    if (smem_xadj<T>(p) > limit || smem_vinv_adj<T>(p, true) > limit || smem_vfwd_adj<T>(p) > limit)
+        return cudaErrorInvalidConfiguration;
+    cudaError_t e;
+#define WV_SET(kernel, bytes)                                                                                   \
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)); \
+    if (e != cudaSuccess) return e;
+    WV_SET((dev::k_vfwd_adj<T>), smem_vfwd_adj<T>(p));
+    WV_SET((dev::k_xadj<T>), smem_xadj<T>(p));
+    WV_SET((dev::k_xr2c_adj<T>), smem_xr2c_adj<T>(p));
+    WV_SET((dev::k_vinv_adj<T, true>), smem_vinv_adj<T>(p, true));
+    WV_SET((dev::k_vinv_adj<T, false>), smem_vinv_adj<T>(p, false));
+#undef WV_SET
+    return cudaSuccess;
+}
+
+int ensure_adjoint(wv_handle* h) {
+    if (h->adjointReady) return WV_SUCCESS;
+    const Plan& p = h->plan;
+    const cudaError_t lim = h->precision == WV_PRECISION_FP64 ? set_smem_limits_adj<double>(p) : set_smem_limits_adj<float>(p);
+    if (lim == cudaErrorInvalidConfiguration)
+        return fail(h, WV_UNSUPPORTED_OPERATION, "The adjoint kernels need more shared memory than one CTA has for this grid.");
+    if (lim != cudaSuccess) return cuda_fail(h, lim, "adjoint set-up");
+    const size_t nt = p.targets.count, nIn = 4 + 2 * nt;
+    const size_t cb = 2 * elem_size(h->precision);
+    cudaError_t e = alloc(h, nt * p.Nz * p.positions * cb, &h->zadj);
+    if (e == cudaSuccess) e = alloc(h, p.Nz * nt * p.Ny * p.kxColumns * cb, &h->yadj);
+    if (e == cudaSuccess) e = alloc(h, p.Nz * nIn * p.Ny * p.kxColumns * cb, &h->yout);
+    if (e == cudaSuccess) e = alloc(h, nIn * p.Nz * p.positions * cb, &h->fadj);
+    const size_t stateBytes = 6 * p.M * sizeof(double);
+    void* tmp = nullptr;
+    for (int i = 1; i < 4 && e == cudaSuccess; ++i) { e = alloc(h, stateBytes, &tmp); h->st[i] = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->kb = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->sb = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->ybacc = static_cast<double*>(tmp); }
+    if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->ybin = static_cast<double*>(tmp); }
+    if (e != cudaSuccess) return cuda_fail(h, e, "adjoint workspace");
+    h->metrics.device_bytes = h->deviceBytes;
+    h->adjointReady = true;
+    return WV_SUCCESS;
+}
+
+// VJP of the nonlinear flux (no damping) at state A: (Fpb, Fmb, F0b) -> (Apb, Amb, A0b).
+template <typename T>
+cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                            const double* Fpb, const double* Fmb, const double* F0b, double* Apb, double* Amb, double* A0b,
+                            cudaStream_t s) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    const double elapsed = t - t0;
+    const int nt = p.targets.count, nIn = 4 + 2 * nt;
+    auto* z = static_cast<dev::cx<T>*>(h->zspec);
+    auto* y = static_cast<dev::cx<T>*>(h->yspec);
+    auto* za = static_cast<dev::cx<T>*>(h->zadj);
+    auto* ya = static_cast<dev::cx<T>*>(h->yadj);
+    auto* yo = static_cast<dev::cx<T>*>(h->yout);
+    auto* fa = static_cast<dev::cx<T>*>(h->fadj);
+    // forward fields of this state
+    dev::k_vinv<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, nullptr);
+    dev::YInvMap map{};
+    map.nOut = nIn;
+    for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
+    for (int t2 = 0; t2 < nt; ++t2) {
+        map.src[4 + t2] = p.targets.q[t2]; map.mulL[4 + t2] = 1;
+        map.src[4 + nt + t2] = 4 + t2;     map.mulL[4 + nt + t2] = 0;
+    }
+    launch_yinv<T>(h, map, z, y, s);
+    // adjoint of projection and forward vertical transform, then inverse y FFTs
+    dev::k_vfwd_adj<T><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd_adj<T>(p), s>>>(d, Fpb, Fmb, F0b, elapsed, za);
+    dev::YInvMap amap{};
+    amap.nOut = nt;
+    for (int c = 0; c < nt; ++c) { amap.src[c] = c; amap.mulL[c] = 0; }
+    launch_yinv<T>(h, amap, za, ya, s);
+    dev::k_xadj<T><<<dim3(p.Ny, p.Nz), 256, smem_xadj<T>(p), s>>>(d, y, ya, yo);
+    launch_yfwd<T>(h, yo, nIn, fa, s);
+    dev::k_vinv_adj<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
+    h->metrics.kernel_launches += 7;
+    return cudaGetLastError();
+}
+
+// VJP of the inverse transform: fields_bar [4][Nz][Ny][Nx] -> (Apb, Amb, A0b).
+template <typename T>
+cudaError_t launch_inverse_vjp(wv_handle* h, double t, double t0, const double* fb, double* Apb, double* Amb, double* A0b,
+                               cudaStream_t s) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    auto* ps = static_cast<dev::cx<T>*>(h->pspec);
+    auto* fa = static_cast<dev::cx<T>*>(h->fadj);
+    dev::k_xr2c_adj<T><<<dim3(p.Ny, p.Nz), 256, smem_xr2c_adj<T>(p), s>>>(d, fb, 4, ps);
+    launch_yfwd<T>(h, ps, 4, fa, s);
+    dev::k_vinv_adj<T, false><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv_adj<T>(p, false), s>>>(d, fa, 4, t - t0, Apb, Amb, A0b);
+    h->metrics.kernel_launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t flux_vjp_any(wv_handle* h, double t, double t0, const double* y, const double* yb, double* out, cudaStream_t s) {
+    const size_t M2 = 2 * h->plan.M;
+    return h->precision == WV_PRECISION_FP64
+               ? launch_flux_vjp<double>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s)
+               : launch_flux_vjp<float>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s);
+}
+
 cudaError_t flux_any(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
                      double* Fm, double* F0, bool damping, cudaStream_t s) {
     return h->precision == WV_PRECISION_FP64 ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s)
@@ -423,6 +557,38 @@ cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t 
     h->metrics.kernel_launches += 5;
     h->metrics.rk4_steps += 1;
     h->metrics.rhs_evaluations += 4;
+    return cudaGetLastError();
+}
+
+// Adjoint of WVFixedStepRK4::step at state y (contiguous [3][M] complex): yb is
+// the cotangent of the state after the step; on return h->ybacc holds the
+// cotangent before the step.  Stage states are recomputed from y.
+cudaError_t rk4_step_vjp(wv_handle* h, const double* y, double t, double t0, double dt, const double* yb, cudaStream_t s) {
+    const size_t n = 6 * h->plan.M;
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
+    const size_t M2 = 2 * h->plan.M;
+    cudaError_t e;
+    auto flux = [&](const double* x, double tt) { return flux_any(h, tt, t0, x, x + M2, x + 2 * M2, h->kbuf, h->kbuf + M2, h->kbuf + 2 * M2, false, s); };
+    e = flux(y, t); if (e != cudaSuccess) return e;
+    dev::k_affine<<<grid, 256, 0, s>>>(y, h->kbuf, 0.5 * dt, h->st[1], n);
+    e = flux(h->st[1], t + 0.5 * dt); if (e != cudaSuccess) return e;
+    dev::k_affine<<<grid, 256, 0, s>>>(y, h->kbuf, 0.5 * dt, h->st[2], n);
+    e = flux(h->st[2], t + 0.5 * dt); if (e != cudaSuccess) return e;
+    dev::k_affine<<<grid, 256, 0, s>>>(y, h->kbuf, dt, h->st[3], n);
+    // backward through the stages
+    dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.0, nullptr, n);
+    e = flux_vjp_any(h, t + dt, t0, h->st[3], h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    dev::k_lincomb<<<grid, 256, 0, s>>>(h->ybacc, 1.0, yb, 1.0, h->sb, n);
+    dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, dt, h->sb, n);
+    e = flux_vjp_any(h, t + 0.5 * dt, t0, h->st[2], h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
+    dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, 0.5 * dt, h->sb, n);
+    e = flux_vjp_any(h, t + 0.5 * dt, t0, h->st[1], h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
+    dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.5 * dt, h->sb, n);
+    e = flux_vjp_any(h, t, t0, y, h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
+    h->metrics.kernel_launches += 11;
     return cudaGetLastError();
 }
 
@@ -936,6 +1102,134 @@ int wv_rk4_steps(wv_handle* h, double* Ap, double* Am, double* A0, double* t, do
     if (e != cudaSuccess) return cuda_fail(h, e, "RK4");
     *t = tt;
     return WV_SUCCESS;
+}
+
+
+// ---- adjoint entry points --------------------------------------------------------------
+
+static int adjoint_preamble(wv_handle* h) {
+    if (h->forcing & WV_FORCING_ADAPTIVE_DAMPING)
+        return fail(h, WV_UNSUPPORTED_OPERATION, "The adjoint covers the nonlinear advection schedule; disable adaptive damping.");
+    cudaSetDevice(h->device);
+    return ensure_adjoint(h);
+}
+
+int wv_flux_vjp_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                       const double* Fpb, const double* Fmb, const double* F0b, double* Apb, double* Amb, double* A0b,
+                       void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    const void* ptrs[] = {Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b};
+    for (const void* q : ptrs) if (!q) return fail(h, WV_INVALID_POINTER, "Flux VJP received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    rc = adjoint_preamble(h); if (rc) return rc;
+    auto s = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64
+        ? launch_flux_vjp<double>(h, t, t0, Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b, s)
+        : launch_flux_vjp<float>(h, t, t0, Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b, s);
+    return finish(h, e, "flux VJP");
+}
+
+int wv_inverse_vjp_device(wv_handle* h, double t, double t0, const double* fb, double* Apb, double* Amb, double* A0b,
+                          void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!fb || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "Inverse VJP received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    rc = ensure_adjoint(h); if (rc) return rc;
+    auto s = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64 ? launch_inverse_vjp<double>(h, t, t0, fb, Apb, Amb, A0b, s)
+                                                            : launch_inverse_vjp<float>(h, t, t0, fb, Apb, Amb, A0b, s);
+    return finish(h, e, "inverse VJP");
+}
+
+static cudaError_t gather3(wv_handle* h, double* dst, const double* a, const double* b, const double* c, cudaStream_t s) {
+    const size_t cb = h->plan.M * 16;
+    const double* src[] = {a, b, c};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(dst) + i * cb, src[i], cb, cudaMemcpyDeviceToDevice, s);
+    return e;
+}
+static cudaError_t scatter3(wv_handle* h, const double* src, double* a, double* b, double* c, cudaStream_t s) {
+    const size_t cb = h->plan.M * 16;
+    double* dst[] = {a, b, c};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i)
+        e = cudaMemcpyAsync(dst[i], reinterpret_cast<const char*>(src) + i * cb, cb, cudaMemcpyDeviceToDevice, s);
+    return e;
+}
+
+int wv_rk4_step_vjp_device(wv_handle* h, const double* Ap, const double* Am, const double* A0, double t, double t0, double dt,
+                           double* Apb, double* Amb, double* A0b, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "RK4 VJP received a null pointer.");
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "RK4 stepping is not reentrant.");
+    rc = adjoint_preamble(h); if (rc) return rc;
+    auto s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = gather3(h, h->state, Ap, Am, A0, s);
+    if (e == cudaSuccess) e = gather3(h, h->ybin, Apb, Amb, A0b, s);
+    if (e == cudaSuccess) e = rk4_step_vjp(h, h->state, t, t0, dt, h->ybin, s);
+    if (e == cudaSuccess) e = scatter3(h, h->ybacc, Apb, Amb, A0b, s);
+    return finish(h, e, "RK4 VJP");
+}
+
+int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, const double* A0, double t, double t0, double dt,
+                          int n, int K, double* Apb, double* Amb, double* A0b, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "RK4 adjoint received a null pointer.");
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
+    if (n < 0 || K < 1) return fail(h, WV_INVALID_CONFIGURATION, "Step count must be nonnegative and the checkpoint interval positive.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "RK4 stepping is not reentrant.");
+    rc = adjoint_preamble(h); if (rc) return rc;
+    auto s = static_cast<cudaStream_t>(stream);
+    const size_t stateBytes = 6 * h->plan.M * sizeof(double);
+    const int ncp = (n + K - 1) / K;
+    cudaError_t e = cudaSuccess;
+    void* tmp = nullptr;
+    while (static_cast<int>(h->checkpoints.size()) < ncp && e == cudaSuccess) {
+        e = alloc(h, stateBytes, &tmp);
+        h->checkpoints.push_back(static_cast<double*>(tmp));
+    }
+    while (static_cast<int>(h->segment.size()) < K && e == cudaSuccess) {
+        e = alloc(h, stateBytes, &tmp);
+        h->segment.push_back(static_cast<double*>(tmp));
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "RK4 adjoint checkpoints");
+    h->metrics.device_bytes = h->deviceBytes;
+    // forward pass with checkpoints; times exactly as WVFixedStepRK4 advances them
+    std::vector<double> times(n + 1);
+    times[0] = t;
+    e = gather3(h, h->state, Ap, Am, A0, s);
+    for (int i = 0; i < n && e == cudaSuccess; ++i) {
+        if (i % K == 0) e = cudaMemcpyAsync(h->checkpoints[i / K], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = rk4_step(h, times[i], t0, dt, s);
+        times[i + 1] = times[i] + dt;
+    }
+    if (e == cudaSuccess) e = gather3(h, h->ybin, Apb, Amb, A0b, s);
+    // backward, one segment at a time
+    for (int seg = ncp - 1; seg >= 0 && e == cudaSuccess; --seg) {
+        const int first = seg * K, last = std::min(n, first + K);
+        e = cudaMemcpyAsync(h->state, h->checkpoints[seg], stateBytes, cudaMemcpyDeviceToDevice, s);
+        for (int i = first; i < last && e == cudaSuccess; ++i) {
+            e = cudaMemcpyAsync(h->segment[i - first], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess && i + 1 < last) e = rk4_step(h, times[i], t0, dt, s);
+        }
+        for (int i = last - 1; i >= first && e == cudaSuccess; --i) {
+            e = rk4_step_vjp(h, h->segment[i - first], times[i], t0, dt, h->ybin, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(h->ybin, h->ybacc, stateBytes, cudaMemcpyDeviceToDevice, s);
+        }
+    }
+    if (e == cudaSuccess) e = scatter3(h, h->ybin, Apb, Amb, A0b, s);
+    return finish(h, e, "RK4 adjoint");
 }
 
 // Flux on the static scratch array: no cudaMalloc, cudaFree or allocating

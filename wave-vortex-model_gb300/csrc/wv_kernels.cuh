@@ -881,3 +881,19 @@ __global__ void k_accumulate_and_stage(double* __restrict__ acc, const double* _
 
 }  // namespace dev
 }  // namespace wvgpu
+
+namespace wvgpu {
+namespace dev {
+// out = a*x + b*y (y may be null); n doubles
+__global__ void k_lincomb(double* __restrict__ out, double a, const double* __restrict__ x, double b,
+                          const double* __restrict__ y, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = y ? a * x[i] + b * y[i] : a * x[i];
+}
+// out += x
+__global__ void k_accumulate(double* __restrict__ out, const double* __restrict__ x, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] += x[i];
+}
+}  // namespace dev
+}  // namespace wvgpu

@@ -144,6 +144,10 @@ def load_library():
     lib.wv_inverse_device.argtypes = [P, D, D, P, P, P, P, P]
     lib.wv_rk4_steps.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int]
     lib.wv_rk4_steps_device.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int, P]
+    lib.wv_flux_vjp_device.argtypes = [P, D, D, P, P, P, P, P, P, P, P, P, P]
+    lib.wv_inverse_vjp_device.argtypes = [P, D, D, P, P, P, P, P]
+    lib.wv_rk4_step_vjp_device.argtypes = [P, P, P, P, D, D, D, P, P, P, P]
+    lib.wv_rk4_adjoint_device.argtypes = [P, P, P, P, D, D, D, ctypes.c_int, ctypes.c_int, P, P, P, P]
     _lib = lib
     return lib
 
@@ -153,7 +157,8 @@ def exported_symbols():
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
-            "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc"]
+            "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc", "wv_flux_vjp_device",
+            "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device"]
 
 
 def describe(configuration: Configuration):
@@ -339,6 +344,41 @@ class WVTransformConstantStratificationKernel:
         self._check(self._lib.wv_rk4_steps(self._h, Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data, ctypes.byref(tt),
                                            float(t0), float(dt), int(steps)))
         return Ap, Am, A0, tt.value
+
+    # -- adjoint (torch CUDA tensors) ---------------------------------------------------
+    def flux_vjp(self, t, t0, Ap, Am, A0, Fpb, Fmb, F0b):
+        """VJP of nonlinearFlux at (Ap, Am, A0): cotangents (Apb, Amb, A0b)."""
+        import torch
+        ins = [self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0, Fpb, Fmb, F0b), ("Ap", "Am", "A0", "Fpb", "Fmb", "F0b"))]
+        out = tuple(torch.empty_like(ins[0]) for _ in range(3))
+        self._check(self._lib.wv_flux_vjp_device(self._h, float(t), float(t0), *(x.data_ptr() for x in ins),
+                                                 *(o.data_ptr() for o in out), self._stream()))
+        return out
+
+    def inverse_vjp(self, t, t0, fields_bar):
+        """VJP of transformWaveVortexToUVWEta: fields cotangent (4, Nz, Ny, Nx) -> (Apb, Amb, A0b)."""
+        import torch
+        out = tuple(torch.empty(self.spectral_shape, dtype=torch.complex128, device=fields_bar.device) for _ in range(3))
+        self._check(self._lib.wv_inverse_vjp_device(self._h, float(t), float(t0), fields_bar.contiguous().data_ptr(),
+                                                    *(o.data_ptr() for o in out), self._stream()))
+        return out
+
+    def rk4_step_vjp(self, Ap, Am, A0, t, t0, dt, Apb, Amb, A0b):
+        """Cotangent before one RK4 step from the cotangent after it (returns new tensors)."""
+        ins = [self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0"))]
+        out = [self._dev_coeff(a, n).clone() for a, n in zip((Apb, Amb, A0b), ("Apb", "Amb", "A0b"))]
+        self._check(self._lib.wv_rk4_step_vjp_device(self._h, *(x.data_ptr() for x in ins), float(t), float(t0), float(dt),
+                                                     *(o.data_ptr() for o in out), self._stream()))
+        return tuple(out)
+
+    def rk4_adjoint(self, Ap, Am, A0, t, t0, dt, steps, checkpoint_every, Apb, Amb, A0b):
+        """Cotangent at t of the state, given the cotangent at t + steps*dt (checkpointed recomputation)."""
+        ins = [self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0"))]
+        out = [self._dev_coeff(a, n).clone() for a, n in zip((Apb, Amb, A0b), ("Apb", "Amb", "A0b"))]
+        self._check(self._lib.wv_rk4_adjoint_device(self._h, *(x.data_ptr() for x in ins), float(t), float(t0), float(dt),
+                                                    int(steps), int(checkpoint_every), *(o.data_ptr() for o in out),
+                                                    self._stream()))
+        return tuple(out)
 
     def setStageInstrumentation(self, enabled):
         """setStageInstrumentation (kernel.cpp:570-581): per-stage device times."""
