@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     return ap.parse_args()
 
 
@@ -250,6 +251,113 @@ def _field_error_after(kd, km, state, dt, steps, torch, np):
     return [float(np.linalg.norm(f32[i] - f64[i]) / np.linalg.norm(f64[i])) for i in range(4)]
 
 
+def _adjoint_timing(wvgpu, precision, stream, torch, np, repeats=2):
+    """Gradient of a final-state misfit through 50 RK4 steps at 128x128x65
+    (400 km x 400 km x 4 km), checkpoints every 10 steps: device time of the
+    forward run against the checkpointed adjoint (forward pass with
+    checkpoints, per-segment recompute, backward sweep)."""
+    Nx, Ny, Nz, steps, K = 128, 128, 65, 50, 10
+    cfg = wvgpu.Configuration(Nx=Nx, Ny=Ny, Nz=Nz, Nj=(2 * (Nz - 1)) // 3, Lx=400e3, Ly=400e3, Lz=4000.0, latitude=33.0)
+    k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision=precision)
+    state = wvgpu.synthetic_state(k, seed=SEED, urms=URMS)
+    dt = wvgpu.cfl_time_step(k, *state)
+    dev0 = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+    # misfit cotangent (u, v, eta)(T) - target at a representative size; its value does not change the cost
+    target = wvgpu.synthetic_state(k, seed=SEED + 1, urms=URMS)
+    misfit = (k.transformWaveVortexToUVWEta(0.0, 0.0, *state) - k.transformWaveVortexToUVWEta(0.0, 0.0, *target))
+    misfit[2] = 0.0
+    yb = k.inverse_vjp(steps * dt, 0.0, torch.from_numpy(np.ascontiguousarray(misfit)).cuda())
+
+    def timed(fn):
+        best = float("inf")
+        for r in range(repeats + 1):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            if r > 0:
+                best = min(best, e0.elapsed_time(e1))
+        return best
+
+    fwd_ms = timed(lambda: k.rk4(*[x.clone() for x in dev0], 0.0, 0.0, dt, steps))
+    adj_ms = timed(lambda: k.rk4_adjoint(*dev0, 0.0, 0.0, dt, steps, K, *yb))
+    out = {"grid": [Nx, Ny, Nz], "steps": steps, "checkpoint_every": K, "dt_s": dt, "forward_ms": fwd_ms,
+           "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+           "device_bytes": k.metrics()["device_bytes"]}
+    k.close()
+    return out
+
+
+ENSEMBLE_GROUPS = [(64, 33), (128, 65), (192, 97)]
+ENSEMBLE_MEMBERS = 32
+
+
+def _ensemble_timing(wvgpu, stream, torch, np, steps=100, single_steps=20):
+    """96-member ensemble of uneven grids (32 each of 64x64x33, 128x128x65,
+    192x192x97; 3.125 km per grid point, Lz = 4 km), mixed precision.  Members
+    seeded independently from the bench spectrum at 0.05-0.2 m/s rms; each
+    group steps at the smallest CFL step of its members.  The ensemble's
+    `steps`-step integration is one CUDA-graph launch; the same members stepped
+    one at a time through single-state handles give the comparison rate."""
+    cfgs, singles, X, dts = [], [], [], []
+    seed = 1000
+    for Nx, Nz in ENSEMBLE_GROUPS:
+        cfg = wvgpu.Configuration(Nx=Nx, Ny=Nx, Nz=Nz, Nj=(2 * (Nz - 1)) // 3, Lx=3125.0 * Nx, Ly=3125.0 * Nx,
+                                  Lz=4000.0, latitude=33.0)
+        k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="mixed")
+        states, dd = [], []
+        for m in range(ENSEMBLE_MEMBERS):
+            A = wvgpu.synthetic_state(k, seed=seed, urms=0.05 + 0.15 * m / (ENSEMBLE_MEMBERS - 1))
+            seed += 1
+            dd.append(wvgpu.cfl_time_step(k, *A))
+            states.append(np.stack(A))
+        cfgs.append(cfg)
+        singles.append(k)
+        X.append(torch.from_numpy(np.ascontiguousarray(np.stack(states))).cuda())
+        dts.append(min(dd))
+    w0 = time.perf_counter()
+    ens = wvgpu.WVEnsemble(cfgs, [ENSEMBLE_MEMBERS] * len(cfgs), precision="mixed", autotune=True)
+    create_s = time.perf_counter() - w0
+    work = [x.clone() for x in X]
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    ens.rk4(work, 0.0, 0.0, dts, steps)  # capture + instantiate + first run
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - w0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ens.rk4(work, 0.0, 0.0, dts, steps)  # same key: replay of the instantiated graph
+    e1.record(stream)
+    e1.synchronize()
+    graph_ms = e0.elapsed_time(e1)
+    member_steps = steps * ENSEMBLE_MEMBERS * len(cfgs)
+    # the same members one at a time, single-state handles
+    single = [x.clone() for x in X]
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k, x, dt in zip(singles, single, dts):
+        for m in range(ENSEMBLE_MEMBERS):
+            k.rk4(x[m, 0], x[m, 1], x[m, 2], 0.0, 0.0, dt, single_steps)
+    e1.record(stream)
+    e1.synchronize()
+    single_ms = e0.elapsed_time(e1)
+    single_rate = single_steps * ENSEMBLE_MEMBERS * len(cfgs) / (single_ms * 1e-3)
+    out = {"members": [[Nx, Nx, Nz, ENSEMBLE_MEMBERS] for Nx, Nz in ENSEMBLE_GROUPS], "precision": "mixed",
+           "steps": steps, "dt_s": dts, "graph_launches_per_call": 1,
+           "value": member_steps / (graph_ms * 1e-3), "unit": "member RK4 steps/s", "ms": graph_ms,
+           "one_at_a_time": {"value": single_rate, "unit": "member RK4 steps/s", "steps": single_steps,
+                             "ms": single_ms},
+           "speedup_vs_one_at_a_time": member_steps / (graph_ms * 1e-3) / single_rate,
+           "first_call_s_with_capture": first_s, "create_s_with_autotune": create_s,
+           "tuning": ens.tuning(), "metrics": ens.metrics()}
+    ens.close()
+    for k in singles:
+        k.close()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -307,6 +415,8 @@ def run_ours(args):
     if rank == 0:
         mixed["rel_field_err_vs_fp64_after_100_steps"] = _field_error_after(k, km, state, dt, 100, torch, np)
     km.close()
+    adjoint = {p: _adjoint_timing(wvgpu, p, stream, torch, np) for p in ("fp64", "mixed")} if rank == 0 else None
+    ensemble = _ensemble_timing(wvgpu, stream, torch, np) if rank == 0 and not args.no_ensemble else None
 
     # end to end through the host-pointer C ABI, pinned host buffers
     host = [torch.empty(a.shape, dtype=torch.complex128, pin_memory=True).numpy() for a in state]
@@ -336,6 +446,8 @@ def run_ours(args):
         "gpu_launches": launches,
         "roofline": roofline,
         "mixed": mixed,
+        "adjoint": adjoint,
+        "ensemble": ensemble,
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

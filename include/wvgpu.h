@@ -238,6 +238,45 @@ int wv_nonlinear_flux_device_noalloc(wv_handle* handle, double t, double t0,
 int wv_rk4_steps_device(wv_handle* handle, double* Ap, double* Am, double* A0,
                         double* t, double t0, double dt, int n_steps, void* stream);
 
+/* ---- ensembles ------------------------------------------------------------------------
+ * No counterpart in the reference, which steps one state per kernel object
+ * (a caller would hold one WVTransformConstantStratificationKernel per member).
+ * An ensemble holds n_groups grids; group g steps members[g] states of
+ * configs[g] side by side (each stage kernel covers all members of the group in
+ * one launch).  wv_ensemble_rk4_device captures the n-step RK4 integration of
+ * every group (one stream per group) into one CUDA graph and launches it once;
+ * a later call with the same groups and step count updates the graph's
+ * parameters instead of capturing anew.  Nonlinear advection schedule.  With
+ * autotune set, creation times each group's flux with every FFT variant its grid
+ * has (warp-register or shared-memory Stockham, per axis) and keeps the fastest. */
+typedef struct wv_ensemble wv_ensemble;
+#define WV_ENSEMBLE_MAX_GROUPS 16
+typedef struct wv_ensemble_tuning {
+    int warp_y_available, warp_x_available;  /* variants the grid has */
+    int stockham_y, stockham_x;              /* chosen: 1 = Stockham, 0 = warp (where available) */
+    int candidates;                          /* variants timed */
+    float candidate_ms[4];                   /* flux time of each (y-major order), ms */
+    float flux_ms;                           /* chosen variant, ms per flux of the whole group */
+} wv_ensemble_tuning;
+typedef struct wv_ensemble_metrics {
+    uint64_t graph_captures, graph_instantiations, graph_updates, graph_launches;
+    uint64_t kernel_launches;                /* kernel nodes replayed */
+    uint64_t member_steps;
+    uint64_t device_bytes;
+} wv_ensemble_metrics;
+int wv_ensemble_create(const wv_config* configs, const int* members, int n_groups, int precision, int autotune,
+                       wv_ensemble** ensemble);
+void wv_ensemble_destroy(wv_ensemble* ensemble);
+const char* wv_ensemble_last_message(const wv_ensemble* ensemble);
+int wv_ensemble_get_sizes(const wv_ensemble* ensemble, int group, wv_sizes* sizes);  /* per member */
+int wv_ensemble_get_tuning(const wv_ensemble* ensemble, int group, wv_ensemble_tuning* tuning);
+int wv_ensemble_get_metrics(const wv_ensemble* ensemble, wv_ensemble_metrics* metrics);
+/* states[g]: device array [members[g]][3][Nkl][Nj] complex (each member's Ap, Am,
+ * A0 back to back), advanced in place.  t[g] (in/out) is group g's time and
+ * dt[g] its step; on return t[g] has advanced by n_steps steps of dt[g]. */
+int wv_ensemble_rk4_device(wv_ensemble* ensemble, double* const* states, double* t, double t0, const double* dt,
+                           int n_steps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

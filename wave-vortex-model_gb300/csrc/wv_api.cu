@@ -67,6 +67,7 @@ struct wv_handle {
     double* ybin = nullptr;
     std::vector<double*> checkpoints;  // multi-step adjoint: saved states
     std::vector<double*> segment;      // multi-step adjoint: states of one segment
+    std::vector<void*> ystore;         // multi-step adjoint: y spectra of each stage flux of one segment
     bool instrument = false;
     cudaEvent_t ev[6] = {};
     wv_stage_times stages{};
@@ -163,11 +164,25 @@ size_t smem_xr2c(const Plan& p) { return (x_len(p) + p.Nx + 8 * x_len(p)) * size
 template <typename T>
 size_t smem_vfwd(const Plan& p, int nch) { return nch * p.zHalf * dev::kVfwdModes * sizeof(dev::cx2t<T>); }
 
+// The dynamic shared-memory cap is a process-wide attribute of each kernel,
+// not of a handle: only ever raise it, so a handle created for a smaller grid
+// cannot shrink the cap below what a live handle for a larger grid launches with.
+std::mutex g_smem_mutex;
+template <typename K>
+cudaError_t raise_smem_limit(K* kernel, int bytes) {
+    std::lock_guard<std::mutex> lock(g_smem_mutex);
+    cudaFuncAttributes a{};
+    cudaError_t e = cudaFuncGetAttributes(&a, reinterpret_cast<const void*>(kernel));
+    if (e != cudaSuccess) return e;
+    if (a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 template <typename T>
 cudaError_t set_smem_limits(const Plan& p) {
     cudaError_t e;
 #define WV_SET(kernel, bytes)                                                                                   \
-    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)); \
+    e = raise_smem_limit(kernel, static_cast<int>(bytes)); \
     if (e != cudaSuccess) return e;
     WV_SET((dev::k_vinv<T, true>), smem_vinv<T>(p));
     WV_SET((dev::k_vinv<T, false>), smem_vinv<T>(p));
@@ -193,13 +208,13 @@ inline int warp_ry(const Plan& p) {
     // FP64 stays on the shared-memory radix-4 Stockham kernels: on the FP64 pipe
     // the radix-2 shuffle stages (64-bit shuffles, the twiddle product evaluated
     // in every lane) cost more than the smem round trips they replace.
-    if (sizeof(T) == 8 || p.Ny % 32 != 0) return 0;
+    if (sizeof(T) == 8 || p.stockhamY || p.Ny % 32 != 0) return 0;
     const int r = static_cast<int>(p.Ny / 32);
     return (r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8 || r == 16) ? r : 0;
 }
 template <typename T>
 inline int warp_rx(const Plan& p) {
-    if (sizeof(T) == 8 || p.Nx % 64 != 0) return 0;
+    if (sizeof(T) == 8 || p.stockhamX || p.Nx % 64 != 0) return 0;
     const int r = static_cast<int>(p.Nx / 64);
     const int rmax = sizeof(T) == 8 ? 4 : 8;  // register budget of the fused x row
     return ((r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8) && r <= rmax) ? r : 0;
@@ -246,17 +261,17 @@ cudaError_t set_smem_limits_w(const Plan& p) {
     cudaError_t e = cudaSuccess;
     const int ry = warp_ry<T>(p), rx = warp_rx<T>(p);
     WV_RSWITCH_Y(ry, {
-        e = cudaFuncSetAttribute(dev::k_yinv_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y_w<T>(p));
+        e = raise_smem_limit(dev::k_yinv_w<T, RR>, (int)smem_y_w<T>(p));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(dev::k_yfwd_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y_w<T>(p));
+            e = raise_smem_limit(dev::k_yfwd_w<T, RR>, (int)smem_y_w<T>(p));
     });
     if (e != cudaSuccess) return e;
     WV_RSWITCH_X(T, rx, {
-        e = cudaFuncSetAttribute(dev::k_xflux_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_xflux_w<T>(p));
+        e = raise_smem_limit(dev::k_xflux_w<T, RR>, (int)smem_xflux_w<T>(p));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(dev::k_xc2r_fields_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_xc2r_w<T>(p, 4));
+            e = raise_smem_limit(dev::k_xc2r_fields_w<T, RR>, (int)smem_xc2r_w<T>(p, 4));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(dev::k_xr2c_fields_w<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_xr2c_w<T>(p));
+            e = raise_smem_limit(dev::k_xr2c_fields_w<T, RR>, (int)smem_xr2c_w<T>(p));
     });
     return e;
 }
@@ -266,11 +281,11 @@ void launch_yinv(wv_handle* h, const dev::YInvMap& map, const dev::cx<T>* z, dev
     const Plan& p = h->plan;
     const int ry = warp_ry<T>(p);
     if (ry) {
-        const dim3 grid(cdiv(p.kxColumns, dev::kWG), p.Nz, map.nOut);
+        const dim3 grid(cdiv(p.kxColumns, dev::kWG), h->dd.zTotal, map.nOut);
         WV_RSWITCH_Y(ry, (dev::k_yinv_w<T, RR><<<grid, 256, smem_y_w<T>(p), s>>>(h->dd, map, z, y)));
         return;
     }
-    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz), 256, smem_y<T>(p), s>>>(h->dd, map, z, 0, y);
+    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), h->dd.zTotal), 256, smem_y<T>(p), s>>>(h->dd, map, z, 0, y);
 }
 
 template <typename T>
@@ -278,11 +293,11 @@ void launch_yfwd(wv_handle* h, const dev::cx<T>* ps, int nch, dev::cx<T>* f, cud
     const Plan& p = h->plan;
     const int ry = warp_ry<T>(p);
     if (ry) {
-        const dim3 grid(cdiv(p.kxColumns, dev::kWG), p.Nz, nch);
+        const dim3 grid(cdiv(p.kxColumns, dev::kWG), h->dd.zTotal, nch);
         WV_RSWITCH_Y(ry, (dev::k_yfwd_w<T, RR><<<grid, 256, smem_y_w<T>(p), s>>>(h->dd, ps, nch, f)));
         return;
     }
-    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), p.Nz, nch), 256, smem_y<T>(p), s>>>(h->dd, ps, nch, f);
+    dev::k_yfwd<T><<<dim3(cdiv(p.kxColumns, dev::kYG), h->dd.zTotal, nch), 256, smem_y<T>(p), s>>>(h->dd, ps, nch, f);
 }
 
 template <typename T>
@@ -290,11 +305,11 @@ void launch_xflux(wv_handle* h, const dev::cx<T>* y, dev::cx<T>* ps, unsigned lo
     const Plan& p = h->plan;
     const int rx = warp_rx<T>(p);
     if (rx) {
-        const dim3 grid(cdiv(p.Ny, dev::kWG), p.Nz);
+        const dim3 grid(cdiv(p.Ny, dev::kWG), h->dd.zTotal);
         WV_RSWITCH_X(T, rx, (dev::k_xflux_w<T, RR><<<grid, 256, smem_xflux_w<T>(p), s>>>(h->dd, y, ps, speed)));
         return;
     }
-    dev::k_xflux<T><<<dim3(p.Ny, p.Nz), 256, smem_xflux<T>(p), s>>>(h->dd, y, ps, speed);
+    dev::k_xflux<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xflux<T>(p), s>>>(h->dd, y, ps, speed);
 }
 
 template <typename T>
@@ -302,11 +317,11 @@ void launch_xc2r(wv_handle* h, const dev::cx<T>* y, double* fields, cudaStream_t
     const Plan& p = h->plan;
     const int rx = warp_rx<T>(p);
     if (rx) {
-        const dim3 grid(cdiv(p.Ny, dev::kWG), p.Nz);
+        const dim3 grid(cdiv(p.Ny, dev::kWG), h->dd.zTotal);
         WV_RSWITCH_X(T, rx, (dev::k_xc2r_fields_w<T, RR><<<grid, 256, smem_xc2r_w<T>(p, 4), s>>>(h->dd, y, 4, fields)));
         return;
     }
-    dev::k_xc2r_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xc2r<T>(p, 4), s>>>(h->dd, y, 4, fields);
+    dev::k_xc2r_fields<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xc2r<T>(p, 4), s>>>(h->dd, y, 4, fields);
 }
 
 template <typename T>
@@ -314,28 +329,30 @@ void launch_xr2c(wv_handle* h, const double* fields, int nch, dev::cx<T>* ps, cu
     const Plan& p = h->plan;
     const int rx = warp_rx<T>(p);
     if (rx) {
-        const dim3 grid(cdiv(p.Ny, dev::kWG), p.Nz);
+        const dim3 grid(cdiv(p.Ny, dev::kWG), h->dd.zTotal);
         WV_RSWITCH_X(T, rx, (dev::k_xr2c_fields_w<T, RR><<<grid, 256, smem_xr2c_w<T>(p), s>>>(h->dd, fields, nch, ps)));
         return;
     }
-    dev::k_xr2c_fields<T><<<dim3(p.Ny, p.Nz), 256, smem_xr2c<T>(p), s>>>(h->dd, fields, nch, ps);
+    dev::k_xr2c_fields<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xr2c<T>(p), s>>>(h->dd, fields, nch, ps);
 }
 
 // One nonlinear flux (+ adaptive damping when requested) on device buffers.
+// yOut, when given, receives the y spectra of the 4+2nt channels (the x pass
+// input) in place of the handle's scratch, for the adjoint to reuse.
 template <typename T>
 cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
-                        double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s) {
+                        double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s, void* yOut = nullptr) {
     const Plan& p = h->plan;
     const auto& d = h->dd;
     const double elapsed = t - t0;
     auto* z = static_cast<dev::cx<T>*>(h->zspec);
-    auto* y = static_cast<dev::cx<T>*>(h->yspec);
+    auto* y = static_cast<dev::cx<T>*>(yOut ? yOut : h->yspec);
     auto* ps = static_cast<dev::cx<T>*>(h->pspec);
     auto* f = static_cast<dev::cx<T>*>(h->fspec);
     const int nt = p.targets.count;
     const bool inst = h->instrument;
     if (inst) cudaEventRecord(h->ev[0], s);
-    dev::k_vinv<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, h->maxSpeed);
+    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, h->maxSpeed);
     if (inst) cudaEventRecord(h->ev[1], s);
     dev::YInvMap map{};
     map.nOut = 4 + 2 * nt;
@@ -350,7 +367,7 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     if (inst) cudaEventRecord(h->ev[3], s);
     launch_yfwd<T>(h, ps, nt, f, s);
     if (inst) cudaEventRecord(h->ev[4], s);
-    dev::k_vfwd<T, true><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nt), s>>>(
+    dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
         d, f, nt, elapsed, Ap, Am, A0, h->maxSpeed, damping ? 1 : 0, Fp, Fm, F0);
     h->metrics.kernel_launches += 5;
     cudaError_t e = cudaGetLastError();
@@ -376,7 +393,7 @@ cudaError_t launch_inverse(wv_handle* h, double t, double t0, const double* Ap, 
     const auto& d = h->dd;
     auto* z = static_cast<dev::cx<T>*>(h->zspec);
     auto* y = static_cast<dev::cx<T>*>(h->yspec);
-    dev::k_vinv<T, false><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, t - t0, z, nullptr);
+    dev::k_vinv<T, false><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, t - t0, z, nullptr);
     dev::YInvMap map{};
     map.nOut = 4;
     for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
@@ -396,7 +413,7 @@ cudaError_t launch_forward(wv_handle* h, const double* fields, double t, double 
     auto* f = static_cast<dev::cx<T>*>(h->fspec);
     launch_xr2c<T>(h, fields, nch, ps, s);
     launch_yfwd<T>(h, ps, nch, f, s);
-    dev::k_vfwd<T, false><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nch), s>>>(
+    dev::k_vfwd<T, false><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nch), s>>>(
         d, f, nch, t - t0, nullptr, nullptr, nullptr, nullptr, 0, Ap, Am, A0);
     h->metrics.kernel_launches += 3;
     return cudaGetLastError();
@@ -425,7 +442,7 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
         return cudaErrorInvalidConfiguration;
     cudaError_t e;
 #define WV_SET(kernel, bytes)                                                                                   \
-    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)); \
+    e = raise_smem_limit(kernel, static_cast<int>(bytes)); \
     if (e != cudaSuccess) return e;
     WV_SET((dev::k_vfwd_adj<T>), smem_vfwd_adj<T>(p));
     WV_SET((dev::k_xadj<T>), smem_xadj<T>(p));
@@ -463,40 +480,57 @@ int ensure_adjoint(wv_handle* h) {
 }
 
 // VJP of the nonlinear flux (no damping) at state A: (Fpb, Fmb, F0b) -> (Apb, Amb, A0b).
+// y spectra of the 4+2nt flux input channels at state A (the first two
+// stages of the flux) into y.
 template <typename T>
-cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
-                            const double* Fpb, const double* Fmb, const double* F0b, double* Apb, double* Amb, double* A0b,
-                            cudaStream_t s) {
+void launch_flux_fields(wv_handle* h, double elapsed, const double* Ap, const double* Am, const double* A0, dev::cx<T>* y,
+                        cudaStream_t s) {
     const Plan& p = h->plan;
     const auto& d = h->dd;
-    const double elapsed = t - t0;
-    const int nt = p.targets.count, nIn = 4 + 2 * nt;
+    const int nt = p.targets.count;
     auto* z = static_cast<dev::cx<T>*>(h->zspec);
-    auto* y = static_cast<dev::cx<T>*>(h->yspec);
-    auto* za = static_cast<dev::cx<T>*>(h->zadj);
-    auto* ya = static_cast<dev::cx<T>*>(h->yadj);
-    auto* yo = static_cast<dev::cx<T>*>(h->yout);
-    auto* fa = static_cast<dev::cx<T>*>(h->fadj);
-    // forward fields of this state
-    dev::k_vinv<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, nullptr);
+    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, nullptr);
     dev::YInvMap map{};
-    map.nOut = nIn;
+    map.nOut = 4 + 2 * nt;
     for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
     for (int t2 = 0; t2 < nt; ++t2) {
         map.src[4 + t2] = p.targets.q[t2]; map.mulL[4 + t2] = 1;
         map.src[4 + nt + t2] = 4 + t2;     map.mulL[4 + nt + t2] = 0;
     }
     launch_yinv<T>(h, map, z, y, s);
+    h->metrics.kernel_launches += 2;
+}
+
+// yIn, when given, holds the y spectra of the flux input channels at this
+// state (kept by the forward flux); otherwise they are recomputed.
+template <typename T>
+cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                            const double* Fpb, const double* Fmb, const double* F0b, double* Apb, double* Amb, double* A0b,
+                            cudaStream_t s, const void* yIn = nullptr) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    const double elapsed = t - t0;
+    const int nt = p.targets.count, nIn = 4 + 2 * nt;
+    auto* za = static_cast<dev::cx<T>*>(h->zadj);
+    auto* ya = static_cast<dev::cx<T>*>(h->yadj);
+    auto* yo = static_cast<dev::cx<T>*>(h->yout);
+    auto* fa = static_cast<dev::cx<T>*>(h->fadj);
+    // forward fields of this state
+    const dev::cx<T>* y = static_cast<const dev::cx<T>*>(yIn);
+    if (!y) {
+        launch_flux_fields<T>(h, elapsed, Ap, Am, A0, static_cast<dev::cx<T>*>(h->yspec), s);
+        y = static_cast<const dev::cx<T>*>(h->yspec);
+    }
     // adjoint of projection and forward vertical transform, then inverse y FFTs
-    dev::k_vfwd_adj<T><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd_adj<T>(p), s>>>(d, Fpb, Fmb, F0b, elapsed, za);
+    dev::k_vfwd_adj<T><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd_adj<T>(p), s>>>(d, Fpb, Fmb, F0b, elapsed, za);
     dev::YInvMap amap{};
     amap.nOut = nt;
     for (int c = 0; c < nt; ++c) { amap.src[c] = c; amap.mulL[c] = 0; }
     launch_yinv<T>(h, amap, za, ya, s);
     dev::k_xadj<T><<<dim3(p.Ny, p.Nz), 256, smem_xadj<T>(p), s>>>(d, y, ya, yo);
     launch_yfwd<T>(h, yo, nIn, fa, s);
-    dev::k_vinv_adj<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
-    h->metrics.kernel_launches += 7;
+    dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
+    h->metrics.kernel_launches += 5;
     return cudaGetLastError();
 }
 
@@ -510,22 +544,31 @@ cudaError_t launch_inverse_vjp(wv_handle* h, double t, double t0, const double* 
     auto* fa = static_cast<dev::cx<T>*>(h->fadj);
     dev::k_xr2c_adj<T><<<dim3(p.Ny, p.Nz), 256, smem_xr2c_adj<T>(p), s>>>(d, fb, 4, ps);
     launch_yfwd<T>(h, ps, 4, fa, s);
-    dev::k_vinv_adj<T, false><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv_adj<T>(p, false), s>>>(d, fa, 4, t - t0, Apb, Amb, A0b);
+    dev::k_vinv_adj<T, false><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv_adj<T>(p, false), s>>>(d, fa, 4, t - t0, Apb, Amb, A0b);
     h->metrics.kernel_launches += 3;
     return cudaGetLastError();
 }
 
-cudaError_t flux_vjp_any(wv_handle* h, double t, double t0, const double* y, const double* yb, double* out, cudaStream_t s) {
+cudaError_t flux_vjp_any(wv_handle* h, double t, double t0, const double* y, const double* yb, double* out, cudaStream_t s,
+                         const void* yIn = nullptr) {
     const size_t M2 = 2 * h->plan.M;
     return h->precision == WV_PRECISION_FP64
-               ? launch_flux_vjp<double>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s)
-               : launch_flux_vjp<float>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s);
+               ? launch_flux_vjp<double>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, yIn)
+               : launch_flux_vjp<float>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, yIn);
 }
 
 cudaError_t flux_any(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
-                     double* Fm, double* F0, bool damping, cudaStream_t s) {
-    return h->precision == WV_PRECISION_FP64 ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s)
-                                             : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s);
+                     double* Fm, double* F0, bool damping, cudaStream_t s, void* yOut = nullptr) {
+    return h->precision == WV_PRECISION_FP64 ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, yOut)
+                                             : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, yOut);
+}
+
+void flux_fields_any(wv_handle* h, double t, double t0, const double* y, void* yOut, cudaStream_t s) {
+    const size_t M2 = 2 * h->plan.M;
+    if (h->precision == WV_PRECISION_FP64)
+        launch_flux_fields<double>(h, t - t0, y, y + M2, y + 2 * M2, static_cast<dev::cx<double>*>(yOut), s);
+    else
+        launch_flux_fields<float>(h, t - t0, y, y + M2, y + 2 * M2, static_cast<dev::cx<float>*>(yOut), s);
 }
 
 // Scheduled RHS on contiguous [3][M] complex state/flux buffers.
@@ -542,7 +585,7 @@ cudaError_t rhs_contiguous(wv_handle* h, double t, double t0, const double* y, d
 // WVFixedStepRK4::step (PortableRuntime/src/WVRungeKutta.cpp:335-462) on the
 // contiguous device state h->state.
 cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t s) {
-    const size_t n = 6 * h->plan.M;
+    const size_t n = 6 * h->plan.M * h->dd.members;
     const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
     cudaError_t e;
     e = rhs_contiguous(h, t, t0, h->state, h->kbuf, s); if (e != cudaSuccess) return e;
@@ -560,36 +603,66 @@ cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t 
     return cudaGetLastError();
 }
 
-// Adjoint of WVFixedStepRK4::step at state y (contiguous [3][M] complex): yb is
-// the cotangent of the state after the step; on return h->ybacc holds the
-// cotangent before the step.  Stage states are recomputed from y.
-cudaError_t rk4_step_vjp(wv_handle* h, const double* y, double t, double t0, double dt, const double* yb, cudaStream_t s) {
+// Stage states of one WVFixedStepRK4 step from y (contiguous [3][M] complex):
+// st1 = y + h/2 k1, st2 = y + h/2 k2, st3 = y + h k3; when yNext is given it
+// also receives the step's result with the same arithmetic as rk4_step.
+// With ys (four buffers), the y spectra of the flux input at y, st1, st2 and
+// st3 are kept for the step's adjoint.
+cudaError_t rk4_stages(wv_handle* h, const double* y, double t, double t0, double dt, double* st1, double* st2, double* st3,
+                       double* yNext, cudaStream_t s, void* const* ys = nullptr) {
     const size_t n = 6 * h->plan.M;
     const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
     const size_t M2 = 2 * h->plan.M;
+    auto flux = [&](const double* x, double tt, int k) {
+        return flux_any(h, tt, t0, x, x + M2, x + 2 * M2, h->kbuf, h->kbuf + M2, h->kbuf + 2 * M2, false, s,
+                        ys ? ys[k] : nullptr);
+    };
+    cudaError_t e = flux(y, t, 0); if (e != cudaSuccess) return e;
+    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, y, 0.5 * dt, st1, 1, n);
+    e = flux(st1, t + 0.5 * dt, 1); if (e != cudaSuccess) return e;
+    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, y, 0.5 * dt, st2, 0, n);
+    e = flux(st2, t + 0.5 * dt, 2); if (e != cudaSuccess) return e;
+    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, y, dt, st3, 0, n);
+    h->metrics.kernel_launches += 3;
+    if (!yNext && ys) flux_fields_any(h, t + dt, t0, st3, ys[3], s);
+    if (yNext) {
+        e = flux(st3, t + dt, 3); if (e != cudaSuccess) return e;
+        dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, nullptr, 0.0, nullptr, 0, n);
+        dev::k_affine<<<grid, 256, 0, s>>>(y, h->acc, dt / 6.0, yNext, n);
+        h->metrics.kernel_launches += 2;
+    }
+    return cudaGetLastError();
+}
+
+// Backward sweep of one RK4 step given its stage states: yb is the cotangent of
+// the state after the step; h->ybacc receives the cotangent before it.
+cudaError_t rk4_backward(wv_handle* h, const double* y, const double* st1, const double* st2, const double* st3, double t,
+                         double t0, double dt, const double* yb, cudaStream_t s, void* const* ys = nullptr) {
+    const size_t n = 6 * h->plan.M;
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
     cudaError_t e;
-    auto flux = [&](const double* x, double tt) { return flux_any(h, tt, t0, x, x + M2, x + 2 * M2, h->kbuf, h->kbuf + M2, h->kbuf + 2 * M2, false, s); };
-    e = flux(y, t); if (e != cudaSuccess) return e;
-    dev::k_affine<<<grid, 256, 0, s>>>(y, h->kbuf, 0.5 * dt, h->st[1], n);
-    e = flux(h->st[1], t + 0.5 * dt); if (e != cudaSuccess) return e;
-    dev::k_affine<<<grid, 256, 0, s>>>(y, h->kbuf, 0.5 * dt, h->st[2], n);
-    e = flux(h->st[2], t + 0.5 * dt); if (e != cudaSuccess) return e;
-    dev::k_affine<<<grid, 256, 0, s>>>(y, h->kbuf, dt, h->st[3], n);
-    // backward through the stages
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.0, nullptr, n);
-    e = flux_vjp_any(h, t + dt, t0, h->st[3], h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    e = flux_vjp_any(h, t + dt, t0, st3, h->kb, h->sb, s, ys ? ys[3] : nullptr); if (e != cudaSuccess) return e;
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->ybacc, 1.0, yb, 1.0, h->sb, n);
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, dt, h->sb, n);
-    e = flux_vjp_any(h, t + 0.5 * dt, t0, h->st[2], h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    e = flux_vjp_any(h, t + 0.5 * dt, t0, st2, h->kb, h->sb, s, ys ? ys[2] : nullptr); if (e != cudaSuccess) return e;
     dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, 0.5 * dt, h->sb, n);
-    e = flux_vjp_any(h, t + 0.5 * dt, t0, h->st[1], h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    e = flux_vjp_any(h, t + 0.5 * dt, t0, st1, h->kb, h->sb, s, ys ? ys[1] : nullptr); if (e != cudaSuccess) return e;
     dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.5 * dt, h->sb, n);
-    e = flux_vjp_any(h, t, t0, y, h->kb, h->sb, s); if (e != cudaSuccess) return e;
+    e = flux_vjp_any(h, t, t0, y, h->kb, h->sb, s, ys ? ys[0] : nullptr); if (e != cudaSuccess) return e;
     dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
-    h->metrics.kernel_launches += 11;
+    h->metrics.kernel_launches += 8;
     return cudaGetLastError();
+}
+
+// Adjoint of one WVFixedStepRK4::step (PortableRuntime/src/WVRungeKutta.cpp:335-462)
+// at state y, stage states recomputed.
+cudaError_t rk4_step_vjp(wv_handle* h, const double* y, double t, double t0, double dt, const double* yb, cudaStream_t s) {
+    cudaError_t e = rk4_stages(h, y, t, t0, dt, h->st[1], h->st[2], h->st[3], nullptr, s);
+    if (e != cudaSuccess) return e;
+    return rk4_backward(h, y, h->st[1], h->st[2], h->st[3], t, t0, dt, yb, s);
 }
 
 int check_times(wv_handle* h, double t, double t0) {
@@ -675,7 +748,7 @@ cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* 
     // k_vinv clears this counter (block 0) before k_xflux accumulates into it.
     auto* speed = reinterpret_cast<unsigned long long*>(base + offs[4]);
     const int nt = p.targets.count;
-    dev::k_vinv<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
     dev::YInvMap map{};
     map.nOut = 4 + 2 * nt;
     for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
@@ -686,7 +759,7 @@ cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* 
     launch_yinv<T>(h, map, z, y, s);
     launch_xflux<T>(h, y, ps, speed, s);
     launch_yfwd<T>(h, ps, nt, f, s);
-    dev::k_vfwd<T, true><<<cdiv(p.Nkl, dev::kVfwdModes), 256, smem_vfwd<T>(p, nt), s>>>(
+    dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
         d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
     return cudaGetLastError();
 }
@@ -743,11 +816,14 @@ void wv_destroy(wv_handle* h) {
     delete h;
 }
 
-int wv_create(const wv_config* config, int precision, wv_handle** out) {
+// A handle for `members` states of one grid stepped side by side (members = 1
+// for the reference's single-state kernel).
+static int create_handle(const wv_config* config, int precision, int members, wv_handle** out) {
     if (!out) return WV_INVALID_POINTER;
     *out = nullptr;
     if (!config) return WV_INVALID_POINTER;
     if (precision != WV_PRECISION_FP64 && precision != WV_PRECISION_MIXED) return WV_INVALID_CONFIGURATION;
+    if (members < 1) return WV_INVALID_CONFIGURATION;
     wv_handle* h = new (std::nothrow) wv_handle();
     if (!h) return WV_ALLOCATION_FAILURE;
     h->precision = precision;
@@ -756,6 +832,8 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     if (!st) { const int code = st.code; delete h; return code; }
     const Descriptor& d = h->desc;
     const Plan& p = h->plan;
+    // plane index m*Nz+z rides in gridDim.y (at most 65535)
+    if (static_cast<size_t>(members) * p.Nz > 65535) { delete h; return WV_INVALID_CONFIGURATION; }
     cudaGetDevice(&h->device);
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     std::vector<double> damping;
@@ -766,6 +844,8 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     }
     auto& dd = h->dd;
     dd.Nx = p.Nx; dd.Ny = p.Ny; dd.Nz = p.Nz; dd.Nj = p.Nj; dd.Nkl = p.Nkl; dd.NxHalf = p.NxHalf; dd.M = p.M;
+    dd.members = members; dd.zTotal = static_cast<int>(members * p.Nz);
+    dd.memberStride = static_cast<long long>(6 * p.M);
     dd.positions = p.positions; dd.kxColumns = p.kxColumns; dd.zHalf = p.zHalf;
     dd.nt = p.targets.count;
     for (int i = 0; i < 4; ++i) dd.tq[i] = p.targets.q[i];
@@ -816,13 +896,14 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     const auto ss = scratch_sizes(p);
     const size_t cb = 2 * elem_size(precision);
     const size_t R = p.Nx * p.Ny * p.Nz;
-    if (e == cudaSuccess) e = alloc(h, ss.z * cb, &h->zspec);
-    if (e == cudaSuccess) e = alloc(h, ss.y * cb, &h->yspec);
-    if (e == cudaSuccess) e = alloc(h, ss.p * cb, &h->pspec);
-    if (e == cudaSuccess) e = alloc(h, ss.f * cb, &h->fspec);
+    const size_t B = static_cast<size_t>(members);
+    if (e == cudaSuccess) e = alloc(h, B * ss.z * cb, &h->zspec);
+    if (e == cudaSuccess) e = alloc(h, B * ss.y * cb, &h->yspec);
+    if (e == cudaSuccess) e = alloc(h, B * ss.p * cb, &h->pspec);
+    if (e == cudaSuccess) e = alloc(h, B * ss.f * cb, &h->fspec);
     void* tmp = nullptr;
-    if (e == cudaSuccess) { e = alloc(h, sizeof(unsigned long long), &tmp); h->maxSpeed = static_cast<unsigned long long*>(tmp); }
-    const size_t stateBytes = 6 * p.M * sizeof(double);
+    if (e == cudaSuccess) { e = alloc(h, B * sizeof(unsigned long long), &tmp); h->maxSpeed = static_cast<unsigned long long*>(tmp); }
+    const size_t stateBytes = B * 6 * p.M * sizeof(double);
     if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->state = static_cast<double*>(tmp); }
     if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->flux = static_cast<double*>(tmp); }
     if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->stage = static_cast<double*>(tmp); }
@@ -841,6 +922,8 @@ int wv_create(const wv_config* config, int precision, wv_handle** out) {
     *out = h;
     return WV_SUCCESS;
 }
+
+int wv_create(const wv_config* config, int precision, wv_handle** out) { return create_handle(config, precision, 1, out); }
 
 const char* wv_last_message(const wv_handle* h) { return h ? h->message.c_str() : "null handle"; }
 
@@ -1199,32 +1282,66 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
         e = alloc(h, stateBytes, &tmp);
         h->checkpoints.push_back(static_cast<double*>(tmp));
     }
-    while (static_cast<int>(h->segment.size()) < K && e == cudaSuccess) {
+    while (static_cast<int>(h->segment.size()) < 4 * K && e == cudaSuccess) {
         e = alloc(h, stateBytes, &tmp);
         h->segment.push_back(static_cast<double*>(tmp));
     }
+    // y spectra of every stage flux of a segment, when half the free memory holds them
+    const size_t yBytes = scratch_sizes(h->plan).y * 2 * elem_size(h->precision);
+    if (e == cudaSuccess && static_cast<int>(h->ystore.size()) < 4 * K) {
+        size_t freeB = 0, totalB = 0;
+        e = cudaMemGetInfo(&freeB, &totalB);
+        const size_t need = (4 * K - h->ystore.size()) * yBytes;
+        if (e == cudaSuccess && need <= freeB / 2) {
+            while (static_cast<int>(h->ystore.size()) < 4 * K && e == cudaSuccess) {
+                e = alloc(h, yBytes, &tmp);
+                h->ystore.push_back(tmp);
+            }
+        }
+    }
     if (e != cudaSuccess) return cuda_fail(h, e, "RK4 adjoint checkpoints");
     h->metrics.device_bytes = h->deviceBytes;
-    // forward pass with checkpoints; times exactly as WVFixedStepRK4 advances them
+    const bool keepY = static_cast<int>(h->ystore.size()) >= 4 * K;
+    // Stage states (and y spectra) of the steps first..last-1 from the state in
+    // segment[0], the state of each next step in the following slot.
     std::vector<double> times(n + 1);
     times[0] = t;
+    for (int i = 0; i < n; ++i) times[i + 1] = times[i] + dt;
+    auto record = [&](int first, int last) {
+        cudaError_t r = cudaSuccess;
+        for (int i = first; i < last && r == cudaSuccess; ++i) {
+            double** q = h->segment.data() + 4 * (i - first);
+            void* const* ys = keepY ? h->ystore.data() + 4 * (i - first) : nullptr;
+            r = rk4_stages(h, q[0], times[i], t0, dt, q[1], q[2], q[3], i + 1 < last ? q[4] : nullptr, s, ys);
+        }
+        return r;
+    };
+    // forward pass: checkpoints at the start of each segment; the last segment
+    // is recorded directly, so its recomputation is skipped
     e = gather3(h, h->state, Ap, Am, A0, s);
-    for (int i = 0; i < n && e == cudaSuccess; ++i) {
-        if (i % K == 0) e = cudaMemcpyAsync(h->checkpoints[i / K], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
-        if (e == cudaSuccess) e = rk4_step(h, times[i], t0, dt, s);
-        times[i + 1] = times[i] + dt;
+    for (int seg = 0; seg < ncp && e == cudaSuccess; ++seg) {
+        const int first = seg * K, last = std::min(n, first + K);
+        if (seg + 1 < ncp) {
+            e = cudaMemcpyAsync(h->checkpoints[seg], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
+            for (int i = first; i < last && e == cudaSuccess; ++i) e = rk4_step(h, times[i], t0, dt, s);
+        } else {
+            e = cudaMemcpyAsync(h->segment[0], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = record(first, last);
+        }
     }
     if (e == cudaSuccess) e = gather3(h, h->ybin, Apb, Amb, A0b, s);
-    // backward, one segment at a time
+    // backward, one segment at a time: recompute the segment from its checkpoint
+    // keeping every step's state and stage states, then step the cotangent back
     for (int seg = ncp - 1; seg >= 0 && e == cudaSuccess; --seg) {
         const int first = seg * K, last = std::min(n, first + K);
-        e = cudaMemcpyAsync(h->state, h->checkpoints[seg], stateBytes, cudaMemcpyDeviceToDevice, s);
-        for (int i = first; i < last && e == cudaSuccess; ++i) {
-            e = cudaMemcpyAsync(h->segment[i - first], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess && i + 1 < last) e = rk4_step(h, times[i], t0, dt, s);
+        if (seg + 1 < ncp) {
+            e = cudaMemcpyAsync(h->segment[0], h->checkpoints[seg], stateBytes, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = record(first, last);
         }
         for (int i = last - 1; i >= first && e == cudaSuccess; --i) {
-            e = rk4_step_vjp(h, h->segment[i - first], times[i], t0, dt, h->ybin, s);
+            double** q = h->segment.data() + 4 * (i - first);
+            void* const* ys = keepY ? h->ystore.data() + 4 * (i - first) : nullptr;
+            e = rk4_backward(h, q[0], q[1], q[2], q[3], times[i], t0, dt, h->ybin, s, ys);
             if (e == cudaSuccess) e = cudaMemcpyAsync(h->ybin, h->ybacc, stateBytes, cudaMemcpyDeviceToDevice, s);
         }
     }
@@ -1258,6 +1375,287 @@ int wv_nonlinear_flux_device_noalloc(wv_handle* h, double t, double t0, const do
     h->metrics.nonlinear_flux_calls++;
     h->metrics.kernel_launches += 5;
     return finish(h, e, "nonlinear flux (static scratch)");
+}
+
+}  // extern "C"
+
+// ---- ensembles ----------------------------------------------------------------------
+// Groups of states on uneven grids.  Each group is one member-batched handle
+// (all its members' planes and columns in one launch per stage); every group
+// runs on its own stream forked from the ensemble's capture stream, and the
+// whole n-step integration of all groups is captured once into a CUDA graph and
+// replayed with one cudaGraphLaunch.  No counterpart in the reference, which
+// steps one state per kernel object.
+
+struct wv_ensemble {
+    std::vector<wv_handle*> groups;
+    std::vector<int> members;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
+    cudaStream_t capture = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    // what the instantiated graph was captured for
+    std::vector<double*> keyStates;
+    std::vector<double> keyDt, keyT;
+    double keyT0 = 0.0;
+    int keySteps = -1;
+    std::vector<wv_ensemble_tuning> tuning;
+    wv_ensemble_metrics metrics{};
+    std::atomic<bool> busy{false};
+    int device = 0;
+    std::string message;
+};
+
+namespace {
+
+int efail(wv_ensemble* e, int code, const std::string& m) {
+    if (e) e->message = m;
+    return code;
+}
+
+// Device time (ms) of `reps` fluxes of one group on its own buffers.
+float time_group_flux(wv_handle* h, int reps, cudaStream_t s, cudaError_t& err) {
+    const size_t M2 = 2 * h->plan.M;
+    cudaEvent_t a = nullptr, b = nullptr;
+    err = cudaEventCreate(&a);
+    if (err == cudaSuccess) err = cudaEventCreate(&b);
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = flux_any(h, 0.0, 0.0, h->state, h->state + M2, h->state + 2 * M2, h->kbuf, h->kbuf + M2,
+                                           h->kbuf + 2 * M2, false, s);
+    if (err == cudaSuccess) err = cudaEventRecord(a, s);
+    for (int r = 0; r < reps && err == cudaSuccess; ++r)
+        err = flux_any(h, 0.0, 0.0, h->state, h->state + M2, h->state + 2 * M2, h->kbuf, h->kbuf + M2, h->kbuf + 2 * M2,
+                       false, s);
+    if (err == cudaSuccess) err = cudaEventRecord(b, s);
+    if (err == cudaSuccess) err = cudaEventSynchronize(b);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, a, b);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    return ms / static_cast<float>(reps > 0 ? reps : 1);
+}
+
+// Per group, the fastest of the FFT variants that exist for its grid: the
+// register-resident warp FFT or the shared-memory Stockham kernel, per axis.
+cudaError_t autotune_group(wv_handle* h, cudaStream_t s, wv_ensemble_tuning& out) {
+    cudaError_t e = cudaMemsetAsync(h->state, 0, 6 * h->plan.M * h->dd.members * sizeof(double), s);
+    Plan& p = h->plan;
+    const bool fp32 = h->precision != WV_PRECISION_FP64;
+    const bool warpY = fp32 && warp_ry<float>(p) != 0, warpX = fp32 && warp_rx<float>(p) != 0;
+    float best = -1.0f;
+    bool bestY = false, bestX = false;
+    out.candidates = 0;
+    for (int vy = 0; vy < (warpY ? 2 : 1) && e == cudaSuccess; ++vy) {
+        for (int vx = 0; vx < (warpX ? 2 : 1) && e == cudaSuccess; ++vx) {
+            p.stockhamY = vy == 1;
+            p.stockhamX = vx == 1;
+            const float ms = time_group_flux(h, 3, s, e);
+            if (e == cudaSuccess && out.candidates < 4) out.candidate_ms[out.candidates] = ms;
+            out.candidates++;
+            if (e == cudaSuccess && (best < 0.0f || ms < best)) { best = ms; bestY = p.stockhamY; bestX = p.stockhamX; }
+        }
+    }
+    p.stockhamY = bestY;
+    p.stockhamX = bestX;
+    out.stockham_y = bestY ? 1 : 0;
+    out.stockham_x = bestX ? 1 : 0;
+    out.warp_y_available = warpY ? 1 : 0;
+    out.warp_x_available = warpX ? 1 : 0;
+    out.flux_ms = best;
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+void wv_ensemble_destroy(wv_ensemble* e) {
+    if (!e) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(e->device);
+    if (e->capture) cudaStreamSynchronize(e->capture);
+    for (cudaStream_t st : e->side) if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    for (cudaEvent_t ev : e->join) if (ev) cudaEventDestroy(ev);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->capture) cudaStreamDestroy(e->capture);
+    for (wv_handle* h : e->groups) wv_destroy(h);
+    cudaSetDevice(prev);
+    delete e;
+}
+
+int wv_ensemble_create(const wv_config* configs, const int* members, int n_groups, int precision, int autotune,
+                       wv_ensemble** out) {
+    if (!out) return WV_INVALID_POINTER;
+    *out = nullptr;
+    if (!configs || !members) return WV_INVALID_POINTER;
+    if (n_groups < 1 || n_groups > WV_ENSEMBLE_MAX_GROUPS) return WV_INVALID_CONFIGURATION;
+    for (int g = 0; g < n_groups; ++g) if (members[g] < 1) return WV_INVALID_CONFIGURATION;
+    wv_ensemble* e = new (std::nothrow) wv_ensemble();
+    if (!e) return WV_ALLOCATION_FAILURE;
+    cudaGetDevice(&e->device);
+    for (int g = 0; g < n_groups; ++g) {
+        wv_handle* h = nullptr;
+        const int rc = create_handle(&configs[g], precision, members[g], &h);
+        if (rc) { wv_ensemble_destroy(e); return rc; }
+        e->groups.push_back(h);
+        e->members.push_back(members[g]);
+    }
+    cudaError_t err = cudaStreamCreateWithFlags(&e->capture, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+    for (int g = 0; g < n_groups && err == cudaSuccess; ++g) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        err = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        e->side.push_back(st);
+        e->join.push_back(ev);
+    }
+    e->tuning.assign(n_groups, wv_ensemble_tuning{});
+    for (int g = 0; g < n_groups && err == cudaSuccess; ++g) {
+        wv_handle* h = e->groups[g];
+        if (autotune) {
+            err = autotune_group(h, e->capture, e->tuning[g]);
+        } else {
+            wv_ensemble_tuning& t = e->tuning[g];
+            t.stockham_y = h->plan.stockhamY ? 1 : 0;
+            t.stockham_x = h->plan.stockhamX ? 1 : 0;
+            t.warp_y_available = h->precision != WV_PRECISION_FP64 && warp_ry<float>(h->plan) != 0;
+            t.warp_x_available = h->precision != WV_PRECISION_FP64 && warp_rx<float>(h->plan) != 0;
+            t.flux_ms = -1.0f;
+        }
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->capture);
+    if (err != cudaSuccess) {
+        const int code = err == cudaErrorMemoryAllocation ? WV_ALLOCATION_FAILURE : WV_FFT_PLAN_FAILURE;
+        wv_ensemble_destroy(e);
+        return code;
+    }
+    size_t bytes = 0;
+    for (wv_handle* h : e->groups) bytes += h->deviceBytes;
+    e->metrics.device_bytes = bytes;
+    *out = e;
+    return WV_SUCCESS;
+}
+
+const char* wv_ensemble_last_message(const wv_ensemble* e) { return e ? e->message.c_str() : "null ensemble"; }
+
+int wv_ensemble_get_sizes(const wv_ensemble* e, int group, wv_sizes* sizes) {
+    if (!e || !sizes) return WV_INVALID_POINTER;
+    if (group < 0 || group >= static_cast<int>(e->groups.size())) return WV_INVALID_CONFIGURATION;
+    return wv_get_sizes(e->groups[group], sizes);
+}
+
+int wv_ensemble_get_tuning(const wv_ensemble* e, int group, wv_ensemble_tuning* tuning) {
+    if (!e || !tuning) return WV_INVALID_POINTER;
+    if (group < 0 || group >= static_cast<int>(e->groups.size())) return WV_INVALID_CONFIGURATION;
+    *tuning = e->tuning[group];
+    return WV_SUCCESS;
+}
+
+int wv_ensemble_get_metrics(const wv_ensemble* e, wv_ensemble_metrics* m) {
+    if (!e || !m) return WV_INVALID_POINTER;
+    *m = e->metrics;
+    return WV_SUCCESS;
+}
+
+int wv_ensemble_rk4_device(wv_ensemble* e, double* const* states, double* t, double t0, const double* dt, int n,
+                           void* stream) {
+    if (!e) return WV_INVALID_POINTER;
+    if (!states || !t || !dt) return efail(e, WV_INVALID_POINTER, "Ensemble RK4 received a null pointer.");
+    const int G = static_cast<int>(e->groups.size());
+    if (!std::isfinite(t0)) return efail(e, WV_INVALID_CONFIGURATION, "Times must be finite.");
+    for (int g = 0; g < G; ++g)
+        if (!std::isfinite(t[g])) return efail(e, WV_INVALID_CONFIGURATION, "Times must be finite.");
+    if (n < 0) return efail(e, WV_INVALID_CONFIGURATION, "RK4 step count must be nonnegative.");
+    for (int g = 0; g < G; ++g) {
+        if (!states[g]) return efail(e, WV_INVALID_POINTER, "Ensemble RK4 received a null group state.");
+        if (!(dt[g] > 0.0) || !std::isfinite(dt[g]))
+            return efail(e, WV_INVALID_CONFIGURATION, "RK4 step sizes must be finite and positive.");
+        if (reinterpret_cast<uintptr_t>(states[g]) % 16)
+            return efail(e, WV_INVALID_POINTER, "Group states must be 16-byte aligned complex arrays.");
+        for (int q = 0; q < g; ++q) {
+            const size_t bg = 6 * e->groups[g]->plan.M * e->members[g] * sizeof(double);
+            const size_t bq = 6 * e->groups[q]->plan.M * e->members[q] * sizeof(double);
+            if (overlaps(states[g], bg, states[q], bq)) return efail(e, WV_OVERLAPPING_ARRAYS, "Group states overlap.");
+        }
+    }
+    if (n == 0) return WV_SUCCESS;
+    Guard guard(e->busy);
+    if (!guard.entered) return efail(e, WV_REENTRANT_EXECUTION, "Ensemble stepping is not reentrant.");
+    cudaSetDevice(e->device);
+    // step times exactly as WVFixedStepRK4 advances them, per group
+    std::vector<double> tEnd(t, t + G);
+    const bool same = e->exec && e->keySteps == n && e->keyT0 == t0 && static_cast<int>(e->keyDt.size()) == G &&
+                      std::equal(e->keyDt.begin(), e->keyDt.end(), dt) && std::equal(e->keyT.begin(), e->keyT.end(), t) &&
+                      std::equal(e->keyStates.begin(), e->keyStates.end(), states);
+    cudaError_t err = cudaSuccess;
+    if (!same) {
+        cudaGraph_t graph = nullptr;
+        err = cudaStreamBeginCapture(e->capture, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) err = cudaEventRecord(e->fork, e->capture);
+        for (int g = 0; g < G && err == cudaSuccess; ++g) {
+            wv_handle* h = e->groups[g];
+            cudaStream_t s = e->side[g];
+            const size_t bytes = 6 * h->plan.M * e->members[g] * sizeof(double);
+            err = cudaStreamWaitEvent(s, e->fork, 0);
+            if (err == cudaSuccess) err = cudaMemcpyAsync(h->state, states[g], bytes, cudaMemcpyDeviceToDevice, s);
+            double tt = t[g];
+            for (int i = 0; i < n && err == cudaSuccess; ++i) {
+                err = rk4_step(h, tt, t0, dt[g], s);
+                tt = tt + dt[g];
+            }
+            if (err == cudaSuccess) err = cudaMemcpyAsync(states[g], h->state, bytes, cudaMemcpyDeviceToDevice, s);
+            if (err == cudaSuccess) err = cudaEventRecord(e->join[g], s);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(e->capture, e->join[g], 0);
+        }
+        const cudaError_t endErr = cudaStreamEndCapture(e->capture, &graph);
+        if (err == cudaSuccess) err = endErr;
+        if (err == cudaSuccess) {
+            // same topology (same groups and step count): update the parameters in place
+            bool updated = false;
+            if (e->exec && e->keySteps == n) {
+                cudaGraphExecUpdateResultInfo info{};
+                updated = cudaGraphExecUpdate(e->exec, graph, &info) == cudaSuccess;
+                if (!updated) cudaGetLastError();
+            }
+            if (!updated) {
+                if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+                err = cudaGraphInstantiate(&e->exec, graph, 0);
+                e->metrics.graph_instantiations++;
+            } else {
+                e->metrics.graph_updates++;
+            }
+            e->metrics.graph_captures++;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (err != cudaSuccess) {
+            if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+            e->keySteps = -1;
+            return efail(e, WV_FFT_EXECUTION_FAILURE, std::string("ensemble graph capture: ") + cudaGetErrorString(err));
+        }
+        e->keyStates.assign(states, states + G);
+        e->keyDt.assign(dt, dt + G);
+        e->keyT.assign(t, t + G);
+        e->keyT0 = t0;
+        e->keySteps = n;
+    }
+    err = cudaGraphLaunch(e->exec, static_cast<cudaStream_t>(stream));
+    if (err != cudaSuccess) return efail(e, WV_FFT_EXECUTION_FAILURE, std::string("ensemble graph launch: ") + cudaGetErrorString(err));
+    e->metrics.graph_launches++;
+    unsigned long long launches = 0;
+    for (int g = 0; g < G; ++g) {
+        launches += static_cast<unsigned long long>(n) * 25;
+        e->metrics.member_steps += static_cast<unsigned long long>(n) * e->members[g];
+    }
+    e->metrics.kernel_launches += launches;
+    for (int g = 0; g < G; ++g) {
+        double tt = t[g];
+        for (int i = 0; i < n; ++i) tt = tt + dt[g];
+        t[g] = tt;
+    }
+    return WV_SUCCESS;
 }
 
 }  // extern "C"

@@ -171,6 +171,12 @@ struct DescDev {
     int nt;          // number of flux targets
     int tq[4];       // target ids (0=u,1=v,2=w,3=eta)
     int hydrostatic;
+    // Ensemble batching: `members` states of this grid side by side, member m's
+    // coefficients at m*memberStride doubles; column buffers [ch][m*Nz+z][pos]
+    // and plane buffers [m*Nz+z][...], so zTotal = members*Nz planes.  A single
+    // state is members = 1.
+    int members, zTotal;
+    long long memberStride;
     // descriptor arrays [M] (j fastest)
     const double* omega;
     const double* UAp;   // complex interleaved
@@ -246,7 +252,13 @@ __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restric
     const int Nj = d.Nj;
     const int m0 = blockIdx.x * kVinvModes;
     const int nm = min(kVinvModes, d.Nkl - m0);
-    if (blockIdx.x == 0 && threadIdx.x == 0 && maxSpeedBits) *maxSpeedBits = 0ull;
+    const int member = blockIdx.y;
+    if (member > 0) {
+        const long long o = member * d.memberStride;
+        Ap += o; Am += o; A0 += o;
+        zspec += (size_t)member * d.Nz * d.positions;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && maxSpeedBits) maxSpeedBits[member] = 0ull;
     for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
         const int mi = it / Nj, j = it - mi * Nj;
         const int mode = m0 + mi;
@@ -351,7 +363,7 @@ __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restric
         const int n2 = Nz - 1 - n;
         auto put = [&](int ch, const T* Ec, const T* Oc, bool sine) {
             // cos family: out[n] = E+O, out[Nz-1-n] = E-O ; sin family: out[Nz-1-n] = O-E
-            cx<T>* base = zspec + (size_t)ch * Nz * P;
+            cx<T>* base = zspec + (size_t)ch * d.zTotal * P;
             const cx<T> lo = mk<T>(Ec[0] + Oc[0], Ec[1] + Oc[1]);
             base[(size_t)n * P + pos] = lo;
             if (cpos >= 0) base[(size_t)n * P + cpos] = mk<T>(lo.x, -lo.y);
@@ -396,7 +408,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_yinv(DescDev d, YInvMap map, const cx<T>* __restrict__ zspec, int nInCh,
                                              cx<T>* __restrict__ yspec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int Ny = d.Ny, Nz = d.Nz, P = d.positions, KX = d.kxColumns;
+    const int Ny = d.Ny, P = d.positions, KX = d.kxColumns;
     cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* bufA = tw + Ny;
     cx<T>* bufB = bufA + kYG * Ny;
@@ -409,7 +421,7 @@ __global__ void __launch_bounds__(256) k_yinv(DescDev d, YInvMap map, const cx<T
     for (int oc = 0; oc < map.nOut; ++oc) {
         for (int i = threadIdx.x; i < kYG * Ny; i += blockDim.x) bufA[i] = mk<T>(T(0), T(0));
         __syncthreads();
-        const cx<T>* in = zspec + ((size_t)map.src[oc] * Nz + z) * P;
+        const cx<T>* in = zspec + ((size_t)map.src[oc] * d.zTotal + z) * P;
         const int pBeg = d.colStart[kx0], pEnd = d.colStart[kx0 + g];
         for (int p = pBeg + threadIdx.x; p < pEnd; p += blockDim.x) {
             // column of p
@@ -571,7 +583,7 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
     if (threadIdx.x == 0) {
         double m = 0.0;
         for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmax(m, red[i]);
-        if (maxSpeedBits) atomicMax(maxSpeedBits, (unsigned long long)__double_as_longlong(m));
+        if (maxSpeedBits) atomicMax(maxSpeedBits + z / d.Nz, (unsigned long long)__double_as_longlong(m));
     }
     // forward real transform of each S_q
     for (int i = threadIdx.x; i < nt * L; i += blockDim.x) {
@@ -665,7 +677,7 @@ __global__ void __launch_bounds__(256) k_xr2c_fields(DescDev d, const double* __
 template <typename T>
 __global__ void __launch_bounds__(256) k_yfwd(DescDev d, const cx<T>* __restrict__ pspec, int nch, cx<T>* __restrict__ fspec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int Ny = d.Ny, Nz = d.Nz, P = d.positions, KX = d.kxColumns;
+    const int Ny = d.Ny, P = d.positions, KX = d.kxColumns;
     cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* bufA = tw + Ny;
     cx<T>* bufB = bufA + kYG * Ny;
@@ -682,7 +694,7 @@ __global__ void __launch_bounds__(256) k_yfwd(DescDev d, const cx<T>* __restrict
     }
     __syncthreads();
     cx<T>* res = fft_lines<T, false>(bufA, bufB, d.fy, g, Ny, tw);
-    cx<T>* out = fspec + ((size_t)c * Nz + z) * P;
+    cx<T>* out = fspec + ((size_t)c * d.zTotal + z) * P;
     const int pBeg = d.colStart[kx0], pEnd = d.colStart[kx0 + g];
     for (int p = pBeg + threadIdx.x; p < pEnd; p += blockDim.x) {
         int gi = 0;
@@ -712,6 +724,14 @@ __global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict
     const int Nj = d.Nj, Nz = d.Nz, Zh = d.zHalf, P = d.positions;
     const int m0 = blockIdx.x * kVfwdModes;
     const int nm = min(kVfwdModes, d.Nkl - m0);
+    const int member = blockIdx.y;
+    if (member > 0) {
+        const long long o = member * d.memberStride;
+        if (Ap) { Ap += o; Am += o; A0 += o; }
+        Fp += o; Fm += o; F0 += o;
+        fspec += (size_t)member * Nz * P;
+        if (maxSpeedBits) maxSpeedBits += member;
+    }
     // folded columns pq[c][n][mode] = (S_n + S_{Nz-1-n}, S_n - S_{Nz-1-n})
     cx2t<T>* pq = reinterpret_cast<cx2t<T>*>(smem_raw);
     for (int it = threadIdx.x; it < nch * Zh * nm; it += blockDim.x) {
@@ -719,7 +739,7 @@ __global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict
         const int rest = it / nm;
         const int n = rest % Zh, c = rest / Zh;
         const int pos = d.modePos[m0 + mm];
-        const cx<T>* col = fspec + (size_t)c * Nz * P + pos;
+        const cx<T>* col = fspec + (size_t)c * d.zTotal * P + pos;
         const cx<T> a = col[(size_t)n * P];
         const int n2 = Nz - 1 - n;
         cx2t<T> v;

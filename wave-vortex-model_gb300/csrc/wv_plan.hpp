@@ -59,6 +59,9 @@ struct Plan {
     std::vector<double> Fcos, Fsin;
     FFTFactors fx, fy;                    // fx: x line length (Nx/2 for even Nx, else Nx)
     std::vector<double> twx, twxN, twy;   // interleaved exp(-2 pi i k / N) for the x line, Nx, Ny
+    // FFT variant per axis: the shared-memory Stockham kernels instead of the
+    // register-resident warp FFTs where both exist (set by the ensemble autotuner).
+    bool stockhamY = false, stockhamX = false;
 };
 
 Status build_plan(const Descriptor& d, Plan& p);

@@ -132,13 +132,13 @@ __global__ void __launch_bounds__(256) k_yinv_w(DescDev d, YInvMap map, const cx
     cx<T>* tile = tw + N;                              // [N][kWG]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int kx0 = blockIdx.x * kWG, z = blockIdx.y, oc = blockIdx.z;
-    const int KX = d.kxColumns, P = d.positions, Nz = d.Nz;
+    const int KX = d.kxColumns, P = d.positions;
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
     for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
     __syncthreads();
     const int kx = kx0 + warp;
     if (kx < KX) {
-        const cx<T>* in = zspec + ((size_t)map.src[oc] * Nz + z) * P;
+        const cx<T>* in = zspec + ((size_t)map.src[oc] * d.zTotal + z) * P;
         const int* ym = d.ymap + (size_t)kx * N;
         const bool mulL = map.mulL[oc] != 0;
         cx<T> v[R];
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256) k_yfwd_w(DescDev d, const cx<T>* __restri
     cx<T>* tile = tw + N;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int kx0 = blockIdx.x * kWG, z = blockIdx.y, c = blockIdx.z;
-    const int KX = d.kxColumns, P = d.positions, Nz = d.Nz;
+    const int KX = d.kxColumns, P = d.positions;
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
     for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
     const int g = min(kWG, KX - kx0);
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) k_yfwd_w(DescDev d, const cx<T>* __restri
 #pragma unroll
     for (int k1 = 0; k1 < R; ++k1) tile[p_index<R>(k1, lane) * kWG + warp] = v[k1];
     __syncwarp();
-    cx<T>* out = fspec + ((size_t)c * Nz + z) * P;
+    cx<T>* out = fspec + ((size_t)c * d.zTotal + z) * P;
     const int pBeg = d.colStart[kx], pEnd = d.colStart[kx + 1];
     for (int p = pBeg + lane; p < pEnd; p += 32) out[p] = tile[d.posKy[p] * kWG + warp];
 }
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __re
         if (atomicAdd(&warpsDone, 1) == rows - 1 && maxSpeedBits) {
             double m = 0.0;
             for (int i = 0; i < rows; ++i) m = fmax(m, warpMax[i]);
-            atomicMax(maxSpeedBits, (unsigned long long)__double_as_longlong(m));
+            atomicMax(maxSpeedBits + z / d.Nz, (unsigned long long)__double_as_longlong(m));
         }
     }
 }

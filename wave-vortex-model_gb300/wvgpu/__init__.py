@@ -72,6 +72,17 @@ class _StageTimes(ctypes.Structure):
                                                "vertical_forward_ms")] + [("fluxes", ctypes.c_uint64)]
 
 
+class _EnsembleTuning(ctypes.Structure):
+    _fields_ = [("warp_y_available", ctypes.c_int), ("warp_x_available", ctypes.c_int), ("stockham_y", ctypes.c_int),
+                ("stockham_x", ctypes.c_int), ("candidates", ctypes.c_int), ("candidate_ms", ctypes.c_float * 4),
+                ("flux_ms", ctypes.c_float)]
+
+
+class _EnsembleMetrics(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("graph_captures", "graph_instantiations", "graph_updates",
+                                               "graph_launches", "kernel_launches", "member_steps", "device_bytes")]
+
+
 class _Metrics(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("nonlinear_flux_calls", "rhs_evaluations", "forward_calls", "inverse_calls",
                                                "rk4_steps", "kernel_launches", "device_bytes")] + \
@@ -148,6 +159,16 @@ def load_library():
     lib.wv_inverse_vjp_device.argtypes = [P, D, D, P, P, P, P, P]
     lib.wv_rk4_step_vjp_device.argtypes = [P, P, P, P, D, D, D, P, P, P, P]
     lib.wv_rk4_adjoint_device.argtypes = [P, P, P, P, D, D, D, ctypes.c_int, ctypes.c_int, P, P, P, P]
+    lib.wv_ensemble_create.argtypes = [ctypes.POINTER(_Config), ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.POINTER(P)]
+    lib.wv_ensemble_destroy.argtypes = [P]
+    lib.wv_ensemble_destroy.restype = None
+    lib.wv_ensemble_last_message.argtypes = [P]
+    lib.wv_ensemble_last_message.restype = ctypes.c_char_p
+    lib.wv_ensemble_get_sizes.argtypes = [P, ctypes.c_int, ctypes.POINTER(_Sizes)]
+    lib.wv_ensemble_get_tuning.argtypes = [P, ctypes.c_int, ctypes.POINTER(_EnsembleTuning)]
+    lib.wv_ensemble_get_metrics.argtypes = [P, ctypes.POINTER(_EnsembleMetrics)]
+    lib.wv_ensemble_rk4_device.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(D), D, ctypes.POINTER(D), ctypes.c_int, P]
     _lib = lib
     return lib
 
@@ -158,7 +179,9 @@ def exported_symbols():
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
             "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc", "wv_flux_vjp_device",
-            "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device"]
+            "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device", "wv_ensemble_create",
+            "wv_ensemble_destroy", "wv_ensemble_last_message", "wv_ensemble_get_sizes", "wv_ensemble_get_tuning",
+            "wv_ensemble_get_metrics", "wv_ensemble_rk4_device"]
 
 
 def describe(configuration: Configuration):
@@ -393,6 +416,93 @@ class WVTransformConstantStratificationKernel:
         m = _Metrics()
         self._check(self._lib.wv_get_metrics(self._h, ctypes.byref(m)))
         return {n: getattr(m, n) for n, _ in _Metrics._fields_}
+
+
+class WVEnsemble:
+    """Groups of states on uneven grids stepped together: group g holds
+    members[g] states of configurations[g], each as a [members, 3, Nkl, Nj]
+    complex128 CUDA tensor (Ap, Am, A0 of each member).  rk4() runs the whole
+    integration of every group as one CUDA-graph launch.  No counterpart in the
+    reference (one kernel object per state there)."""
+
+    def __init__(self, configurations, members, precision: str = "mixed", autotune: bool = True):
+        lib = load_library()
+        if len(configurations) != len(members) or not configurations:
+            raise WVKernelError(1, "One member count per configuration is required.")
+        self.configurations = list(configurations)
+        self.members = [int(m) for m in members]
+        self.precision = precision
+        p = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED}[precision]
+        G = len(self.configurations)
+        cfgs = (_Config * G)(*(c._c() for c in self.configurations))
+        mem = (ctypes.c_int * G)(*self.members)
+        h = ctypes.c_void_p()
+        rc = lib.wv_ensemble_create(cfgs, mem, G, p, int(bool(autotune)), ctypes.byref(h))
+        if rc != 0:
+            for c in self.configurations:
+                describe(c)
+            raise WVKernelError(rc, "GPU ensemble creation failed")
+        self._h = h
+        self._lib = lib
+        self.sizes = []
+        for g in range(G):
+            s = _Sizes()
+            lib.wv_ensemble_get_sizes(h, g, ctypes.byref(s))
+            self.sizes.append({n: int(getattr(s, n)) for n, _ in _Sizes._fields_})
+        self.state_shapes = [(m, 3, s["Nkl"], c.Nj) for m, s, c in zip(self.members, self.sizes, self.configurations)]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.wv_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WVKernelError(rc, self._lib.wv_ensemble_last_message(self._h).decode())
+
+    def tuning(self):
+        out = []
+        for g in range(len(self.members)):
+            t = _EnsembleTuning()
+            self._check(self._lib.wv_ensemble_get_tuning(self._h, g, ctypes.byref(t)))
+            out.append({"warp_y_available": bool(t.warp_y_available), "warp_x_available": bool(t.warp_x_available),
+                        "y": "stockham" if t.stockham_y or not t.warp_y_available else "warp",
+                        "x": "stockham" if t.stockham_x or not t.warp_x_available else "warp",
+                        "candidate_ms": list(t.candidate_ms)[:max(0, min(4, t.candidates))], "flux_ms": t.flux_ms})
+        return out
+
+    def metrics(self):
+        m = _EnsembleMetrics()
+        self._check(self._lib.wv_ensemble_get_metrics(self._h, ctypes.byref(m)))
+        return {n: int(getattr(m, n)) for n, _ in _EnsembleMetrics._fields_}
+
+    def rk4(self, states, t, t0, dt, steps):
+        """Advances every group's states in place.  t and dt: one time and one
+        step per group (or a scalar for all).  Returns the groups' times after
+        `steps` steps."""
+        import torch
+        G = len(self.members)
+        if len(states) != G:
+            raise WVKernelError(2, "One state tensor per group is required.")
+        for x, shape in zip(states, self.state_shapes):
+            if x.dtype != torch.complex128 or tuple(x.shape) != shape or not x.is_contiguous() or not x.is_cuda:
+                raise WVKernelError(2, f"Group states must be contiguous complex128 CUDA tensors of shape {shape}.")
+        dts = [float(dt)] * G if np.isscalar(dt) else [float(x) for x in dt]
+        ts = [float(t)] * G if np.isscalar(t) else [float(x) for x in t]
+        if len(dts) != G or len(ts) != G:
+            raise WVKernelError(2, "One time and one step per group are required.")
+        ptrs = (ctypes.c_void_p * G)(*(x.data_ptr() for x in states))
+        dd = (ctypes.c_double * G)(*dts)
+        tt = (ctypes.c_double * G)(*ts)
+        self._check(self._lib.wv_ensemble_rk4_device(self._h, ptrs, tt, float(t0), dd, int(steps),
+                                                     WVTransformConstantStratificationKernel._stream()))
+        return list(tt)
 
 
 # ---------------------------------------------------------------------------
