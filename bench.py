@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--profile-flux", choices=["fp64", "mixed"], default=None,
+                    help="only run --profile-count nonlinear fluxes of the 256x256x129 workload (for ncu captures)")
+    ap.add_argument("--profile-count", type=int, default=3)
     return ap.parse_args()
 
 
@@ -497,9 +500,32 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_profile_case(args):
+    """A few nonlinear fluxes of the benchmark state, nothing else: the launch
+    sequence is vinv, yinv, x products, yfwd, vfwd per flux."""
+    import numpy as np
+    import torch
+    import wvgpu
+    from wvgpu import build
+    build.build()
+    k = wvgpu.WVTransformConstantStratificationKernel(configuration(wvgpu), precision=args.profile_flux)
+    state = wvgpu.synthetic_state(k, seed=SEED, urms=URMS)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+    out = tuple(torch.empty_like(dev[0]) for _ in range(3))
+    torch.cuda.synchronize()
+    for _ in range(args.profile_count):
+        k.nonlinearFlux(0.0, 0.0, *dev, out=out)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_flux": args.profile_flux, "fluxes": args.profile_count,
+                      "launches": k.metrics()["kernel_launches"]}))
+    k.close()
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile_flux:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

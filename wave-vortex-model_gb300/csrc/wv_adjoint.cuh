@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict
             for (int t = 0; t < nt; ++t) {
                 if (d.tq[t] == c) {  // x-derivative row of target c: (i k)^* = -i k
                     const cx<T> g = gspec[(3 + 3 * t) * KX + k];
-                    const T kk = T(d.rowK[k]);
+                    const T kk = row_k<T>(d)[k];
                     v = mk<T>(v.x + kk * g.y, v.y - kk * g.x);
                 }
             }
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __rest
             cx<T> v = fadj[((size_t)ch * Nz + zz) * P + p];
             if (ych >= 0) {
                 const cx<T> g = fadj[((size_t)ych * Nz + zz) * P + p];
-                const T l = T(d.rowL[d.posKy[p]]);
+                const T l = row_l<T>(d)[d.posKy[p]];
                 v = mk<T>(v.x + l * g.y, v.y - l * g.x);  // + (-i l) g
             }
             return v;

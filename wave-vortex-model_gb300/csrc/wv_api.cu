@@ -125,6 +125,43 @@ std::vector<double> interleave(const std::vector<wvgpu::cdouble>& v) {
 template <typename T>
 std::vector<T> cast(const std::vector<double>& v) { return std::vector<T>(v.begin(), v.end()); }
 
+// Flux projection of the mixed form, folded per (mode, j) in FP64 and rounded
+// once to FP32 (projectFluxTargetMode, kernel.cpp:396-431, written as one
+// linear map of the channel values u, v, w, eta):
+//   f0   = i Du u + i Dv v + Dn eta
+//   wave = Cu u + Cv v + Cw w,   b = Npm eta - B f0,   cp = wave + b,  cm = wave - b
+// Layout [M][12]: Cu.re Cu.im Cv.re Cv.im | Cw.re Cw.im Du Dv | Dn Npm B 0.
+// The inertial row (mode 0) keeps its own formula in the kernel.
+std::vector<float> mixed_flux_projection(const wvgpu::Descriptor& d) {
+    std::vector<float> out(12 * d.M, 0.0f);
+    const bool hydro = d.c.is_hydrostatic;
+    const size_t Nj = d.c.Nj;
+    for (size_t w = 0; w < d.Nkl; ++w) {
+        for (size_t j = 0; j < Nj; ++j) {
+            const size_t idx = j + Nj * w;
+            float* o = out.data() + 12 * idx;
+            double cu[2] = {0, 0}, cv[2] = {0, 0}, cw[2] = {0, 0};
+            if (hydro) {
+                const double ar = d.ApmD[idx].real(), ai = d.ApmD[idx].imag();
+                cu[0] = -d.k[w] * ai; cu[1] = d.k[w] * ar;   // i k ApmD
+                cv[0] = -d.l[w] * ai; cv[1] = d.l[w] * ar;   // i l ApmD
+            } else {
+                cu[0] = d.cosAlpha[w] * d.ApmDScaled[idx];
+                cv[0] = d.sinAlpha[w] * d.ApmDScaled[idx];
+                cw[1] = (d.Kh[w] / 2.0) * d.apmWProjectionPrefactor[j];
+            }
+            o[0] = float(cu[0]); o[1] = float(cu[1]); o[2] = float(cv[0]); o[3] = float(cv[1]);
+            o[4] = float(cw[0]); o[5] = float(cw[1]);
+            o[6] = float(-d.l[w] * d.A0FromVorticity[idx]);
+            o[7] = float(d.k[w] * d.A0FromVorticity[idx]);
+            o[8] = float(d.A0FromBuoyancy[idx]);
+            o[9] = float(d.ApmN[idx]);
+            o[10] = float(d.NA0[idx] * d.ApmN[idx]);
+        }
+    }
+    return out;
+}
+
 size_t elem_size(int precision) { return precision == WV_PRECISION_FP64 ? sizeof(double) : sizeof(float); }
 
 // Scratch element counts (complex) of the flux pipeline.
@@ -351,8 +388,10 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     auto* f = static_cast<dev::cx<T>*>(h->fspec);
     const int nt = p.targets.count;
     const bool inst = h->instrument;
+    // max |u_h| is reduced only when adaptive damping consumes it
+    unsigned long long* speed = damping ? h->maxSpeed : nullptr;
     if (inst) cudaEventRecord(h->ev[0], s);
-    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, h->maxSpeed);
+    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
     if (inst) cudaEventRecord(h->ev[1], s);
     dev::YInvMap map{};
     map.nOut = 4 + 2 * nt;
@@ -363,12 +402,12 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     }
     launch_yinv<T>(h, map, z, y, s);
     if (inst) cudaEventRecord(h->ev[2], s);
-    launch_xflux<T>(h, y, ps, h->maxSpeed, s);
+    launch_xflux<T>(h, y, ps, speed, s);
     if (inst) cudaEventRecord(h->ev[3], s);
     launch_yfwd<T>(h, ps, nt, f, s);
     if (inst) cudaEventRecord(h->ev[4], s);
     dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
-        d, f, nt, elapsed, Ap, Am, A0, h->maxSpeed, damping ? 1 : 0, Fp, Fm, F0);
+        d, f, nt, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
     h->metrics.kernel_launches += 5;
     cudaError_t e = cudaGetLastError();
     if (inst && e == cudaSuccess) {
@@ -745,8 +784,8 @@ cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* 
     auto* y = reinterpret_cast<dev::cx<T>*>(base + offs[1]);
     auto* ps = reinterpret_cast<dev::cx<T>*>(base + offs[2]);
     auto* f = reinterpret_cast<dev::cx<T>*>(base + offs[3]);
-    // k_vinv clears this counter (block 0) before k_xflux accumulates into it.
-    auto* speed = reinterpret_cast<unsigned long long*>(base + offs[4]);
+    // No damping on this entry, so no max-speed reduction (offs[4] stays reserved).
+    unsigned long long* speed = nullptr;
     const int nt = p.targets.count;
     dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
     dev::YInvMap map{};
@@ -893,6 +932,13 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     };
     upT(p.Ccos, &dd.Ccos); upT(p.Csin, &dd.Csin); upT(p.CcosM, &dd.CcosM); upT(p.CsinM, &dd.CsinM);
     upT(p.Fcos, &dd.Fcos); upT(p.Fsin, &dd.Fsin); upT(p.twx, &dd.twx); upT(p.twxN, &dd.twxN); upT(p.twy, &dd.twy);
+    upT(p.rowK, &dd.tRowK); upT(p.rowL, &dd.tRowL);
+    if (precision == WV_PRECISION_MIXED && e == cudaSuccess) {
+        const std::vector<float> proj = mixed_flux_projection(d);
+        const float* q = nullptr;
+        e = upload(h, proj, &q);
+        dd.fProj = q;
+    }
     const auto ss = scratch_sizes(p);
     const size_t cb = 2 * elem_size(precision);
     const size_t R = p.Nx * p.Ny * p.Nz;

@@ -219,6 +219,11 @@ struct DescDev {
     const unsigned char* modeFlags;
     const double* rowK;     // [kxColumns]
     const double* rowL;     // [Ny]
+    const void* tRowK;      // rowK, rowL in the working type of the xy stage
+    const void* tRowL;
+    // MIXED handles: flux projection coefficients per (mode, j), 12 floats each:
+    // Cu, Cv, Cw (complex), Du, Dv (imaginary parts), Dn, Npm, B; see k_vfwd.
+    const float* fProj;
     const void* Ccos;       // T[zHalf][Nj]
     const void* Csin;
     const void* CcosM;
@@ -232,6 +237,13 @@ struct DescDev {
     int xLen;               // Nx/2 (even) or Nx (odd)
     FFTDev fx, fy;          // fx factors xLen
 };
+
+// Row wavenumbers in the working type T of the xy stage.
+template <typename T>
+__device__ __forceinline__ const T* row_k(const DescDev& d) { return static_cast<const T*>(d.tRowK); }
+template <typename T>
+__device__ __forceinline__ const T* row_l(const DescDev& d) { return static_cast<const T*>(d.tRowL); }
+
 
 // ---------------------------------------------------------------------------
 // vinv: evolved field spectra + vertical inverse contraction.
@@ -430,7 +442,7 @@ __global__ void __launch_bounds__(256) k_yinv(DescDev d, YInvMap map, const cx<T
             const int ky = d.posKy[p];
             cx<T> v = in[p];
             if (map.mulL[oc]) {
-                const T l = T(d.rowL[ky]);
+                const T l = row_l<T>(d)[ky];
                 v = mk<T>(-l * v.y, l * v.x);
             }
             bufA[gi * Ny + ky] = v;
@@ -457,12 +469,12 @@ __global__ void __launch_bounds__(256) k_yinv(DescDev d, YInvMap map, const cx<T
 // Half-spectrum value at 0 <= k <= Nx/2 (zero for k >= KX), optionally times
 // i*k_row; imaginary parts at k = 0 and k = Nx/2 are dropped (c2r semantics).
 template <typename T>
-__device__ __forceinline__ cx<T> half_at(const cx<T>* h, int k, int KX, int Nx, const double* rowK, bool useK) {
+__device__ __forceinline__ cx<T> half_at(const cx<T>* h, int k, int KX, int Nx, const T* rowK, bool useK) {
     if (k >= KX) return mk<T>(T(0), T(0));
     cx<T> v = h[k];
     if (k == 0 || 2 * k == Nx) v.y = T(0);
     if (useK) {
-        const T kk = T(rowK[k]);
+        const T kk = rowK[k];
         v = mk<T>(-kk * v.y, kk * v.x);
     }
     return v;
@@ -474,14 +486,14 @@ __device__ __forceinline__ cx<T> c2r_line_entry(const DescDev& d, const cx<T>* h
     const int Nx = d.Nx, KX = d.kxColumns;
     if (d.xEven) {
         const int M = Nx >> 1;
-        const cx<T> a = half_at<T>(h, k, KX, Nx, d.rowK, useK);
-        const cx<T> b = cconj<T>(half_at<T>(h, M - k, KX, Nx, d.rowK, useK));
+        const cx<T> a = half_at<T>(h, k, KX, Nx, row_k<T>(d), useK);
+        const cx<T> b = cconj<T>(half_at<T>(h, M - k, KX, Nx, row_k<T>(d), useK));
         const cx<T> e = cadd<T>(a, b);
         const cx<T> o = cmul<T>(csub<T>(a, b), cconj<T>(twN[k]));  // * exp(+2 pi i k/Nx)
         return mk<T>(e.x - o.y, e.y + o.x);                        // e + i o
     }
-    if (2 * k <= Nx) return half_at<T>(h, k, KX, Nx, d.rowK, useK);
-    return cconj<T>(half_at<T>(h, Nx - k, KX, Nx, d.rowK, useK));
+    if (2 * k <= Nx) return half_at<T>(h, k, KX, Nx, row_k<T>(d), useK);
+    return cconj<T>(half_at<T>(h, Nx - k, KX, Nx, row_k<T>(d), useK));
 }
 
 // Real sample x of the row from the inverse-transformed line.
@@ -566,24 +578,30 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
     }
     // quadratic products S_q = -(u q_x + v q_y + w q_z) and max horizontal speed
     T* S = reinterpret_cast<T*>(bufA);  // [nt][Nx] reals (bufA holds 16 L >= 4 Nx reals)
-    double vmax = 0.0;
+    // max |u_h| (only when a consumer asked for it): max of u^2 + v^2, one sqrt
+    // at the end -- sqrt is correctly rounded and monotone, so this equals the
+    // max over points of sqrt(u^2 + v^2)
+    const bool wantSpeed = maxSpeedBits != nullptr;
+    double vmax2 = 0.0;
     for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
         const T U = phys[0 * Nx + x], V = phys[1 * Nx + x], W = phys[2 * Nx + x];
         for (int t = 0; t < nt; ++t) {
             const T qx = phys[(3 + 3 * t) * Nx + x], qy = phys[(4 + 3 * t) * Nx + x], qz = phys[(5 + 3 * t) * Nx + x];
             S[t * Nx + x] = -(U * qx + V * qy + W * qz);
         }
-        const double sp = sqrt(double(U) * double(U) + double(V) * double(V));
-        vmax = fmax(vmax, sp);
+        if (wantSpeed) vmax2 = fmax(vmax2, double(U) * double(U) + double(V) * double(V));
     }
-    for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-    __shared__ double red[32];
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmax(m, red[i]);
-        if (maxSpeedBits) atomicMax(maxSpeedBits + z / d.Nz, (unsigned long long)__double_as_longlong(m));
+    __syncthreads();  // S complete before the forward real transforms read it
+    if (wantSpeed) {
+        for (int o = 16; o > 0; o >>= 1) vmax2 = fmax(vmax2, __shfl_xor_sync(0xffffffffu, vmax2, o));
+        __shared__ double red[32];
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax2;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double m = 0.0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmax(m, red[i]);
+            atomicMax(maxSpeedBits + z / d.Nz, (unsigned long long)__double_as_longlong(sqrt(m)));
+        }
     }
     // forward real transform of each S_q
     for (int i = threadIdx.x; i < nt * L; i += blockDim.x) {
@@ -765,8 +783,8 @@ __global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict
         const bool evenJ = (j & 1) == 0;
         const T* fc = Fc + (size_t)j * Zh;
         const T* fs = Fs + (size_t)j * Zh;
-        // forward vertical transform of each channel
-        zd val[4] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+        // forward vertical transform of each channel (stored frame -> canonical)
+        T vr[4] = {T(0), T(0), T(0), T(0)}, vi[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             if (c >= nch) break;
@@ -785,10 +803,56 @@ __global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict
                 re += f * s.x;
                 im += f * s.y;
             }
-            zd z{double(re), double(im)};
-            if (conj) z = zconj(z);
-            val[c] = z;
+            vr[c] = re;
+            vi[c] = conj ? -im : im;
         }
+        if constexpr (FLUX && sizeof(T) == 4) {
+            // MIXED flux: projection with the folded FP32 coefficients and an FP32
+            // phase after FP64 angle reduction; FP64 only for the angle and the stores.
+            float2 ch[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (c >= nch) break;
+                ch[d.tq[c]] = make_float2(float(vr[c]), float(vi[c]));
+            }
+            const float2 U = ch[0], V = ch[1], Wc = ch[2], N = ch[3];
+            const float4* pj = reinterpret_cast<const float4*>(d.fProj + 12 * (size_t)idx);
+            const float4 p0 = pj[0], p1 = pj[1], p2 = pj[2];
+            const float f0r = -p1.z * U.y - p1.w * V.y + p2.x * N.x;
+            const float f0i = p1.z * U.x + p1.w * V.x + p2.x * N.y;
+            float cpr, cpi, cmr, cmi;
+            if (w == 0) {
+                const float sc = float(d.inertialScale[j]);
+                cpr = sc * (U.x + V.y);
+                cpi = sc * (U.y - V.x);
+                cmr = cpr;
+                cmi = -cpi;
+            } else {
+                const float wr = p0.x * U.x - p0.y * U.y + p0.z * V.x - p0.w * V.y + p1.x * Wc.x - p1.y * Wc.y;
+                const float wi = p0.x * U.y + p0.y * U.x + p0.z * V.y + p0.w * V.x + p1.x * Wc.y + p1.y * Wc.x;
+                const float br = p2.y * N.x - p2.z * f0r, bi = p2.y * N.y - p2.z * f0i;
+                cpr = wr + br; cpi = wi + bi; cmr = wr - br; cmi = wi - bi;
+            }
+            const double ang = d.omega[idx] * elapsed;
+            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+            float sn, cs;
+            sincosf(float(red), &sn, &cs);
+            zd fp{double(cpr * cs + cpi * sn), double(cpi * cs - cpr * sn)};   // (cp) * conj(p)
+            zd fm{double(cmr * cs - cmi * sn), double(cmr * sn + cmi * cs)};   // (cm) * p
+            zd f0{double(f0r), double(f0i)};
+            if (applyDamping) {
+                const double sd = __dmul_rn(maxSpeed, d.damping[idx]);
+                fp = zadd(fp, zscale(zload(Ap + 2 * idx), sd));
+                fm = zadd(fm, zscale(zload(Am + 2 * idx), sd));
+                f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sd));
+            }
+            zstore(Fp + 2 * idx, fp);
+            zstore(Fm + 2 * idx, fm);
+            zstore(F0 + 2 * idx, f0);
+        } else {
+        zd val[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) val[c] = zd{double(vr[c]), double(vi[c])};
     const double k = d.k[w], l = d.l[w];
         double s, cph;
         sincos(d.omega[idx] * elapsed, &s, &cph);
@@ -876,6 +940,7 @@ __global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict
             zstore(Fm + 2 * idx, zmul(cm, p));
             zstore(F0 + 2 * idx, a0);
         }
+        }  // FP64 projection
     }
 }
 

@@ -120,6 +120,16 @@ __device__ __forceinline__ int p_index(int k1, int lane) { return k1 + R * brev_
 
 constexpr int kWG = 8;  // kx columns (y pass) or rows (x pass) per CTA: one per warp
 
+// Slot of element (row y, column c) of an [N][kWG] transpose tile, N = 32*R:
+// columns XOR-swizzled by bits of (y>>1) ^ (y/R >> 2).  A warp storing the
+// rows k1 + R*brev5(lane) of one column (fft_P's output) meets 2-way bank
+// conflicts at most; loading the rows lane + 32r of one column, or sweeping
+// the tile row-major, meets none (checked for R = 1, 2, 3, 4, 6, 8, 16).
+template <int R>
+__device__ __forceinline__ int tile_at(int y, int c) {
+    return y * kWG + (c ^ (((y >> 1) ^ ((y / R) >> 2)) & (kWG - 1)));
+}
+
 // ---------------------------------------------------------------------------
 // y inverse: CTA = (8 kx columns, plane z, output channel); warp = one column.
 
@@ -148,21 +158,21 @@ __global__ void __launch_bounds__(256) k_yinv_w(DescDev d, YInvMap map, const cx
             const int pos = ym[y];
             cx<T> val = pos >= 0 ? in[pos] : mk<T>(T(0), T(0));
             if (mulL) {
-                const T l = T(d.rowL[y]);
+                const T l = row_l<T>(d)[y];
                 val = mk<T>(-l * val.y, l * val.x);
             }
             v[r] = val;
         }
         fft_P<T, R, true>(v, tw, lane);
 #pragma unroll
-        for (int k1 = 0; k1 < R; ++k1) tile[p_index<R>(k1, lane) * kWG + warp] = v[k1];
+        for (int k1 = 0; k1 < R; ++k1) tile[tile_at<R>(p_index<R>(k1, lane), warp)] = v[k1];
     }
     __syncthreads();
     const int g = min(kWG, KX - kx0);
     cx<T>* out = yspec + (((size_t)z * map.nOut + oc) * N) * KX + kx0;
     for (int i = threadIdx.x; i < N * kWG; i += blockDim.x) {
         const int y = i / kWG, gi = i - y * kWG;
-        if (gi < g) out[(size_t)y * KX + gi] = tile[i];
+        if (gi < g) out[(size_t)y * KX + gi] = tile[tile_at<R>(y, gi)];
     }
 }
 
@@ -183,22 +193,22 @@ __global__ void __launch_bounds__(256) k_yfwd_w(DescDev d, const cx<T>* __restri
     const cx<T>* in = pspec + (((size_t)z * nch + c) * N) * KX + kx0;
     for (int i = threadIdx.x; i < N * kWG; i += blockDim.x) {
         const int y = i / kWG, gi = i - y * kWG;
-        tile[i] = gi < g ? in[(size_t)y * KX + gi] : mk<T>(T(0), T(0));
+        tile[tile_at<R>(y, gi)] = gi < g ? in[(size_t)y * KX + gi] : mk<T>(T(0), T(0));
     }
     __syncthreads();
     const int kx = kx0 + warp;
     if (kx >= KX) return;
     cx<T> v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = tile[(lane + 32 * r) * kWG + warp];
+    for (int r = 0; r < R; ++r) v[r] = tile[tile_at<R>(lane + 32 * r, warp)];
     fft_P<T, R, false>(v, tw, lane);
     __syncwarp();
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) tile[p_index<R>(k1, lane) * kWG + warp] = v[k1];
+    for (int k1 = 0; k1 < R; ++k1) tile[tile_at<R>(p_index<R>(k1, lane), warp)] = v[k1];
     __syncwarp();
     cx<T>* out = fspec + ((size_t)c * d.zTotal + z) * P;
     const int pBeg = d.colStart[kx], pEnd = d.colStart[kx + 1];
-    for (int p = pBeg + lane; p < pEnd; p += 32) out[p] = tile[d.posKy[p] * kWG + warp];
+    for (int p = pBeg + lane; p < pEnd; p += 32) out[p] = tile[tile_at<R>(d.posKy[p], warp)];
 }
 
 // ---------------------------------------------------------------------------
@@ -243,11 +253,15 @@ __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __re
     c2r_row<T, R>(d, row + 0 * cstride, false, twL, twN, lane, U);
     c2r_row<T, R>(d, row + 1 * cstride, false, twL, twN, lane, V);
     c2r_row<T, R>(d, row + 2 * cstride, false, twL, twN, lane, W);
-    double vmax = 0.0;
+    // max |u_h| only when a consumer asked for it (max of u^2 + v^2, one sqrt at the end)
+    const bool wantSpeed = maxSpeedBits != nullptr;
+    double vmax2 = 0.0;
+    if (wantSpeed) {
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-        vmax = fmax(vmax, sqrt(double(U[k].x) * double(U[k].x) + double(V[k].x) * double(V[k].x)));
-        vmax = fmax(vmax, sqrt(double(U[k].y) * double(U[k].y) + double(V[k].y) * double(V[k].y)));
+        for (int k = 0; k < R; ++k) {
+            vmax2 = fmax(vmax2, double(U[k].x) * double(U[k].x) + double(V[k].x) * double(V[k].x));
+            vmax2 = fmax(vmax2, double(U[k].y) * double(U[k].y) + double(V[k].y) * double(V[k].y));
+        }
     }
 #pragma unroll 1
     for (int t = 0; t < nt; ++t) {
@@ -274,17 +288,18 @@ __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __re
         for (int k = lane; k < KX; k += 32) out[k] = r2c_value<T>(d, line, k, twN);
         __syncwarp();
     }
+    if (!wantSpeed) return;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    for (int o = 16; o > 0; o >>= 1) vmax2 = fmax(vmax2, __shfl_xor_sync(0xffffffffu, vmax2, o));
     // one atomic per CTA: the rows of this CTA reduce through shared memory
     if (lane == 0) {
-        warpMax[warp] = vmax;
+        warpMax[warp] = vmax2;
         __threadfence_block();
         const int rows = min(kWG, Ny - (int)blockIdx.x * kWG);
-        if (atomicAdd(&warpsDone, 1) == rows - 1 && maxSpeedBits) {
+        if (atomicAdd(&warpsDone, 1) == rows - 1) {
             double m = 0.0;
             for (int i = 0; i < rows; ++i) m = fmax(m, warpMax[i]);
-            atomicMax(maxSpeedBits + z / d.Nz, (unsigned long long)__double_as_longlong(m));
+            atomicMax(maxSpeedBits + z / d.Nz, (unsigned long long)__double_as_longlong(sqrt(m)));
         }
     }
 }
