@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--profile-flux", choices=["fp64", "mixed"], default=None,
                     help="only run --profile-count nonlinear fluxes of the 256x256x129 workload (for ncu captures)")
     ap.add_argument("--profile-count", type=int, default=3)
+    ap.add_argument("--profile-vjp", action="store_true", help="with --profile-flux: also run as many flux VJPs")
     return ap.parse_args()
 
 
@@ -515,6 +516,9 @@ def run_profile_case(args):
     torch.cuda.synchronize()
     for _ in range(args.profile_count):
         k.nonlinearFlux(0.0, 0.0, *dev, out=out)
+    if args.profile_vjp:
+        for _ in range(args.profile_count):
+            k.flux_vjp(0.0, 0.0, *dev, *out)
     torch.cuda.synchronize()
     print(json.dumps({"profile_flux": args.profile_flux, "fluxes": args.profile_count,
                       "launches": k.metrics()["kernel_launches"]}))

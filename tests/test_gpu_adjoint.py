@@ -189,9 +189,13 @@ def test_misfit_gradient_finite_differences(wv):
     k.close()
 
 
-def test_mixed_adjoint_close_to_fp64(wv):
-    """Mixed-precision VJP against the FP64 VJP (same state and cotangent)."""
-    c = O.Config(Nx=64, Ny=64, Nz=33, Nj=21, Lx=400e3, Ly=400e3, Lz=4000.0, latitude=33.0)
+@pytest.mark.parametrize("Nx,Nz,hydro", [(64, 33, False), (128, 65, False), (256, 129, False), (128, 65, True), (96, 49, False)])
+def test_mixed_adjoint_close_to_fp64(wv, Nx, Nz, hydro):
+    """Mixed-precision VJP against the FP64 VJP (same state and cotangent); the
+    mixed x pass adjoint runs on the warp FFTs for Nx = 64 R and on the
+    shared-memory kernel otherwise (Nx = 96)."""
+    c = O.Config(Nx=Nx, Ny=Nx, Nz=Nz, Nj=O.default_nj(Nz), Lx=3125.0 * Nx, Ly=3125.0 * Nx, Lz=4000.0, latitude=33.0,
+                 isHydrostatic=hydro)
     d = O.build_descriptor(c)
     rng = np.random.default_rng(9)
     A = O.spectrum_state(d, seed=3, urms=0.1)
@@ -201,7 +205,7 @@ def test_mixed_adjoint_close_to_fp64(wv):
     a = k64.flux_vjp(0.0, 0.0, *(dev(x) for x in A), *(dev(x) for x in Fb))
     b = k32.flux_vjp(0.0, 0.0, *(dev(x) for x in A), *(dev(x) for x in Fb))
     errs = [rel_err(host(y), host(x)) for x, y in zip(a, b)]
-    print("mixed vs fp64 flux VJP max-relative error (Apb, Amb, A0b):", errs)
+    print(f"mixed vs fp64 flux VJP max-relative error (Apb, Amb, A0b) {Nx}x{Nx}x{Nz} hydro={hydro}:", errs)
     assert max(errs) <= 1e-3
     k64.close()
     k32.close()

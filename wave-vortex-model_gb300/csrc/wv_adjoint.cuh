@@ -33,6 +33,45 @@ __global__ void __launch_bounds__(256) k_vfwd_adj(DescDev d, const double* __res
         const int mm = it % nm, j = it / nm;
         const int w = d.modeWV[m0 + mm];
         const int idx = j + Nj * w;
+        if constexpr (sizeof(T) == 4) {
+            // MIXED: transpose of the folded FP32 projection of k_vfwd, FP32 phase
+            // after FP64 angle reduction
+            const double ang = d.omega[idx] * elapsed;
+            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+            float sn, cs;
+            sincosf(float(red), &sn, &cs);
+            const float2 fpb = make_float2(float(Fpb[2 * idx]), float(Fpb[2 * idx + 1]));
+            const float2 fmb = make_float2(float(Fmb[2 * idx]), float(Fmb[2 * idx + 1]));
+            const float2 a0b = make_float2(float(F0b[2 * idx]), float(F0b[2 * idx + 1]));
+            const float2 cpb = make_float2(fpb.x * cs - fpb.y * sn, fpb.x * sn + fpb.y * cs);  // Fp_bar * p
+            const float2 cmb = make_float2(fmb.x * cs + fmb.y * sn, fmb.y * cs - fmb.x * sn);  // Fm_bar * conj(p)
+            float2 ch[4];
+            if (w == 0) {
+                const float sc = float(d.inertialScale[j]);
+                const float2 tot = make_float2(cpb.x + cmb.x, cpb.y - cmb.y);  // cp_bar + conj(cm_bar)
+                ch[0] = make_float2(sc * tot.x, sc * tot.y);
+                ch[1] = make_float2(-sc * tot.y, sc * tot.x);
+                ch[2] = make_float2(0.f, 0.f);
+                const float dn = d.fProj[12 * (size_t)idx + 8];
+                ch[3] = make_float2(dn * a0b.x, dn * a0b.y);
+            } else {
+                const float4* pj = reinterpret_cast<const float4*>(d.fProj + 12 * (size_t)idx);
+                const float4 p0 = pj[0], p1 = pj[1], p2 = pj[2];
+                const float2 wb = make_float2(cpb.x + cmb.x, cpb.y + cmb.y);
+                const float2 bb = make_float2(cpb.x - cmb.x, cpb.y - cmb.y);
+                const float2 f0b = make_float2(a0b.x - p2.z * bb.x, a0b.y - p2.z * bb.y);
+                // conj(C) * wave_bar - i D * f0_bar
+                ch[0] = make_float2(p0.x * wb.x + p0.y * wb.y + p1.z * f0b.y, p0.x * wb.y - p0.y * wb.x - p1.z * f0b.x);
+                ch[1] = make_float2(p0.z * wb.x + p0.w * wb.y + p1.w * f0b.y, p0.z * wb.y - p0.w * wb.x - p1.w * f0b.x);
+                ch[2] = make_float2(p1.x * wb.x + p1.y * wb.y, p1.x * wb.y - p1.y * wb.x);
+                ch[3] = make_float2(p2.y * bb.x + p2.x * f0b.x, p2.y * bb.y + p2.x * f0b.y);
+            }
+            for (int t = 0; t < nt; ++t) {
+                const float2 v = ch[d.tq[t]];
+                vb[(t * Nj + j) * kVfwdModes + mm] = mk<T>(T(v.x), T(v.y));
+            }
+            continue;
+        }
         double s, c;
         sincos(d.omega[idx] * elapsed, &s, &c);
         const zd fpb = zload(Fpb + 2 * idx), fmb = zload(Fmb + 2 * idx), a0b = zload(F0b + 2 * idx);
@@ -77,8 +116,8 @@ __global__ void __launch_bounds__(256) k_vfwd_adj(DescDev d, const double* __res
         }
     }
     __syncthreads();
-    const T* Fc = reinterpret_cast<const T*>(d.Fcos);
-    const T* Fs = reinterpret_cast<const T*>(d.Fsin);
+    const T* Fc = reinterpret_cast<const T*>(d.FcosT);   // [Zh][Nj]
+    const T* Fs = reinterpret_cast<const T*>(d.FsinT);
     for (int it = threadIdx.x; it < nm * Zh; it += blockDim.x) {
         const int n = it / nm, mm = it - n * nm;
         const int mode = m0 + mm;
@@ -89,9 +128,10 @@ __global__ void __launch_bounds__(256) k_vfwd_adj(DescDev d, const double* __res
             const bool cosine = d.tq[t] < 2;
             const T* F = cosine ? Fc : Fs;
             T E[2] = {T(0), T(0)}, O[2] = {T(0), T(0)};
+            const T* Fn = F + (size_t)n * Nj;
             for (int j = 0; j < Nj; ++j) {
                 const cx<T> v = vb[(t * Nj + j) * kVfwdModes + mm];
-                const T f = F[(size_t)j * Zh + n];
+                const T f = Fn[j];
                 if (j & 1) { O[0] += f * v.x; O[1] += f * v.y; } else { E[0] += f * v.x; E[1] += f * v.y; }
             }
             cx<T>* base = zadj + (size_t)t * Nz * P;
@@ -112,9 +152,11 @@ __global__ void __launch_bounds__(256) k_vfwd_adj(DescDev d, const double* __res
 // ---------------------------------------------------------------------------
 // x pass adjoint, one CTA per (y, z) row (shared-memory Stockham FFTs).
 
+// physIn, when given, holds the forward real rows [z][nReal][y][Nx] (as
+// k_xflux keeps them); otherwise they are recomputed from yspec.
 template <typename T>
 __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict__ yspec, const cx<T>* __restrict__ yadj,
-                                             cx<T>* __restrict__ yout) {
+                                             cx<T>* __restrict__ yout, const T* __restrict__ physIn) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Nx = d.Nx, Ny = d.Ny, KX = d.kxColumns, nt = d.nt, L = d.xLen;
     const int nIn = 4 + 2 * nt;
@@ -133,9 +175,16 @@ __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict
     const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
     for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = twg[i];
     for (int i = threadIdx.x; i < Nx; i += blockDim.x) twN[i] = twgN[i];
-    for (int i = threadIdx.x; i < nIn * KX; i += blockDim.x) {
-        const int c = i / KX, k = i - c * KX;
-        specF[i] = yspec[(((size_t)z * nIn + c) * Ny + y) * KX + k];
+    if (physIn) {
+        for (int i = threadIdx.x; i < nReal * Nx; i += blockDim.x) {
+            const int r = i / Nx, x = i - r * Nx;
+            phys[i] = physIn[(((size_t)z * nReal + r) * Ny + y) * Nx + x];
+        }
+    } else {
+        for (int i = threadIdx.x; i < nIn * KX; i += blockDim.x) {
+            const int c = i / KX, k = i - c * KX;
+            specF[i] = yspec[(((size_t)z * nIn + c) * Ny + y) * KX + k];
+        }
     }
     for (int i = threadIdx.x; i < nt * KX; i += blockDim.x) {
         const int c = i / KX, k = i - c * KX;
@@ -152,9 +201,9 @@ __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict
         else if (kind == 1) { ch = 4 + t; useK = false; }
         else { ch = 4 + nt + t; useK = false; }
     };
-    // c2r: forward rows (nReal) then adjoint rows (nt)
+    // c2r: forward rows (nReal, unless kept) then adjoint rows (nt)
     const int nC2R = nReal + nt;
-    for (int rb = 0; rb < nC2R; rb += 8) {
+    for (int rb = physIn ? nReal : 0; rb < nC2R; rb += 8) {
         const int nr = min(8, nC2R - rb);
         for (int i = threadIdx.x; i < nr * L; i += blockDim.x) {
             const int li = i / L, k = i - li * L;
@@ -323,40 +372,72 @@ __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __rest
         pq[(oc * Zh + n) * kVinvModes + mm] = v;
     }
     __syncthreads();
-    const T* Cc = reinterpret_cast<const T*>(d.Ccos);
-    const T* Cs = reinterpret_cast<const T*>(d.Csin);
-    const T* Ccm = reinterpret_cast<const T*>(d.CcosM);
-    const T* Csm = reinterpret_cast<const T*>(d.CsinM);
+    const T* Cc = reinterpret_cast<const T*>(d.CcosT);   // [Nj][Zh]
+    const T* Cs = reinterpret_cast<const T*>(d.CsinT);
+    const T* Ccm = reinterpret_cast<const T*>(d.CcosMT);
+    const T* Csm = reinterpret_cast<const T*>(d.CsinMT);
     for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
         const int mm = it % nm, j = it / nm;
         const int w = d.modeWV[m0 + mm];
         const int idx = j + Nj * w;
         const bool evenJ = (j & 1) == 0;
         // transposed inverse matrices: cos family uses (S_n + S_{N-1-n}) for even j
-        auto contract = [&](int oc, const T* C, bool cosine) -> zd {
+        auto contract = [&](int oc, const T* C, bool cosine) -> cx<T> {
             const bool useP = cosine ? evenJ : !evenJ;
             T re = T(0), im = T(0);
             const cx2t<T>* col = pq + (size_t)oc * Zh * kVinvModes + mm;
+            const T* Cj = C + (size_t)j * Zh;
             for (int n = 0; n < Zh; ++n) {
                 const cx2t<T> v = col[n * kVinvModes];
-                const T f = C[(size_t)n * Nj + j];
+                const T f = Cj[n];
                 const cx<T> sv = useP ? v.p : v.q;
                 re += f * sv.x;
                 im += f * sv.y;
             }
-            return zd{double(re), double(im)};
+            return mk<T>(re, im);
         };
-        zd ub = contract(0, Cc, true), vbv = contract(1, Cc, true), wb = contract(2, Cs, false), nb = contract(3, Cs, false);
+        cx<T> ubT = contract(0, Cc, true), vbT = contract(1, Cc, true), wbT = contract(2, Cs, false), nbT = contract(3, Cs, false);
         if (FLUX) {
             for (int t = 0; t < nt; ++t) {
                 const int q = d.tq[t];
-                const zd zb = (q < 2) ? contract(4 + t, Csm, false) : contract(4 + t, Ccm, true);
-                if (q == 0) ub = zadd(ub, zb);
-                if (q == 1) vbv = zadd(vbv, zb);
-                if (q == 2) wb = zadd(wb, zb);
-                if (q == 3) nb = zadd(nb, zb);
+                const cx<T> zb = (q < 2) ? contract(4 + t, Csm, false) : contract(4 + t, Ccm, true);
+                if (q == 0) ubT = cadd<T>(ubT, zb);
+                if (q == 1) vbT = cadd<T>(vbT, zb);
+                if (q == 2) wbT = cadd<T>(wbT, zb);
+                if (q == 3) nbT = cadd<T>(nbT, zb);
             }
         }
+        if constexpr (sizeof(T) == 4) {
+            // MIXED: assembly adjoint with the FP32 field factors, FP32 phase after
+            // FP64 angle reduction
+            const float2 uap = *reinterpret_cast<const float2*>(d.fUAp + 2 * idx);
+            const float2 vap = *reinterpret_cast<const float2*>(d.fVAp + 2 * idx);
+            const float2 wap = *reinterpret_cast<const float2*>(d.fWAp + 2 * idx);
+            const float2 ua0 = *reinterpret_cast<const float2*>(d.fUA0 + 2 * idx);
+            const float2 va0 = *reinterpret_cast<const float2*>(d.fVA0 + 2 * idx);
+            const float nap = d.fNAp[idx], na0 = d.fNA0[idx];
+            auto cm = [](float2 a, cx<T> b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+            auto cjm = [](float2 a, cx<T> b) { return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); };
+            const float2 t1 = cjm(uap, ubT), t2 = cjm(vap, vbT), t3 = cjm(wap, wbT);
+            const float2 ape = make_float2(t1.x + t2.x + t3.x + nap * nbT.x, t1.y + t2.y + t3.y + nap * nbT.y);
+            const float2 s1 = cm(uap, ubT), s2 = cm(vap, vbT);
+            const float2 ame = make_float2(s1.x + s2.x + t3.x - nap * nbT.x, s1.y + s2.y + t3.y - nap * nbT.y);
+            const float2 r1 = cjm(ua0, ubT), r2 = cjm(va0, vbT);
+            const float2 a0 = make_float2(r1.x + r2.x + na0 * nbT.x, r1.y + r2.y + na0 * nbT.y);
+            const double ang = d.omega[idx] * elapsed;
+            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+            float sn, cs;
+            sincosf(float(red), &sn, &cs);
+            Apb[2 * idx] = double(ape.x * cs + ape.y * sn);   // ape * conj(p)
+            Apb[2 * idx + 1] = double(ape.y * cs - ape.x * sn);
+            Amb[2 * idx] = double(ame.x * cs - ame.y * sn);   // ame * p
+            Amb[2 * idx + 1] = double(ame.x * sn + ame.y * cs);
+            A0b[2 * idx] = double(a0.x);
+            A0b[2 * idx + 1] = double(a0.y);
+            continue;
+        }
+        const zd ub{double(ubT.x), double(ubT.y)}, vbv{double(vbT.x), double(vbT.y)};
+        const zd wb{double(wbT.x), double(wbT.y)}, nb{double(nbT.x), double(nbT.y)};
         // assembly adjoint (coefficientValueForField on evolved coefficients)
         const zd uap = zload(d.UAp + 2 * idx), vap = zload(d.VAp + 2 * idx), wap = zload(d.WAp + 2 * idx);
         const zd ua0 = zload(d.UA0 + 2 * idx), va0 = zload(d.VA0 + 2 * idx);

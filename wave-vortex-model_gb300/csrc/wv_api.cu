@@ -67,7 +67,7 @@ struct wv_handle {
     double* ybin = nullptr;
     std::vector<double*> checkpoints;  // multi-step adjoint: saved states
     std::vector<double*> segment;      // multi-step adjoint: states of one segment
-    std::vector<void*> ystore;         // multi-step adjoint: y spectra of each stage flux of one segment
+    std::vector<void*> ystore;         // multi-step adjoint: x-pass real rows of each stage flux of one segment
     bool instrument = false;
     cudaEvent_t ev[6] = {};
     wv_stage_times stages{};
@@ -338,15 +338,17 @@ void launch_yfwd(wv_handle* h, const dev::cx<T>* ps, int nch, dev::cx<T>* f, cud
 }
 
 template <typename T>
-void launch_xflux(wv_handle* h, const dev::cx<T>* y, dev::cx<T>* ps, unsigned long long* speed, cudaStream_t s) {
+void launch_xflux(wv_handle* h, const dev::cx<T>* y, dev::cx<T>* ps, unsigned long long* speed, cudaStream_t s,
+                  void* physOut = nullptr) {
     const Plan& p = h->plan;
     const int rx = warp_rx<T>(p);
     if (rx) {
         const dim3 grid(cdiv(p.Ny, dev::kWG), h->dd.zTotal);
-        WV_RSWITCH_X(T, rx, (dev::k_xflux_w<T, RR><<<grid, 256, smem_xflux_w<T>(p), s>>>(h->dd, y, ps, speed)));
+        WV_RSWITCH_X(T, rx, (dev::k_xflux_w<T, RR><<<grid, 256, smem_xflux_w<T>(p), s>>>(h->dd, y, ps, speed,
+                                                                                           static_cast<dev::cx<T>*>(physOut))));
         return;
     }
-    dev::k_xflux<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xflux<T>(p), s>>>(h->dd, y, ps, speed);
+    dev::k_xflux<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xflux<T>(p), s>>>(h->dd, y, ps, speed, static_cast<T*>(physOut));
 }
 
 template <typename T>
@@ -374,16 +376,16 @@ void launch_xr2c(wv_handle* h, const double* fields, int nch, dev::cx<T>* ps, cu
 }
 
 // One nonlinear flux (+ adaptive damping when requested) on device buffers.
-// yOut, when given, receives the y spectra of the 4+2nt channels (the x pass
-// input) in place of the handle's scratch, for the adjoint to reuse.
+// physOut, when given, receives the x pass's real rows (U, V, W and the
+// derivatives of every target) for the adjoint to reuse.
 template <typename T>
 cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
-                        double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s, void* yOut = nullptr) {
+                        double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s, void* physOut = nullptr) {
     const Plan& p = h->plan;
     const auto& d = h->dd;
     const double elapsed = t - t0;
     auto* z = static_cast<dev::cx<T>*>(h->zspec);
-    auto* y = static_cast<dev::cx<T>*>(yOut ? yOut : h->yspec);
+    auto* y = static_cast<dev::cx<T>*>(h->yspec);
     auto* ps = static_cast<dev::cx<T>*>(h->pspec);
     auto* f = static_cast<dev::cx<T>*>(h->fspec);
     const int nt = p.targets.count;
@@ -402,7 +404,7 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     }
     launch_yinv<T>(h, map, z, y, s);
     if (inst) cudaEventRecord(h->ev[2], s);
-    launch_xflux<T>(h, y, ps, speed, s);
+    launch_xflux<T>(h, y, ps, speed, s, physOut);
     if (inst) cudaEventRecord(h->ev[3], s);
     launch_yfwd<T>(h, ps, nt, f, s);
     if (inst) cudaEventRecord(h->ev[4], s);
@@ -468,6 +470,11 @@ size_t smem_xadj(const Plan& p) {
     return (L + p.Nx + (nIn + nt) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (2 * nReal + nt) * p.Nx * sizeof(T);
 }
 template <typename T>
+size_t smem_xadj_w(const Plan& p) {
+    const size_t L = p.Nx / 2;
+    return (3 * L + dev::kWG * (L + 4 * p.kxColumns)) * sizeof(dev::cx<T>);
+}
+template <typename T>
 size_t smem_xr2c_adj(const Plan& p) { return (x_len(p) + p.Nx + 8 * x_len(p)) * sizeof(dev::cx<T>) + 4 * p.Nx * sizeof(T); }
 template <typename T>
 size_t smem_vinv_adj(const Plan& p, bool flux) {
@@ -485,6 +492,11 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
     if (e != cudaSuccess) return e;
     WV_SET((dev::k_vfwd_adj<T>), smem_vfwd_adj<T>(p));
     WV_SET((dev::k_xadj<T>), smem_xadj<T>(p));
+    {
+        const int rx = warp_rx<T>(p);
+        WV_RSWITCH_X(T, rx, e = raise_smem_limit(dev::k_xadj_w<T, RR>, (int)smem_xadj_w<T>(p)));
+        if (e != cudaSuccess) return e;
+    }
     WV_SET((dev::k_xr2c_adj<T>), smem_xr2c_adj<T>(p));
     WV_SET((dev::k_vinv_adj<T, true>), smem_vinv_adj<T>(p, true));
     WV_SET((dev::k_vinv_adj<T, false>), smem_vinv_adj<T>(p, false));
@@ -540,12 +552,12 @@ void launch_flux_fields(wv_handle* h, double elapsed, const double* Ap, const do
     h->metrics.kernel_launches += 2;
 }
 
-// yIn, when given, holds the y spectra of the flux input channels at this
-// state (kept by the forward flux); otherwise they are recomputed.
+// physIn, when given, holds the forward x pass's real rows at this state
+// (kept by the forward flux); otherwise the forward fields are recomputed.
 template <typename T>
 cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
                             const double* Fpb, const double* Fmb, const double* F0b, double* Apb, double* Amb, double* A0b,
-                            cudaStream_t s, const void* yIn = nullptr) {
+                            cudaStream_t s, const void* physIn = nullptr) {
     const Plan& p = h->plan;
     const auto& d = h->dd;
     const double elapsed = t - t0;
@@ -555,18 +567,22 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
     auto* yo = static_cast<dev::cx<T>*>(h->yout);
     auto* fa = static_cast<dev::cx<T>*>(h->fadj);
     // forward fields of this state
-    const dev::cx<T>* y = static_cast<const dev::cx<T>*>(yIn);
-    if (!y) {
-        launch_flux_fields<T>(h, elapsed, Ap, Am, A0, static_cast<dev::cx<T>*>(h->yspec), s);
-        y = static_cast<const dev::cx<T>*>(h->yspec);
-    }
+    const dev::cx<T>* y = static_cast<const dev::cx<T>*>(h->yspec);
+    if (!physIn) launch_flux_fields<T>(h, elapsed, Ap, Am, A0, static_cast<dev::cx<T>*>(h->yspec), s);
     // adjoint of projection and forward vertical transform, then inverse y FFTs
     dev::k_vfwd_adj<T><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd_adj<T>(p), s>>>(d, Fpb, Fmb, F0b, elapsed, za);
     dev::YInvMap amap{};
     amap.nOut = nt;
     for (int c = 0; c < nt; ++c) { amap.src[c] = c; amap.mulL[c] = 0; }
     launch_yinv<T>(h, amap, za, ya, s);
-    dev::k_xadj<T><<<dim3(p.Ny, p.Nz), 256, smem_xadj<T>(p), s>>>(d, y, ya, yo);
+    const int rx = warp_rx<T>(p);
+    if (rx) {
+        const dim3 grid(cdiv(p.Ny, dev::kWG), p.Nz);
+        WV_RSWITCH_X(T, rx, (dev::k_xadj_w<T, RR><<<grid, 256, smem_xadj_w<T>(p), s>>>(
+                                 d, y, ya, yo, static_cast<const dev::cx<T>*>(physIn))));
+    } else {
+        dev::k_xadj<T><<<dim3(p.Ny, p.Nz), 256, smem_xadj<T>(p), s>>>(d, y, ya, yo, static_cast<const T*>(physIn));
+    }
     launch_yfwd<T>(h, yo, nIn, fa, s);
     dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
     h->metrics.kernel_launches += 5;
@@ -589,25 +605,17 @@ cudaError_t launch_inverse_vjp(wv_handle* h, double t, double t0, const double* 
 }
 
 cudaError_t flux_vjp_any(wv_handle* h, double t, double t0, const double* y, const double* yb, double* out, cudaStream_t s,
-                         const void* yIn = nullptr) {
+                         const void* physIn = nullptr) {
     const size_t M2 = 2 * h->plan.M;
     return h->precision == WV_PRECISION_FP64
-               ? launch_flux_vjp<double>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, yIn)
-               : launch_flux_vjp<float>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, yIn);
+               ? launch_flux_vjp<double>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, physIn)
+               : launch_flux_vjp<float>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, physIn);
 }
 
 cudaError_t flux_any(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
-                     double* Fm, double* F0, bool damping, cudaStream_t s, void* yOut = nullptr) {
-    return h->precision == WV_PRECISION_FP64 ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, yOut)
-                                             : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, yOut);
-}
-
-void flux_fields_any(wv_handle* h, double t, double t0, const double* y, void* yOut, cudaStream_t s) {
-    const size_t M2 = 2 * h->plan.M;
-    if (h->precision == WV_PRECISION_FP64)
-        launch_flux_fields<double>(h, t - t0, y, y + M2, y + 2 * M2, static_cast<dev::cx<double>*>(yOut), s);
-    else
-        launch_flux_fields<float>(h, t - t0, y, y + M2, y + 2 * M2, static_cast<dev::cx<float>*>(yOut), s);
+                     double* Fm, double* F0, bool damping, cudaStream_t s, void* physOut = nullptr) {
+    return h->precision == WV_PRECISION_FP64 ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut)
+                                             : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut);
 }
 
 // Scheduled RHS on contiguous [3][M] complex state/flux buffers.
@@ -645,8 +653,8 @@ cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t 
 // Stage states of one WVFixedStepRK4 step from y (contiguous [3][M] complex):
 // st1 = y + h/2 k1, st2 = y + h/2 k2, st3 = y + h k3; when yNext is given it
 // also receives the step's result with the same arithmetic as rk4_step.
-// With ys (four buffers), the y spectra of the flux input at y, st1, st2 and
-// st3 are kept for the step's adjoint.
+// With ys (four buffers), the x pass's real rows at y, st1, st2 and st3 are
+// kept for the step's adjoint (st3's flux then runs even without yNext).
 cudaError_t rk4_stages(wv_handle* h, const double* y, double t, double t0, double dt, double* st1, double* st2, double* st3,
                        double* yNext, cudaStream_t s, void* const* ys = nullptr) {
     const size_t n = 6 * h->plan.M;
@@ -663,7 +671,7 @@ cudaError_t rk4_stages(wv_handle* h, const double* y, double t, double t0, doubl
     e = flux(st2, t + 0.5 * dt, 2); if (e != cudaSuccess) return e;
     dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, y, dt, st3, 0, n);
     h->metrics.kernel_launches += 3;
-    if (!yNext && ys) flux_fields_any(h, t + dt, t0, st3, ys[3], s);
+    if (!yNext && ys) { e = flux(st3, t + dt, 3); if (e != cudaSuccess) return e; }
     if (yNext) {
         e = flux(st3, t + dt, 3); if (e != cudaSuccess) return e;
         dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, nullptr, 0.0, nullptr, 0, n);
@@ -933,6 +941,18 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     upT(p.Ccos, &dd.Ccos); upT(p.Csin, &dd.Csin); upT(p.CcosM, &dd.CcosM); upT(p.CsinM, &dd.CsinM);
     upT(p.Fcos, &dd.Fcos); upT(p.Fsin, &dd.Fsin); upT(p.twx, &dd.twx); upT(p.twxN, &dd.twxN); upT(p.twy, &dd.twy);
     upT(p.rowK, &dd.tRowK); upT(p.rowL, &dd.tRowL);
+    {
+        auto transpose = [](const std::vector<double>& a, size_t rows, size_t cols) {
+            std::vector<double> t(a.size());
+            for (size_t r = 0; r < rows; ++r)
+                for (size_t c = 0; c < cols; ++c) t[c * rows + r] = a[r * cols + c];
+            return t;
+        };
+        const size_t Zh = p.zHalf, Nj = p.Nj;
+        upT(transpose(p.Ccos, Zh, Nj), &dd.CcosT); upT(transpose(p.Csin, Zh, Nj), &dd.CsinT);
+        upT(transpose(p.CcosM, Zh, Nj), &dd.CcosMT); upT(transpose(p.CsinM, Zh, Nj), &dd.CsinMT);
+        upT(transpose(p.Fcos, Nj, Zh), &dd.FcosT); upT(transpose(p.Fsin, Nj, Zh), &dd.FsinT);
+    }
     if (precision == WV_PRECISION_MIXED && e == cudaSuccess) {
         const std::vector<float> proj = mixed_flux_projection(d);
         const float* q = nullptr;
@@ -1332,8 +1352,9 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
         e = alloc(h, stateBytes, &tmp);
         h->segment.push_back(static_cast<double*>(tmp));
     }
-    // y spectra of every stage flux of a segment, when half the free memory holds them
-    const size_t yBytes = scratch_sizes(h->plan).y * 2 * elem_size(h->precision);
+    // real rows of the x pass of every stage flux of a segment, when half the
+    // free memory holds them
+    const size_t yBytes = (3 + 3 * h->plan.targets.count) * h->plan.Nx * h->plan.Ny * h->plan.Nz * elem_size(h->precision);
     if (e == cudaSuccess && static_cast<int>(h->ystore.size()) < 4 * K) {
         size_t freeB = 0, totalB = 0;
         e = cudaMemGetInfo(&freeB, &totalB);

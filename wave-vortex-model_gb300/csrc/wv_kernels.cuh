@@ -230,6 +230,13 @@ struct DescDev {
     const void* CsinM;
     const void* Fcos;       // T[Nj][zHalf]
     const void* Fsin;
+    // transposed copies for the adjoint kernels (contiguous along their inner loop)
+    const void* CcosT;      // T[Nj][zHalf]
+    const void* CsinT;
+    const void* CcosMT;
+    const void* CsinMT;
+    const void* FcosT;      // T[zHalf][Nj]
+    const void* FsinT;
     const void* twx;        // cx<T>[xLen]: twiddles of the x line FFT (length Nx/2 for even Nx, else Nx)
     const void* twxN;       // cx<T>[Nx]: exp(-2 pi i k/Nx) for the real-FFT split/merge
     const void* twy;        // cx<T>[Ny]
@@ -528,9 +535,10 @@ __device__ __forceinline__ cx<T> r2c_value(const DescDev& d, const cx<T>* line, 
 // ---------------------------------------------------------------------------
 // xflux: one CTA per (y, z) row.
 
+// physOut, when given, receives the real rows [z][nReal][y][Nx] for the adjoint.
 template <typename T>
 __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
-                                              unsigned long long* __restrict__ maxSpeedBits) {
+                                              unsigned long long* __restrict__ maxSpeedBits, T* __restrict__ physOut) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Nx = d.Nx, Ny = d.Ny, KX = d.kxColumns, nt = d.nt, L = d.xLen;
     const int nIn = 4 + 2 * nt;          // U V W N, q_y..., q_z...
@@ -576,6 +584,11 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
         }
         __syncthreads();
     }
+    if (physOut)
+        for (int i = threadIdx.x; i < nReal * Nx; i += blockDim.x) {
+            const int r = i / Nx, x = i - r * Nx;
+            physOut[(((size_t)z * nReal + r) * Ny + y) * Nx + x] = phys[i];
+        }
     // quadratic products S_q = -(u q_x + v q_y + w q_z) and max horizontal speed
     T* S = reinterpret_cast<T*>(bufA);  // [nt][Nx] reals (bufA holds 16 L >= 4 Nx reals)
     // max |u_h| (only when a consumer asked for it): max of u^2 + v^2, one sqrt

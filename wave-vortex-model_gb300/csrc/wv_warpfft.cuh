@@ -224,9 +224,11 @@ __device__ __forceinline__ void c2r_row(const DescDev& d, const cx<T>* h, bool u
     fft_P<T, R, true>(v, twL, lane);
 }
 
+// physOut, when given, receives the real rows as complex pairs in register
+// order: [z][nReal][y][L], entry k*32 + lane = register k of lane `lane`.
 template <typename T, int R>
 __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
-                                                unsigned long long* __restrict__ maxSpeedBits) {
+                                                unsigned long long* __restrict__ maxSpeedBits, cx<T>* __restrict__ physOut) {
     constexpr int L = 32 * R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double warpMax[kWG];
@@ -253,6 +255,13 @@ __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __re
     c2r_row<T, R>(d, row + 0 * cstride, false, twL, twN, lane, U);
     c2r_row<T, R>(d, row + 1 * cstride, false, twL, twN, lane, V);
     c2r_row<T, R>(d, row + 2 * cstride, false, twL, twN, lane, W);
+    const int nReal = 3 + 3 * nt;
+    auto keep = [&](int r, const cx<T> (&x)[R]) {
+        cx<T>* o = physOut + (((size_t)z * nReal + r) * Ny + y) * L + lane;
+#pragma unroll
+        for (int k = 0; k < R; ++k) o[32 * k] = x[k];
+    };
+    if (physOut) { keep(0, U); keep(1, V); keep(2, W); }
     // max |u_h| only when a consumer asked for it (max of u^2 + v^2, one sqrt at the end)
     const bool wantSpeed = maxSpeedBits != nullptr;
     double vmax2 = 0.0;
@@ -271,6 +280,7 @@ __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __re
         for (int kind = 0; kind < 3; ++kind) {
             const int ch = kind == 0 ? q : (kind == 1 ? 4 + t : 4 + nt + t);
             c2r_row<T, R>(d, row + ch * cstride, kind == 0, twL, twN, lane, v);
+            if (physOut) keep(3 + 3 * t + kind, v);
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const cx<T> m = kind == 0 ? U[k] : (kind == 1 ? V[k] : W[k]);
@@ -301,6 +311,127 @@ __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __re
             for (int i = 0; i < rows; ++i) m = fmax(m, warpMax[i]);
             atomicMax(maxSpeedBits + z / d.Nz, (unsigned long long)__double_as_longlong(sqrt(m)));
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// x pass adjoint (transpose of k_xflux_w), one warp per (y, z) row, 8 rows per
+// CTA.  Forward rows U, V, W and the gradients of the value rows stay in
+// registers; per target: adjoint row s (c2r with interior kx at weight 1/2,
+// i.e. 0.5 c2r(h) + 0.5 Re h[0]), the forward rows q_x, q_y, q_z, and the
+// gradient rows -s U, -s V, -s W through r2c with interior kx doubled.  The
+// -i k x-derivative gradient is parked per warp in shared memory and added to
+// its value channel at the end.  Output in the forward y-spectrum layout.
+
+template <typename T, int R>
+__device__ __forceinline__ void r2c_row_to_line(cx<T> (&g)[R], const cx<T>* twL, cx<T>* line, int lane) {
+    fft_Q<T, R, false>(g, twL, lane);
+#pragma unroll
+    for (int qq = 0; qq < R; ++qq) line[lane + 32 * qq] = g[qq];
+    __syncwarp();
+}
+
+// physIn, when given, holds the forward real rows as k_xflux_w keeps them;
+// otherwise they are recomputed from yspec.
+template <typename T, int R>
+__global__ void __launch_bounds__(256, 2) k_xadj_w(DescDev d, const cx<T>* __restrict__ yspec, const cx<T>* __restrict__ yadj,
+                                                cx<T>* __restrict__ yout, const cx<T>* __restrict__ physIn) {
+    constexpr int L = 32 * R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Ny = d.Ny, KX = d.kxColumns, nt = d.nt;
+    const int nIn = 4 + 2 * nt;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int z = blockIdx.y;
+    const int y = blockIdx.x * kWG + warp;
+    cx<T>* twL = reinterpret_cast<cx<T>*>(smem_raw);   // [L]
+    cx<T>* twN = twL + L;                               // [2L]
+    cx<T>* line = twN + 2 * L + warp * (L + 4 * KX);    // per warp: [L] line, [4][KX] x-derivative parts
+    cx<T>* xpart = line + L;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
+    const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) twL[i] = twg[i];
+    for (int i = threadIdx.x; i < 2 * L; i += blockDim.x) twN[i] = twgN[i];
+    __syncthreads();
+    if (y >= Ny) return;
+    const size_t cstride = (size_t)Ny * KX;
+    const cx<T>* row = yspec + (((size_t)z * nIn) * Ny + y) * KX;
+    const cx<T>* arow = yadj + (((size_t)z * nt) * Ny + y) * KX;
+    cx<T>* orow = yout + (((size_t)z * nIn) * Ny + y) * KX;
+    for (int i = lane; i < 4 * KX; i += 32) xpart[i] = mk<T>(T(0), T(0));
+    __syncwarp();
+    cx<T> U[R], V[R], W[R], gu[R], gv[R], gw[R], sb[R], v[R], g[R];
+    const int nReal = 3 + 3 * nt;
+    // forward real row r (register order)
+    auto fwdRow = [&](int r, int ch, bool useK, cx<T> (&x)[R]) {
+        if (physIn) {
+            const cx<T>* src = physIn + (((size_t)z * nReal + r) * Ny + y) * L + lane;
+#pragma unroll
+            for (int k = 0; k < R; ++k) x[k] = src[32 * k];
+        } else {
+            c2r_row<T, R>(d, row + ch * cstride, useK, twL, twN, lane, x);
+        }
+    };
+    fwdRow(0, 0, false, U);
+    fwdRow(1, 1, false, V);
+    fwdRow(2, 2, false, W);
+#pragma unroll
+    for (int k = 0; k < R; ++k) { gu[k] = mk<T>(T(0), T(0)); gv[k] = gu[k]; gw[k] = gu[k]; }
+    // half-spectrum r2c of g into output channel ch (or the x-derivative part of value channel q)
+    auto put = [&](cx<T> (&gr)[R], int ch, int xq) {
+        r2c_row_to_line<T, R>(gr, twL, line, lane);
+        for (int k = lane; k < KX; k += 32) {
+            cx<T> val = r2c_value<T>(d, line, k, twN);
+            if (k > 0) val = mk<T>(T(2) * val.x, T(2) * val.y);
+            if (xq >= 0) {
+                const T kk = row_k<T>(d)[k];
+                xpart[xq * KX + k] = mk<T>(kk * val.y, -kk * val.x);   // (i k)^* = -i k
+            } else {
+                orow[(size_t)ch * cstride + k] = val;
+            }
+        }
+        __syncwarp();
+    };
+#pragma unroll 1
+    for (int t = 0; t < nt; ++t) {
+        const int q = d.tq[t];
+        c2r_row<T, R>(d, arow + t * cstride, false, twL, twN, lane, sb);
+        const T h0 = arow[t * cstride].x;  // imaginary part dropped by c2r
+#pragma unroll
+        for (int k = 0; k < R; ++k) sb[k] = mk<T>(T(0.5) * sb[k].x + T(0.5) * h0, T(0.5) * sb[k].y + T(0.5) * h0);
+#pragma unroll 1
+        for (int kind = 0; kind < 3; ++kind) {
+            const int ch = kind == 0 ? q : (kind == 1 ? 4 + t : 4 + nt + t);
+            fwdRow(3 + 3 * t + kind, ch, kind == 0, v);
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const cx<T> p = mk<T>(sb[k].x * v[k].x, sb[k].y * v[k].y);
+                if (kind == 0) gu[k] = mk<T>(gu[k].x - p.x, gu[k].y - p.y);
+                else if (kind == 1) gv[k] = mk<T>(gv[k].x - p.x, gv[k].y - p.y);
+                else gw[k] = mk<T>(gw[k].x - p.x, gw[k].y - p.y);
+                const cx<T> m = kind == 0 ? U[k] : (kind == 1 ? V[k] : W[k]);
+                g[k] = mk<T>(-sb[k].x * m.x, -sb[k].y * m.y);
+            }
+            // gradient of q_x (x-derivative of channel q), q_y (channel 4+t), q_z (channel 4+nt+t)
+            put(g, ch, kind == 0 ? q : -1);
+        }
+    }
+    // value channels: r2c of the accumulated gradients plus the x-derivative parts
+    for (int c = 0; c < 4; ++c) {
+        if (c < 3) {
+            if (c == 0) r2c_row_to_line<T, R>(gu, twL, line, lane);
+            else if (c == 1) r2c_row_to_line<T, R>(gv, twL, line, lane);
+            else r2c_row_to_line<T, R>(gw, twL, line, lane);
+        }
+        for (int k = lane; k < KX; k += 32) {
+            cx<T> val = mk<T>(T(0), T(0));
+            if (c < 3) {
+                val = r2c_value<T>(d, line, k, twN);
+                if (k > 0) val = mk<T>(T(2) * val.x, T(2) * val.y);
+            }
+            const cx<T> xp = xpart[c * KX + k];
+            orow[(size_t)c * cstride + k] = mk<T>(val.x + xp.x, val.y + xp.y);
+        }
+        __syncwarp();
     }
 }
 
