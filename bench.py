@@ -414,10 +414,23 @@ def run_ours(args):
     mixed_value = world * args.steps / max_over_ranks(mixed_ms / 1e3)
     mixed = {"value": mixed_value, "unit": UNIT, "ms_per_step": mixed_ms / args.steps,
              "speedup_vs_fp64": mixed_value / value,
-             "dtype": "f32 xy transforms, products and vertical contractions; f64 phases, projection, RK4",
+             "dtype": "f32 xy transforms and products; vertical inverse as split-BF16 (3 pieces, 6 products) tcgen05 "
+                      "GEMMs with f32 accumulators; f32 forward contraction and projection; f64 phase angles and RK4",
+             "vertical_kernel": "tensor cores (tcgen05.mma)",
              "roofline": _stage_profile(km, devm, tm, t0, dt, "mixed", torch)}
     if rank == 0:
         mixed["rel_field_err_vs_fp64_after_100_steps"] = _field_error_after(k, km, state, dt, 100, torch, np)
+    mixed["device_status"] = km.device_status()
+    # the same with the vertical inverse transform on the CUDA cores instead of the tensor cores
+    km.set_vertical_kernel("cuda")
+    cc_ms, tm = _time_steps(km, devm, tm, t0, dt, args.steps, args.warmup, stream, barrier, flush, torch)
+    cc_value = world * args.steps / max_over_ranks(cc_ms / 1e3)
+    mixed["cuda_core_vertical"] = {
+        "value": cc_value, "unit": UNIT, "ms_per_step": cc_ms / args.steps, "speedup_vs_fp64": cc_value / value,
+        "stage_ms_per_flux": _stage_profile(km, devm, tm, t0, dt, "mixed", torch)["stage_ms_per_flux"]}
+    if rank == 0:
+        mixed["cuda_core_vertical"]["rel_field_err_vs_fp64_after_100_steps"] = _field_error_after(k, km, state, dt, 100,
+                                                                                                 torch, np)
     km.close()
     adjoint = {p: _adjoint_timing(wvgpu, p, stream, torch, np) for p in ("fp64", "mixed")} if rank == 0 else None
     ensemble = _ensemble_timing(wvgpu, stream, torch, np) if rank == 0 and not args.no_ensemble else None

@@ -138,6 +138,20 @@ typedef struct wv_stage_times {
  * CUDA events between its five stages on its stream and waits for them, adding
  * the elapsed device time to the handle's stage times (reset on enable). */
 int wv_set_stage_instrumentation(wv_handle* handle, int enabled);
+
+/* Kernel of the flux's vertical inverse transform in the mixed form.  No
+ * counterpart in the reference.  WV_VERTICAL_TENSOR_CORES runs the dense
+ * contraction as split-BF16 GEMMs on the tensor cores (tcgen05.mma, three BF16
+ * pieces per operand, six cross products, FP32 accumulators in tensor memory);
+ * available on mixed-precision handles with Nz <= 255 (else
+ * WV_UNSUPPORTED_OPERATION) and the default there; WV_VERTICAL_CUDA_CORES
+ * otherwise and on FP64 handles. */
+#define WV_VERTICAL_CUDA_CORES 0
+#define WV_VERTICAL_TENSOR_CORES 1
+int wv_set_vertical_kernel(wv_handle* handle, int kind);
+/* Device status word of the handle (synchronous read): bit 0 is set when a
+ * bounded wait inside a kernel ran out (the kernel returned without hanging). */
+int wv_get_device_status(wv_handle* handle, unsigned* status);
 int wv_get_stage_times(const wv_handle* handle, wv_stage_times* times);
 
 /* ---- operators (host pointers) ------------------------------------------------------ */
@@ -253,9 +267,11 @@ typedef struct wv_ensemble wv_ensemble;
 #define WV_ENSEMBLE_MAX_GROUPS 16
 typedef struct wv_ensemble_tuning {
     int warp_y_available, warp_x_available;  /* variants the grid has */
+    int tensor_vertical_available;
     int stockham_y, stockham_x;              /* chosen: 1 = Stockham, 0 = warp (where available) */
+    int vertical;                            /* chosen vertical-transform kernel (WV_VERTICAL_*) */
     int candidates;                          /* variants timed */
-    float candidate_ms[4];                   /* flux time of each (y-major order), ms */
+    float candidate_ms[8];                   /* flux time of each (vertical, y, x order), ms */
     float flux_ms;                           /* chosen variant, ms per flux of the whole group */
 } wv_ensemble_tuning;
 typedef struct wv_ensemble_metrics {
@@ -271,6 +287,8 @@ const char* wv_ensemble_last_message(const wv_ensemble* ensemble);
 int wv_ensemble_get_sizes(const wv_ensemble* ensemble, int group, wv_sizes* sizes);  /* per member */
 int wv_ensemble_get_tuning(const wv_ensemble* ensemble, int group, wv_ensemble_tuning* tuning);
 int wv_ensemble_get_metrics(const wv_ensemble* ensemble, wv_ensemble_metrics* metrics);
+/* Vertical-transform kernel of every group (as wv_set_vertical_kernel); overrides the autotuner. */
+int wv_ensemble_set_vertical_kernel(wv_ensemble* ensemble, int kind);
 /* states[g]: device array [members[g]][3][Nkl][Nj] complex (each member's Ap, Am,
  * A0 back to back), advanced in place.  t[g] (in/out) is group g's time and
  * dt[g] its step; on return t[g] has advanced by n_steps steps of dt[g]. */

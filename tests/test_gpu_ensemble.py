@@ -80,8 +80,10 @@ def test_ensemble_autotune_and_graph_update(wv):
     ens = wv.WVEnsemble([g[0] for g in groups], [g[2].shape[0] for g in groups], precision="mixed", autotune=True)
     tune = ens.tuning()
     print("ensemble autotune:", tune)
-    # the 64 grid has warp and Stockham variants on both axes; 48 has Stockham only
-    assert tune[0]["warp_y_available"] and tune[0]["warp_x_available"] and len(tune[0]["candidate_ms"]) == 4
+    # the 64 grid has warp and Stockham variants on both axes and both vertical
+    # kernels (8 candidates); 48 has Stockham only (2: the vertical kernels)
+    assert tune[0]["warp_y_available"] and tune[0]["warp_x_available"] and len(tune[0]["candidate_ms"]) == 8
+    assert len(tune[2]["candidate_ms"]) == 2
     assert not tune[2]["warp_y_available"] and not tune[2]["warp_x_available"]
     X = [g[2].clone() for g in groups]
     dts = [g[3] for g in groups]

@@ -11,6 +11,7 @@
 #include "wv_plan.hpp"
 #include "wv_warpfft.cuh"
 #include "wv_adjoint.cuh"
+#include "wv_vinv_tc.cuh"
 
 #include <cuda_runtime.h>
 
@@ -69,6 +70,9 @@ struct wv_handle {
     std::vector<double*> segment;      // multi-step adjoint: states of one segment
     std::vector<void*> ystore;         // multi-step adjoint: x-pass real rows of each stage flux of one segment
     bool instrument = false;
+    bool tcAvailable = false;  // tensor-core vertical transform built for this handle
+    bool verticalTC = false;   // ... and selected (default: on where built)
+    size_t tcSmem = 0;
     cudaEvent_t ev[6] = {};
     wv_stage_times stages{};
 };
@@ -124,6 +128,50 @@ std::vector<double> interleave(const std::vector<wvgpu::cdouble>& v) {
 
 template <typename T>
 std::vector<T> cast(const std::vector<double>& v) { return std::vector<T>(v.begin(), v.end()); }
+
+// BF16 with round-to-nearest-even from an FP32 value (host), and back.
+uint16_t bf16_rne(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return static_cast<uint16_t>(u >> 16);
+}
+double bf16_value(uint16_t h) {
+    const uint32_t u = static_cast<uint32_t>(h) << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// The folded inverse matrices Ccos, Csin, CcosM, CsinM ([zHalf][Nj], FP64) as
+// three BF16 pieces each (hi, the rounded remainder, the rounded remainder of
+// that), laid out for the tensor-core vertical transform: row n < NP, column
+// kk < K with even j = 2 kk in kk < KE and odd j = 2 (kk - KE) + 1 after it,
+// canonical no-swizzle K-major core matrices; zeros outside the matrix.
+std::vector<uint16_t> tc_vertical_blob(const Plan& p, int NP, int KE, int K) {
+    const size_t split = static_cast<size_t>(NP) * K;  // BF16 entries per piece
+    std::vector<uint16_t> out(4 * 3 * split, 0);
+    const std::vector<double>* mats[4] = {&p.Ccos, &p.Csin, &p.CcosM, &p.CsinM};
+    const int Zh = static_cast<int>(p.zHalf), Nj = static_cast<int>(p.Nj);
+    for (int m = 0; m < 4; ++m)
+        for (int n = 0; n < Zh; ++n)
+            for (int kk = 0; kk < K; ++kk) {
+                const int j = kk < KE ? 2 * kk : 2 * (kk - KE) + 1;
+                if (j >= Nj || (kk >= KE && kk - KE >= (Nj / 2))) continue;
+                if (kk < KE && kk >= (Nj + 1) / 2) continue;
+                const double c = (*mats[m])[static_cast<size_t>(n) * Nj + j];
+                const uint16_t hb = bf16_rne(static_cast<float>(c));
+                const double r1 = c - bf16_value(hb);
+                const uint16_t mb = bf16_rne(static_cast<float>(r1));
+                const double r2 = r1 - bf16_value(mb);
+                const uint16_t lb = bf16_rne(static_cast<float>(r2));
+                const size_t e = dev::tc_kmajor_offset(n, kk, K) / 2;
+                out[(static_cast<size_t>(m) * 3 + 0) * split + e] = hb;
+                out[(static_cast<size_t>(m) * 3 + 1) * split + e] = mb;
+                out[(static_cast<size_t>(m) * 3 + 2) * split + e] = lb;
+            }
+    return out;
+}
 
 // Flux projection of the mixed form, folded per (mode, j) in FP64 and rounded
 // once to FP32 (projectFluxTargetMode, kernel.cpp:396-431, written as one
@@ -393,7 +441,15 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     // max |u_h| is reduced only when adaptive damping consumes it
     unsigned long long* speed = damping ? h->maxSpeed : nullptr;
     if (inst) cudaEventRecord(h->ev[0], s);
-    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    if constexpr (sizeof(T) == 4) {
+        if (h->verticalTC)
+            dev::k_vinv_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcSmem, s>>>(
+                d, Ap, Am, A0, elapsed, reinterpret_cast<float2*>(z), speed);
+        else
+            dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    } else {
+        dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    }
     if (inst) cudaEventRecord(h->ev[1], s);
     dev::YInvMap map{};
     map.nOut = 4 + 2 * nt;
@@ -959,6 +1015,30 @@ static int create_handle(const wv_config* config, int precision, int members, wv
         e = upload(h, proj, &q);
         dd.fProj = q;
     }
+    if (e == cudaSuccess) {
+        unsigned* st = nullptr;
+        e = alloc(h, sizeof(unsigned), reinterpret_cast<void**>(&st));
+        if (e == cudaSuccess) e = cudaMemset(st, 0, sizeof(unsigned));
+        dd.status = st;
+    }
+    if (precision == WV_PRECISION_MIXED && e == cudaSuccess) {
+        // tensor-core vertical transform: four accumulators of N <= 128 columns
+        const int NP = static_cast<int>((p.zHalf + 15) / 16 * 16);
+        const int KE = static_cast<int>(((p.Nj + 1) / 2 + 15) / 16 * 16), KO = static_cast<int>((p.Nj / 2 + 15) / 16 * 16);
+        const int K = KE + KO;
+        const size_t smem = 6 * (256u * K) + 3 * static_cast<size_t>(NP / 8) * 16u * K;
+        if (NP <= 128 && smem <= 220 * 1024) {
+            const std::vector<uint16_t> blob = tc_vertical_blob(p, NP, KE, K);
+            const uint16_t* q = nullptr;
+            e = upload(h, blob, &q);
+            dd.tcB = reinterpret_cast<const unsigned short*>(q);
+            dd.tcN = NP; dd.tcKE = KE; dd.tcK = K;
+            h->tcSmem = smem;
+            if (e == cudaSuccess) e = raise_smem_limit(dev::k_vinv_tc, static_cast<int>(smem));
+            h->tcAvailable = e == cudaSuccess;
+            h->verticalTC = h->tcAvailable;  // default where built (faster at 256x256x129, same accuracy)
+        }
+    }
     const auto ss = scratch_sizes(p);
     const size_t cb = 2 * elem_size(precision);
     const size_t R = p.Nx * p.Ny * p.Nz;
@@ -1005,6 +1085,24 @@ int wv_get_metrics(const wv_handle* h, wv_metrics* m) {
     if (!h || !m) return WV_INVALID_POINTER;
     *m = h->metrics;
     return WV_SUCCESS;
+}
+
+int wv_set_vertical_kernel(wv_handle* h, int kind) {
+    if (!h) return WV_INVALID_POINTER;
+    if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES)
+        return fail(h, WV_INVALID_CONFIGURATION, "Unknown vertical-transform kernel.");
+    if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
+        return fail(h, WV_UNSUPPORTED_OPERATION,
+                    "The tensor-core vertical transform needs a mixed-precision handle with Nz <= 255.");
+    h->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
+    return WV_SUCCESS;
+}
+
+int wv_get_device_status(wv_handle* h, unsigned* status) {
+    if (!h || !status) return WV_INVALID_POINTER;
+    cudaSetDevice(h->device);
+    const cudaError_t e = cudaMemcpy(status, h->dd.status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    return finish(h, e, "device status");
 }
 
 int wv_set_stage_instrumentation(wv_handle* h, int enabled) {
@@ -1510,24 +1608,32 @@ cudaError_t autotune_group(wv_handle* h, cudaStream_t s, wv_ensemble_tuning& out
     const bool fp32 = h->precision != WV_PRECISION_FP64;
     const bool warpY = fp32 && warp_ry<float>(p) != 0, warpX = fp32 && warp_rx<float>(p) != 0;
     float best = -1.0f;
-    bool bestY = false, bestX = false;
+    bool bestY = false, bestX = false, bestTC = false;
     out.candidates = 0;
-    for (int vy = 0; vy < (warpY ? 2 : 1) && e == cudaSuccess; ++vy) {
-        for (int vx = 0; vx < (warpX ? 2 : 1) && e == cudaSuccess; ++vx) {
-            p.stockhamY = vy == 1;
-            p.stockhamX = vx == 1;
-            const float ms = time_group_flux(h, 3, s, e);
-            if (e == cudaSuccess && out.candidates < 4) out.candidate_ms[out.candidates] = ms;
-            out.candidates++;
-            if (e == cudaSuccess && (best < 0.0f || ms < best)) { best = ms; bestY = p.stockhamY; bestX = p.stockhamX; }
+    for (int vt = 0; vt < (h->tcAvailable ? 2 : 1) && e == cudaSuccess; ++vt) {
+        for (int vy = 0; vy < (warpY ? 2 : 1) && e == cudaSuccess; ++vy) {
+            for (int vx = 0; vx < (warpX ? 2 : 1) && e == cudaSuccess; ++vx) {
+                h->verticalTC = vt == 1;
+                p.stockhamY = vy == 1;
+                p.stockhamX = vx == 1;
+                const float ms = time_group_flux(h, 3, s, e);
+                if (e == cudaSuccess && out.candidates < 8) out.candidate_ms[out.candidates] = ms;
+                out.candidates++;
+                if (e == cudaSuccess && (best < 0.0f || ms < best)) {
+                    best = ms; bestY = p.stockhamY; bestX = p.stockhamX; bestTC = h->verticalTC;
+                }
+            }
         }
     }
     p.stockhamY = bestY;
     p.stockhamX = bestX;
+    h->verticalTC = bestTC;
     out.stockham_y = bestY ? 1 : 0;
     out.stockham_x = bestX ? 1 : 0;
+    out.vertical = bestTC ? WV_VERTICAL_TENSOR_CORES : WV_VERTICAL_CUDA_CORES;
     out.warp_y_available = warpY ? 1 : 0;
     out.warp_x_available = warpX ? 1 : 0;
+    out.tensor_vertical_available = h->tcAvailable ? 1 : 0;
     out.flux_ms = best;
     return e;
 }
@@ -1590,6 +1696,8 @@ int wv_ensemble_create(const wv_config* configs, const int* members, int n_group
             t.stockham_x = h->plan.stockhamX ? 1 : 0;
             t.warp_y_available = h->precision != WV_PRECISION_FP64 && warp_ry<float>(h->plan) != 0;
             t.warp_x_available = h->precision != WV_PRECISION_FP64 && warp_rx<float>(h->plan) != 0;
+            t.tensor_vertical_available = h->tcAvailable ? 1 : 0;
+            t.vertical = WV_VERTICAL_CUDA_CORES;
             t.flux_ms = -1.0f;
         }
     }
@@ -1618,6 +1726,22 @@ int wv_ensemble_get_tuning(const wv_ensemble* e, int group, wv_ensemble_tuning* 
     if (!e || !tuning) return WV_INVALID_POINTER;
     if (group < 0 || group >= static_cast<int>(e->groups.size())) return WV_INVALID_CONFIGURATION;
     *tuning = e->tuning[group];
+    return WV_SUCCESS;
+}
+
+int wv_ensemble_set_vertical_kernel(wv_ensemble* e, int kind) {
+    if (!e) return WV_INVALID_POINTER;
+    if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES)
+        return efail(e, WV_INVALID_CONFIGURATION, "Unknown vertical-transform kernel.");
+    for (wv_handle* h : e->groups)
+        if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
+            return efail(e, WV_UNSUPPORTED_OPERATION,
+                         "The tensor-core vertical transform needs mixed-precision groups with Nz <= 255.");
+    for (size_t g = 0; g < e->groups.size(); ++g) {
+        e->groups[g]->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
+        e->tuning[g].vertical = kind;
+    }
+    e->keySteps = -1;  // captured kernels changed: capture anew
     return WV_SUCCESS;
 }
 

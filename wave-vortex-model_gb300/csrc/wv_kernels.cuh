@@ -240,6 +240,13 @@ struct DescDev {
     const void* twx;        // cx<T>[xLen]: twiddles of the x line FFT (length Nx/2 for even Nx, else Nx)
     const void* twxN;       // cx<T>[Nx]: exp(-2 pi i k/Nx) for the real-FFT split/merge
     const void* twy;        // cx<T>[Ny]
+    // MIXED handles with the tensor-core vertical transform: the four folded
+    // inverse matrices split into three BF16 pieces each, in the canonical
+    // no-swizzle K-major layout [matrix][piece][N rows][K]; N = Zh rounded up to
+    // 16, K = KE (even j) + odd j, each rounded up to 16.
+    const unsigned short* tcB;
+    int tcN, tcKE, tcK;
+    unsigned* status;       // device status word (bit 0: a bounded wait ran out)
     int xEven;              // Nx even: real rows go through half-length complex FFTs
     int xLen;               // Nx/2 (even) or Nx (odd)
     FFTDev fx, fy;          // fx factors xLen

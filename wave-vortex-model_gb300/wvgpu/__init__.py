@@ -73,8 +73,9 @@ class _StageTimes(ctypes.Structure):
 
 
 class _EnsembleTuning(ctypes.Structure):
-    _fields_ = [("warp_y_available", ctypes.c_int), ("warp_x_available", ctypes.c_int), ("stockham_y", ctypes.c_int),
-                ("stockham_x", ctypes.c_int), ("candidates", ctypes.c_int), ("candidate_ms", ctypes.c_float * 4),
+    _fields_ = [("warp_y_available", ctypes.c_int), ("warp_x_available", ctypes.c_int),
+                ("tensor_vertical_available", ctypes.c_int), ("stockham_y", ctypes.c_int), ("stockham_x", ctypes.c_int),
+                ("vertical", ctypes.c_int), ("candidates", ctypes.c_int), ("candidate_ms", ctypes.c_float * 8),
                 ("flux_ms", ctypes.c_float)]
 
 
@@ -144,6 +145,8 @@ def load_library():
     lib.wv_get_metrics.argtypes = [P, ctypes.POINTER(_Metrics)]
     lib.wv_set_forcing.argtypes = [P, ctypes.c_uint32]
     lib.wv_set_stage_instrumentation.argtypes = [P, ctypes.c_int]
+    lib.wv_set_vertical_kernel.argtypes = [P, ctypes.c_int]
+    lib.wv_get_device_status.argtypes = [P, ctypes.POINTER(ctypes.c_uint)]
     lib.wv_get_stage_times.argtypes = [P, ctypes.POINTER(_StageTimes)]
     for name in ("wv_nonlinear_flux", "wv_evaluate_rhs"):
         getattr(lib, name).argtypes = [P, D, D, P, P, P, P, P, P]
@@ -168,6 +171,7 @@ def load_library():
     lib.wv_ensemble_get_sizes.argtypes = [P, ctypes.c_int, ctypes.POINTER(_Sizes)]
     lib.wv_ensemble_get_tuning.argtypes = [P, ctypes.c_int, ctypes.POINTER(_EnsembleTuning)]
     lib.wv_ensemble_get_metrics.argtypes = [P, ctypes.POINTER(_EnsembleMetrics)]
+    lib.wv_ensemble_set_vertical_kernel.argtypes = [P, ctypes.c_int]
     lib.wv_ensemble_rk4_device.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(D), D, ctypes.POINTER(D), ctypes.c_int, P]
     _lib = lib
     return lib
@@ -176,12 +180,13 @@ def load_library():
 def exported_symbols():
     """Names of the C entry points this binding expects (declared in include/wvgpu.h)."""
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
-            "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
+            "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times",
+            "wv_set_vertical_kernel", "wv_get_device_status", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
             "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc", "wv_flux_vjp_device",
             "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device", "wv_ensemble_create",
             "wv_ensemble_destroy", "wv_ensemble_last_message", "wv_ensemble_get_sizes", "wv_ensemble_get_tuning",
-            "wv_ensemble_get_metrics", "wv_ensemble_rk4_device"]
+            "wv_ensemble_get_metrics", "wv_ensemble_set_vertical_kernel", "wv_ensemble_rk4_device"]
 
 
 def describe(configuration: Configuration):
@@ -403,6 +408,16 @@ class WVTransformConstantStratificationKernel:
                                                     self._stream()))
         return tuple(out)
 
+    def set_vertical_kernel(self, kind):
+        """'cuda' (CUDA-core contraction) or 'tensor' (tcgen05 split-BF16 GEMMs; mixed handles)."""
+        self._check(self._lib.wv_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1}[kind]))
+
+    def device_status(self):
+        """Device status word (bit 0: a bounded in-kernel wait ran out)."""
+        v = ctypes.c_uint(0)
+        self._check(self._lib.wv_get_device_status(self._h, ctypes.byref(v)))
+        return int(v.value)
+
     def setStageInstrumentation(self, enabled):
         """setStageInstrumentation (kernel.cpp:570-581): per-stage device times."""
         self._check(self._lib.wv_set_stage_instrumentation(self._h, int(bool(enabled))))
@@ -472,10 +487,16 @@ class WVEnsemble:
             t = _EnsembleTuning()
             self._check(self._lib.wv_ensemble_get_tuning(self._h, g, ctypes.byref(t)))
             out.append({"warp_y_available": bool(t.warp_y_available), "warp_x_available": bool(t.warp_x_available),
+                        "tensor_vertical_available": bool(t.tensor_vertical_available),
                         "y": "stockham" if t.stockham_y or not t.warp_y_available else "warp",
                         "x": "stockham" if t.stockham_x or not t.warp_x_available else "warp",
-                        "candidate_ms": list(t.candidate_ms)[:max(0, min(4, t.candidates))], "flux_ms": t.flux_ms})
+                        "vertical": "tensor" if t.vertical == 1 else "cuda",
+                        "candidate_ms": list(t.candidate_ms)[:max(0, min(8, t.candidates))], "flux_ms": t.flux_ms})
         return out
+
+    def set_vertical_kernel(self, kind):
+        """'cuda' or 'tensor' for every group (overrides the autotuner's choice)."""
+        self._check(self._lib.wv_ensemble_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1}[kind]))
 
     def metrics(self):
         m = _EnsembleMetrics()
