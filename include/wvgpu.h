@@ -247,6 +247,46 @@ int wv_nonlinear_flux_device_noalloc(wv_handle* handle, double t, double t0,
                                      const double* Ap, const double* Am, const double* A0,
                                      double* Fp, double* Fm, double* F0, void* stream);
 
+/* nonlinearFluxWithAdvectionFields (kernel.cpp:1148-1158): the flux and the
+ * advecting velocity (u, v, w) it used, fields [Nx, Ny, Nz, 3] (x fastest).
+ * nonlinearFluxUsingAdvectionFields (kernel.cpp:1160-1171): the flux with the
+ * given (u, v, w) as the advecting velocity (the derivatives of the advected
+ * fields still come from the state).  transformWaveVortexToUVW (kernel.cpp:696-717):
+ * (u, v, w) only.  Host- and device-pointer forms; the fields must not overlap
+ * the state or flux arrays (WV_OVERLAPPING_ARRAYS). */
+int wv_nonlinear_flux_with_advection_fields(wv_handle* handle, double t, double t0,
+                                            const double* Ap, const double* Am, const double* A0,
+                                            double* Fp, double* Fm, double* F0, double* fields);
+int wv_nonlinear_flux_using_advection_fields(wv_handle* handle, double t, double t0,
+                                             const double* Ap, const double* Am, const double* A0,
+                                             double* Fp, double* Fm, double* F0, const double* fields);
+int wv_inverse_uvw(wv_handle* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                   double* fields);
+int wv_nonlinear_flux_with_advection_fields_device(wv_handle* handle, double t, double t0,
+                                                   const double* Ap, const double* Am, const double* A0,
+                                                   double* Fp, double* Fm, double* F0, double* fields, void* stream);
+int wv_nonlinear_flux_using_advection_fields_device(wv_handle* handle, double t, double t0,
+                                                    const double* Ap, const double* Am, const double* A0,
+                                                    double* Fp, double* Fm, double* F0, const double* fields, void* stream);
+int wv_inverse_uvw_device(wv_handle* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                          double* fields, void* stream);
+
+/* transformStateFieldDerivatives (kernel.cpp:719-743): (d/dx, d/dy, d/dz) of
+ * field 0..3 (u, v, w, eta) at the state, out [Nx, Ny, Nz, 3]. */
+int wv_field_derivatives(wv_handle* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                         int field, double* out);
+int wv_field_derivatives_device(wv_handle* handle, double t, double t0, const double* Ap, const double* Am,
+                                const double* A0, int field, double* out, void* stream);
+
+/* advectFGridScalar (kernel.cpp:1032-1138): rhs = -(u ds/dx + v ds/dy + w ds/dz)
+ * of an F-grid scalar s [Nx, Ny, Nz] advected by fields (u, v, w) [Nx, Ny, Nz, 3],
+ * spectral derivatives on the full half spectrum; with antialias set, rhs is
+ * filtered to the transform's (2/3-disk) rows.  The first call allocates the
+ * scalar pipeline's descriptor and scratch. */
+int wv_advect_fgrid_scalar(wv_handle* handle, const double* scalar, const double* fields, int antialias, double* rhs);
+int wv_advect_fgrid_scalar_device(wv_handle* handle, const double* scalar, const double* fields, int antialias,
+                                  double* rhs, void* stream);
+
 /* Runs n_steps RK4 steps on device-resident state; the time is kept on the host
  * (t in/out) exactly as WVFixedStepRK4 advances it (t <- t + dt per step). */
 int wv_rk4_steps_device(wv_handle* handle, double* Ap, double* Am, double* A0,

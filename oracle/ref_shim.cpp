@@ -148,6 +148,66 @@ int wvref_rhs(void* handle, double t, double t0, const double* Ap, const double*
     return status ? 0 : fail(h, status);
 }
 
+// nonlinearFluxWithAdvectionFields: flux plus the advecting (u, v, w), [Nx, Ny, Nz, 3].
+int wvref_flux_with_advection(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                              double* Fp, double* Fm, double* F0, double* fields) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVState state{t, t0, {cview(Ap, s), cview(Am, s), cview(A0, s)}};
+    WVFlux flux{mview(Fp, s), mview(Fm, s), mview(F0, s)};
+    WVRealFieldBundleView view{fields, {c.Nx, c.Ny, c.Nz, 3}};
+    const auto status = h->kernel->nonlinearFluxWithAdvectionFields(state, flux, view);
+    return status ? 0 : fail(h, status);
+}
+
+// nonlinearFluxUsingAdvectionFields: flux advected by the given (u, v, w).
+int wvref_flux_using_advection(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                               double* Fp, double* Fm, double* F0, const double* fields) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVState state{t, t0, {cview(Ap, s), cview(Am, s), cview(A0, s)}};
+    WVFlux flux{mview(Fp, s), mview(Fm, s), mview(F0, s)};
+    WVRealFieldBundleConstView view{fields, {c.Nx, c.Ny, c.Nz, 3}};
+    const auto status = h->kernel->nonlinearFluxUsingAdvectionFields(state, flux, view);
+    return status ? 0 : fail(h, status);
+}
+
+// transformWaveVortexToUVW: [Nx, Ny, Nz, 3].
+int wvref_inverse_uvw(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0, double* fields) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVState state{t, t0, {cview(Ap, s), cview(Am, s), cview(A0, s)}};
+    WVRealFieldBundleView view{fields, {c.Nx, c.Ny, c.Nz, 3}};
+    const auto status = h->kernel->transformWaveVortexToUVW(state, view);
+    return status ? 0 : fail(h, status);
+}
+
+// transformStateFieldDerivatives: (d/dx, d/dy, d/dz) of field 0..3 (u, v, w, eta), [Nx, Ny, Nz, 3].
+int wvref_field_derivatives(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0, int field,
+                            double* out) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVState state{t, t0, {cview(Ap, s), cview(Am, s), cview(A0, s)}};
+    WVRealFieldBundleView view{out, {c.Nx, c.Ny, c.Nz, 3}};
+    const auto status = h->kernel->transformStateFieldDerivatives(state, static_cast<WVDynamicalField>(field), view);
+    return status ? 0 : fail(h, status);
+}
+
+// advectFGridScalar: -(u d/dx + v d/dy + w d/dz) of an F-grid scalar [Nx, Ny, Nz].
+int wvref_advect_scalar(void* handle, const double* scalar, const double* fields, int antialias, double* rhs) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    WVRealVolumeConstView sv{scalar, {c.Nx, c.Ny, c.Nz}};
+    WVRealFieldBundleConstView fv{fields, {c.Nx, c.Ny, c.Nz, 3}};
+    WVRealVolumeView rv{rhs, {c.Nx, c.Ny, c.Nz}};
+    const auto status = h->kernel->advectFGridScalar(sv, fv, antialias != 0, rv);
+    return status ? 0 : fail(h, status);
+}
+
 int wvref_forward(void* handle, const double* fields, double t, double t0, double* Ap, double* Am, double* A0) {
     auto* h = static_cast<RefHandle*>(handle);
     const auto& c = h->kernel->descriptor().configuration();

@@ -570,11 +570,16 @@ def _project_target(desc, S, target, p, Fp, Fm, F0):
     F0 += A0c
 
 
-def nonlinear_flux(desc, Ap, Am, A0, t, t0):
-    """nonlinearFluxImpl (kernel.cpp:1173-1244): returns (Fp, Fm, F0)."""
+def nonlinear_flux(desc, Ap, Am, A0, t, t0, advection=None):
+    """nonlinearFluxImpl (kernel.cpp:1173-1244): returns (Fp, Fm, F0).  With
+    `advection` (3, Nz, Ny, Nx) given, that velocity advects the state's fields
+    (nonlinearFluxUsingAdvectionFields, kernel.cpp:1160-1171)."""
     c = desc.c
     p = phase(desc, t, t0)
-    U, V, W = velocity_fields(desc, Ap, Am, A0, t, t0)
+    if advection is None:
+        U, V, W = velocity_fields(desc, Ap, Am, A0, t, t0)
+    else:
+        U, V, W = advection
     Fp = np.zeros_like(Ap)
     Fm = np.zeros_like(Ap)
     F0 = np.zeros_like(Ap)
@@ -584,6 +589,85 @@ def nonlinear_flux(desc, Ap, Am, A0, t, t0):
         S = -(U * dx + V * dy + W * dz)
         _project_target(desc, S, q, p, Fp, Fm, F0)
     return Fp, Fm, F0
+
+
+def flux_with_advection(desc, Ap, Am, A0, t, t0):
+    """nonlinearFluxWithAdvectionFields (kernel.cpp:1148-1158): (Fp, Fm, F0), (u, v, w)."""
+    adv = velocity_fields(desc, Ap, Am, A0, t, t0)
+    return nonlinear_flux(desc, Ap, Am, A0, t, t0, advection=adv), adv
+
+
+def inverse_uvw(desc, Ap, Am, A0, t, t0):
+    """transformWaveVortexToUVW (kernel.cpp:696-717): (3, Nz, Ny, Nx)."""
+    return velocity_fields(desc, Ap, Am, A0, t, t0)
+
+
+def scalar_wavenumbers(desc):
+    """Row wavenumbers of the F-grid scalar pipeline (kernel.cpp:1067-1072): k over
+    the NxHalf columns with k = 0 at an even-Nx Nyquist column, l over the Ny rows
+    by signed mode index (the even-Ny Nyquist row keeps its negative l)."""
+    c = desc.c
+    NxHalf = c.Nx // 2 + 1
+    kIndex = np.arange(NxHalf)
+    k = 2.0 * PI * kIndex / c.Lx
+    if c.Nx % 2 == 0:
+        k[c.Nx // 2] = 0.0
+    lIndex = np.arange(c.Ny)
+    lMode = np.where(lIndex < (c.Ny + 1) // 2, lIndex, lIndex - c.Ny)
+    l = 2.0 * PI * lMode / c.Ly
+    return k, l
+
+
+def scalar_antialias_rows(desc):
+    """Half-spectrum rows kept by the scalar antialias (kernel.cpp:466-471): storage
+    rows of every WV mode, their Hermitian completion and source rows."""
+    c = desc.c
+    keep = np.zeros(c.Ny * (c.Nx // 2 + 1), dtype=bool)
+    keep[desc.storageRow] = True
+    if len(desc.completionRows):
+        keep[desc.completionRows] = True
+        keep[desc.completionSources] = True
+    return keep
+
+
+def advect_fgrid_scalar(desc, scalar, advection, antialias):
+    """advectFGridScalar (kernel.cpp:1032-1138): -(u ds/dx + v ds/dy + w ds/dz) of
+    an F-grid scalar (Nz, Ny, Nx) with spectral derivatives: x, y by the
+    half-spectrum r2c/c2r pair; z by forward DCT-I (normalizeForwardDCT), times
+    -m_j on the interior modes, normalizeInverseDST and DST-I on the interior
+    points; self-conjugate rows real.  With `antialias`, the result is filtered to
+    the transform's rows (antialiasScalarInPlace, kernel.cpp:1008-1030)."""
+    c = desc.c
+    Nz = c.Nz
+    NxHalf = c.Nx // 2 + 1
+    hs = 1.0 / float(c.Nx * c.Ny)
+    k, l = scalar_wavenumbers(desc)
+    val = _rfft2(scalar, -1) * hs                          # (Nz, Ny, NxHalf)
+    cx = val * (1j * k)[None, None, :]
+    cy = val * (1j * l)[None, :, None]
+    d = (_dct1(val.real, 0) + 1j * _dct1(val.imag, 0)) * (1.0 / float(Nz - 1))
+    d[Nz - 1] *= 0.5
+    m = PI * np.arange(Nz) / c.Lz
+    d[1:Nz - 1] *= -m[1:Nz - 1, None, None]
+    d[0] = 0.0
+    d[Nz - 1] = 0.0
+    d[1:Nz - 1] *= 0.5
+    cz = np.zeros_like(d)
+    inner = d[1:Nz - 1]
+    cz[1:Nz - 1] = _dst1(inner.real, 0) + 1j * _dst1(inner.imag, 0)
+    spec = np.stack([cx, cy, cz])                          # (3, Nz, Ny, NxHalf)
+    rows = np.asarray(desc.selfConjugateRows, dtype=np.int64)
+    if len(rows):
+        ky, kx = rows // NxHalf, rows % NxHalf
+        spec[:, :, ky, kx] = spec[:, :, ky, kx].real
+    dx, dy, dz = _irfft2(spec, (c.Ny, c.Nx), -1)
+    U, V, W = advection
+    rhs = -(U * dx + V * dy + W * dz)
+    if antialias:
+        keep = scalar_antialias_rows(desc).reshape(c.Ny, NxHalf)
+        H = _rfft2(rhs, -1) * np.where(keep, hs, 0.0)[None, :, :]
+        rhs = _irfft2(H, (c.Ny, c.Nx), -1)
+    return rhs
 
 
 def forward(desc, fields, t, t0):

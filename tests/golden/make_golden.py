@@ -111,6 +111,47 @@ class Ref:
         self.check(self.lib.wvref_inverse(self.h, ctypes.c_double(t), ctypes.c_double(t0), P(Ap), P(Am), P(A0), P(out)))
         return out
 
+    def _fields(self, nch):
+        c = self.case
+        return np.zeros((nch, c["Nz"], c["Ny"], c["Nx"]))
+
+    def flux_with_advection(self, Ap, Am, A0, t, t0):
+        F = self._c3()
+        adv = self._fields(3)
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        self.check(self.lib.wvref_flux_with_advection(self.h, ctypes.c_double(t), ctypes.c_double(t0), P(Ap), P(Am), P(A0),
+                                                      P(F[0]), P(F[1]), P(F[2]), P(adv)))
+        return F, adv
+
+    def flux_using_advection(self, Ap, Am, A0, t, t0, adv):
+        F = self._c3()
+        adv = np.ascontiguousarray(adv)
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        self.check(self.lib.wvref_flux_using_advection(self.h, ctypes.c_double(t), ctypes.c_double(t0), P(Ap), P(Am), P(A0),
+                                                       P(F[0]), P(F[1]), P(F[2]), P(adv)))
+        return F
+
+    def inverse_uvw(self, Ap, Am, A0, t, t0):
+        out = self._fields(3)
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        self.check(self.lib.wvref_inverse_uvw(self.h, ctypes.c_double(t), ctypes.c_double(t0), P(Ap), P(Am), P(A0), P(out)))
+        return out
+
+    def field_derivatives(self, Ap, Am, A0, t, t0, field):
+        out = self._fields(3)
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        self.check(self.lib.wvref_field_derivatives(self.h, ctypes.c_double(t), ctypes.c_double(t0), P(Ap), P(Am), P(A0),
+                                                    ctypes.c_int(field), P(out)))
+        return out
+
+    def advect_scalar(self, scalar, adv, antialias):
+        c = self.case
+        out = np.zeros((c["Nz"], c["Ny"], c["Nx"]))
+        scalar, adv = np.ascontiguousarray(scalar), np.ascontiguousarray(adv)
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        self.check(self.lib.wvref_advect_scalar(self.h, P(scalar), P(adv), ctypes.c_int(int(antialias)), P(out)))
+        return out
+
     def rk4(self, Ap, Am, A0, t, t0, dt, steps):
         Ap, Am, A0 = Ap.copy(), Am.copy(), A0.copy()
         tt = ctypes.c_double(t)
@@ -167,6 +208,18 @@ def main():
         else:
             rk_in = (Ap, Am, A0, t, t0)
         Kp, Km, K0, tK = r.rk4(rk_in[0], rk_in[1], rk_in[2], rk_in[3], rk_in[4], case["dt"], case["steps"])
+        # advection-field entry points, state-field derivatives and F-grid scalar advection
+        (Wp, Wm, W0), adv = r.flux_with_advection(Ap, Am, A0, t, t0)
+        rng2 = np.random.Generator(np.random.PCG64(base + 5))
+        given = rng2.standard_normal((3, case["Nz"], case["Ny"], case["Nx"])) * 0.05
+        Up, Um, U0 = r.flux_using_advection(Ap, Am, A0, t, t0, given)
+        uvw = r.inverse_uvw(Ap, Am, A0, t, t0)
+        fields_deriv = {}
+        for q in ((0, 1, 3) if case["isHydrostatic"] else (0, 1, 2, 3)):
+            fields_deriv[f"deriv_{q}"] = r.field_derivatives(Ap, Am, A0, t, t0, q)
+        scalar = rng2.standard_normal((case["Nz"], case["Ny"], case["Nx"]))
+        scal_rhs = r.advect_scalar(scalar, given, False)
+        scal_rhs_aa = r.advect_scalar(scalar, given, True)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"),
             Ap=Ap, Am=Am, A0=A0, t=t, t0=t0,
@@ -174,6 +227,8 @@ def main():
             fields=fields, Bp=Bp, Bm=Bm, B0=B0, inverse=inv,
             rk_Ap=rk_in[0], rk_Am=rk_in[1], rk_A0=rk_in[2], rk_t=rk_in[3], rk_t0=rk_in[4],
             rk_dt=case["dt"], rk_steps=case["steps"], Kp=Kp, Km=Km, K0=K0, rk_tout=tK,
+            with_Fp=Wp, with_Fm=Wm, with_F0=W0, with_fields=adv, given_fields=given, using_Fp=Up, using_Fm=Um, using_F0=U0,
+            uvw=uvw, scalar=scalar, scalar_rhs=scal_rhs, scalar_rhs_aa=scal_rhs_aa, **fields_deriv,
             **{f"desc_{k}": v for k, v in desc.items()},
         )
         cfg = {k: v for k, v in case.items()}

@@ -89,3 +89,44 @@ def test_invalid_configuration_rejected():
     with pytest.raises(O.OracleError) as e:
         O.build_descriptor(c)
     assert e.value.code == O.INVALID_CONFIGURATION
+
+
+# ---- advection-field entry points, UVW inverse, state-field derivatives and
+#      F-grid scalar advection against the reference's own outputs
+
+@pytest.mark.parametrize("name", sorted(golden_cases()))
+def test_oracle_flux_with_and_using_advection_fields(name):
+    c = config_from_case(golden_cases()[name])
+    d = O.build_descriptor(c)
+    g = load_golden(name)
+    args = (g["Ap"], g["Am"], g["A0"], float(g["t"]), float(g["t0"]))
+    (Fp, Fm, F0), adv = O.flux_with_advection(d, *args)
+    for a, b in zip((Fp, Fm, F0), (g["with_Fp"], g["with_Fm"], g["with_F0"])):
+        assert rel_err(a, b) <= 1e-12
+    assert rel_err(adv, g["with_fields"]) <= 1e-12
+    F = O.nonlinear_flux(d, *args, advection=g["given_fields"])
+    for a, b in zip(F, (g["using_Fp"], g["using_Fm"], g["using_F0"])):
+        assert rel_err(a, b) <= 1e-12
+    assert rel_err(O.inverse_uvw(d, *args), g["uvw"]) <= 1e-12
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases()))
+def test_oracle_field_derivatives(name):
+    cf = golden_cases()[name]
+    c = config_from_case(cf)
+    d = O.build_descriptor(c)
+    g = load_golden(name)
+    for q in ((0, 1, 3) if cf["isHydrostatic"] else (0, 1, 2, 3)):
+        got = O.derivative_fields(d, g["Ap"], g["Am"], g["A0"], float(g["t"]), float(g["t0"]), q)
+        assert rel_err(got, g[f"deriv_{q}"]) <= 1e-12, q
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases()))
+@pytest.mark.parametrize("antialias", [False, True])
+def test_oracle_fgrid_scalar_advection(name, antialias):
+    c = config_from_case(golden_cases()[name])
+    d = O.build_descriptor(c)
+    g = load_golden(name)
+    got = O.advect_fgrid_scalar(d, g["scalar"], g["given_fields"], antialias)
+    ref = g["scalar_rhs_aa"] if antialias else g["scalar_rhs"]
+    assert rel_err(got, ref) <= 1e-12

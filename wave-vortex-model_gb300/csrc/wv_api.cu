@@ -12,6 +12,7 @@
 #include "wv_warpfft.cuh"
 #include "wv_adjoint.cuh"
 #include "wv_vinv_tc.cuh"
+#include "wv_scalar.cuh"
 
 #include <cuda_runtime.h>
 
@@ -73,6 +74,16 @@ struct wv_handle {
     bool tcAvailable = false;  // tensor-core vertical transform built for this handle
     bool verticalTC = false;   // ... and selected (default: on where built)
     size_t tcSmem = 0;
+    // F-grid scalar advection (built on first use): full-spectrum descriptor copy,
+    // z-derivative matrix, per-position flags and scratch
+    bool scalarReady = false;
+    dev::DescDev sd{};
+    const void* scalarD = nullptr;
+    const unsigned char* scalarFlags = nullptr;
+    void* scalarP = nullptr;      // [z][3][y][NxHalf] complex (x r2c / y inverse side)
+    void* scalarF = nullptr;      // [4][z][pos] complex (y forward side)
+    double* scalarGrad = nullptr; // [3][R] doubles
+    double* scalarRhs = nullptr;  // [R] doubles (host-pointer entry)
     cudaEvent_t ev[6] = {};
     wv_stage_times stages{};
 };
@@ -362,15 +373,17 @@ cudaError_t set_smem_limits_w(const Plan& p) {
 }
 
 template <typename T>
-void launch_yinv(wv_handle* h, const dev::YInvMap& map, const dev::cx<T>* z, dev::cx<T>* y, cudaStream_t s) {
+void launch_yinv(wv_handle* h, const dev::YInvMap& map, const dev::cx<T>* z, dev::cx<T>* y, cudaStream_t s,
+                 const dev::DescDev* over = nullptr) {
     const Plan& p = h->plan;
+    const dev::DescDev& dd = over ? *over : h->dd;
     const int ry = warp_ry<T>(p);
     if (ry) {
-        const dim3 grid(cdiv(p.kxColumns, dev::kWG), h->dd.zTotal, map.nOut);
-        WV_RSWITCH_Y(ry, (dev::k_yinv_w<T, RR><<<grid, 256, smem_y_w<T>(p), s>>>(h->dd, map, z, y)));
+        const dim3 grid(cdiv(p.kxColumns, dev::kWG), dd.zTotal, map.nOut);
+        WV_RSWITCH_Y(ry, (dev::k_yinv_w<T, RR><<<grid, 256, smem_y_w<T>(p), s>>>(dd, map, z, y)));
         return;
     }
-    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), h->dd.zTotal), 256, smem_y<T>(p), s>>>(h->dd, map, z, 0, y);
+    dev::k_yinv<T><<<dim3(cdiv(p.kxColumns, dev::kYG), dd.zTotal), 256, smem_y<T>(p), s>>>(dd, map, z, 0, y);
 }
 
 template <typename T>
@@ -387,28 +400,32 @@ void launch_yfwd(wv_handle* h, const dev::cx<T>* ps, int nch, dev::cx<T>* f, cud
 
 template <typename T>
 void launch_xflux(wv_handle* h, const dev::cx<T>* y, dev::cx<T>* ps, unsigned long long* speed, cudaStream_t s,
-                  void* physOut = nullptr) {
+                  void* physOut = nullptr, double* advOut = nullptr, const double* advIn = nullptr) {
     const Plan& p = h->plan;
     const int rx = warp_rx<T>(p);
     if (rx) {
         const dim3 grid(cdiv(p.Ny, dev::kWG), h->dd.zTotal);
         WV_RSWITCH_X(T, rx, (dev::k_xflux_w<T, RR><<<grid, 256, smem_xflux_w<T>(p), s>>>(h->dd, y, ps, speed,
-                                                                                           static_cast<dev::cx<T>*>(physOut))));
+                                                                                           static_cast<dev::cx<T>*>(physOut),
+                                                                                           advOut, advIn)));
         return;
     }
-    dev::k_xflux<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xflux<T>(p), s>>>(h->dd, y, ps, speed, static_cast<T*>(physOut));
+    dev::k_xflux<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xflux<T>(p), s>>>(h->dd, y, ps, speed, static_cast<T*>(physOut),
+                                                                           advOut, advIn);
 }
 
 template <typename T>
-void launch_xc2r(wv_handle* h, const dev::cx<T>* y, double* fields, cudaStream_t s) {
+void launch_xc2r(wv_handle* h, const dev::cx<T>* y, double* fields, cudaStream_t s, int nch = 4,
+                 const dev::DescDev* over = nullptr) {
     const Plan& p = h->plan;
+    const dev::DescDev& dd = over ? *over : h->dd;
     const int rx = warp_rx<T>(p);
     if (rx) {
-        const dim3 grid(cdiv(p.Ny, dev::kWG), h->dd.zTotal);
-        WV_RSWITCH_X(T, rx, (dev::k_xc2r_fields_w<T, RR><<<grid, 256, smem_xc2r_w<T>(p, 4), s>>>(h->dd, y, 4, fields)));
+        const dim3 grid(cdiv(p.Ny, dev::kWG), dd.zTotal);
+        WV_RSWITCH_X(T, rx, (dev::k_xc2r_fields_w<T, RR><<<grid, 256, smem_xc2r_w<T>(p, 4), s>>>(dd, y, nch, fields)));
         return;
     }
-    dev::k_xc2r_fields<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xc2r<T>(p, 4), s>>>(h->dd, y, 4, fields);
+    dev::k_xc2r_fields<T><<<dim3(p.Ny, dd.zTotal), 256, smem_xc2r<T>(p, 4), s>>>(dd, y, nch, fields);
 }
 
 template <typename T>
@@ -428,7 +445,8 @@ void launch_xr2c(wv_handle* h, const double* fields, int nch, dev::cx<T>* ps, cu
 // derivatives of every target) for the adjoint to reuse.
 template <typename T>
 cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
-                        double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s, void* physOut = nullptr) {
+                        double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s, void* physOut = nullptr,
+                        double* advOut = nullptr, const double* advIn = nullptr) {
     const Plan& p = h->plan;
     const auto& d = h->dd;
     const double elapsed = t - t0;
@@ -460,7 +478,7 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     }
     launch_yinv<T>(h, map, z, y, s);
     if (inst) cudaEventRecord(h->ev[2], s);
-    launch_xflux<T>(h, y, ps, speed, s, physOut);
+    launch_xflux<T>(h, y, ps, speed, s, physOut, advOut, advIn);
     if (inst) cudaEventRecord(h->ev[3], s);
     launch_yfwd<T>(h, ps, nt, f, s);
     if (inst) cudaEventRecord(h->ev[4], s);
@@ -483,19 +501,182 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     return e;
 }
 
+// ---- F-grid scalar advection ------------------------------------------------------
+// Full-spectrum copy of the handle's descriptor (every (kx, ky) row active,
+// pos = kx Ny + ky), the scalar pipeline's row wavenumbers (k = 0 at an even-Nx
+// Nyquist column, l by signed mode), the per-position flags (bit 0
+// self-conjugate row, bit 1 kept by the antialias) and the vertical-derivative
+// matrix (kernel.cpp:1066-1110, 466-471).
+int ensure_scalar(wv_handle* h) {
+    if (h->scalarReady) return WV_SUCCESS;
+    const Descriptor& d = h->desc;
+    const Plan& p = h->plan;
+    const size_t Nx = p.Nx, Ny = p.Ny, Nz = p.Nz, NxHalf = Nx / 2 + 1, P = NxHalf * Ny;
+    if (Nz < 3) return fail(h, WV_UNSUPPORTED_OPERATION, "F-grid scalar advection needs Nz >= 3.");
+    std::vector<int32_t> posKy(P), colStart(NxHalf + 1), ymap(NxHalf * Ny);
+    for (size_t kx = 0; kx <= NxHalf; ++kx) colStart[kx] = static_cast<int32_t>(kx * Ny);
+    for (size_t q = 0; q < P; ++q) posKy[q] = static_cast<int32_t>(q % Ny);
+    for (size_t q = 0; q < NxHalf * Ny; ++q) ymap[q] = static_cast<int32_t>(q);
+    const double pi = 3.141592653589793238462643383279502884;
+    std::vector<double> rowK(NxHalf), rowL(Ny);
+    for (size_t kx = 0; kx < NxHalf; ++kx)
+        rowK[kx] = (Nx % 2 == 0 && kx == Nx / 2) ? 0.0 : 2.0 * pi * static_cast<double>(kx) / d.c.Lx;
+    for (size_t ky = 0; ky < Ny; ++ky) {
+        const long long lm = ky < (Ny + 1) / 2 ? static_cast<long long>(ky) : static_cast<long long>(ky) - static_cast<long long>(Ny);
+        rowL[ky] = 2.0 * pi * static_cast<double>(lm) / d.c.Ly;
+    }
+    std::vector<unsigned char> flags(P, 0);
+    auto posOfRow = [&](uint64_t row) { const size_t kx = row % NxHalf, ky = row / NxHalf; return kx * Ny + ky; };
+    for (uint64_t r : d.selfConjugateRows) flags[posOfRow(r)] |= 1;
+    for (uint64_t r : d.storageRow) flags[posOfRow(r)] |= 2;
+    for (uint64_t r : d.completionRows) flags[posOfRow(r)] |= 2;
+    for (uint64_t r : d.completionSources) flags[posOfRow(r)] |= 2;
+    // D[z][z'] = sum_{j=1}^{Nz-2} 2 sin(pi j z/(Nz-1)) (-m_j / 2) / (Nz-1) C[j][z'], interior z only;
+    // C = the unnormalized DCT-I, m_j = pi j / Lz
+    std::vector<double> D(Nz * Nz, 0.0);
+    const long long Np = static_cast<long long>(Nz) - 1;
+    auto sinpi = [&](long long a) { return std::sin(pi * static_cast<double>(a % (2 * Np)) / static_cast<double>(Np)); };
+    auto cospi = [&](long long a) { return std::cos(pi * static_cast<double>(a % (2 * Np)) / static_cast<double>(Np)); };
+    for (size_t z = 1; z + 1 < Nz; ++z)
+        for (size_t zp = 0; zp < Nz; ++zp) {
+            double acc = 0.0;
+            for (size_t j = 1; j + 1 < Nz; ++j) {
+                const double C = zp == 0 ? 1.0 : (zp == Nz - 1 ? ((j % 2) ? -1.0 : 1.0) : 2.0 * cospi(static_cast<long long>(j * zp)));
+                const double mj = pi * static_cast<double>(j) / d.c.Lz;
+                acc += 2.0 * sinpi(static_cast<long long>(j * z)) * (-0.5 * mj) * (1.0 / static_cast<double>(Np)) * C;
+            }
+            D[z * Nz + zp] = acc;
+        }
+    dev::DescDev sd = h->dd;
+    sd.kxColumns = static_cast<int>(NxHalf);
+    sd.positions = static_cast<int>(P);
+    sd.members = 1;
+    sd.zTotal = static_cast<int>(Nz);
+    sd.c2rUseK = 0;
+    cudaError_t e = cudaSuccess;
+    auto up = [&](const auto& v, auto** dst) { if (e == cudaSuccess) e = upload(h, v, dst); };
+    up(posKy, &sd.posKy);
+    up(colStart, &sd.colStart);
+    up(ymap, &sd.ymap);
+    const unsigned char* fl = nullptr;
+    up(flags, &fl);
+    h->scalarFlags = fl;
+    const size_t cb = 2 * elem_size(h->precision);
+    auto upT = [&](const std::vector<double>& v, const void** dst) {
+        if (e != cudaSuccess) return;
+        if (h->precision == WV_PRECISION_FP64) { const double* q = nullptr; e = upload(h, v, &q); *dst = q; }
+        else { const std::vector<float> f = cast<float>(v); const float* q = nullptr; e = upload(h, f, &q); *dst = q; }
+    };
+    upT(rowK, &sd.tRowK);
+    upT(rowL, &sd.tRowL);
+    upT(D, &h->scalarD);
+    const size_t R = Nx * Ny * Nz;
+    if (e == cudaSuccess) e = alloc(h, 3 * Nz * Ny * NxHalf * cb, &h->scalarP);
+    if (e == cudaSuccess) e = alloc(h, 4 * Nz * P * cb, &h->scalarF);
+    void* g = nullptr;
+    if (e == cudaSuccess) { e = alloc(h, 3 * R * sizeof(double), &g); h->scalarGrad = static_cast<double*>(g); }
+    if (e == cudaSuccess) { e = alloc(h, R * sizeof(double), &g); h->scalarRhs = static_cast<double*>(g); }
+    // shared memory of the full-width c2r (kx_columns = NxHalf) and of the derivative kernel
+    const size_t L = x_len(p);
+    const size_t smC2R = (L + Nx + 3 * NxHalf + 8 * L) * cb;
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64 ? raise_smem_limit(dev::k_xc2r_fields<double>, static_cast<int>(smC2R))
+                                              : raise_smem_limit(dev::k_xc2r_fields<float>, static_cast<int>(smC2R));
+    const size_t smD = Nz * dev::kScalarCols * cb;
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64 ? raise_smem_limit(dev::k_scalar_derivs<double>, static_cast<int>(smD))
+                                              : raise_smem_limit(dev::k_scalar_derivs<float>, static_cast<int>(smD));
+    if (e != cudaSuccess) return cuda_fail(h, e, "scalar advection set-up");
+    h->sd = sd;
+    h->scalarReady = true;
+    h->metrics.device_bytes = h->deviceBytes;
+    return WV_SUCCESS;
+}
+
+// advectFGridScalar (kernel.cpp:1032-1138) on the shared-memory FFT kernels.
+template <typename T>
+cudaError_t launch_scalar_advection(wv_handle* h, const double* scalar, const double* adv, bool antialias, double* rhs,
+                                    cudaStream_t s) {
+    const Plan& p = h->plan;
+    const dev::DescDev& sd = h->sd;
+    const int Ny = static_cast<int>(p.Ny), Nz = static_cast<int>(p.Nz), KX = sd.kxColumns, P = sd.positions;
+    const size_t R = p.Nx * p.Ny * p.Nz, L = x_len(p);
+    const double hs = 1.0 / static_cast<double>(p.Nx * p.Ny);
+    auto* sp = static_cast<dev::cx<T>*>(h->scalarP);
+    auto* sf = static_cast<dev::cx<T>*>(h->scalarF);
+    const auto* D = static_cast<const T*>(h->scalarD);
+    const size_t cb = sizeof(dev::cx<T>);
+    const size_t smR2C = (L + p.Nx + 8 * L) * cb + 4 * p.Nx * sizeof(T);
+    const size_t smC2R3 = (L + p.Nx + 3 * KX + 8 * L) * cb, smC2R1 = (L + p.Nx + 1 * KX + 8 * L) * cb;
+    const unsigned gridE = static_cast<unsigned>(std::min<size_t>((R + 255) / 256, 152 * 16));
+    // x r2c, y forward FFT of the scalar (channel 3 of sf), column derivatives (channels 0..2)
+    dev::k_xr2c_fields<T><<<dim3(Ny, Nz), 256, smR2C, s>>>(sd, scalar, 1, sp);
+    dev::cx<T>* sf3 = sf + (size_t)3 * Nz * P;
+    dev::k_yfwd<T><<<dim3(cdiv(KX, dev::kYG), Nz, 1), 256, smem_y<T>(p), s>>>(sd, sp, 1, sf3);
+    dev::k_scalar_derivs<T><<<cdiv(P, dev::kScalarCols), 256, Nz * dev::kScalarCols * cb, s>>>(sd, sf3, D, h->scalarFlags, hs, sf);
+    dev::YInvMap map{};
+    map.nOut = 3;
+    for (int c = 0; c < 3; ++c) { map.src[c] = c; map.mulL[c] = 0; }
+    dev::k_yinv<T><<<dim3(cdiv(KX, dev::kYG), Nz), 256, smem_y<T>(p), s>>>(sd, map, sf, 0, sp);
+    dev::k_xc2r_fields<T><<<dim3(Ny, Nz), 256, smC2R3, s>>>(sd, sp, 3, h->scalarGrad);
+    dev::k_scalar_rhs<<<gridE, 256, 0, s>>>(h->scalarGrad, adv, R, rhs);
+    h->metrics.kernel_launches += 6;
+    if (antialias) {
+        dev::k_xr2c_fields<T><<<dim3(Ny, Nz), 256, smR2C, s>>>(sd, rhs, 1, sp);
+        dev::k_yfwd<T><<<dim3(cdiv(KX, dev::kYG), Nz, 1), 256, smem_y<T>(p), s>>>(sd, sp, 1, sf);
+        dev::k_scalar_mask<T><<<static_cast<unsigned>(std::min<size_t>((size_t(Nz) * P + 255) / 256, 152 * 16)), 256, 0, s>>>(
+            sd, sf, h->scalarFlags, hs);
+        dev::YInvMap m1{};
+        m1.nOut = 1;
+        m1.src[0] = 0; m1.mulL[0] = 0;
+        dev::k_yinv<T><<<dim3(cdiv(KX, dev::kYG), Nz), 256, smem_y<T>(p), s>>>(sd, m1, sf, 0, sp);
+        dev::k_xc2r_fields<T><<<dim3(Ny, Nz), 256, smC2R1, s>>>(sd, sp, 1, rhs);
+        h->metrics.kernel_launches += 5;
+    }
+    return cudaGetLastError();
+}
+
+// (d/dx, d/dy, d/dz) of field q (0..3 = u, v, w, eta) at the state
+// (transformStateFieldDerivatives, kernel.cpp:719-743): the flux's own stages
+// with q as the only target -- vinv gives q and q_z, the y pass q (later times
+// i k), i l q and q_z, the x pass c2r of the three with i k on the first.
+template <typename T>
+cudaError_t launch_field_derivatives(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                                     int q, double* out, cudaStream_t s) {
+    const Plan& p = h->plan;
+    dev::DescDev d = h->dd;
+    d.nt = 1;
+    d.tq[0] = q;
+    d.c2rUseK = 1;
+    auto* z = static_cast<dev::cx<T>*>(h->zspec);
+    auto* y = static_cast<dev::cx<T>*>(h->yspec);
+    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, t - t0, z,
+                                                                                                   nullptr);
+    dev::YInvMap map{};
+    map.nOut = 3;
+    map.src[0] = q; map.mulL[0] = 0;
+    map.src[1] = q; map.mulL[1] = 1;
+    map.src[2] = 4; map.mulL[2] = 0;
+    launch_yinv<T>(h, map, z, y, s, &d);
+    launch_xc2r<T>(h, y, out, s, 3, &d);
+    h->metrics.kernel_launches += 3;
+    return cudaGetLastError();
+}
+
+// nch = 4: (u, v, w, eta); nch = 3: (u, v, w) (transformWaveVortexToUVW).
 template <typename T>
 cudaError_t launch_inverse(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
-                           double* fields, cudaStream_t s) {
+                           double* fields, cudaStream_t s, int nch = 4) {
     const Plan& p = h->plan;
     const auto& d = h->dd;
     auto* z = static_cast<dev::cx<T>*>(h->zspec);
     auto* y = static_cast<dev::cx<T>*>(h->yspec);
     dev::k_vinv<T, false><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, t - t0, z, nullptr);
     dev::YInvMap map{};
-    map.nOut = 4;
-    for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
+    map.nOut = nch;
+    for (int c = 0; c < nch; ++c) { map.src[c] = c; map.mulL[c] = 0; }
     launch_yinv<T>(h, map, z, y, s);
-    launch_xc2r<T>(h, y, fields, s);
+    launch_xc2r<T>(h, y, fields, s, nch);
     h->metrics.kernel_launches += 3;
     return cudaGetLastError();
 }
@@ -669,9 +850,11 @@ cudaError_t flux_vjp_any(wv_handle* h, double t, double t0, const double* y, con
 }
 
 cudaError_t flux_any(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
-                     double* Fm, double* F0, bool damping, cudaStream_t s, void* physOut = nullptr) {
-    return h->precision == WV_PRECISION_FP64 ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut)
-                                             : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut);
+                     double* Fm, double* F0, bool damping, cudaStream_t s, void* physOut = nullptr, double* advOut = nullptr,
+                     const double* advIn = nullptr) {
+    return h->precision == WV_PRECISION_FP64
+               ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut, advOut, advIn)
+               : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut, advOut, advIn);
 }
 
 // Scheduled RHS on contiguous [3][M] complex state/flux buffers.
@@ -1182,6 +1365,225 @@ int wv_inverse_device(wv_handle* h, double t, double t0, const double* Ap, const
                               : launch_inverse<float>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream));
     h->metrics.inverse_calls++;
     return finish(h, e, "inverse transform");
+}
+
+// ---- advection fields (nonlinearFluxWithAdvectionFields / UsingAdvectionFields, kernel.cpp:1148-1171;
+//      transformWaveVortexToUVW, kernel.cpp:696-717) ----------------------------------------
+
+static int advection_entry_checks(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                                  double* Fp, double* Fm, double* F0, const double* fields, const char* what) {
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
+    if (!fields) return fail(h, WV_INVALID_POINTER, std::string(what) + " pointer must be nonnull.");
+    if (h->dd.members != 1) return fail(h, WV_UNSUPPORTED_OPERATION, "Advection fields are per single-state handle.");
+    const size_t fb = 3 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
+    for (const void* p : {static_cast<const void*>(Ap), static_cast<const void*>(Am), static_cast<const void*>(A0),
+                          static_cast<const void*>(Fp), static_cast<const void*>(Fm), static_cast<const void*>(F0)})
+        if (overlaps(fields, fb, p, cb))
+            return fail(h, WV_OVERLAPPING_ARRAYS, std::string(what) + " must not overlap the state or flux arrays.");
+    return WV_SUCCESS;
+}
+
+int wv_nonlinear_flux_with_advection_fields_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am,
+                                                   const double* A0, double* Fp, double* Fm, double* F0, double* fields,
+                                                   void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = advection_entry_checks(h, t, t0, Ap, Am, A0, Fp, Fm, F0, fields, "Advection fields"); if (rc) return rc;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const cudaError_t e = flux_any(h, t, t0, Ap, Am, A0, Fp, Fm, F0, false, static_cast<cudaStream_t>(stream), nullptr, fields);
+    h->metrics.nonlinear_flux_calls++;
+    return finish(h, e, "nonlinear flux");
+}
+
+int wv_nonlinear_flux_using_advection_fields_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am,
+                                                    const double* A0, double* Fp, double* Fm, double* F0,
+                                                    const double* fields, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = advection_entry_checks(h, t, t0, Ap, Am, A0, Fp, Fm, F0, fields, "Prepared advection fields"); if (rc) return rc;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const cudaError_t e =
+        flux_any(h, t, t0, Ap, Am, A0, Fp, Fm, F0, false, static_cast<cudaStream_t>(stream), nullptr, nullptr, fields);
+    h->metrics.nonlinear_flux_calls++;
+    return finish(h, e, "nonlinear flux");
+}
+
+int wv_inverse_uvw_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                          double* fields, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Inverse transform received a null pointer.");
+    const size_t fb = 3 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
+    for (const void* in : {static_cast<const void*>(Ap), static_cast<const void*>(Am), static_cast<const void*>(A0)})
+        if (overlaps(fields, fb, in, cb)) return fail(h, WV_OVERLAPPING_ARRAYS, "Inverse spatial output must not overlap coefficient inputs.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64
+                              ? launch_inverse<double>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream), 3)
+                              : launch_inverse<float>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream), 3);
+    h->metrics.inverse_calls++;
+    return finish(h, e, "inverse transform");
+}
+
+// Host-pointer forms: state, flux and fields through the handle's device mirrors.
+static int host_advection_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                               double* Fp, double* Fm, double* F0, double* fieldsOut, const double* fieldsIn) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !Fp || !Fm || !F0 || !(fieldsOut || fieldsIn))
+        return fail(h, WV_INVALID_POINTER, "Nonlinear flux received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16, M2 = 2 * h->plan.M;
+    const size_t fb = 3 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double);
+    auto s = h->stream;
+    cudaError_t e = cudaSuccess;
+    const double* in[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, in[c], cb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && fieldsIn) e = cudaMemcpyAsync(h->fields, fieldsIn, fb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = flux_any(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->flux, h->flux + M2, h->flux + 2 * M2, false, s,
+                     nullptr, fieldsOut ? h->fields : nullptr, fieldsIn ? h->fields : nullptr);
+    double* out[] = {Fp, Fm, F0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(out[c], reinterpret_cast<char*>(h->flux) + c * cb, cb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && fieldsOut) e = cudaMemcpyAsync(fieldsOut, h->fields, fb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    h->metrics.nonlinear_flux_calls++;
+    return finish(h, e, "nonlinear flux");
+}
+
+int wv_nonlinear_flux_with_advection_fields(wv_handle* h, double t, double t0, const double* Ap, const double* Am,
+                                            const double* A0, double* Fp, double* Fm, double* F0, double* fields) {
+    return host_advection_flux(h, t, t0, Ap, Am, A0, Fp, Fm, F0, fields, nullptr);
+}
+
+int wv_nonlinear_flux_using_advection_fields(wv_handle* h, double t, double t0, const double* Ap, const double* Am,
+                                             const double* A0, double* Fp, double* Fm, double* F0, const double* fields) {
+    return host_advection_flux(h, t, t0, Ap, Am, A0, Fp, Fm, F0, nullptr, fields);
+}
+
+int wv_inverse_uvw(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* fields) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (!Ap || !Am || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Inverse transform received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16, M2 = 2 * h->plan.M;
+    const size_t fb = 3 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double);
+    auto s = h->stream;
+    cudaError_t e = cudaSuccess;
+    const double* in[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, in[c], cb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64
+                ? launch_inverse<double>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s, 3)
+                : launch_inverse<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s, 3);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fields, h->fields, fb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    h->metrics.inverse_calls++;
+    return finish(h, e, "inverse transform");
+}
+
+int wv_field_derivatives_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                                int field, double* out, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (field < 0 || field > 3) return fail(h, WV_INVALID_CONFIGURATION, "Unknown dynamical field derivative target.");
+    if (!Ap || !Am || !A0 || !out) return fail(h, WV_INVALID_POINTER, "Field derivatives received a null pointer.");
+    if (h->dd.members != 1) return fail(h, WV_UNSUPPORTED_OPERATION, "Field derivatives are per single-state handle.");
+    const size_t fb = 3 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
+    for (const void* in : {static_cast<const void*>(Ap), static_cast<const void*>(Am), static_cast<const void*>(A0)})
+        if (overlaps(out, fb, in, cb)) return fail(h, WV_OVERLAPPING_ARRAYS, "Field derivatives must not overlap coefficient inputs.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    auto s = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64
+                              ? launch_field_derivatives<double>(h, t, t0, Ap, Am, A0, field, out, s)
+                              : launch_field_derivatives<float>(h, t, t0, Ap, Am, A0, field, out, s);
+    return finish(h, e, "field derivatives");
+}
+
+static int scalar_entry_checks(wv_handle* h, const double* scalar, const double* fields, const double* rhs) {
+    if (!scalar || !rhs) return fail(h, WV_INVALID_POINTER, "F-grid scalar input and output pointers must be nonnull.");
+    if (!fields) return fail(h, WV_INVALID_POINTER, "Advection fields pointer must be nonnull.");
+    if (h->dd.members != 1) return fail(h, WV_UNSUPPORTED_OPERATION, "Scalar advection is per single-state handle.");
+    const size_t bytes = h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double);
+    if (overlaps(scalar, bytes, rhs, bytes) || overlaps(fields, 3 * bytes, scalar, bytes) || overlaps(fields, 3 * bytes, rhs, bytes))
+        return fail(h, WV_OVERLAPPING_ARRAYS, "Tracer scalar, velocity, and RHS arrays must not overlap.");
+    return WV_SUCCESS;
+}
+
+int wv_advect_fgrid_scalar_device(wv_handle* h, const double* scalar, const double* fields, int antialias, double* rhs,
+                                  void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = scalar_entry_checks(h, scalar, fields, rhs); if (rc) return rc;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    rc = ensure_scalar(h); if (rc) return rc;
+    auto s = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64
+                              ? launch_scalar_advection<double>(h, scalar, fields, antialias != 0, rhs, s)
+                              : launch_scalar_advection<float>(h, scalar, fields, antialias != 0, rhs, s);
+    return finish(h, e, "scalar advection");
+}
+
+int wv_advect_fgrid_scalar(wv_handle* h, const double* scalar, const double* fields, int antialias, double* rhs) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = scalar_entry_checks(h, scalar, fields, rhs); if (rc) return rc;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    rc = ensure_scalar(h); if (rc) return rc;
+    const size_t R = h->plan.Nx * h->plan.Ny * h->plan.Nz, bytes = R * sizeof(double);
+    auto s = h->stream;
+    // h->fields holds 4 R doubles: the scalar in the first R, (u, v, w) in the next 3 R
+    double* dScalar = h->fields;
+    double* dAdv = h->fields + R;
+    double* dRhs = h->scalarRhs;
+    cudaError_t e = cudaMemcpyAsync(dScalar, scalar, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dAdv, fields, 3 * bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64 ? launch_scalar_advection<double>(h, dScalar, dAdv, antialias != 0, dRhs, s)
+                                              : launch_scalar_advection<float>(h, dScalar, dAdv, antialias != 0, dRhs, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rhs, dRhs, bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return finish(h, e, "scalar advection");
+}
+
+int wv_field_derivatives(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, int field,
+                         double* out) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    if (field < 0 || field > 3) return fail(h, WV_INVALID_CONFIGURATION, "Unknown dynamical field derivative target.");
+    if (!Ap || !Am || !A0 || !out) return fail(h, WV_INVALID_POINTER, "Field derivatives received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16, M2 = 2 * h->plan.M;
+    const size_t fb = 3 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double);
+    auto s = h->stream;
+    cudaError_t e = cudaSuccess;
+    const double* in[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, in[c], cb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64
+                ? launch_field_derivatives<double>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, field, h->fields, s)
+                : launch_field_derivatives<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, field, h->fields, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, h->fields, fb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return finish(h, e, "field derivatives");
 }
 
 int wv_forward_device(wv_handle* h, const double* fields, double t, double t0, double* Ap, double* Am, double* A0, void* stream) {

@@ -247,6 +247,7 @@ struct DescDev {
     const unsigned short* tcB;
     int tcN, tcKE, tcK;
     unsigned* status;       // device status word (bit 0: a bounded wait ran out)
+    int c2rUseK;            // k_xc2r_fields(_w): bit c set -> channel c is multiplied by i k (x derivative)
     int xEven;              // Nx even: real rows go through half-length complex FFTs
     int xLen;               // Nx/2 (even) or Nx (odd)
     FFTDev fx, fy;          // fx factors xLen
@@ -543,9 +544,12 @@ __device__ __forceinline__ cx<T> r2c_value(const DescDev& d, const cx<T>* line, 
 // xflux: one CTA per (y, z) row.
 
 // physOut, when given, receives the real rows [z][nReal][y][Nx] for the adjoint.
+// advOut, when given, receives the advecting (u, v, w) as doubles [3][z][y][Nx];
+// advIn, when given, replaces them (nonlinearFlux With/Using AdvectionFields).
 template <typename T>
 __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
-                                              unsigned long long* __restrict__ maxSpeedBits, T* __restrict__ physOut) {
+                                              unsigned long long* __restrict__ maxSpeedBits, T* __restrict__ physOut,
+                                              double* __restrict__ advOut, const double* __restrict__ advIn) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Nx = d.Nx, Ny = d.Ny, KX = d.kxColumns, nt = d.nt, L = d.xLen;
     const int nIn = 4 + 2 * nt;          // U V W N, q_y..., q_z...
@@ -588,6 +592,16 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
         for (int i = threadIdx.x; i < nr * Nx; i += blockDim.x) {
             const int li = i / Nx, x = i - li * Nx;
             phys[(rb + li) * Nx + x] = c2r_sample<T>(d, res + li * L, x);
+        }
+        __syncthreads();
+    }
+    if (advIn || advOut) {
+        const size_t R3 = (size_t)Nx * Ny * d.Nz;
+        for (int i = threadIdx.x; i < 3 * Nx; i += blockDim.x) {
+            const int c = i / Nx, x = i - c * Nx;
+            const size_t g = (size_t)c * R3 + ((size_t)z * Ny + y) * Nx + x;
+            if (advIn) phys[i] = T(advIn[g]);
+            else advOut[g] = double(phys[i]);
         }
         __syncthreads();
     }
@@ -663,7 +677,7 @@ __global__ void __launch_bounds__(256) k_xc2r_fields(DescDev d, const cx<T>* __r
     __syncthreads();
     for (int i = threadIdx.x; i < nch * L; i += blockDim.x) {
         const int li = i / L, k = i - li * L;
-        bufA[li * L + k] = c2r_line_entry<T>(d, spec + li * KX, k, false, twN);
+        bufA[li * L + k] = c2r_line_entry<T>(d, spec + li * KX, k, ((d.c2rUseK >> li) & 1) != 0, twN);
     }
     __syncthreads();
     cx<T>* res = fft_lines<T, true>(bufA, bufB, d.fx, nch, L, tw);

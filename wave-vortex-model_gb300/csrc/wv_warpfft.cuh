@@ -226,9 +226,13 @@ __device__ __forceinline__ void c2r_row(const DescDev& d, const cx<T>* h, bool u
 
 // physOut, when given, receives the real rows as complex pairs in register
 // order: [z][nReal][y][L], entry k*32 + lane = register k of lane `lane`.
+// advOut / advIn: the advecting (u, v, w) as doubles [3][z][y][Nx], written out
+// or taken in place of the reconstructed ones (sample pair 2n, 2n+1 of the row
+// sits in register k of lane l with n = k + R brev5(l)).
 template <typename T, int R>
 __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
-                                                unsigned long long* __restrict__ maxSpeedBits, cx<T>* __restrict__ physOut) {
+                                                unsigned long long* __restrict__ maxSpeedBits, cx<T>* __restrict__ physOut,
+                                                double* __restrict__ advOut, const double* __restrict__ advIn) {
     constexpr int L = 32 * R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double warpMax[kWG];
@@ -261,6 +265,24 @@ __global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __re
 #pragma unroll
         for (int k = 0; k < R; ++k) o[32 * k] = x[k];
     };
+    if (advIn || advOut) {
+        const size_t R3 = (size_t)(2 * L) * Ny * d.Nz;
+        const size_t rowOff = ((size_t)z * Ny + y) * (2 * L);
+        cx<T>* vel[3] = {U, V, W};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const size_t g = (size_t)c * R3 + rowOff + 2 * (size_t)p_index<R>(k, lane);
+                if (advIn) {
+                    const double2 a = *reinterpret_cast<const double2*>(advIn + g);
+                    vel[c][k] = mk<T>(T(a.x), T(a.y));
+                } else {
+                    *reinterpret_cast<double2*>(advOut + g) = make_double2(double(vel[c][k].x), double(vel[c][k].y));
+                }
+            }
+        }
+    }
     if (physOut) { keep(0, U); keep(1, V); keep(2, W); }
     // max |u_h| only when a consumer asked for it (max of u^2 + v^2, one sqrt at the end)
     const bool wantSpeed = maxSpeedBits != nullptr;
@@ -463,7 +485,7 @@ __global__ void __launch_bounds__(256) k_xc2r_fields_w(DescDev d, const cx<T>* _
     const size_t R3 = (size_t)Nx * Ny * Nz;
     for (int c = 0; c < nch; ++c) {
         cx<T> v[R];
-        c2r_row<T, R>(d, spec + c * KX, false, twL, twN, lane, v);
+        c2r_row<T, R>(d, spec + c * KX, ((d.c2rUseK >> c) & 1) != 0, twL, twN, lane, v);
 #pragma unroll
         for (int k1 = 0; k1 < R; ++k1) line[p_index<R>(k1, lane)] = v[k1];
         __syncwarp();

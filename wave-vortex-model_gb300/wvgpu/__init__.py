@@ -156,6 +156,15 @@ def load_library():
     lib.wv_forward_device.argtypes = [P, P, D, D, P, P, P, P]
     lib.wv_inverse.argtypes = [P, D, D, P, P, P, P]
     lib.wv_inverse_device.argtypes = [P, D, D, P, P, P, P, P]
+    lib.wv_inverse_uvw.argtypes = [P, D, D, P, P, P, P]
+    lib.wv_field_derivatives.argtypes = [P, D, D, P, P, P, ctypes.c_int, P]
+    lib.wv_field_derivatives_device.argtypes = [P, D, D, P, P, P, ctypes.c_int, P, P]
+    lib.wv_advect_fgrid_scalar.argtypes = [P, P, P, ctypes.c_int, P]
+    lib.wv_advect_fgrid_scalar_device.argtypes = [P, P, P, ctypes.c_int, P, P]
+    lib.wv_inverse_uvw_device.argtypes = [P, D, D, P, P, P, P, P]
+    for name in ("wv_nonlinear_flux_with_advection_fields", "wv_nonlinear_flux_using_advection_fields"):
+        getattr(lib, name).argtypes = [P, D, D, P, P, P, P, P, P, P]
+        getattr(lib, name + "_device").argtypes = [P, D, D, P, P, P, P, P, P, P, P]
     lib.wv_rk4_steps.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int]
     lib.wv_rk4_steps_device.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int, P]
     lib.wv_flux_vjp_device.argtypes = [P, D, D, P, P, P, P, P, P, P, P, P, P]
@@ -184,7 +193,11 @@ def exported_symbols():
             "wv_set_vertical_kernel", "wv_get_device_status", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
             "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc", "wv_flux_vjp_device",
-            "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device", "wv_ensemble_create",
+            "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device",
+            "wv_nonlinear_flux_with_advection_fields", "wv_nonlinear_flux_using_advection_fields", "wv_inverse_uvw",
+            "wv_nonlinear_flux_with_advection_fields_device", "wv_nonlinear_flux_using_advection_fields_device",
+            "wv_inverse_uvw_device", "wv_field_derivatives", "wv_field_derivatives_device", "wv_advect_fgrid_scalar",
+            "wv_advect_fgrid_scalar_device", "wv_ensemble_create",
             "wv_ensemble_destroy", "wv_ensemble_last_message", "wv_ensemble_get_sizes", "wv_ensemble_get_tuning",
             "wv_ensemble_get_metrics", "wv_ensemble_set_vertical_kernel", "wv_ensemble_rk4_device"]
 
@@ -308,6 +321,101 @@ class WVTransformConstantStratificationKernel:
         self._check(fn(self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data, F[0].ctypes.data,
                        F[1].ctypes.data, F[2].ctypes.data))
         return F
+
+    def nonlinearFluxWithAdvectionFields(self, t, t0, Ap, Am, A0):
+        """nonlinearFluxWithAdvectionFields (kernel.cpp:1148-1158): ((Fp, Fm, F0), fields (3, Nz, Ny, Nx))."""
+        if _is_torch(Ap):
+            import torch
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            F = tuple(torch.empty_like(Ap) for _ in range(3))
+            adv = torch.empty((3,) + self.spatial_shape, dtype=torch.float64, device=Ap.device)
+            self._check(self._lib.wv_nonlinear_flux_with_advection_fields_device(
+                self._h, float(t), float(t0), Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(), *(f.data_ptr() for f in F),
+                adv.data_ptr(), self._stream()))
+            return F, adv
+        Ap, Am, A0 = (self._host_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        F = tuple(np.empty(self.spectral_shape, np.complex128) for _ in range(3))
+        adv = np.empty((3,) + self.spatial_shape)
+        self._check(self._lib.wv_nonlinear_flux_with_advection_fields(
+            self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data, *(f.ctypes.data for f in F),
+            adv.ctypes.data))
+        return F, adv
+
+    def nonlinearFluxUsingAdvectionFields(self, t, t0, Ap, Am, A0, fields):
+        """nonlinearFluxUsingAdvectionFields (kernel.cpp:1160-1171): the flux advected by fields (3, Nz, Ny, Nx)."""
+        if _is_torch(Ap):
+            import torch
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            fields = fields.contiguous()
+            if tuple(fields.shape) != (3,) + self.spatial_shape or fields.dtype != torch.float64:
+                raise WVKernelError(2, "Prepared advection fields must be float64 of shape [Nx,Ny,Nz,3].")
+            F = tuple(torch.empty_like(Ap) for _ in range(3))
+            self._check(self._lib.wv_nonlinear_flux_using_advection_fields_device(
+                self._h, float(t), float(t0), Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(), *(f.data_ptr() for f in F),
+                fields.data_ptr(), self._stream()))
+            return F
+        Ap, Am, A0 = (self._host_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        fields = np.ascontiguousarray(fields, dtype=np.float64)
+        if fields.shape != (3,) + self.spatial_shape:
+            raise WVKernelError(2, "Prepared advection fields must be float64 of shape [Nx,Ny,Nz,3].")
+        F = tuple(np.empty(self.spectral_shape, np.complex128) for _ in range(3))
+        self._check(self._lib.wv_nonlinear_flux_using_advection_fields(
+            self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data, *(f.ctypes.data for f in F),
+            fields.ctypes.data))
+        return F
+
+    def transformWaveVortexToUVW(self, t, t0, Ap, Am, A0):
+        """transformWaveVortexToUVW (kernel.cpp:696-717): fields (3, Nz, Ny, Nx)."""
+        if _is_torch(Ap):
+            import torch
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            out = torch.empty((3,) + self.spatial_shape, dtype=torch.float64, device=Ap.device)
+            self._check(self._lib.wv_inverse_uvw_device(self._h, float(t), float(t0), Ap.data_ptr(), Am.data_ptr(),
+                                                        A0.data_ptr(), out.data_ptr(), self._stream()))
+            return out
+        Ap, Am, A0 = (self._host_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        out = np.empty((3,) + self.spatial_shape)
+        self._check(self._lib.wv_inverse_uvw(self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data,
+                                             out.ctypes.data))
+        return out
+
+    def transformStateFieldDerivatives(self, t, t0, Ap, Am, A0, field):
+        """transformStateFieldDerivatives (kernel.cpp:719-743): (d/dx, d/dy, d/dz) of
+        field 0..3 / 'u', 'v', 'w', 'eta' as (3, Nz, Ny, Nx)."""
+        q = {"u": 0, "v": 1, "w": 2, "eta": 3}.get(field, field)
+        if _is_torch(Ap):
+            import torch
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            out = torch.empty((3,) + self.spatial_shape, dtype=torch.float64, device=Ap.device)
+            self._check(self._lib.wv_field_derivatives_device(self._h, float(t), float(t0), Ap.data_ptr(), Am.data_ptr(),
+                                                              A0.data_ptr(), int(q), out.data_ptr(), self._stream()))
+            return out
+        Ap, Am, A0 = (self._host_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        out = np.empty((3,) + self.spatial_shape)
+        self._check(self._lib.wv_field_derivatives(self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data,
+                                                   A0.ctypes.data, int(q), out.ctypes.data))
+        return out
+
+    def advectFGridScalar(self, scalar, advectionFields, shouldAntialias=True):
+        """advectFGridScalar (kernel.cpp:1032-1138): -(u ds/dx + v ds/dy + w ds/dz), (Nz, Ny, Nx)."""
+        if _is_torch(scalar):
+            import torch
+            scalar = scalar.contiguous()
+            adv = advectionFields.contiguous()
+            if tuple(scalar.shape) != self.spatial_shape or tuple(adv.shape) != (3,) + self.spatial_shape:
+                raise WVKernelError(2, "F-grid scalar input and output must have shape [Nx,Ny,Nz].")
+            out = torch.empty_like(scalar)
+            self._check(self._lib.wv_advect_fgrid_scalar_device(self._h, scalar.data_ptr(), adv.data_ptr(),
+                                                                int(bool(shouldAntialias)), out.data_ptr(), self._stream()))
+            return out
+        scalar = np.ascontiguousarray(scalar, dtype=np.float64)
+        adv = np.ascontiguousarray(advectionFields, dtype=np.float64)
+        if scalar.shape != self.spatial_shape or adv.shape != (3,) + self.spatial_shape:
+            raise WVKernelError(2, "F-grid scalar input and output must have shape [Nx,Ny,Nz].")
+        out = np.empty(self.spatial_shape)
+        self._check(self._lib.wv_advect_fgrid_scalar(self._h, scalar.ctypes.data, adv.ctypes.data,
+                                                     int(bool(shouldAntialias)), out.ctypes.data))
+        return out
 
     def evaluateRightHandSide(self, t, t0, Ap, Am, A0, out=None):
         return self.nonlinearFlux(t, t0, Ap, Am, A0, out=out, scheduled=True)
