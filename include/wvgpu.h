@@ -278,6 +278,13 @@ int wv_field_derivatives(wv_handle* handle, double t, double t0, const double* A
 int wv_field_derivatives_device(wv_handle* handle, double t, double t0, const double* Ap, const double* Am,
                                 const double* A0, int field, double* out, void* stream);
 
+/* transformToSpatialDomainWith{F,G}AllDerivatives (kernel.cpp:819-863): value and
+ * (d/dx, d/dy, d/dz) of the F (ffamily = 1) or G (ffamily = 0) field family of
+ * (Apm, A0) [Nj, Nkl] complex, fields [Nx, Ny, Nz, 4]. */
+int wv_family_derivatives(wv_handle* handle, int ffamily, const double* Apm, const double* A0, double* fields);
+int wv_family_derivatives_device(wv_handle* handle, int ffamily, const double* Apm, const double* A0, double* fields,
+                                 void* stream);
+
 /* advectFGridScalar (kernel.cpp:1032-1138): rhs = -(u ds/dx + v ds/dy + w ds/dz)
  * of an F-grid scalar s [Nx, Ny, Nz] advected by fields (u, v, w) [Nx, Ny, Nz, 3],
  * spectral derivatives on the full half spectrum; with antialias set, rhs is

@@ -208,6 +208,18 @@ int wvref_advect_scalar(void* handle, const double* scalar, const double* fields
     return status ? 0 : fail(h, status);
 }
 
+// transformToSpatialDomainWith{F,G}AllDerivatives: (value, d/dx, d/dy, d/dz) of the
+// F (ffamily = 1) or G field family of (Apm, A0), [Nx, Ny, Nz, 4].
+int wvref_family_derivatives(void* handle, int ffamily, const double* Apm, const double* A0, double* fields) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto& c = h->kernel->descriptor().configuration();
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVRealFieldBundleView view{fields, {c.Nx, c.Ny, c.Nz, 4}};
+    const auto status = ffamily ? h->kernel->transformToSpatialDomainWithFAllDerivatives(cview(Apm, s), cview(A0, s), view)
+                                : h->kernel->transformToSpatialDomainWithGAllDerivatives(cview(Apm, s), cview(A0, s), view);
+    return status ? 0 : fail(h, status);
+}
+
 int wvref_forward(void* handle, const double* fields, double t, double t0, double* Ap, double* Am, double* A0) {
     auto* h = static_cast<RefHandle*>(handle);
     const auto& c = h->kernel->descriptor().configuration();

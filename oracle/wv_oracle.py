@@ -602,6 +602,35 @@ def inverse_uvw(desc, Ap, Am, A0, t, t0):
     return velocity_fields(desc, Ap, Am, A0, t, t0)
 
 
+def family_derivatives(desc, Apm, A0, ffamily):
+    """transformToSpatialDomainWith{F,G}AllDerivatives (kernel.cpp:819-863) with
+    fieldFamilyDerivativeSpectrum (WVCoefficientFormulas.hpp:60-73): value =
+    Apm waveScale + A0 geostrophicScale (F: fWaveScale, Fg; G: gWaveScale, Gg),
+    its i k, i l and -m (F) / +m (G) derivatives; F values are cosine-family
+    (inverse DCT x 0.5) with a sine-family z derivative (inverse DST x 0.5,
+    endpoints 0), G the other way round.  Returns (4, Nz, Ny, Nx)."""
+    kC = desc.k[:, None]
+    lC = desc.l[:, None]
+    mC = desc.m[None, :]
+    if ffamily:
+        val = Apm * desc.arrays["fWaveScale"] + A0 * desc.Fg[None, :]
+    else:
+        val = Apm * desc.gWaveScale[None, :] + A0 * desc.Gg[None, :]
+    x = val * (1j * kC)
+    y = val * (1j * lC)
+    zz = val * (-mC if ffamily else mC)
+    cos_ = lambda v: _inverse_columns_cos(desc, v * 0.5)
+    def sin_(v):
+        v = v * 0.5
+        v[:, 0] = 0.0
+        return _inverse_columns_sin(desc, v)
+    if ffamily:
+        cols = np.stack([cos_(val), cos_(x), cos_(y), sin_(zz)])
+    else:
+        cols = np.stack([sin_(val), sin_(x), sin_(y), cos_(zz)])
+    return _half_rows_to_spatial(desc, _columns_to_half(desc, cols))
+
+
 def scalar_wavenumbers(desc):
     """Row wavenumbers of the F-grid scalar pipeline (kernel.cpp:1067-1072): k over
     the NxHalf columns with k = 0 at an even-Nx Nyquist column, l over the Ny rows

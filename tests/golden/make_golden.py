@@ -152,6 +152,12 @@ class Ref:
         self.check(self.lib.wvref_advect_scalar(self.h, P(scalar), P(adv), ctypes.c_int(int(antialias)), P(out)))
         return out
 
+    def family_derivatives(self, ffamily, Apm, A0):
+        out = self._fields(4)
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        self.check(self.lib.wvref_family_derivatives(self.h, ctypes.c_int(int(ffamily)), P(Apm), P(A0), P(out)))
+        return out
+
     def rk4(self, Ap, Am, A0, t, t0, dt, steps):
         Ap, Am, A0 = Ap.copy(), Am.copy(), A0.copy()
         tt = ctypes.c_double(t)
@@ -220,6 +226,9 @@ def main():
         scalar = rng2.standard_normal((case["Nz"], case["Ny"], case["Nx"]))
         scal_rhs = r.advect_scalar(scalar, given, False)
         scal_rhs_aa = r.advect_scalar(scalar, given, True)
+        Apm = seeded(shape, base + 6, 1e-3)
+        fall = r.family_derivatives(True, Apm, A0)
+        gall = r.family_derivatives(False, Apm, A0)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"),
             Ap=Ap, Am=Am, A0=A0, t=t, t0=t0,
@@ -229,6 +238,7 @@ def main():
             rk_dt=case["dt"], rk_steps=case["steps"], Kp=Kp, Km=Km, K0=K0, rk_tout=tK,
             with_Fp=Wp, with_Fm=Wm, with_F0=W0, with_fields=adv, given_fields=given, using_Fp=Up, using_Fm=Um, using_F0=U0,
             uvw=uvw, scalar=scalar, scalar_rhs=scal_rhs, scalar_rhs_aa=scal_rhs_aa, **fields_deriv,
+            Apm=Apm, fall=fall, gall=gall,
             **{f"desc_{k}": v for k, v in desc.items()},
         )
         cfg = {k: v for k, v in case.items()}

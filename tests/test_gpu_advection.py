@@ -144,3 +144,30 @@ def test_field_derivatives_vs_oracle_midsize(wv):
         ref, floors = O.noise_floor(lambda *a: (O.derivative_fields(*a),), d, *A, 300.0, 0.0, q)
         assert rel_err(got.cpu().numpy(), ref[0]) <= parity_tolerance(floors[0]), q
     k.close()
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases()))
+def test_family_derivatives_match_reference(wv, name):
+    import torch
+    c = config_from_case(golden_cases()[name])
+    g = load_golden(name)
+    k = wv.WVTransformConstantStratificationKernel(to_wv(wv, c))
+    assert rel_err(k.transformToSpatialDomainWithFAllDerivatives(g["Apm"], g["A0"]), g["fall"]) <= FP64_REL_TOL
+    assert rel_err(k.transformToSpatialDomainWithGAllDerivatives(g["Apm"], g["A0"]), g["gall"]) <= FP64_REL_TOL
+    dev = [torch.from_numpy(np.ascontiguousarray(g[n])).cuda() for n in ("Apm", "A0")]
+    assert rel_err(k.transformToSpatialDomainWithFAllDerivatives(*dev).cpu().numpy(), g["fall"]) <= FP64_REL_TOL
+    k.close()
+
+
+def test_family_derivatives_vs_oracle_midsize(wv):
+    c = O.Config(Nx=64, Ny=48, Nz=33, Nj=21, Lx=400e3, Ly=300e3, Lz=4000.0, latitude=33.0)
+    d = O.build_descriptor(c)
+    rng = np.random.default_rng(23)
+    Apm = rng.standard_normal((d.Nkl, c.Nj)) + 1j * rng.standard_normal((d.Nkl, c.Nj))
+    A0 = rng.standard_normal((d.Nkl, c.Nj)) + 1j * rng.standard_normal((d.Nkl, c.Nj))
+    k = wv.WVTransformConstantStratificationKernel(to_wv(wv, c))
+    for ff in (True, False):
+        got = k._family(ff, Apm, A0)
+        ref, floors = O.noise_floor(lambda *a: (O.family_derivatives(*a),), d, Apm, A0, ff)
+        assert rel_err(got, ref[0]) <= parity_tolerance(floors[0]), ff
+    k.close()

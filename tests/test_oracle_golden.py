@@ -130,3 +130,12 @@ def test_oracle_fgrid_scalar_advection(name, antialias):
     got = O.advect_fgrid_scalar(d, g["scalar"], g["given_fields"], antialias)
     ref = g["scalar_rhs_aa"] if antialias else g["scalar_rhs"]
     assert rel_err(got, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases()))
+def test_oracle_family_derivatives(name):
+    c = config_from_case(golden_cases()[name])
+    d = O.build_descriptor(c)
+    g = load_golden(name)
+    assert rel_err(O.family_derivatives(d, g["Apm"], g["A0"], True), g["fall"]) <= 1e-12
+    assert rel_err(O.family_derivatives(d, g["Apm"], g["A0"], False), g["gall"]) <= 1e-12

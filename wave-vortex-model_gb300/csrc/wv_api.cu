@@ -663,6 +663,33 @@ cudaError_t launch_field_derivatives(wv_handle* h, double t, double t0, const do
     return cudaGetLastError();
 }
 
+// (value, d/dx, d/dy, d/dz) of the F or G field family of (Apm, A0)
+// (transformToSpatialDomainWith{F,G}AllDerivatives, kernel.cpp:819-863).
+template <typename T>
+cudaError_t launch_family_derivatives(wv_handle* h, bool ffamily, const double* Apm, const double* A0, double* out,
+                                      cudaStream_t s) {
+    const Plan& p = h->plan;
+    dev::DescDev d = h->dd;
+    d.c2rUseK = 2;  // channel 1: x derivative
+    auto* z = static_cast<dev::cx<T>*>(h->zspec);
+    auto* y = static_cast<dev::cx<T>*>(h->yspec);
+    const size_t sm = p.Nj * dev::kVinvModes * sizeof(dev::cx<T>);
+    if (ffamily)
+        dev::k_vinv_family<T, true><<<cdiv(p.Nkl, dev::kVinvModes), 256, sm, s>>>(d, Apm, A0, z);
+    else
+        dev::k_vinv_family<T, false><<<cdiv(p.Nkl, dev::kVinvModes), 256, sm, s>>>(d, Apm, A0, z);
+    dev::YInvMap map{};
+    map.nOut = 4;
+    map.src[0] = 0; map.mulL[0] = 0;   // value
+    map.src[1] = 0; map.mulL[1] = 0;   // i k value (in x)
+    map.src[2] = 0; map.mulL[2] = 1;   // i l value
+    map.src[3] = 1; map.mulL[3] = 0;   // z derivative
+    launch_yinv<T>(h, map, z, y, s, &d);
+    launch_xc2r<T>(h, y, out, s, 4, &d);
+    h->metrics.kernel_launches += 3;
+    return cudaGetLastError();
+}
+
 // nch = 4: (u, v, w, eta); nch = 3: (u, v, w) (transformWaveVortexToUVW).
 template <typename T>
 cudaError_t launch_inverse(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
@@ -1155,6 +1182,7 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     WV_UP(d.ApmDScaled, ApmDScaled); WV_UP(ApmD, ApmD); WV_UP(damping, damping);
     WV_UP(d.k, k); WV_UP(d.l, l); WV_UP(d.Kh, Kh); WV_UP(d.cosAlpha, cosAlpha); WV_UP(d.sinAlpha, sinAlpha);
     WV_UP(inertial, inertialScale); WV_UP(apmw, apmWPrefactor);
+    WV_UP(d.fWaveScale, fWaveScale); WV_UP(d.gWaveScale, gWaveScale); WV_UP(d.Fg, Fg); WV_UP(d.Gg, Gg);
     WV_UP(posKy, posKy); WV_UP(colStart, colStart); WV_UP(ymap, ymap); WV_UP(modeWV, modeWV); WV_UP(modePos, modePos); WV_UP(modeComp, modeCompPos);
     WV_UP(p.modeFlags, modeFlags);
     WV_UP(p.rowK, rowK); WV_UP(p.rowL, rowL);
@@ -1511,6 +1539,43 @@ int wv_field_derivatives_device(wv_handle* h, double t, double t0, const double*
                               ? launch_field_derivatives<double>(h, t, t0, Ap, Am, A0, field, out, s)
                               : launch_field_derivatives<float>(h, t, t0, Ap, Am, A0, field, out, s);
     return finish(h, e, "field derivatives");
+}
+
+int wv_family_derivatives_device(wv_handle* h, int ffamily, const double* Apm, const double* A0, double* fields,
+                                 void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!Apm || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Field-family derivatives received a null pointer.");
+    if (h->dd.members != 1) return fail(h, WV_UNSUPPORTED_OPERATION, "Field-family derivatives are per single-state handle.");
+    const size_t fb = 4 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
+    if (overlaps(fields, fb, Apm, cb) || overlaps(fields, fb, A0, cb))
+        return fail(h, WV_OVERLAPPING_ARRAYS, "Field derivative output must not overlap coefficient inputs.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    auto s = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64
+                              ? launch_family_derivatives<double>(h, ffamily != 0, Apm, A0, fields, s)
+                              : launch_family_derivatives<float>(h, ffamily != 0, Apm, A0, fields, s);
+    return finish(h, e, "field-family derivatives");
+}
+
+int wv_family_derivatives(wv_handle* h, int ffamily, const double* Apm, const double* A0, double* fields) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!Apm || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Field-family derivatives received a null pointer.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16, M2 = 2 * h->plan.M;
+    const size_t fb = 4 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double);
+    auto s = h->stream;
+    cudaError_t e = cudaMemcpyAsync(h->state, Apm, cb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->state + M2, A0, cb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = h->precision == WV_PRECISION_FP64 ? launch_family_derivatives<double>(h, ffamily != 0, h->state, h->state + M2, h->fields, s)
+                                              : launch_family_derivatives<float>(h, ffamily != 0, h->state, h->state + M2, h->fields, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fields, h->fields, fb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return finish(h, e, "field-family derivatives");
 }
 
 static int scalar_entry_checks(wv_handle* h, const double* scalar, const double* fields, const double* rhs) {

@@ -248,6 +248,11 @@ struct DescDev {
     int tcN, tcKE, tcK;
     unsigned* status;       // device status word (bit 0: a bounded wait ran out)
     int c2rUseK;            // k_xc2r_fields(_w): bit c set -> channel c is multiplied by i k (x derivative)
+    // field-family scales (transformToSpatialDomainWith{F,G}AllDerivatives)
+    const double* fWaveScale;   // [M]
+    const double* gWaveScale;   // [Nj]
+    const double* Fg;           // [Nj]
+    const double* Gg;           // [Nj]
     int xEven;              // Nx even: real rows go through half-length complex FFTs
     int xLen;               // Nx/2 (even) or Nx (odd)
     FFTDev fx, fy;          // fx factors xLen
@@ -414,6 +419,69 @@ __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restric
                     else if (q == 2) put(4 + t, E[6], O[6], false);
                     else put(4 + t, E[7], O[7], false);
                 }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// vinv_family: value and z derivative of the F (FFAMILY) or G field family of
+// (Apm, A0) per retained column (fieldFamilyDerivativeSpectrum,
+// WVCoefficientFormulas.hpp:60-73): value = Apm waveScale + A0 geostrophicScale
+// in the stored frame, F values through the cosine matrix and their -m z
+// derivative through CsinM; G values through the sine matrix and their +m z
+// derivative through CcosM -> zspec[0 | 1][z][pos].
+
+template <typename T, bool FFAMILY>
+__global__ void __launch_bounds__(256) k_vinv_family(DescDev d, const double* __restrict__ Apm, const double* __restrict__ A0,
+                                                    cx<T>* __restrict__ zspec) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* fld = reinterpret_cast<cx<T>*>(smem_raw);  // [Nj][modes]
+    const int Nj = d.Nj;
+    const int m0 = blockIdx.x * kVinvModes;
+    const int nm = min(kVinvModes, d.Nkl - m0);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it / Nj, j = it - mi * Nj;
+        const int mode = m0 + mi;
+        const int w = d.modeWV[mode];
+        const unsigned char flags = d.modeFlags[mode];
+        const int idx = j + Nj * w;
+        const double ws = FFAMILY ? d.fWaveScale[idx] : d.gWaveScale[j];
+        const double gs = FFAMILY ? d.Fg[j] : d.Gg[j];
+        const zd v = zadd(zscale(zload(Apm + 2 * idx), ws), zscale(zload(A0 + 2 * idx), gs));
+        double re = v.re, im = v.im;
+        if (flags & 1) im = -im;
+        if (flags & 2) im = 0.0;
+        fld[j * kVinvModes + mi] = mk<T>(T(re), T(im));
+    }
+    __syncthreads();
+    const int Zh = d.zHalf, Nz = d.Nz, P = d.positions;
+    const T* Cv = reinterpret_cast<const T*>(FFAMILY ? d.Ccos : d.Csin);
+    const T* Cz = reinterpret_cast<const T*>(FFAMILY ? d.CsinM : d.CcosM);
+    for (int it = threadIdx.x; it < nm * Zh; it += blockDim.x) {
+        const int n = it / nm, mm = it - n * nm;
+        const int mode = m0 + mm;
+        T E[2][2] = {{T(0), T(0)}, {T(0), T(0)}}, O[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
+        for (int j = 0; j < Nj; ++j) {
+            const cx<T> v = fld[j * kVinvModes + mm];
+            const T a = Cv[n * Nj + j], b = Cz[n * Nj + j];
+            T (&A)[2][2] = (j & 1) ? O : E;
+            A[0][0] += a * v.x; A[0][1] += a * v.y;
+            A[1][0] += b * v.x; A[1][1] += b * v.y;
+        }
+        const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
+        const int n2 = Nz - 1 - n;
+        for (int ch = 0; ch < 2; ++ch) {
+            // cosine family: out[n2] = E - O; sine family: O - E
+            const bool sine = FFAMILY ? ch == 1 : ch == 0;
+            cx<T>* base = zspec + (size_t)ch * d.zTotal * P;
+            const cx<T> lo = mk<T>(E[ch][0] + O[ch][0], E[ch][1] + O[ch][1]);
+            base[(size_t)n * P + pos] = lo;
+            if (cpos >= 0) base[(size_t)n * P + cpos] = mk<T>(lo.x, -lo.y);
+            if (n2 != n) {
+                const cx<T> hi = sine ? mk<T>(O[ch][0] - E[ch][0], O[ch][1] - E[ch][1]) : mk<T>(E[ch][0] - O[ch][0], E[ch][1] - O[ch][1]);
+                base[(size_t)n2 * P + pos] = hi;
+                if (cpos >= 0) base[(size_t)n2 * P + cpos] = mk<T>(hi.x, -hi.y);
             }
         }
     }

@@ -160,6 +160,8 @@ def load_library():
     lib.wv_field_derivatives.argtypes = [P, D, D, P, P, P, ctypes.c_int, P]
     lib.wv_field_derivatives_device.argtypes = [P, D, D, P, P, P, ctypes.c_int, P, P]
     lib.wv_advect_fgrid_scalar.argtypes = [P, P, P, ctypes.c_int, P]
+    lib.wv_family_derivatives.argtypes = [P, ctypes.c_int, P, P, P]
+    lib.wv_family_derivatives_device.argtypes = [P, ctypes.c_int, P, P, P, P]
     lib.wv_advect_fgrid_scalar_device.argtypes = [P, P, P, ctypes.c_int, P, P]
     lib.wv_inverse_uvw_device.argtypes = [P, D, D, P, P, P, P, P]
     for name in ("wv_nonlinear_flux_with_advection_fields", "wv_nonlinear_flux_using_advection_fields"):
@@ -197,7 +199,7 @@ def exported_symbols():
             "wv_nonlinear_flux_with_advection_fields", "wv_nonlinear_flux_using_advection_fields", "wv_inverse_uvw",
             "wv_nonlinear_flux_with_advection_fields_device", "wv_nonlinear_flux_using_advection_fields_device",
             "wv_inverse_uvw_device", "wv_field_derivatives", "wv_field_derivatives_device", "wv_advect_fgrid_scalar",
-            "wv_advect_fgrid_scalar_device", "wv_ensemble_create",
+            "wv_advect_fgrid_scalar_device", "wv_family_derivatives", "wv_family_derivatives_device", "wv_ensemble_create",
             "wv_ensemble_destroy", "wv_ensemble_last_message", "wv_ensemble_get_sizes", "wv_ensemble_get_tuning",
             "wv_ensemble_get_metrics", "wv_ensemble_set_vertical_kernel", "wv_ensemble_rk4_device"]
 
@@ -395,6 +397,27 @@ class WVTransformConstantStratificationKernel:
         self._check(self._lib.wv_field_derivatives(self._h, float(t), float(t0), Ap.ctypes.data, Am.ctypes.data,
                                                    A0.ctypes.data, int(q), out.ctypes.data))
         return out
+
+    def _family(self, ffamily, Apm, A0):
+        if _is_torch(Apm):
+            import torch
+            Apm, A0 = self._dev_coeff(Apm, "Apm"), self._dev_coeff(A0, "A0")
+            out = torch.empty((4,) + self.spatial_shape, dtype=torch.float64, device=Apm.device)
+            self._check(self._lib.wv_family_derivatives_device(self._h, int(ffamily), Apm.data_ptr(), A0.data_ptr(),
+                                                               out.data_ptr(), self._stream()))
+            return out
+        Apm, A0 = self._host_coeff(Apm, "Apm"), self._host_coeff(A0, "A0")
+        out = np.empty((4,) + self.spatial_shape)
+        self._check(self._lib.wv_family_derivatives(self._h, int(ffamily), Apm.ctypes.data, A0.ctypes.data, out.ctypes.data))
+        return out
+
+    def transformToSpatialDomainWithFAllDerivatives(self, Apm, A0):
+        """kernel.cpp:819-840: (value, d/dx, d/dy, d/dz) of the F field family, (4, Nz, Ny, Nx)."""
+        return self._family(True, Apm, A0)
+
+    def transformToSpatialDomainWithGAllDerivatives(self, Apm, A0):
+        """kernel.cpp:842-863: (value, d/dx, d/dy, d/dz) of the G field family, (4, Nz, Ny, Nx)."""
+        return self._family(False, Apm, A0)
 
     def advectFGridScalar(self, scalar, advectionFields, shouldAntialias=True):
         """advectFGridScalar (kernel.cpp:1032-1138): -(u ds/dx + v ds/dy + w ds/dz), (Nz, Ny, Nx)."""
