@@ -51,6 +51,9 @@ def parse():
                     help="only run --profile-count nonlinear fluxes of the 256x256x129 workload (for ncu captures)")
     ap.add_argument("--profile-count", type=int, default=3)
     ap.add_argument("--profile-vjp", action="store_true", help="with --profile-flux: also run as many flux VJPs")
+    ap.add_argument("--workload", choices=["c1", "c2"], default="c1",
+                    help="c2: 512x512x257 mixed vs FP64 over --c2-steps RK4 steps (field error and energy drift)")
+    ap.add_argument("--c2-steps", type=int, default=200)
     return ap.parse_args()
 
 
@@ -514,6 +517,60 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def _energy(k, state, t, t0, np):
+    """0.5 <u^2 + v^2 + w^2 + N0^2 eta^2> over the grid (trapezoid weights in z):
+    a physical-space energy diagnostic for drift."""
+    f = k.transformWaveVortexToUVWEta(t, t0, *state)
+    wz = np.ones(f.shape[1])
+    wz[0] = wz[-1] = 0.5
+    N0 = k.configuration.N0
+    e = f[0] ** 2 + f[1] ** 2 + f[2] ** 2 + (N0 * f[3]) ** 2
+    return 0.5 * float(np.sum(e * wz[:, None, None]) / (np.sum(wz) * f.shape[2] * f.shape[3]))
+
+
+def run_workload_c2(args):
+    """512x512x257 over the 800 km x 800 km x 4 km domain of the 256 workload, seeded
+    spectrum state at 0.1 m/s (seed 2), dt = 0.5 CFL: RK4 steps/s of the FP64 and the
+    mixed form, per-field relative L2 error of the mixed form against FP64 after
+    the run, and the energy drift of both."""
+    import numpy as np
+    import torch
+    import wvgpu
+    from wvgpu import build
+    build.build()
+    cfg = wvgpu.Configuration(Nx=512, Ny=512, Nz=257, Nj=170, Lx=800e3, Ly=800e3, Lz=4000.0, N0=5.2e-3, latitude=33.0)
+    k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    km = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="mixed")
+    state = wvgpu.synthetic_state(k, seed=2, urms=URMS)
+    dt = wvgpu.cfl_time_step(k, *state)
+    stream = torch.cuda.current_stream()
+    out = {"workload": "512x512x257, 800 km x 800 km x 4 km, N0 5.2e-3, lat 33, 0.1 m/s rms seeded spectrum (seed 2), "
+                       "dt = 0.5 x CFL", "steps": args.c2_steps, "dt_s": dt, "unit": UNIT}
+    E0 = _energy(k, state, 0.0, 0.0, np)
+    for name, kk in (("fp64", k), ("mixed", km)):
+        dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+        kk.rk4(*[x.clone() for x in dev], 0.0, 0.0, dt, 2)  # warm
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, _, _, tT = kk.rk4(*dev, 0.0, 0.0, dt, args.c2_steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        final = [x.cpu().numpy() for x in dev]
+        out[name] = {"value": args.c2_steps / (ms * 1e-3), "ms_per_step": ms / args.c2_steps,
+                     "energy_drift": (_energy(k, final, tT, 0.0, np) - E0) / E0}
+        out[name + "_state"] = final
+    f64 = k.transformWaveVortexToUVWEta(tT, 0.0, *out.pop("fp64_state"))
+    f32 = k.transformWaveVortexToUVWEta(tT, 0.0, *out.pop("mixed_state"))
+    out["mixed"]["rel_field_err_vs_fp64"] = [float(np.linalg.norm(f32[i] - f64[i]) / np.linalg.norm(f64[i])) for i in range(4)]
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["mixed"]["vertical_kernel"] = "cuda cores (the tensor-core transform needs Nz <= 255)"
+    print(json.dumps(out), flush=True)
+    k.close()
+    km.close()
+
+
 def run_profile_case(args):
     """A few nonlinear fluxes of the benchmark state, nothing else: the launch
     sequence is vinv, yinv, x products, yfwd, vfwd per flux."""
@@ -542,6 +599,8 @@ def main():
     args = parse()
     if args.profile_flux:
         run_profile_case(args)
+    elif args.workload == "c2":
+        run_workload_c2(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -248,6 +248,22 @@ def main():
         print(f"{name}: Nkl={r.Nkl} M={r.M}")
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
+    # configs[0] end to end: the single internal wave (kMode=1, lMode=0, j=1, u = 0.05 m/s)
+    # under {nonlinear advection, adaptive damping}, 60 RK4 steps of dt = 10 s to t = 600 s
+    case = CASES["c0_16x16x9"]
+    r = Ref(lib, case)
+    shape = (r.Nkl, case["Nj"])
+    desc = r.descriptor()
+    Sp = np.zeros(shape, np.complex128)
+    idx = int(np.nonzero((desc["kMode"] == 1) & (desc["lMode"] == 0))[0][0])
+    Sp[idx, 1] = 0.05 / (2.0 * abs(desc["fWaveScale"].reshape(shape)[idx, 1]))
+    zero = np.zeros(shape, np.complex128)
+    Kp, Km, K0, tK = r.rk4(Sp, zero, zero, 0.0, 0.0, 10.0, 60)
+    fields = r.inverse(Kp, Km, K0, tK, 0.0)
+    np.savez_compressed(os.path.join(HERE, "c0_t600.npz"), Ap=Sp, Am=zero, A0=zero, dt=10.0, steps=60,
+                        Kp=Kp, Km=Km, K0=K0, t=tK, fields=fields)
+    lib.wvref_destroy(r.h)
+    print(f"c0_t600: t = {tK}")
 
 
 if __name__ == "__main__":

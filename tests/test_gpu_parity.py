@@ -218,3 +218,21 @@ def test_stage_instrumentation(wv):
     for a, b in zip(F1, F2):
         assert np.array_equal(a, b)
     k.close()
+
+
+def test_configs0_single_wave_to_t600_matches_reference(wv):
+    """configs[0] end to end: 16x16x9, single internal wave (kMode=1, lMode=0, j=1,
+    u = 0.05 m/s) under {nonlinear advection, adaptive damping}, 60 RK4 steps of
+    10 s to t = 600 s, field by field against the reference FP64 path (its own
+    run, tests/golden/c0_t600.npz)."""
+    import os
+    c = config_from_case(golden_cases()["c0_16x16x9"])
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "c0_t600.npz"))
+    k = wv.WVTransformConstantStratificationKernel(to_wv(wv, c))
+    k.set_forcing(nonlinear=True, adaptive_damping=True)
+    Ap, Am, A0, t = k.rk4(g["Ap"], g["Am"], g["A0"], 0.0, 0.0, float(g["dt"]), int(g["steps"]))
+    assert t == float(g["t"])
+    for a, b in zip((Ap, Am, A0), (g["Kp"], g["Km"], g["K0"])):
+        assert rel_err(a, b) <= FP64_REL_TOL
+    assert rel_err(k.transformWaveVortexToUVWEta(t, 0.0, Ap, Am, A0), g["fields"]) <= FP64_REL_TOL
+    k.close()
