@@ -51,6 +51,8 @@ def parse():
                     help="only run --profile-count nonlinear fluxes of the 256x256x129 workload (for ncu captures)")
     ap.add_argument("--profile-count", type=int, default=3)
     ap.add_argument("--profile-vjp", action="store_true", help="with --profile-flux: also run as many flux VJPs")
+    ap.add_argument("--profile-size", type=int, default=256,
+                    help="with --profile-flux: grid N x N x (N/2+1) over 3.125 km x N (256: the benchmark workload)")
     ap.add_argument("--workload", choices=["c1", "c2"], default="c1",
                     help="c2: 512x512x257 mixed vs FP64 over --c2-steps RK4 steps (field error and energy drift)")
     ap.add_argument("--c2-steps", type=int, default=200)
@@ -579,7 +581,10 @@ def run_profile_case(args):
     import wvgpu
     from wvgpu import build
     build.build()
-    k = wvgpu.WVTransformConstantStratificationKernel(configuration(wvgpu), precision=args.profile_flux)
+    N = args.profile_size
+    cfg = configuration(wvgpu) if N == 256 else wvgpu.Configuration(
+        Nx=N, Ny=N, Nz=N // 2 + 1, Nj=N // 3, Lx=3125.0 * N, Ly=3125.0 * N, Lz=4000.0, N0=5.2e-3, latitude=33.0)
+    k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision=args.profile_flux)
     state = wvgpu.synthetic_state(k, seed=SEED, urms=URMS)
     dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
     out = tuple(torch.empty_like(dev[0]) for _ in range(3))

@@ -144,8 +144,8 @@ int wv_set_stage_instrumentation(wv_handle* handle, int enabled);
  * contraction as split-BF16 GEMMs on the tensor cores (tcgen05.mma, three BF16
  * pieces per operand, six cross products, FP32 accumulators in tensor memory);
  * available on mixed-precision handles with Nz <= 255 (else
- * WV_UNSUPPORTED_OPERATION) and the default there; WV_VERTICAL_CUDA_CORES
- * otherwise and on FP64 handles. */
+ * WV_UNSUPPORTED_OPERATION) and the default there when its blocks of 32 retained
+ * columns (one per SM) fill the GPU; WV_VERTICAL_CUDA_CORES otherwise. */
 #define WV_VERTICAL_CUDA_CORES 0
 #define WV_VERTICAL_TENSOR_CORES 1
 int wv_set_vertical_kernel(wv_handle* handle, int kind);

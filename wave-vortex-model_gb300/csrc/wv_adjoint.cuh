@@ -324,13 +324,18 @@ __global__ void __launch_bounds__(256) k_xr2c_adj(DescDev d, const double* __res
 // y-spectrum layout (U V W N, y-derivative per target, z-derivative per
 // target); otherwise U V W N only (inverse transform).
 
+// Retained columns per CTA of the transposed vertical inverse: 4 keeps its folded
+// columns (8 channels x Zh x modes x 16 bytes in FP32) small enough for six CTAs
+// per SM, which its latency-bound gathers need.
+constexpr int kVinvAdjModes = 4;
+
 template <typename T, bool FLUX>
 __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __restrict__ fadj, int nchIn, double elapsed,
                                                  double* __restrict__ Apb, double* __restrict__ Amb, double* __restrict__ A0b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Nj = d.Nj, Nz = d.Nz, Zh = d.zHalf, P = d.positions, nt = d.nt;
-    const int m0 = blockIdx.x * kVinvModes;
-    const int nm = min(kVinvModes, d.Nkl - m0);
+    const int m0 = blockIdx.x * kVinvAdjModes;
+    const int nm = min(kVinvAdjModes, d.Nkl - m0);
     const int nOutCh = FLUX ? 4 + nt : 4;  // value channels U V W N, then z-derivative per target
     cx2t<T>* pq = reinterpret_cast<cx2t<T>*>(smem_raw);  // [nOutCh][Zh][modes]
     // gather (stored rows + conjugated completion rows, -i l on y-derivative channels), fold z <-> Nz-1-z
@@ -369,7 +374,7 @@ __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __rest
         cx2t<T> v;
         if (n2 == n) { v.p = a; v.q = a; }
         else { const cx<T> b = colval(n2); v.p = cadd<T>(a, b); v.q = csub<T>(a, b); }
-        pq[(oc * Zh + n) * kVinvModes + mm] = v;
+        pq[(oc * Zh + n) * kVinvAdjModes + mm] = v;
     }
     __syncthreads();
     const T* Cc = reinterpret_cast<const T*>(d.CcosT);   // [Nj][Zh]
@@ -385,10 +390,10 @@ __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __rest
         auto contract = [&](int oc, const T* C, bool cosine) -> cx<T> {
             const bool useP = cosine ? evenJ : !evenJ;
             T re = T(0), im = T(0);
-            const cx2t<T>* col = pq + (size_t)oc * Zh * kVinvModes + mm;
+            const cx2t<T>* col = pq + (size_t)oc * Zh * kVinvAdjModes + mm;
             const T* Cj = C + (size_t)j * Zh;
             for (int n = 0; n < Zh; ++n) {
-                const cx2t<T> v = col[n * kVinvModes];
+                const cx2t<T> v = col[n * kVinvAdjModes];
                 const T f = Cj[n];
                 const cx<T> sv = useP ? v.p : v.q;
                 re += f * sv.x;

@@ -742,7 +742,7 @@ template <typename T>
 size_t smem_xr2c_adj(const Plan& p) { return (x_len(p) + p.Nx + 8 * x_len(p)) * sizeof(dev::cx<T>) + 4 * p.Nx * sizeof(T); }
 template <typename T>
 size_t smem_vinv_adj(const Plan& p, bool flux) {
-    return (flux ? 4 + p.targets.count : 4) * p.zHalf * dev::kVinvModes * sizeof(dev::cx2t<T>);
+    return (flux ? 4 + p.targets.count : 4) * p.zHalf * dev::kVinvAdjModes * sizeof(dev::cx2t<T>);
 }
 
 template <typename T>
@@ -848,7 +848,7 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
         dev::k_xadj<T><<<dim3(p.Ny, p.Nz), 256, smem_xadj<T>(p), s>>>(d, y, ya, yo, static_cast<const T*>(physIn));
     }
     launch_yfwd<T>(h, yo, nIn, fa, s);
-    dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
+    dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvAdjModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
     h->metrics.kernel_launches += 5;
     return cudaGetLastError();
 }
@@ -863,7 +863,7 @@ cudaError_t launch_inverse_vjp(wv_handle* h, double t, double t0, const double* 
     auto* fa = static_cast<dev::cx<T>*>(h->fadj);
     dev::k_xr2c_adj<T><<<dim3(p.Ny, p.Nz), 256, smem_xr2c_adj<T>(p), s>>>(d, fb, 4, ps);
     launch_yfwd<T>(h, ps, 4, fa, s);
-    dev::k_vinv_adj<T, false><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv_adj<T>(p, false), s>>>(d, fa, 4, t - t0, Apb, Amb, A0b);
+    dev::k_vinv_adj<T, false><<<dim3(cdiv(p.Nkl, dev::kVinvAdjModes), d.members), 256, smem_vinv_adj<T>(p, false), s>>>(d, fa, 4, t - t0, Apb, Amb, A0b);
     h->metrics.kernel_launches += 3;
     return cudaGetLastError();
 }
@@ -1247,7 +1247,11 @@ static int create_handle(const wv_config* config, int precision, int members, wv
             h->tcSmem = smem;
             if (e == cudaSuccess) e = raise_smem_limit(dev::k_vinv_tc, static_cast<int>(smem));
             h->tcAvailable = e == cudaSuccess;
-            h->verticalTC = h->tcAvailable;  // default where built (faster at 256x256x129, same accuracy)
+            // default where its one-CTA-per-SM blocks of 32 columns fill the GPU (faster
+            // from 256x256x129 up, same accuracy); smaller grids keep the CUDA-core kernel
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+            h->verticalTC = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
         }
     }
     const auto ss = scratch_sizes(p);
