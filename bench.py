@@ -51,6 +51,8 @@ def parse():
                     help="only run --profile-count nonlinear fluxes of the 256x256x129 workload (for ncu captures)")
     ap.add_argument("--profile-count", type=int, default=3)
     ap.add_argument("--profile-vjp", action="store_true", help="with --profile-flux: also run as many flux VJPs")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="with --profile-flux: one checkpointed RK4 adjoint of 20 steps, checkpoints every 10, instead")
     ap.add_argument("--profile-size", type=int, default=256,
                     help="with --profile-flux: grid N x N x (N/2+1) over 3.125 km x N (256: the benchmark workload)")
     ap.add_argument("--workload", choices=["c1", "c2"], default="c1",
@@ -589,6 +591,13 @@ def run_profile_case(args):
     dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
     out = tuple(torch.empty_like(dev[0]) for _ in range(3))
     torch.cuda.synchronize()
+    if args.profile_adjoint:
+        dt = wvgpu.cfl_time_step(k, *state)
+        k.rk4_adjoint(*dev, 0.0, 0.0, dt, 20, 10, *dev)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_adjoint": args.profile_flux, "launches": k.metrics()["kernel_launches"]}))
+        k.close()
+        return
     for _ in range(args.profile_count):
         k.nonlinearFlux(0.0, 0.0, *dev, out=out)
     if args.profile_vjp:

@@ -284,6 +284,61 @@ __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict
     }
 }
 
+// ---------------------------------------------------------------------------
+// y forward of the x-pass adjoint's output with the y-derivative channels folded
+// back onto their source channel: out channel c = FFT_y(A) + (-i l) FFT_y(B)
+// (B = -1: FFT_y(A) alone), gathered to the active rows -> fspec[c][z][pos].
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_yfwd_pair(DescDev d, YFwdPairMap map, const cx<T>* __restrict__ pspec, int nIn,
+                                                  cx<T>* __restrict__ fspec) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Ny = d.Ny, P = d.positions, KX = d.kxColumns;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* bufA = tw + Ny;
+    cx<T>* bufB = bufA + kYG * Ny;
+    cx<T>* keep = bufB + kYG * Ny;  // FFT of channel A while B is transformed
+    const int kx0 = blockIdx.x * kYG;
+    const int z = blockIdx.y;
+    const int c = blockIdx.z;
+    const int g = min(kYG, KX - kx0);
+    const int a = map.srcA[c], b = map.srcB[c];
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
+    for (int i = threadIdx.x; i < Ny; i += blockDim.x) tw[i] = twg[i];
+    auto load = [&](int ch) {
+        const cx<T>* in = pspec + (((size_t)z * nIn + ch) * Ny) * KX;
+        for (int i = threadIdx.x; i < g * Ny; i += blockDim.x) {
+            const int y = i / g, gi = i - y * g;
+            bufA[gi * Ny + y] = in[(size_t)y * KX + kx0 + gi];
+        }
+        __syncthreads();
+    };
+    load(a);
+    cx<T>* res = fft_lines<T, false>(bufA, bufB, d.fy, g, Ny, tw);
+    for (int i = threadIdx.x; i < g * Ny; i += blockDim.x) keep[i] = res[i];
+    __syncthreads();
+    cx<T>* resB = nullptr;
+    if (b >= 0) {
+        load(b);
+        resB = fft_lines<T, false>(bufA, bufB, d.fy, g, Ny, tw);
+    }
+    cx<T>* out = fspec + ((size_t)c * d.zTotal + z) * P;
+    const T* rl = row_l<T>(d);
+    const int pBeg = d.colStart[kx0], pEnd = d.colStart[kx0 + g];
+    for (int p = pBeg + threadIdx.x; p < pEnd; p += blockDim.x) {
+        int gi = 0;
+        while (gi + 1 < g && p >= d.colStart[kx0 + gi + 1]) ++gi;
+        const int ky = d.posKy[p];
+        cx<T> v = keep[gi * Ny + ky];
+        if (b >= 0) {
+            const cx<T> w = resB[gi * Ny + ky];
+            const T l = rl[ky];
+            v = mk<T>(v.x + l * w.y, v.y - l * w.x);
+        }
+        out[p] = v;
+    }
+}
+
 // x r2c of field rows with interior kx doubled (adjoint of the inverse transform's c2r)
 template <typename T>
 __global__ void __launch_bounds__(256) k_xr2c_adj(DescDev d, const double* __restrict__ fields, int nch, cx<T>* __restrict__ pspec) {
@@ -346,22 +401,10 @@ __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __rest
         const int mode = m0 + mm;
         const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
         const unsigned char flags = d.modeFlags[mode];
-        int ch = oc, ych = -1;
-        if (oc < 4) {
-            if (FLUX)
-                for (int t = 0; t < nt; ++t) if (d.tq[t] == oc) ych = 4 + t;
-        } else {
-            ch = 4 + nt + (oc - 4);
-        }
-        auto rowval = [&](int p, int zz) -> cx<T> {
-            cx<T> v = fadj[((size_t)ch * Nz + zz) * P + p];
-            if (ych >= 0) {
-                const cx<T> g = fadj[((size_t)ych * Nz + zz) * P + p];
-                const T l = row_l<T>(d)[d.posKy[p]];
-                v = mk<T>(v.x + l * g.y, v.y - l * g.x);  // + (-i l) g
-            }
-            return v;
-        };
+        // FLUX input is folded by k_yfwd_pair: value channels 0..3 already carry their
+        // (-i l) y-derivative parts, z-derivative channels follow at 4..4+nt
+        const int ch = oc;
+        auto rowval = [&](int p, int zz) -> cx<T> { return fadj[((size_t)ch * Nz + zz) * P + p]; };
         auto colval = [&](int zz) -> cx<T> {
             cx<T> v = rowval(pos, zz);
             if (cpos >= 0) { const cx<T> c = rowval(cpos, zz); v = mk<T>(v.x + c.x, v.y - c.y); }

@@ -70,6 +70,9 @@ struct wv_handle {
     std::vector<double*> checkpoints;  // multi-step adjoint: saved states
     std::vector<double*> segment;      // multi-step adjoint: states of one segment
     std::vector<void*> ystore;         // multi-step adjoint: x-pass real rows of each stage flux of one segment
+    cudaStream_t adjStream = nullptr;  // multi-step adjoint: recomputation of the next segment
+    double* ybAlt = nullptr;           // multi-step adjoint: second cotangent buffer
+    cudaEvent_t slotReady[2] = {}, slotFree[2] = {}, fwdDone = nullptr;
     bool instrument = false;
     bool tcAvailable = false;  // tensor-core vertical transform built for this handle
     bool verticalTC = false;   // ... and selected (default: on where built)
@@ -739,6 +742,10 @@ size_t smem_xadj_w(const Plan& p) {
     return (3 * L + dev::kWG * (L + 4 * p.kxColumns)) * sizeof(dev::cx<T>);
 }
 template <typename T>
+size_t smem_ypair(const Plan& p) { return (p.Ny + 3 * dev::kYG * p.Ny) * sizeof(dev::cx<T>); }
+template <typename T>
+size_t smem_ypair_w(const Plan& p) { return (p.Ny + 2 * dev::kWG * p.Ny) * sizeof(dev::cx<T>); }
+template <typename T>
 size_t smem_xr2c_adj(const Plan& p) { return (x_len(p) + p.Nx + 8 * x_len(p)) * sizeof(dev::cx<T>) + 4 * p.Nx * sizeof(T); }
 template <typename T>
 size_t smem_vinv_adj(const Plan& p, bool flux) {
@@ -756,6 +763,12 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
     if (e != cudaSuccess) return e;
     WV_SET((dev::k_vfwd_adj<T>), smem_vfwd_adj<T>(p));
     WV_SET((dev::k_xadj<T>), smem_xadj<T>(p));
+    WV_SET((dev::k_yfwd_pair<T>), smem_ypair<T>(p));
+    {
+        const int ry = warp_ry<T>(p);
+        WV_RSWITCH_Y(ry, e = raise_smem_limit(dev::k_yfwd_pair_w<T, RR>, (int)smem_ypair_w<T>(p)));
+        if (e != cudaSuccess) return e;
+    }
     {
         const int rx = warp_rx<T>(p);
         WV_RSWITCH_X(T, rx, e = raise_smem_limit(dev::k_xadj_w<T, RR>, (int)smem_xadj_w<T>(p)));
@@ -847,7 +860,25 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
     } else {
         dev::k_xadj<T><<<dim3(p.Ny, p.Nz), 256, smem_xadj<T>(p), s>>>(d, y, ya, yo, static_cast<const T*>(physIn));
     }
-    launch_yfwd<T>(h, yo, nIn, fa, s);
+    // y forward with each target's y-derivative channel folded onto its value channel
+    dev::YFwdPairMap pm{};
+    pm.nOut = 4 + nt;
+    for (int c = 0; c < 4; ++c) { pm.srcA[c] = c; pm.srcB[c] = -1; }
+    for (int t2 = 0; t2 < nt; ++t2) {
+        pm.srcB[p.targets.q[t2]] = 4 + t2;
+        pm.srcA[4 + t2] = 4 + nt + t2;
+        pm.srcB[4 + t2] = -1;
+    }
+    {
+        const int ry = warp_ry<T>(p);
+        if (ry) {
+            const dim3 grid(cdiv(p.kxColumns, dev::kWG), d.zTotal, pm.nOut);
+            WV_RSWITCH_Y(ry, (dev::k_yfwd_pair_w<T, RR><<<grid, 256, smem_ypair_w<T>(p), s>>>(d, pm, yo, nIn, fa)));
+        } else {
+            dev::k_yfwd_pair<T><<<dim3(cdiv(p.kxColumns, dev::kYG), d.zTotal, pm.nOut), 256, smem_ypair<T>(p), s>>>(d, pm, yo,
+                                                                                                              nIn, fa);
+        }
+    }
     dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvAdjModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
     h->metrics.kernel_launches += 5;
     return cudaGetLastError();
@@ -950,22 +981,24 @@ cudaError_t rk4_stages(wv_handle* h, const double* y, double t, double t0, doubl
 // Backward sweep of one RK4 step given its stage states: yb is the cotangent of
 // the state after the step; h->ybacc receives the cotangent before it.
 cudaError_t rk4_backward(wv_handle* h, const double* y, const double* st1, const double* st2, const double* st3, double t,
-                         double t0, double dt, const double* yb, cudaStream_t s, void* const* ys = nullptr) {
+                         double t0, double dt, const double* yb, cudaStream_t s, void* const* ys = nullptr,
+                         double* ybOut = nullptr) {
+    if (!ybOut) ybOut = h->ybacc;
     const size_t n = 6 * h->plan.M;
     const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
     cudaError_t e;
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.0, nullptr, n);
     e = flux_vjp_any(h, t + dt, t0, st3, h->kb, h->sb, s, ys ? ys[3] : nullptr); if (e != cudaSuccess) return e;
-    dev::k_lincomb<<<grid, 256, 0, s>>>(h->ybacc, 1.0, yb, 1.0, h->sb, n);
+    dev::k_lincomb<<<grid, 256, 0, s>>>(ybOut, 1.0, yb, 1.0, h->sb, n);
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, dt, h->sb, n);
     e = flux_vjp_any(h, t + 0.5 * dt, t0, st2, h->kb, h->sb, s, ys ? ys[2] : nullptr); if (e != cudaSuccess) return e;
-    dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
+    dev::k_accumulate<<<grid, 256, 0, s>>>(ybOut, h->sb, n);
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, 0.5 * dt, h->sb, n);
     e = flux_vjp_any(h, t + 0.5 * dt, t0, st1, h->kb, h->sb, s, ys ? ys[1] : nullptr); if (e != cudaSuccess) return e;
-    dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
+    dev::k_accumulate<<<grid, 256, 0, s>>>(ybOut, h->sb, n);
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.5 * dt, h->sb, n);
     e = flux_vjp_any(h, t, t0, y, h->kb, h->sb, s, ys ? ys[0] : nullptr); if (e != cudaSuccess) return e;
-    dev::k_accumulate<<<grid, 256, 0, s>>>(h->ybacc, h->sb, n);
+    dev::k_accumulate<<<grid, 256, 0, s>>>(ybOut, h->sb, n);
     h->metrics.kernel_launches += 8;
     return cudaGetLastError();
 }
@@ -1123,7 +1156,10 @@ void wv_destroy(wv_handle* h) {
     cudaGetDevice(&prev);
     cudaSetDevice(h->device);
     if (h->stream) { cudaStreamSynchronize(h->stream); cudaStreamDestroy(h->stream); }
+    if (h->adjStream) { cudaStreamSynchronize(h->adjStream); cudaStreamDestroy(h->adjStream); }
     for (auto& ev : h->ev) if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : {h->slotReady[0], h->slotReady[1], h->slotFree[0], h->slotFree[1], h->fwdDone})
+        if (ev) cudaEventDestroy(ev);
     for (void* p : h->allocations) cudaFree(p);
     cudaSetDevice(prev);
     delete h;
@@ -1917,38 +1953,56 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
         e = alloc(h, stateBytes, &tmp);
         h->checkpoints.push_back(static_cast<double*>(tmp));
     }
-    while (static_cast<int>(h->segment.size()) < 4 * K && e == cudaSuccess) {
+    // real rows of the x pass of every stage flux of a segment, in one or (when
+    // half the free memory holds them) two segment slots; two slots let the
+    // recomputation of the next segment run on a side stream during the
+    // backward sweep of the current one
+    const size_t yBytes = (3 + 3 * h->plan.targets.count) * h->plan.Nx * h->plan.Ny * h->plan.Nz * elem_size(h->precision);
+    int slots = 0;
+    if (e == cudaSuccess) {
+        size_t freeB = 0, totalB = 0;
+        e = cudaMemGetInfo(&freeB, &totalB);
+        for (int want = 2; want >= 1 && e == cudaSuccess && slots == 0; --want) {
+            const size_t haveY = h->ystore.size(), haveS = h->segment.size();
+            const size_t needY = static_cast<size_t>(std::max<int>(0, 4 * K * want - static_cast<int>(haveY))) * yBytes;
+            const size_t needS = static_cast<size_t>(std::max<int>(0, 4 * K * want - static_cast<int>(haveS))) * stateBytes;
+            if (needY + needS <= freeB / 2) slots = want;
+        }
+    }
+    const int nSlots = std::max(slots, 1);
+    while (static_cast<int>(h->segment.size()) < 4 * K * nSlots && e == cudaSuccess) {
         e = alloc(h, stateBytes, &tmp);
         h->segment.push_back(static_cast<double*>(tmp));
     }
-    // real rows of the x pass of every stage flux of a segment, when half the
-    // free memory holds them
-    const size_t yBytes = (3 + 3 * h->plan.targets.count) * h->plan.Nx * h->plan.Ny * h->plan.Nz * elem_size(h->precision);
-    if (e == cudaSuccess && static_cast<int>(h->ystore.size()) < 4 * K) {
-        size_t freeB = 0, totalB = 0;
-        e = cudaMemGetInfo(&freeB, &totalB);
-        const size_t need = (4 * K - h->ystore.size()) * yBytes;
-        if (e == cudaSuccess && need <= freeB / 2) {
-            while (static_cast<int>(h->ystore.size()) < 4 * K && e == cudaSuccess) {
-                e = alloc(h, yBytes, &tmp);
-                h->ystore.push_back(tmp);
-            }
+    while (slots > 0 && static_cast<int>(h->ystore.size()) < 4 * K * slots && e == cudaSuccess) {
+        e = alloc(h, yBytes, &tmp);
+        h->ystore.push_back(tmp);
+    }
+    if (e == cudaSuccess && !h->ybAlt) { e = alloc(h, stateBytes, &tmp); h->ybAlt = static_cast<double*>(tmp); }
+    const bool pipelined = slots == 2;
+    if (e == cudaSuccess && pipelined && !h->adjStream) {
+        e = cudaStreamCreateWithFlags(&h->adjStream, cudaStreamNonBlocking);
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+            e = cudaEventCreateWithFlags(&h->slotReady[i], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->slotFree[i], cudaEventDisableTiming);
         }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->fwdDone, cudaEventDisableTiming);
     }
     if (e != cudaSuccess) return cuda_fail(h, e, "RK4 adjoint checkpoints");
     h->metrics.device_bytes = h->deviceBytes;
-    const bool keepY = static_cast<int>(h->ystore.size()) >= 4 * K;
-    // Stage states (and y spectra) of the steps first..last-1 from the state in
-    // segment[0], the state of each next step in the following slot.
+    const bool keepY = slots > 0;
     std::vector<double> times(n + 1);
     times[0] = t;
     for (int i = 0; i < n; ++i) times[i + 1] = times[i] + dt;
-    auto record = [&](int first, int last) {
+    auto slotOf = [&](int seg) { return pipelined ? (seg & 1) : 0; };
+    // Stage states (and real rows) of the steps first..last-1 from the state in the
+    // slot's first entry, the state of each next step in the following entry.
+    auto record = [&](int first, int last, int slot, cudaStream_t st) {
         cudaError_t r = cudaSuccess;
         for (int i = first; i < last && r == cudaSuccess; ++i) {
-            double** q = h->segment.data() + 4 * (i - first);
-            void* const* ys = keepY ? h->ystore.data() + 4 * (i - first) : nullptr;
-            r = rk4_stages(h, q[0], times[i], t0, dt, q[1], q[2], q[3], i + 1 < last ? q[4] : nullptr, s, ys);
+            double** q = h->segment.data() + 4 * K * slot + 4 * (i - first);
+            void* const* ys = keepY ? h->ystore.data() + 4 * K * slot + 4 * (i - first) : nullptr;
+            r = rk4_stages(h, q[0], times[i], t0, dt, q[1], q[2], q[3], i + 1 < last ? q[4] : nullptr, st, ys);
         }
         return r;
     };
@@ -1961,29 +2015,52 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
             e = cudaMemcpyAsync(h->checkpoints[seg], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
             for (int i = first; i < last && e == cudaSuccess; ++i) e = rk4_step(h, times[i], t0, dt, s);
         } else {
-            e = cudaMemcpyAsync(h->segment[0], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess) e = record(first, last);
+            const int sl = slotOf(seg);
+            e = cudaMemcpyAsync(h->segment[4 * K * sl], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = record(first, last, sl, s);
         }
     }
     if (e == cudaSuccess) e = gather3(h, h->ybin, Apb, Amb, A0b, s);
-    // backward, one segment at a time: recompute the segment from its checkpoint
-    // keeping every step's state and stage states, then step the cotangent back
+    if (e == cudaSuccess && pipelined) {
+        e = cudaEventRecord(h->fwdDone, s);
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventRecord(h->slotFree[i], s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->adjStream, h->fwdDone, 0);
+    }
+    // backward, one segment at a time; segment seg-1 is recomputed from its
+    // checkpoint (on the side stream when pipelined) while segment seg steps the
+    // cotangent back.  The cotangent alternates between two buffers.
+    double* ybCur = h->ybin;
+    double* ybNext = h->ybAlt;
     for (int seg = ncp - 1; seg >= 0 && e == cudaSuccess; --seg) {
         const int first = seg * K, last = std::min(n, first + K);
-        if (seg + 1 < ncp) {
+        const int sl = slotOf(seg);
+        if (pipelined) {
+            if (seg >= 1) {
+                const int ps = slotOf(seg - 1), pf = (seg - 1) * K, pl = std::min(n, pf + K);
+                e = cudaStreamWaitEvent(h->adjStream, h->slotFree[ps], 0);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(h->segment[4 * K * ps], h->checkpoints[seg - 1], stateBytes, cudaMemcpyDeviceToDevice,
+                                        h->adjStream);
+                if (e == cudaSuccess) e = record(pf, pl, ps, h->adjStream);
+                if (e == cudaSuccess) e = cudaEventRecord(h->slotReady[ps], h->adjStream);
+            }
+            if (e == cudaSuccess && seg + 1 < ncp) e = cudaStreamWaitEvent(s, h->slotReady[sl], 0);
+        } else if (seg + 1 < ncp) {
             e = cudaMemcpyAsync(h->segment[0], h->checkpoints[seg], stateBytes, cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess) e = record(first, last);
+            if (e == cudaSuccess) e = record(first, last, 0, s);
         }
         for (int i = last - 1; i >= first && e == cudaSuccess; --i) {
-            double** q = h->segment.data() + 4 * (i - first);
-            void* const* ys = keepY ? h->ystore.data() + 4 * (i - first) : nullptr;
-            e = rk4_backward(h, q[0], q[1], q[2], q[3], times[i], t0, dt, h->ybin, s, ys);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(h->ybin, h->ybacc, stateBytes, cudaMemcpyDeviceToDevice, s);
+            double** q = h->segment.data() + 4 * K * sl + 4 * (i - first);
+            void* const* ys = keepY ? h->ystore.data() + 4 * K * sl + 4 * (i - first) : nullptr;
+            e = rk4_backward(h, q[0], q[1], q[2], q[3], times[i], t0, dt, ybCur, s, ys, ybNext);
+            std::swap(ybCur, ybNext);
         }
+        if (e == cudaSuccess && pipelined) e = cudaEventRecord(h->slotFree[sl], s);
     }
-    if (e == cudaSuccess) e = scatter3(h, h->ybin, Apb, Amb, A0b, s);
+    if (e == cudaSuccess) e = scatter3(h, ybCur, Apb, Amb, A0b, s);
     return finish(h, e, "RK4 adjoint");
 }
+
 
 // Flux on the static scratch array: no cudaMalloc, cudaFree or allocating
 // library call.  See include/wvgpu.h for who needs it and its limits.

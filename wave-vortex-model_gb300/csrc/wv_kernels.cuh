@@ -499,6 +499,13 @@ struct YInvMap {
     int mulL[16];
 };
 
+// Output channel c of k_yfwd_pair(_w) = FFT_y(srcA[c]) + (-i l) FFT_y(srcB[c]) (srcB < 0: none).
+struct YFwdPairMap {
+    int nOut;
+    int srcA[8];
+    int srcB[8];
+};
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_yinv(DescDev d, YInvMap map, const cx<T>* __restrict__ zspec, int nInCh,
                                              cx<T>* __restrict__ yspec) {

@@ -457,6 +457,62 @@ __global__ void __launch_bounds__(256, 2) k_xadj_w(DescDev d, const cx<T>* __res
     }
 }
 
+// y forward of the x-pass adjoint's output, y-derivative channels folded onto
+// their source channel (see k_yfwd_pair); one warp per kx column.
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_yfwd_pair_w(DescDev d, YFwdPairMap map, const cx<T>* __restrict__ pspec, int nIn,
+                                                    cx<T>* __restrict__ fspec) {
+    constexpr int N = 32 * R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tileA = tw + N;
+    cx<T>* tileB = tileA + N * kWG;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int kx0 = blockIdx.x * kWG, z = blockIdx.y, c = blockIdx.z;
+    const int KX = d.kxColumns, P = d.positions;
+    const int a = map.srcA[c], b = map.srcB[c];
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twy);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
+    const int g = min(kWG, KX - kx0);
+    auto fill = [&](int ch, cx<T>* tile) {
+        const cx<T>* in = pspec + (((size_t)z * nIn + ch) * N) * KX + kx0;
+        for (int i = threadIdx.x; i < N * kWG; i += blockDim.x) {
+            const int y = i / kWG, gi = i - y * kWG;
+            tile[tile_at<R>(y, gi)] = gi < g ? in[(size_t)y * KX + gi] : mk<T>(T(0), T(0));
+        }
+    };
+    fill(a, tileA);
+    if (b >= 0) fill(b, tileB);
+    __syncthreads();
+    const int kx = kx0 + warp;
+    if (kx >= KX) return;
+    auto transform = [&](cx<T>* tile) {
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = tile[tile_at<R>(lane + 32 * r, warp)];
+        fft_P<T, R, false>(v, tw, lane);
+        __syncwarp();
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) tile[tile_at<R>(p_index<R>(k1, lane), warp)] = v[k1];
+        __syncwarp();
+    };
+    transform(tileA);
+    if (b >= 0) transform(tileB);
+    cx<T>* out = fspec + ((size_t)c * d.zTotal + z) * P;
+    const T* rl = row_l<T>(d);
+    const int pBeg = d.colStart[kx], pEnd = d.colStart[kx + 1];
+    for (int p = pBeg + lane; p < pEnd; p += 32) {
+        const int ky = d.posKy[p];
+        cx<T> v = tileA[tile_at<R>(ky, warp)];
+        if (b >= 0) {
+            const cx<T> w = tileB[tile_at<R>(ky, warp)];
+            const T l = rl[ky];
+            v = mk<T>(v.x + l * w.y, v.y - l * w.x);
+        }
+        out[p] = v;
+    }
+}
+
 // inverse fields: c2r of nch channels to fields[ch][z][y][x]
 template <typename T, int R>
 __global__ void __launch_bounds__(256) k_xc2r_fields_w(DescDev d, const cx<T>* __restrict__ yspec, int nch,
