@@ -342,6 +342,82 @@ int wv_ensemble_set_vertical_kernel(wv_ensemble* ensemble, int kind);
 int wv_ensemble_rk4_device(wv_ensemble* ensemble, double* const* states, double* t, double t0, const double* dt,
                            int n_steps, void* stream);
 
+/* ---- adaptive RK23 ---------------------------------------------------------------------
+ * WVAdaptiveRK23 (PortableRuntime/include/WaveVortexRuntime/WVRungeKutta.hpp:112-196,
+ * PortableRuntime/src/WVRungeKutta.cpp:554-983): Bogacki-Shampine 3(2) pair with
+ * first-same-as-last reuse and the "matlab-ode23-v1" step-size controller, over the
+ * handle's scheduled right-hand side (wv_evaluate_rhs).  Stage states, derivatives and
+ * the error norm stay on the device; the controller reads one double per attempt. */
+typedef struct wv_rk23 wv_rk23;
+/* WVAdaptiveRK23Options (WVRungeKutta.hpp:112-120). */
+typedef struct wv_rk23_options {
+    double relative_tolerance;                  /* 1e-3 */
+    double absolute_tolerance_scale;            /* 1e-6: scales the per-coefficient energy tolerances */
+    double safety_factor;                       /* 0.8 */
+    double rejection_floor_factor;              /* 0.5 */
+    double maximum_step_factor;                 /* 5 */
+    double maximum_step_size;                   /* +inf */
+    uint64_t maximum_recorded_step_diagnostics; /* 512 */
+} wv_rk23_options;
+/* WVAdaptiveRK23StepDiagnostic (WVRungeKutta.hpp:122-130). */
+typedef struct wv_rk23_step_diagnostic {
+    double initial_time;
+    double accepted_step_size;
+    double normalized_error;
+    double next_step_size;
+    uint64_t rejected_attempt_count;
+    uint64_t rhs_evaluation_count;
+    uint8_t reused_fsal_derivative;
+} wv_rk23_step_diagnostic;
+/* The RK23 fields of WVIntegratorMetrics (WVRungeKutta.hpp:14-50). */
+typedef struct wv_rk23_metrics {
+    uint64_t rhs_evaluations;
+    uint64_t accepted_steps;
+    uint64_t rejected_steps;
+    uint64_t fsal_reuses;
+    uint64_t fsal_invalidations;
+    uint64_t rejected_initial_derivative_reuses;
+    uint64_t dense_output_evaluations;
+    double last_proposed_step_size;
+    double last_accepted_step_size;
+    double normalized_error;
+    double next_step_size;
+    uint64_t workspace_bytes;
+} wv_rk23_metrics;
+void wv_rk23_default_options(wv_rk23_options* options);
+/* Binds an integrator to a handle (the handle must outlive it).  Builds the absolute
+ * tolerances (WVWaveVortexCoefficientErrorPolicy, PortableRuntime/src/WVForcingEngine.cpp:79-168)
+ * and allocates five state-sized device buffers. */
+int wv_rk23_create(wv_handle* handle, const wv_rk23_options* options, wv_rk23** integrator);
+void wv_rk23_destroy(wv_rk23* integrator);
+const char* wv_rk23_last_message(const wv_rk23* integrator);
+/* prepareStateAfterRestart (WVRungeKutta.cpp:645-657): forgets the stored derivative,
+ * the accepted step and the diagnostics. */
+int wv_rk23_prepare_after_restart(wv_rk23* integrator);
+/* WVAdaptiveRK23::step on device-resident state (each [Nj, Nkl] complex), updated in
+ * place; *t advances by the accepted step.  Synchronizes the stream once per attempt. */
+int wv_rk23_step_device(wv_rk23* integrator, double* Ap, double* Am, double* A0, double* t, double t0,
+                        double proposed_step, void* stream);
+/* WVAdaptiveRK23::advanceToTime (WVRungeKutta.cpp:892-912); *t ends at final_time. */
+int wv_rk23_advance_to_time_device(wv_rk23* integrator, double* Ap, double* Am, double* A0, double* t, double t0,
+                                   double final_time, double initial_step, void* stream);
+/* Host-pointer form of wv_rk23_advance_to_time_device. */
+int wv_rk23_advance_to_time(wv_rk23* integrator, double* Ap, double* Am, double* A0, double* t, double t0,
+                            double final_time, double initial_step);
+/* WVAdaptiveRK23::evaluateDenseOutput (WVRungeKutta.cpp:914-981) into device arrays. */
+int wv_rk23_dense_output_device(wv_rk23* integrator, double time, double* Ap, double* Am, double* A0, void* stream);
+int wv_rk23_next_step_size(const wv_rk23* integrator, double* next_step_size);
+/* Interval of the last accepted step; WV_UNSUPPORTED_OPERATION when there is none. */
+int wv_rk23_last_accepted_step(const wv_rk23* integrator, double* initial_time, double* final_time);
+int wv_rk23_get_metrics(const wv_rk23* integrator, wv_rk23_metrics* metrics);
+/* Copies up to capacity recorded diagnostics; *count receives the number recorded. */
+int wv_rk23_get_diagnostics(const wv_rk23* integrator, wv_rk23_step_diagnostic* diagnostics, uint64_t capacity,
+                            uint64_t* count);
+/* Audit hash of the absolute tolerances (WVAdaptiveRK23::toleranceHash, WVRungeKutta.cpp:26-37,
+ * 602-613): FNV-1a over the doubles rounded to 32 significand bits; component_hashes
+ * receives the three per-component hashes (A+, A-, A0) when not NULL. */
+int wv_rk23_tolerance_hash(const wv_rk23* integrator, uint64_t* hash, uint64_t* component_hashes);
+
 #ifdef __cplusplus
 }
 #endif

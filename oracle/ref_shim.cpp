@@ -255,4 +255,57 @@ int wvref_rk4(void* handle, double* Ap, double* Am, double* A0, double* t, doubl
     return 0;
 }
 
+// Adaptive RK23 through the reference integrator (WVAdaptiveRK23,
+// PortableRuntime/src/WVRungeKutta.cpp:554-983): a fresh integrator with
+// options {rtol, atolScale, safety, floor, maxFactor, maxStep} advances the
+// state from *t to finalTime.  diag receives up to cap diagnostics as
+// {initialTime, step, error, next, rejected, evaluations, reusedFSAL};
+// counts = {accepted, rejected, rhs evaluations, fsal reuses}; hashes =
+// {toleranceHash, three component hashes}.  When dense is non-null the
+// interpolant of the last accepted step is evaluated at denseTime into it
+// ([3][M] complex).
+int wvref_rk23_advance(void* handle, const double* opts, double* Ap, double* Am, double* A0, double* t, double t0,
+                       double finalTime, double initialStep, double* diag, int cap, int* nDiag,
+                       unsigned long long* counts, double* nextStep, unsigned long long* hashes, double denseTime,
+                       double* dense) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVAdaptiveRK23Options o;
+    o.relativeTolerance = opts[0];
+    o.absoluteToleranceScale = opts[1];
+    o.safetyFactor = opts[2];
+    o.rejectionFloorFactor = opts[3];
+    o.maximumStepFactor = opts[4];
+    o.maximumStepSize = opts[5];
+    WVAdaptiveRK23 rk(*h->system, o);
+    WVMutableIntegrationState state{{*t, t0, {mview(Ap, s), mview(Am, s), mview(A0, s)}}, nullptr, 0};
+    auto status = rk.prepareStateAfterRestart(state);
+    if (!status) return fail(h, status);
+    status = rk.advanceToTime(state, finalTime, initialStep);
+    if (!status) return fail(h, status);
+    *t = state.waveVortex.t;
+    const auto& d = rk.stepDiagnostics();
+    *nDiag = static_cast<int>(d.size());
+    for (int i = 0; i < cap && i < static_cast<int>(d.size()); ++i) {
+        double* r = diag + 7 * i;
+        r[0] = d[i].initialTime; r[1] = d[i].acceptedStepSize; r[2] = d[i].normalizedError; r[3] = d[i].nextStepSize;
+        r[4] = static_cast<double>(d[i].rejectedAttemptCount); r[5] = static_cast<double>(d[i].rightHandSideEvaluationCount);
+        r[6] = d[i].reusedFSALDerivative ? 1.0 : 0.0;
+    }
+    counts[0] = rk.metrics().acceptedStepCount;
+    counts[1] = rk.metrics().rejectedStepCount;
+    counts[2] = rk.metrics().rightHandSideEvaluationCount;
+    counts[3] = rk.metrics().fsalReuseCount;
+    *nextStep = rk.nextStepSize();
+    hashes[0] = rk.toleranceHash();
+    for (int c = 0; c < 3; ++c) hashes[1 + c] = rk.toleranceComponentHashes()[c];
+    if (dense) {
+        const std::size_t M = s.elementCount();
+        WVMutableIntegrationState out{{0.0, t0, {mview(dense, s), mview(dense + 2 * M, s), mview(dense + 4 * M, s)}}, nullptr, 0};
+        status = rk.evaluateDenseOutput(denseTime, out);
+        if (!status) return fail(h, status);
+    }
+    return 0;
+}
+
 } // extern "C"

@@ -818,6 +818,238 @@ def rk4(desc, Ap, Am, A0, t, t0, h, steps, damping=None):
 
 
 # ---------------------------------------------------------------------------
+# Adaptive RK23 (WVAdaptiveRK23, PortableRuntime/src/WVRungeKutta.cpp:554-983)
+
+
+def rk23_tolerances(desc, abs_scale):
+    """Absolute tolerances of the coefficients, (wave, vortex) each (Nkl, Nj):
+    wave for A+ and A-, vortex for A0 (WVWaveVortexCoefficientErrorPolicy::create,
+    PortableRuntime/src/WVForcingEngine.cpp:79-168).  Radial shells of width
+    dK = the widest gap between distinct |K_h| share their width equally among
+    their coefficients; tolerance = abs_scale * sqrt(share / energy factor)."""
+    c = desc.c
+    if not (math.isfinite(abs_scale) and abs_scale > 0.0):
+        raise OracleError(1, "Adaptive absolute-tolerance scale must be finite and positive.")
+    Kh = [float(v) for v in desc.Kh]
+    radii = sorted(set(abs(v) for v in Kh))
+    if len(radii) < 2:
+        raise OracleError(1, "Adaptive tolerances require at least two distinct horizontal radial wavenumbers.")
+    dK = 0.0
+    for a, b in zip(radii[:-1], radii[1:]):
+        dK = max(dK, b - a)
+    centres = []
+    centre = 0.0
+    while centre <= radii[-1] + 0.5 * dK:
+        centres.append(centre)
+        centre += dK
+    shell = []
+    members = [0] * len(centres)
+    for kh in Kh:
+        for b, ce in enumerate(centres):
+            if ce - 0.5 * dK < kh <= ce + 0.5 * dK:
+                shell.append(b)
+                members[b] += 1
+                break
+        else:
+            raise OracleError(1, "A horizontal mode was not assigned to an adaptive radial tolerance bin.")
+    wave = np.ones((len(Kh), c.Nj))
+    vortex = np.ones((len(Kh), c.Nj))
+    f2 = desc.f * desc.f
+    N02 = c.N0 * c.N0
+    for i, kh in enumerate(Kh):
+        ce = centres[shell[i]]
+        share = (ce + 0.5 * dK - max(ce - 0.5 * dK, 0.0)) / members[shell[i]]
+        for j in range(c.Nj):
+            m = float(desc.m[j])
+            we = 0.0
+            if kh == 0.0:
+                we = c.Lz if j == 0 else (N02 / (c.g * m * m) if c.isHydrostatic else (N02 - f2) / (c.g * m * m))
+            elif j > 0:
+                we = 2.0 * (N02 / (c.g * m * m) if c.isHydrostatic else (N02 - f2) / (c.g * (m * m + kh * kh)))
+            ve = 0.0
+            if kh > 0.0:
+                ld2 = 0.0 if j == 0 else f2 / (c.g * float(desc.h0[j]))
+                ve = float(desc.h0[j]) / (kh * kh + ld2)
+            elif j > 0:
+                ve = c.g / 2.0
+            if we > 0.0 and math.isfinite(we):
+                wave[i, j] = abs_scale * math.sqrt(share / we)
+            if ve > 0.0 and math.isfinite(ve):
+                vortex[i, j] = abs_scale * math.sqrt(share / ve)
+    return wave, vortex
+
+
+def rk23_tolerance_hash(components):
+    """toleranceHash / toleranceComponentHashes (WVRungeKutta.cpp:26-37,602-613):
+    FNV-1a over the tolerances rounded to 32 significand bits."""
+    mask = (1 << 64) - 1
+    total = 1469598103934665603
+    per = []
+    for comp in components:
+        bits = np.ascontiguousarray(comp, dtype=np.float64).reshape(-1).view(np.uint64)
+        hc = 1469598103934665603
+        for b in bits.tolist():
+            v = (b + 0x80000) & ~0xFFFFF & mask
+            total = ((total ^ v) * 1099511628211) & mask
+            hc = ((hc ^ v) * 1099511628211) & mask
+        per.append(hc)
+    return total, per
+
+
+RK23_DEFAULTS = dict(rtol=1e-3, atol_scale=1e-6, safety=0.8, floor=0.5, max_factor=5.0, max_step=math.inf,
+                     max_diagnostics=512)
+
+
+class RK23:
+    """WVAdaptiveRK23 over a right-hand side f(y, t) -> list of arrays, y a list
+    of complex arrays with absolute tolerances atol (same shapes): Bogacki-
+    Shampine 3(2) stages, first-same-as-last reuse, the "matlab-ode23-v1"
+    controller (WVRungeKutta.cpp:660-890), advanceToTime (:892-912) and the
+    cubic dense output (:914-981).  State constraints of the constant-
+    stratification system (forcing-amplitude restoration) are empty for the
+    advection and damping schedules and so are omitted."""
+
+    B = (2.0 / 9.0 - 7.0 / 24.0, 1.0 / 3.0 - 0.25, 4.0 / 9.0 - 1.0 / 3.0)
+
+    def __init__(self, f, atol, **options):
+        self.f = f
+        self.atol = atol
+        self.o = {**RK23_DEFAULTS, **options}
+        self.k1 = self.k4 = None
+        self.fsal = False
+        self.next_step = 0.0
+        self.accepted = None
+        self.evaluations = 0
+        self.accepted_steps = 0
+        self.rejected_steps = 0
+        self.fsal_reuses = 0
+        self.diagnostics = []
+
+    @staticmethod
+    def time_tolerance(a, b):
+        return 8.0 * np.finfo(float).eps * max(1.0, abs(a), abs(b))
+
+    def _eval(self, y, t):
+        self.evaluations += 1
+        return [np.asarray(v) for v in self.f(y, t)]
+
+    def step(self, y, t, proposed):
+        """Returns (y_next, t_next) of one accepted step."""
+        o = self.o
+        if not (proposed > 0.0 and math.isfinite(proposed)):
+            raise OracleError(1, "RK23 step size must be finite and positive.")
+        self.accepted = None
+        h = min(proposed, o["max_step"])
+        have_first = reused = False
+        if self.fsal:
+            self.k1 = self.k4
+            have_first = reused = True
+            self.fsal = False
+            self.fsal_reuses += 1
+        rejected = evals = 0
+        while True:
+            if not math.isfinite(h) or not (t + h > t):
+                raise OracleError(9, "RK23 cannot advance time with the proposed step.")
+            if not have_first:
+                self.k1 = self._eval(y, t)
+                evals += 1
+                have_first = True
+            k1 = self.k1
+            stage = [y[c] + (0.5 * h) * k1[c] for c in range(3)]
+            k2 = self._eval(stage, t + 0.5 * h)
+            stage = [y[c] + (0.75 * h) * k2[c] for c in range(3)]
+            k3 = self._eval(stage, t + 0.75 * h)
+            s1, s2, s3 = h * (2.0 / 9.0), h * (1.0 / 3.0), h * (4.0 / 9.0)
+            cand = [((y[c] + s1 * k1[c]) + s2 * k2[c]) + s3 * k3[c] for c in range(3)]
+            k4 = self._eval(cand, t + h)
+            evals += 3
+            b1, b2, b3 = self.B
+            error = 0.0
+            for c in range(3):
+                e = h * (((b1 * k1[c] + b2 * k2[c]) + b3 * k3[c]) - 0.125 * k4[c])
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    scale = np.maximum(self.atol[c], o["rtol"] * np.maximum(np.abs(y[c]), np.abs(cand[c])))
+                    ratio = np.abs(e) / scale
+                if not np.all(np.isfinite(ratio)):
+                    error = math.inf
+                    break
+                error = max(error, float(np.max(ratio)) if ratio.size else 0.0)
+            ok = math.isfinite(error) and error <= 1.0
+            factor = 1.0
+            if ok:
+                if rejected == 0:
+                    temp = 1.25 * np.cbrt(error)
+                    factor = 1.0 / temp if temp > 0.2 else o["max_factor"]
+            elif rejected == 0:
+                factor = max(o["floor"], o["safety"] * error ** (-1.0 / 3.0))
+            else:
+                factor = o["floor"]
+            self.next_step = min(o["max_step"], h * factor)
+            self.normalized_error = error
+            if ok:
+                self.k2, self.k3, self.k4 = k2, k3, k4
+                self.accepted = (t, t + h, cand)
+                self.accepted_steps += 1
+                self.fsal = True
+                if len(self.diagnostics) < o["max_diagnostics"]:
+                    self.diagnostics.append((t, h, error, self.next_step, rejected, evals, reused))
+                return cand, t + h
+            rejected += 1
+            self.rejected_steps += 1
+            h = self.next_step
+            if not (h > 0.0) or t + h == t:
+                raise OracleError(9, "RK23 step size underflowed after rejection.")
+
+    def advance_to_time(self, y, t, final, h):
+        if final < t or not math.isfinite(final):
+            raise OracleError(1, "RK23 cannot advance backward or to a nonfinite time.")
+        while t < final:
+            remaining = final - t
+            if remaining <= self.time_tolerance(t, final):
+                break
+            y, t = self.step(y, t, min(h, remaining))
+            h = self.next_step
+        return y, final
+
+    def dense_output(self, time):
+        if self.accepted is None:
+            raise OracleError(10, "RK23 dense output is unavailable.")
+        ti, tf, end = self.accepted
+        h = tf - ti
+        tol = self.time_tolerance(ti, tf)
+        if time < ti - tol or time > tf + tol:
+            raise OracleError(1, "Dense-output time is outside the accepted interval.")
+        theta = 0.0 if h == 0 else (time - ti) / h
+        if abs(time - ti) <= tol:
+            theta = 0.0
+        if abs(time - tf) <= tol:
+            theta = 1.0
+        theta = max(0.0, min(1.0, theta))
+        t2 = theta * theta
+        t3 = t2 * theta
+        w = (theta - (4.0 / 3.0) * t2 + (5.0 / 9.0) * t3 - 2.0 / 9.0, t2 - (2.0 / 3.0) * t3 - 1.0 / 3.0,
+             (4.0 / 3.0) * t2 - (8.0 / 9.0) * t3 - 4.0 / 9.0, -t2 + t3)
+        ks = (self.k1, self.k2, self.k3, self.k4)
+        out = []
+        for c in range(3):
+            v = end[c].copy()
+            for d in range(4):
+                v = v + (h * w[d]) * ks[d][c]
+            out.append(v)
+        return out
+
+
+def rk23_advance(desc, Ap, Am, A0, t, t0, final, initial, damping=None, **options):
+    """Adaptive RK23 of the wave-vortex state on the scheduled right-hand side
+    from t to final; returns (Ap, Am, A0, t, integrator)."""
+    o = {**RK23_DEFAULTS, **options}
+    wave, vortex = rk23_tolerances(desc, o["atol_scale"])
+    rk = RK23(lambda y, tt: rhs(desc, *y, tt, t0, damping), [wave, wave, vortex], **options)
+    y, t = rk.advance_to_time([Ap, Am, A0], t, final, initial)
+    return y[0], y[1], y[2], t, rk
+
+
+# ---------------------------------------------------------------------------
 # Energy flux diagnostic (@WVTransform/energyFluxFromNonlinearFlux.m:37-44 with
 # total-energy factors of the flow components)
 

@@ -44,3 +44,19 @@ def parity_tolerance(floor):
     (two valid orderings of the oracle) exceeds the reference's 1e-12 gate:
     within 3x that measured floor, never looser than needed."""
     return max(FP64_REL_TOL, 3.0 * floor)
+
+
+# Adaptive RK23 fixture runs (tests/golden/rk23.npz) and the golden case each uses.
+RK23_RUNS = {"odd": "odd_15x13x9", "c0": "c0_16x16x9", "hd": "hydro_damp_12x10x11"}
+
+
+def rk23_run(key):
+    """Inputs and reference outputs of one RK23 fixture run."""
+    g = load_golden("rk23")
+    cf = golden_cases()[RK23_RUNS[key]]
+    o = g[f"{key}_opts"]
+    options = dict(rtol=float(o[0]), atol_scale=float(o[1]), safety=float(o[2]), floor=float(o[3]),
+                   max_factor=float(o[4]), max_step=float(o[5]))
+    out = {n: g[f"{key}_{n}"] for n in ("Ap", "Am", "A0", "Kp", "Km", "K0", "diag", "counts", "hashes", "dense")}
+    out.update({n: float(g[f"{key}_{n}"]) for n in ("t", "t0", "final", "initial", "tout", "next", "dense_time")})
+    return cf, options, out

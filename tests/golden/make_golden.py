@@ -6,7 +6,8 @@ forcing engine) with its exact direct-DFT FFT engine on small seeded cases.
 The outputs are written as .npz files next to this script; tests compare the
 numpy oracle (oracle/wv_oracle.py) and the GPU path against them.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT] [--rk23]
+        (--rk23 regenerates only the adaptive RK23 fixture, rk23.npz)
 """
 from __future__ import annotations
 
@@ -166,6 +167,27 @@ class Ref:
                                       ctypes.c_double(dt), ctypes.c_int(steps)))
         return Ap, Am, A0, tt.value
 
+    def rk23(self, Ap, Am, A0, t, t0, final, initial, opts, dense_time=None):
+        """opts = (rtol, atol_scale, safety, floor, max_factor, max_step)."""
+        Ap, Am, A0 = Ap.copy(), Am.copy(), A0.copy()
+        tt = ctypes.c_double(t)
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        o = (ctypes.c_double * 6)(*opts)
+        cap = 4096
+        diag = np.zeros((cap, 7))
+        nd = ctypes.c_int()
+        counts = (ctypes.c_ulonglong * 4)()
+        nxt = ctypes.c_double()
+        hashes = (ctypes.c_ulonglong * 4)()
+        dense = np.zeros((3,) + Ap.shape, np.complex128) if dense_time is not None else None
+        self.check(self.lib.wvref_rk23_advance(
+            self.h, o, P(Ap), P(Am), P(A0), ctypes.byref(tt), ctypes.c_double(t0), ctypes.c_double(final),
+            ctypes.c_double(initial), P(diag), ctypes.c_int(cap), ctypes.byref(nd), counts, ctypes.byref(nxt), hashes,
+            ctypes.c_double(dense_time if dense_time is not None else 0.0), P(dense) if dense is not None else None))
+        n = min(nd.value, cap)
+        return dict(Ap=Ap, Am=Am, A0=A0, t=tt.value, diag=diag[:n].copy(), counts=np.array(list(counts), np.uint64),
+                    next=nxt.value, hashes=np.array(list(hashes), np.uint64), dense=dense)
+
 
 def load_lib(reference_root):
     if not os.path.exists(LIB):
@@ -266,5 +288,56 @@ def main():
     print(f"c0_t600: t = {tK}")
 
 
+# Adaptive RK23 runs through the reference integrator (WVAdaptiveRK23):
+#   odd:  seeded state, default options, t 100 -> 200 from a 5 s initial step
+#   c0:   the single internal wave under {advection, damping} to t = 600 s
+#   hd:   hydrostatic with damping, every option away from its default
+RK23_RUNS = {
+    "odd": dict(case="odd_15x13x9", scale=1e-3, t=100.0, t0=0.0, final=200.0, initial=5.0,
+                opts=(1e-3, 1e-6, 0.8, 0.5, 5.0, float("inf"))),
+    "c0": dict(case="c0_16x16x9", scale=None, t=0.0, t0=0.0, final=600.0, initial=10.0,
+               opts=(1e-3, 1e-6, 0.8, 0.5, 5.0, float("inf"))),
+    "hd": dict(case="hydro_damp_12x10x11", scale=3e-3, t=50.0, t0=-3.0, final=56.0, initial=40.0,
+               opts=(1e-5, 1e-7, 0.9, 0.3, 2.0, 15.0)),
+}
+
+
+def make_rk23(lib):
+    out = {}
+    for key, run in RK23_RUNS.items():
+        case = CASES[run["case"]]
+        r = Ref(lib, case)
+        shape = (r.Nkl, case["Nj"])
+        desc = r.descriptor()
+        if run["scale"] is None:
+            Ap = np.zeros(shape, np.complex128)
+            idx = int(np.nonzero((desc["kMode"] == 1) & (desc["lMode"] == 0))[0][0])
+            Ap[idx, 1] = 0.05 / (2.0 * abs(desc["fWaveScale"].reshape(shape)[idx, 1]))
+            Am = np.zeros(shape, np.complex128)
+            A0 = np.zeros(shape, np.complex128)
+        else:
+            base = sum(ord(ch) for ch in run["case"]) + 100
+            Ap = seeded(shape, base + 1, run["scale"])
+            Am = seeded(shape, base + 2, run["scale"])
+            A0 = seeded(shape, base + 3, run["scale"])
+        # dense output at the midpoint of the last accepted step: run once to learn it
+        first = r.rk23(Ap, Am, A0, run["t"], run["t0"], run["final"], run["initial"], run["opts"])
+        last = first["diag"][-1]
+        mid = last[0] + 0.5 * last[1]
+        res = r.rk23(Ap, Am, A0, run["t"], run["t0"], run["final"], run["initial"], run["opts"], dense_time=mid)
+        out.update({f"{key}_Ap": Ap, f"{key}_Am": Am, f"{key}_A0": A0, f"{key}_t": run["t"], f"{key}_t0": run["t0"],
+                    f"{key}_final": run["final"], f"{key}_initial": run["initial"], f"{key}_opts": np.array(run["opts"]),
+                    f"{key}_Kp": res["Ap"], f"{key}_Km": res["Am"], f"{key}_K0": res["A0"], f"{key}_tout": res["t"],
+                    f"{key}_diag": res["diag"], f"{key}_counts": res["counts"], f"{key}_next": res["next"],
+                    f"{key}_hashes": res["hashes"], f"{key}_dense_time": mid, f"{key}_dense": res["dense"]})
+        lib.wvref_destroy(r.h)
+        print(f"rk23 {key}: counts {res['counts'].tolist()} t = {res['t']}")
+    np.savez_compressed(os.path.join(HERE, "rk23.npz"), **out)
+
+
 if __name__ == "__main__":
-    main()
+    if "--rk23" in sys.argv:
+        make_rk23(load_lib(next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")))
+    else:
+        main()
+        make_rk23(load_lib(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))

@@ -7,6 +7,7 @@
 // (ExecutionGuard, CompiledKernel/src/WVTransformConstantStratificationKernel.cpp:76-84).
 #include "wvgpu.h"
 #include "wv_descriptor.hpp"
+#include "wv_internal.hpp"
 #include "wv_kernels.cuh"
 #include "wv_plan.hpp"
 #include "wv_warpfft.cuh"
@@ -1111,6 +1112,13 @@ cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* 
 }
 
 }  // namespace
+
+namespace wvgpu {
+const Descriptor& handle_descriptor(const wv_handle* h) { return h->desc; }
+int handle_device(const wv_handle* h) { return h->device; }
+void* handle_stream(const wv_handle* h) { return h->stream; }
+bool handle_is_single_state(const wv_handle* h) { return h->dd.members == 1; }
+}  // namespace wvgpu
 
 extern "C" {
 

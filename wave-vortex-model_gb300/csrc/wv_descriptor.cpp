@@ -261,4 +261,66 @@ Status adaptive_damping_operator(const Descriptor& d, std::vector<double>& dampi
     return {};
 }
 
+Status adaptive_error_tolerances(const Descriptor& d, double absoluteScale, std::vector<double>& wave,
+                                 std::vector<double>& vortex) {
+    const auto& c = d.c;
+    if (!std::isfinite(absoluteScale) || !(absoluteScale > 0.0))
+        return {WV_INVALID_CONFIGURATION, "Adaptive absolute-tolerance scale must be finite and positive."};
+    wave.assign(d.M, 1.0);
+    vortex.assign(d.M, 1.0);
+    // Radial shells of width dK (the widest gap between distinct |K_h|) centred
+    // on 0, dK, 2 dK, ...; each coefficient of a shell gets an equal share of
+    // the shell's width as its energy.
+    std::vector<double> radii(d.Kh.begin(), d.Kh.end());
+    for (double& r : radii) r = std::abs(r);
+    std::sort(radii.begin(), radii.end());
+    radii.erase(std::unique(radii.begin(), radii.end()), radii.end());
+    if (radii.size() < 2)
+        return {WV_INVALID_CONFIGURATION, "Adaptive tolerances require at least two distinct horizontal radial wavenumbers."};
+    double dK = 0.0;
+    for (size_t i = 1; i < radii.size(); ++i) dK = std::max(dK, radii[i] - radii[i - 1]);
+    if (!(dK > 0.0) || !std::isfinite(dK)) return {WV_INVALID_CONFIGURATION, "Adaptive radial tolerance spacing is invalid."};
+    std::vector<double> centres;
+    for (double centre = 0.0; centre <= radii.back() + 0.5 * dK; centre += dK) centres.push_back(centre);
+    std::vector<size_t> shell(d.Nkl, centres.size()), members(centres.size(), 0);
+    for (size_t iMode = 0; iMode < d.Nkl; ++iMode) {
+        for (size_t b = 0; b < centres.size(); ++b)
+            if (centres[b] - 0.5 * dK < d.Kh[iMode] && d.Kh[iMode] <= centres[b] + 0.5 * dK) {
+                shell[iMode] = b;
+                ++members[b];
+                break;
+            }
+        if (shell[iMode] == centres.size())
+            return {WV_INVALID_CONFIGURATION, "A horizontal mode was not assigned to an adaptive radial tolerance bin."};
+    }
+    const double f2 = d.f * d.f, N02 = c.N0 * c.N0;
+    for (size_t iMode = 0; iMode < d.Nkl; ++iMode) {
+        const double Kh = d.Kh[iMode], Kh2 = Kh * Kh;
+        const double centre = centres[shell[iMode]];
+        const double width = centre + 0.5 * dK - std::max(centre - 0.5 * dK, 0.0);
+        const double share = width / static_cast<double>(members[shell[iMode]]);
+        for (size_t iJ = 0; iJ < c.Nj; ++iJ) {
+            const size_t index = iJ + c.Nj * iMode;
+            const double m = d.m[iJ];
+            // energy per unit squared amplitude of the wave (A+/A-) and vortex (A0) parts
+            double waveEnergy = 0.0;
+            if (Kh == 0.0) {
+                waveEnergy = iJ == 0 ? c.Lz : (c.is_hydrostatic ? N02 / (c.g * m * m) : (N02 - f2) / (c.g * m * m));
+            } else if (iJ > 0) {
+                waveEnergy = 2.0 * (c.is_hydrostatic ? N02 / (c.g * m * m) : (N02 - f2) / (c.g * (m * m + Kh2)));
+            }
+            double vortexEnergy = 0.0;
+            if (Kh > 0.0) {
+                const double Ld2Inverse = iJ == 0 ? 0.0 : f2 / (c.g * d.h0[iJ]);
+                vortexEnergy = d.h0[iJ] / (Kh2 + Ld2Inverse);
+            } else if (iJ > 0) {
+                vortexEnergy = c.g / 2.0;
+            }
+            if (waveEnergy > 0.0 && std::isfinite(waveEnergy)) wave[index] = absoluteScale * std::sqrt(share / waveEnergy);
+            if (vortexEnergy > 0.0 && std::isfinite(vortexEnergy)) vortex[index] = absoluteScale * std::sqrt(share / vortexEnergy);
+        }
+    }
+    return {};
+}
+
 }  // namespace wvgpu

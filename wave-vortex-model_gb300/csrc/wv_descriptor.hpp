@@ -50,4 +50,11 @@ Status build_descriptor(const wv_config& c, Descriptor& d);
 // Adaptive-damping operator [Nj, Nkl] (PortableRuntime/src/WVForcingEngine.cpp:30-38,352-381).
 Status adaptive_damping_operator(const Descriptor& d, std::vector<double>& damping);
 
+// Absolute error tolerances of the adaptive RK23 controller, [Nj, Nkl] each:
+// wave for A+ and A-, vortex for A0 (WVWaveVortexCoefficientErrorPolicy::create,
+// PortableRuntime/src/WVForcingEngine.cpp:79-168).  Entries without a finite
+// positive energy factor keep 1.
+Status adaptive_error_tolerances(const Descriptor& d, double absoluteScale, std::vector<double>& wave,
+                                 std::vector<double>& vortex);
+
 }  // namespace wvgpu

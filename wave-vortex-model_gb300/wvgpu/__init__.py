@@ -90,6 +90,27 @@ class _Metrics(ctypes.Structure):
                [("last_max_horizontal_speed", ctypes.c_double)]
 
 
+class _RK23Options(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("relative_tolerance", "absolute_tolerance_scale", "safety_factor",
+                                               "rejection_floor_factor", "maximum_step_factor", "maximum_step_size")] + \
+               [("maximum_recorded_step_diagnostics", ctypes.c_uint64)]
+
+
+class _RK23Diagnostic(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("initial_time", "accepted_step_size", "normalized_error",
+                                               "next_step_size")] + \
+               [("rejected_attempt_count", ctypes.c_uint64), ("rhs_evaluation_count", ctypes.c_uint64),
+                ("reused_fsal_derivative", ctypes.c_uint8)]
+
+
+class _RK23Metrics(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("rhs_evaluations", "accepted_steps", "rejected_steps", "fsal_reuses",
+                                               "fsal_invalidations", "rejected_initial_derivative_reuses",
+                                               "dense_output_evaluations")] + \
+               [(n, ctypes.c_double) for n in ("last_proposed_step_size", "last_accepted_step_size", "normalized_error",
+                                               "next_step_size")] + [("workspace_bytes", ctypes.c_uint64)]
+
+
 @dataclass
 class Configuration:
     """WVTransformConstantStratificationConfiguration (WVKernelTypes.hpp:129-146)."""
@@ -184,6 +205,24 @@ def load_library():
     lib.wv_ensemble_get_metrics.argtypes = [P, ctypes.POINTER(_EnsembleMetrics)]
     lib.wv_ensemble_set_vertical_kernel.argtypes = [P, ctypes.c_int]
     lib.wv_ensemble_rk4_device.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(D), D, ctypes.POINTER(D), ctypes.c_int, P]
+    lib.wv_rk23_default_options.argtypes = [ctypes.POINTER(_RK23Options)]
+    lib.wv_rk23_default_options.restype = None
+    lib.wv_rk23_create.argtypes = [P, ctypes.POINTER(_RK23Options), ctypes.POINTER(P)]
+    lib.wv_rk23_destroy.argtypes = [P]
+    lib.wv_rk23_destroy.restype = None
+    lib.wv_rk23_last_message.argtypes = [P]
+    lib.wv_rk23_last_message.restype = ctypes.c_char_p
+    lib.wv_rk23_prepare_after_restart.argtypes = [P]
+    lib.wv_rk23_step_device.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, P]
+    lib.wv_rk23_advance_to_time_device.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, D, P]
+    lib.wv_rk23_advance_to_time.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, D]
+    lib.wv_rk23_dense_output_device.argtypes = [P, D, P, P, P, P]
+    lib.wv_rk23_next_step_size.argtypes = [P, ctypes.POINTER(D)]
+    lib.wv_rk23_last_accepted_step.argtypes = [P, ctypes.POINTER(D), ctypes.POINTER(D)]
+    lib.wv_rk23_get_metrics.argtypes = [P, ctypes.POINTER(_RK23Metrics)]
+    lib.wv_rk23_get_diagnostics.argtypes = [P, ctypes.POINTER(_RK23Diagnostic), ctypes.c_uint64,
+                                            ctypes.POINTER(ctypes.c_uint64)]
+    lib.wv_rk23_tolerance_hash.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     _lib = lib
     return lib
 
@@ -201,7 +240,11 @@ def exported_symbols():
             "wv_inverse_uvw_device", "wv_field_derivatives", "wv_field_derivatives_device", "wv_advect_fgrid_scalar",
             "wv_advect_fgrid_scalar_device", "wv_family_derivatives", "wv_family_derivatives_device", "wv_ensemble_create",
             "wv_ensemble_destroy", "wv_ensemble_last_message", "wv_ensemble_get_sizes", "wv_ensemble_get_tuning",
-            "wv_ensemble_get_metrics", "wv_ensemble_set_vertical_kernel", "wv_ensemble_rk4_device"]
+            "wv_ensemble_get_metrics", "wv_ensemble_set_vertical_kernel", "wv_ensemble_rk4_device",
+            "wv_rk23_default_options", "wv_rk23_create", "wv_rk23_destroy", "wv_rk23_last_message",
+            "wv_rk23_prepare_after_restart", "wv_rk23_step_device", "wv_rk23_advance_to_time_device",
+            "wv_rk23_advance_to_time", "wv_rk23_dense_output_device", "wv_rk23_next_step_size",
+            "wv_rk23_last_accepted_step", "wv_rk23_get_metrics", "wv_rk23_get_diagnostics", "wv_rk23_tolerance_hash"]
 
 
 def describe(configuration: Configuration):
@@ -655,6 +698,130 @@ class WVEnsemble:
         self._check(self._lib.wv_ensemble_rk4_device(self._h, ptrs, tt, float(t0), dd, int(steps),
                                                      WVTransformConstantStratificationKernel._stream()))
         return list(tt)
+
+
+@dataclass
+class WVAdaptiveRK23Options:
+    """WVAdaptiveRK23Options (PortableRuntime/include/WaveVortexRuntime/WVRungeKutta.hpp:112-120)."""
+
+    relativeTolerance: float = 1e-3
+    absoluteToleranceScale: float = 1e-6
+    safetyFactor: float = 0.8
+    rejectionFloorFactor: float = 0.5
+    maximumStepFactor: float = 5.0
+    maximumStepSize: float = math.inf
+    maximumRecordedStepDiagnostics: int = 512
+
+    def _c(self):
+        return _RK23Options(self.relativeTolerance, self.absoluteToleranceScale, self.safetyFactor,
+                            self.rejectionFloorFactor, self.maximumStepFactor, self.maximumStepSize,
+                            int(self.maximumRecordedStepDiagnostics))
+
+
+class WVAdaptiveRK23:
+    """Adaptive Bogacki-Shampine RK23 over a kernel handle's scheduled
+    right-hand side (WVAdaptiveRK23, PortableRuntime/src/WVRungeKutta.cpp:554-983):
+    step(), advanceToTime(), evaluateDenseOutput(), nextStepSize(), metrics()
+    and stepDiagnostics() with the reference's meaning.  States are torch CUDA
+    complex128 tensors advanced in place, or numpy arrays (advanceToTime only,
+    copied).  The kernel must outlive the integrator."""
+
+    controllerIdentifier = "matlab-ode23-v1"
+
+    def __init__(self, kernel, options: WVAdaptiveRK23Options | None = None):
+        self.kernel = kernel
+        self.options = options or WVAdaptiveRK23Options()
+        self._lib = kernel._lib
+        h = ctypes.c_void_p()
+        rc = self._lib.wv_rk23_create(kernel._h, ctypes.byref(self.options._c()), ctypes.byref(h))
+        if rc != 0:
+            raise WVKernelError(rc, "Adaptive RK23 creation failed (options, tolerances or device allocation).")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.wv_rk23_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WVKernelError(rc, self._lib.wv_rk23_last_message(self._h).decode())
+
+    def prepareStateAfterRestart(self):
+        self._check(self._lib.wv_rk23_prepare_after_restart(self._h))
+
+    def step(self, Ap, Am, A0, t, t0, proposedStepSize):
+        """One accepted step of the CUDA state (in place); returns the new time."""
+        Ap, Am, A0 = (self.kernel._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        tt = ctypes.c_double(float(t))
+        self._check(self._lib.wv_rk23_step_device(self._h, Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(), ctypes.byref(tt),
+                                                  float(t0), float(proposedStepSize), self.kernel._stream()))
+        return tt.value
+
+    def advanceToTime(self, Ap, Am, A0, t, t0, finalTime, initialStepSize):
+        """Advances to finalTime.  torch CUDA states in place (returns finalTime);
+        numpy states are copied (returns (Ap, Am, A0, finalTime))."""
+        tt = ctypes.c_double(float(t))
+        if _is_torch(Ap):
+            Ap, Am, A0 = (self.kernel._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            self._check(self._lib.wv_rk23_advance_to_time_device(
+                self._h, Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(), ctypes.byref(tt), float(t0), float(finalTime),
+                float(initialStepSize), self.kernel._stream()))
+            return tt.value
+        Ap, Am, A0 = (self.kernel._host_coeff(a, n).copy() for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        self._check(self._lib.wv_rk23_advance_to_time(self._h, Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data,
+                                                      ctypes.byref(tt), float(t0), float(finalTime),
+                                                      float(initialStepSize)))
+        return Ap, Am, A0, tt.value
+
+    def evaluateDenseOutput(self, time):
+        """State at `time` inside the last accepted step (new CUDA tensors)."""
+        import torch
+        out = tuple(torch.empty(self.kernel.spectral_shape, dtype=torch.complex128, device="cuda") for _ in range(3))
+        self._check(self._lib.wv_rk23_dense_output_device(self._h, float(time), *(o.data_ptr() for o in out),
+                                                          self.kernel._stream()))
+        return out
+
+    def nextStepSize(self):
+        v = ctypes.c_double()
+        self._check(self._lib.wv_rk23_next_step_size(self._h, ctypes.byref(v)))
+        return v.value
+
+    def lastAcceptedStep(self):
+        """(initialTime, finalTime) of the last accepted step, or None."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        rc = self._lib.wv_rk23_last_accepted_step(self._h, ctypes.byref(a), ctypes.byref(b))
+        return None if rc == 10 else (self._check(rc), (a.value, b.value))[1]
+
+    def metrics(self):
+        m = _RK23Metrics()
+        self._check(self._lib.wv_rk23_get_metrics(self._h, ctypes.byref(m)))
+        return {n: getattr(m, n) for n, _ in _RK23Metrics._fields_}
+
+    def stepDiagnostics(self):
+        """List of dicts (initialTime, acceptedStepSize, normalizedError, nextStepSize,
+        rejectedAttemptCount, rightHandSideEvaluationCount, reusedFSALDerivative)."""
+        n = ctypes.c_uint64()
+        self._check(self._lib.wv_rk23_get_diagnostics(self._h, None, 0, ctypes.byref(n)))
+        buf = (_RK23Diagnostic * max(1, n.value))()
+        self._check(self._lib.wv_rk23_get_diagnostics(self._h, buf, n.value, ctypes.byref(n)))
+        return [dict(initialTime=d.initial_time, acceptedStepSize=d.accepted_step_size, normalizedError=d.normalized_error,
+                     nextStepSize=d.next_step_size, rejectedAttemptCount=d.rejected_attempt_count,
+                     rightHandSideEvaluationCount=d.rhs_evaluation_count,
+                     reusedFSALDerivative=bool(d.reused_fsal_derivative)) for d in buf[:n.value]]
+
+    def toleranceHash(self):
+        """(toleranceHash, [hash of A+, A-, A0 tolerances])."""
+        h = ctypes.c_uint64()
+        comp = (ctypes.c_uint64 * 3)()
+        self._check(self._lib.wv_rk23_tolerance_hash(self._h, ctypes.byref(h), comp))
+        return h.value, list(comp)
 
 
 # ---------------------------------------------------------------------------
