@@ -418,6 +418,55 @@ int wv_rk23_get_diagnostics(const wv_rk23* integrator, wv_rk23_step_diagnostic* 
  * receives the three per-component hashes (A+, A-, A0) when not NULL. */
 int wv_rk23_tolerance_hash(const wv_rk23* integrator, uint64_t* hash, uint64_t* component_hashes);
 
+/* ---- integration system with integrated observers ---------------------------------------
+ * WVConstantStratificationIntegrationSystem with Lagrangian particles and three-dimensional
+ * tracers (PortableRuntime/src/WVConstantStratificationIntegrationSystem.cpp:112-400): one
+ * scheduled flux per right-hand side also yields the advection fields (u, v, w), which every
+ * tracer (advectFGridScalar) and every particle group (velocity at the particle positions)
+ * shares.  The packed state is Ap, Am, A0 ([Nj, Nkl] complex each) followed by the additional
+ * blocks in order: for each particle group x, y[, z] (count doubles each; x and y unwrapped,
+ * periodicity applied only when sampling), then for each tracer a [Nx, Ny, Nz] field. */
+typedef struct wv_system wv_system;
+/* WVPositionInterpolation (PortableRuntime/include/WaveVortexRuntime/WVObserverContracts.hpp:32). */
+#define WV_INTERPOLATION_LINEAR 0
+#define WV_INTERPOLATION_SPLINE 1
+/* WVLagrangianParticles (WVLagrangianParticles.hpp): one particle group. */
+typedef struct wv_particle_group {
+    uint64_t count;
+    int xy_only;                 /* x, y blocks only; depth fixed per particle */
+    int interpolation;           /* WV_INTERPOLATION_* for the advecting velocity */
+    const double* z_fixed;       /* host [count]: depths of xy-only particles (NULL otherwise) */
+    double horizontal_tolerance; /* absolute tolerance of the x and y blocks (adaptive RK23) */
+    double vertical_tolerance;   /* absolute tolerance of the z block */
+} wv_particle_group;
+/* WVTracer (WVTracer.hpp): one three-dimensional tracer. */
+typedef struct wv_tracer {
+    int antialias;               /* shouldAntialias of the tracer's scalar advection */
+    double absolute_tolerance;
+} wv_tracer;
+/* Binds a system to a handle (which must outlive it); the handle's forcing schedule applies. */
+int wv_system_create(wv_handle* handle, const wv_particle_group* groups, int n_groups, const wv_tracer* tracers,
+                     int n_tracers, wv_system** system);
+void wv_system_destroy(wv_system* system);
+const char* wv_system_last_message(const wv_system* system);
+/* Doubles of the packed state, and offset / length (in doubles) of each additional block. */
+int wv_system_get_layout(const wv_system* system, uint64_t* state_doubles, uint64_t* n_blocks, uint64_t* offsets,
+                         uint64_t* lengths, uint64_t capacity);
+/* evaluateRightHandSide (WVConstantStratificationIntegrationSystem.cpp:295-400) on packed
+ * device arrays. */
+int wv_system_rhs_device(wv_system* system, double t, double t0, const double* state, double* rhs, void* stream);
+/* WVFixedStepRK4::step over the packed state, n_steps times (device and host forms). */
+int wv_system_rk4_device(wv_system* system, double* state, double* t, double t0, double dt, int n_steps, void* stream);
+int wv_system_rk4(wv_system* system, double* state, double* t, double t0, double dt, int n_steps);
+/* Adaptive RK23 over a system's packed state: the additional blocks enter the error norm with
+ * their absolute tolerances (UnifiedErrorPolicy, WVConstantStratificationIntegrationSystem.cpp:47-86). */
+int wv_rk23_create_for_system(wv_system* system, const wv_rk23_options* options, wv_rk23** integrator);
+int wv_rk23_system_step_device(wv_rk23* integrator, double* state, double* t, double t0, double proposed_step,
+                               void* stream);
+int wv_rk23_system_advance_to_time_device(wv_rk23* integrator, double* state, double* t, double t0, double final_time,
+                                          double initial_step, void* stream);
+int wv_rk23_system_dense_output_device(wv_rk23* integrator, double time, double* state, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <vector>
 
 using namespace wavevortex;
 using namespace wavevortex::runtime;
@@ -66,6 +67,28 @@ int fail(RefHandle* h, const WVKernelStatus& status) {
 
 WVComplexConstView cview(const double* p, WVShape2D s) { return {reinterpret_cast<const WVComplex64*>(p), s}; }
 WVComplexView mview(double* p, WVShape2D s) { return {reinterpret_cast<WVComplex64*>(p), s}; }
+
+struct RefSystem {
+    std::unique_ptr<WVConstantStratificationIntegrationSystem> system;
+    std::string message;
+    std::size_t M = 0;
+};
+
+int sys_fail(RefSystem* h, const WVKernelStatus& status) {
+    if (h) h->message = status.message;
+    return static_cast<int>(status.code);
+}
+
+// Views of a packed additional state (blocks back to back, layout order).
+std::vector<WVAdditionalStateBlockView> blockViews(const WVConstantStratificationIntegrationSystem& s, double* packed) {
+    std::vector<WVAdditionalStateBlockView> v;
+    std::size_t off = 0;
+    for (const auto& b : s.stateLayout().additionalBlocks()) {
+        v.push_back({&b, packed + off, nullptr});
+        off += b.elementCount;
+    }
+    return v;
+}
 
 } // namespace
 
@@ -305,6 +328,166 @@ int wvref_rk23_advance(void* handle, const double* opts, double* Ap, double* Am,
         status = rk.evaluateDenseOutput(denseTime, out);
         if (!status) return fail(h, status);
     }
+    return 0;
+}
+
+// ---- integration system with integrated observers -------------------------------
+// WVConstantStratificationIntegrationSystem (PortableRuntime/src/
+// WVConstantStratificationIntegrationSystem.cpp:112-400) built from an observer
+// descriptor: particle groups (x, y[, z] state blocks, linear or spline
+// advection interpolation) then three-dimensional tracers, in that block order.
+// groups: counts[g], xyOnly[g], interp[g] (0 linear, 1 spline), tolH[g] (x, y
+// blocks), tolV[g] (z block); x, y, z concatenated over groups (z is the fixed
+// depth of xy-only particles).  tracers: antialias[i], tolT[i].
+int wvref_system_create(const std::uint64_t* sizes, const double* values, const std::uint8_t* flags, int schedule,
+                        int nGroups, const int* counts, const int* xyOnly, const int* interp, const double* tolH,
+                        const double* tolV, const double* x, const double* y, const double* z, int nTracers,
+                        const int* antialias, const double* tolT, void** out) {
+    *out = nullptr;
+    auto h = std::make_unique<RefSystem>();
+    const auto c = makeConfiguration(sizes, values, flags);
+    WVTransformConstantStratificationDescriptor transform;
+    auto status = WVTransformConstantStratificationDescriptor::create(c, transform);
+    if (!status) return static_cast<int>(status.code);
+    h->M = transform.spectralShape().elementCount();
+    WVPortableObserverRecord record;
+    const std::vector<std::size_t> shape{c.Nj, transform.Nkl()};
+    for (const char* name : {"Ap", "Am", "A0"})
+        record.stateBlocks.push_back({name, WVStateScalarType::complex64, shape, WVToleranceKind::coefficientEnergyScaled,
+                                      1e-6, WVStateOwnership::integratorOwned, WVRestartRequirement::requiredDynamicState});
+    auto addReal = [&](const std::string& name, std::vector<std::size_t> dims, double tol) {
+        record.stateBlocks.push_back({name, WVStateScalarType::real64, std::move(dims), WVToleranceKind::uniformAbsolute,
+                                      tol, WVStateOwnership::integratorOwned, WVRestartRequirement::requiredDynamicState});
+    };
+    WVObserverRecord coefficients;
+    coefficients.identifier = "coefficients";
+    coefficients.name = "Wave-vortex coefficients";
+    coefficients.typeIdentifier = "WVCoefficients";
+    coefficients.stateBlockIdentifiers = {"Ap", "Am", "A0"};
+    record.observers.push_back(coefficients);
+    std::size_t off = 0;
+    for (int g = 0; g < nGroups; ++g) {
+        const std::string id = "particles" + std::to_string(g);
+        const std::size_t n = static_cast<std::size_t>(counts[g]);
+        addReal(id + "-x", {n}, tolH[g]);
+        addReal(id + "-y", {n}, tolH[g]);
+        if (!xyOnly[g]) addReal(id + "-z", {n}, tolV[g]);
+        WVObserverRecord o;
+        o.identifier = id;
+        o.name = id;
+        o.typeIdentifier = "WVLagrangianParticles";
+        o.stateBlockIdentifiers = {id + "-x", id + "-y"};
+        if (!xyOnly[g]) o.stateBlockIdentifiers.push_back(id + "-z");
+        o.x.assign(x + off, x + off + n);
+        o.y.assign(y + off, y + off + n);
+        o.z.assign(z + off, z + off + n);
+        o.isXYOnly = xyOnly[g] != 0;
+        o.advectionInterpolation = interp[g] ? WVPositionInterpolation::spline : WVPositionInterpolation::linear;
+        o.trackedFieldInterpolation = WVPositionInterpolation::linear;
+        o.fieldNames = {"u"};
+        o.horizontalAbsoluteTolerance = tolH[g];
+        o.verticalAbsoluteTolerance = tolV[g];
+        record.observers.push_back(o);
+        off += n;
+    }
+    for (int i = 0; i < nTracers; ++i) {
+        const std::string id = "tracer" + std::to_string(i);
+        addReal(id, {c.Nx, c.Ny, c.Nz}, tolT[i]);
+        WVObserverRecord o;
+        o.identifier = id;
+        o.name = id;
+        o.typeIdentifier = "WVTracer";
+        o.stateBlockIdentifiers = {id};
+        o.shouldAntialias = antialias[i] != 0;
+        record.observers.push_back(o);
+    }
+    std::shared_ptr<const WVExtensionCatalog> catalog;
+    status = makeBuiltInExtensionCatalog(catalog);
+    if (!status) return static_cast<int>(status.code);
+    WVPortableObserverDescriptor descriptor;
+    status = WVPortableObserverDescriptor::create(record, catalog, descriptor);
+    if (!status) { h->message = status.message; *out = h.release(); return static_cast<int>(status.code); }
+    WVFrozenForcingSchedule frozen;
+    frozen.entries.push_back(forcingEntry("WVNonlinearAdvection", "nonlinear", WVForcingStage::spatial, 127));
+    if (schedule == 1) frozen.entries.push_back(forcingEntry("WVAdaptiveDamping", "adaptive", WVForcingStage::spectral, 100));
+    status = WVConstantStratificationIntegrationSystem::create(c, frozen, descriptor, catalog,
+                                                               std::make_unique<WVReferenceFFTEngine>(), h->system);
+    if (!status) { h->message = status.message; *out = h.release(); return static_cast<int>(status.code); }
+    *out = h.release();
+    return 0;
+}
+
+void wvref_system_destroy(void* s) { delete static_cast<RefSystem*>(s); }
+const char* wvref_system_message(void* s) { return s ? static_cast<RefSystem*>(s)->message.c_str() : ""; }
+
+// Number of doubles in the packed additional state.
+std::uint64_t wvref_system_extra(void* s) {
+    std::uint64_t n = 0;
+    for (const auto& b : static_cast<RefSystem*>(s)->system->stateLayout().additionalBlocks()) n += b.elementCount;
+    return n;
+}
+
+// evaluateRightHandSide on (Ap, Am, A0, extra) -> (Fp, Fm, F0, extraRhs).
+int wvref_system_rhs(void* sp, double t, double t0, double* Ap, double* Am, double* A0, double* extra, double* Fp,
+                     double* Fm, double* F0, double* extraRhs) {
+    auto* h = static_cast<RefSystem*>(sp);
+    const auto shape = h->system->stateLayout().coefficientShape();
+    auto inViews = blockViews(*h->system, extra);
+    auto outViews = blockViews(*h->system, extraRhs);
+    WVMutableIntegrationState state{{t, t0, {mview(Ap, shape), mview(Am, shape), mview(A0, shape)}}, inViews.data(),
+                                    inViews.size()};
+    std::vector<WVAdditionalStateBlockConstView> cviews;
+    const auto view = integrationConstView(state, cviews);
+    WVIntegrationFlux flux{{mview(Fp, shape), mview(Fm, shape), mview(F0, shape)}, outViews.data(), outViews.size()};
+    const auto status = h->system->evaluateRightHandSide(view, flux);
+    return status ? 0 : sys_fail(h, status);
+}
+
+// WVFixedStepRK4 over the system: steps of dt, state in place, *t advanced.
+int wvref_system_rk4(void* sp, double* Ap, double* Am, double* A0, double* extra, double* t, double t0, double dt,
+                     int steps) {
+    auto* h = static_cast<RefSystem*>(sp);
+    const auto shape = h->system->stateLayout().coefficientShape();
+    auto views = blockViews(*h->system, extra);
+    WVMutableIntegrationState state{{*t, t0, {mview(Ap, shape), mview(Am, shape), mview(A0, shape)}}, views.data(),
+                                    views.size()};
+    WVFixedStepRK4 rk4(*h->system);
+    auto status = rk4.prepareStateAfterRestart(state);
+    for (int i = 0; i < steps && status; ++i) status = rk4.step(state, dt);
+    if (!status) return sys_fail(h, status);
+    *t = state.waveVortex.t;
+    return 0;
+}
+
+// WVAdaptiveRK23 over the system (options as wvref_rk23_advance; counts =
+// {accepted, rejected, rhs evaluations, fsal reuses}).
+int wvref_system_rk23(void* sp, const double* opts, double* Ap, double* Am, double* A0, double* extra, double* t,
+                      double t0, double finalTime, double initialStep, unsigned long long* counts, double* nextStep,
+                      double* steps, int cap) {
+    auto* h = static_cast<RefSystem*>(sp);
+    const auto shape = h->system->stateLayout().coefficientShape();
+    auto views = blockViews(*h->system, extra);
+    WVMutableIntegrationState state{{*t, t0, {mview(Ap, shape), mview(Am, shape), mview(A0, shape)}}, views.data(),
+                                    views.size()};
+    WVAdaptiveRK23Options o;
+    o.relativeTolerance = opts[0];
+    o.absoluteToleranceScale = opts[1];
+    o.safetyFactor = opts[2];
+    o.rejectionFloorFactor = opts[3];
+    o.maximumStepFactor = opts[4];
+    o.maximumStepSize = opts[5];
+    WVAdaptiveRK23 rk(*h->system, o);
+    auto status = rk.prepareStateAfterRestart(state);
+    if (status) status = rk.advanceToTime(state, finalTime, initialStep);
+    if (!status) return sys_fail(h, status);
+    *t = state.waveVortex.t;
+    counts[0] = rk.metrics().acceptedStepCount;
+    counts[1] = rk.metrics().rejectedStepCount;
+    counts[2] = rk.metrics().rightHandSideEvaluationCount;
+    counts[3] = rk.metrics().fsalReuseCount;
+    *nextStep = rk.nextStepSize();
+    const auto& d = rk.stepDiagnostics();
+    for (int i = 0; i < cap && i < static_cast<int>(d.size()); ++i) steps[i] = d[i].acceptedStepSize;
     return 0;
 }
 

@@ -955,17 +955,17 @@ class RK23:
                 evals += 1
                 have_first = True
             k1 = self.k1
-            stage = [y[c] + (0.5 * h) * k1[c] for c in range(3)]
+            stage = [y[c] + (0.5 * h) * k1[c] for c in range(len(y))]
             k2 = self._eval(stage, t + 0.5 * h)
-            stage = [y[c] + (0.75 * h) * k2[c] for c in range(3)]
+            stage = [y[c] + (0.75 * h) * k2[c] for c in range(len(y))]
             k3 = self._eval(stage, t + 0.75 * h)
             s1, s2, s3 = h * (2.0 / 9.0), h * (1.0 / 3.0), h * (4.0 / 9.0)
-            cand = [((y[c] + s1 * k1[c]) + s2 * k2[c]) + s3 * k3[c] for c in range(3)]
+            cand = [((y[c] + s1 * k1[c]) + s2 * k2[c]) + s3 * k3[c] for c in range(len(y))]
             k4 = self._eval(cand, t + h)
             evals += 3
             b1, b2, b3 = self.B
             error = 0.0
-            for c in range(3):
+            for c in range(len(y)):
                 e = h * (((b1 * k1[c] + b2 * k2[c]) + b3 * k3[c]) - 0.125 * k4[c])
                 with np.errstate(divide="ignore", invalid="ignore"):
                     scale = np.maximum(self.atol[c], o["rtol"] * np.maximum(np.abs(y[c]), np.abs(cand[c])))
@@ -1031,12 +1031,220 @@ class RK23:
              (4.0 / 3.0) * t2 - (8.0 / 9.0) * t3 - 4.0 / 9.0, -t2 + t3)
         ks = (self.k1, self.k2, self.k3, self.k4)
         out = []
-        for c in range(3):
+        for c in range(len(end)):
             v = end[c].copy()
             for d in range(4):
                 v = v + (h * w[d]) * ks[d][c]
             out.append(v)
         return out
+
+
+def _wrapped(c, L):
+    """wrapped() of WVFieldEvaluationService.cpp:107-114."""
+    v = math.fmod(c, L)
+    if v < 0.0:
+        v += L
+    if v >= L:
+        v = 0.0
+    return v
+
+
+def particle_velocity_linear(desc, fields, x, y, z, nch):
+    """Linear branch of evaluateMovingImpl (WVFieldEvaluationService.cpp:1951-1985):
+    trilinear interpolation of fields (3, Nz, Ny, Nx) at unwrapped (x, y) and z,
+    periodic in x and y, zero outside -Lz <= z <= 0.  Returns (nch, n)."""
+    c = desc.c
+    dx, dy, dz = c.Lx / c.Nx, c.Ly / c.Ny, c.Lz / (c.Nz - 1)
+    out = np.zeros((nch, len(x)))
+    for p in range(len(x)):
+        xx, yy, zz = _wrapped(float(x[p]), c.Lx), _wrapped(float(y[p]), c.Ly), float(z[p])
+        if not (-c.Lz <= zz <= 0.0):
+            continue
+        x0 = min(int(math.floor(xx / dx)), c.Nx - 1)
+        y0 = min(int(math.floor(yy / dy)), c.Ny - 1)
+        nz = (zz + c.Lz) / dz
+        z0 = min(int(max(0.0, math.floor(nz))), c.Nz - 2)
+        wx1 = (xx - x0 * dx) / dx
+        wy1 = (yy - y0 * dy) / dy
+        wz1 = min(max(nz - z0, 0.0), 1.0)
+        xi, yi = (x0, (x0 + 1) % c.Nx), (y0, (y0 + 1) % c.Ny)
+        wx, wy, wz = (1.0 - wx1, wx1), (1.0 - wy1, wy1), (1.0 - wz1, wz1)
+        for ch in range(nch):
+            v = 0.0
+            for iz in range(2):
+                for iy in range(2):
+                    for ix in range(2):
+                        v += float(fields[ch][z0 + iz, yi[iy], xi[ix]]) * wx[ix] * wy[iy] * wz[iz]
+            out[ch, p] = v
+    return out
+
+
+def spline_weights(n, origin, spacing, query, shift=0):
+    """SplineSystem::weightsInto (WVFieldEvaluationService.cpp:116-230): weights
+    over all n points of the not-a-knot cubic spline through uniform samples,
+    linear for n = 2 and quadratic for n = 3; `shift` rotates the result back
+    (restoreOriginalOrdering)."""
+    normalized = (query - origin) / spacing
+    if n == 2:
+        shifted = np.array([1.0 - normalized, normalized])
+    elif n == 3:
+        shifted = np.array([(normalized - 1.0) * (normalized - 2.0) / 2.0, -normalized * (normalized - 2.0),
+                            normalized * (normalized - 1.0) / 2.0])
+    else:
+        interval = 0 if normalized <= 0.0 else int(math.floor(normalized))
+        interval = min(interval, n - 2)
+        fraction = min(max(normalized - interval, 0.0), 1.0)
+        first, second = 1.0 - fraction, fraction
+        A = np.zeros((n, n))
+        A[0, :3] = (-1.0, 2.0, -1.0)
+        for r in range(1, n - 1):
+            A[r, r - 1:r + 2] = (1.0, 4.0, 1.0)
+        A[n - 1, n - 3:] = (-1.0, 2.0, -1.0)
+        rhs = np.zeros(n)
+        rhs[interval] = (first ** 3 - first) * spacing * spacing / 6.0
+        rhs[interval + 1] = (second ** 3 - second) * spacing * spacing / 6.0
+        cvec = np.linalg.solve(A.T, rhs)
+        shifted = np.zeros(n)
+        shifted[interval] += first
+        shifted[interval + 1] += second
+        scale = 6.0 / (spacing * spacing)
+        for r in range(1, n - 1):
+            shifted[r - 1] += scale * cvec[r]
+            shifted[r] -= 2.0 * scale * cvec[r]
+            shifted[r + 1] += scale * cvec[r]
+    out = np.zeros(n)
+    for s in range(n):
+        out[(s + n - shift % n) % n] += shifted[s]
+    return out
+
+
+def particle_velocity_spline(desc, fields, x, y, z, nch):
+    """Spline branch of evaluateMovingImpl (WVFieldEvaluationService.cpp:1986-2016):
+    x and y move four cells away from the periodic seam when within three
+    cells of it, weights over the whole grid, value = sum f wx wy wz."""
+    c = desc.c
+    dx, dy, dz = c.Lx / c.Nx, c.Ly / c.Ny, c.Lz / (c.Nz - 1)
+    out = np.zeros((nch, len(x)))
+    for p in range(len(x)):
+        xx, yy, zz = _wrapped(float(x[p]), c.Lx), _wrapped(float(y[p]), c.Ly), float(z[p])
+        if not (-c.Lz <= zz <= 0.0):
+            continue
+        xl = min(int(math.floor(xx / dx)), c.Nx - 1)
+        yl = min(int(math.floor(yy / dy)), c.Ny - 1)
+        xb = xl < 3 or xl > c.Nx - 4
+        yb = yl < 3 or yl > c.Ny - 4
+        xq = _wrapped(xx + 4.0 * dx, c.Lx) if xb else xx
+        yq = _wrapped(yy + 4.0 * dy, c.Ly) if yb else yy
+        if not (xq <= (c.Nx - 1) * dx and yq <= (c.Ny - 1) * dy):
+            continue
+        wx = spline_weights(c.Nx, 0.0, dx, xq, 4 if xb else 0)
+        wy = spline_weights(c.Ny, 0.0, dy, yq, 4 if yb else 0)
+        wz = spline_weights(c.Nz, -c.Lz, dz, zz, 0)
+        for ch in range(nch):
+            out[ch, p] = float(np.einsum("zyx,x,y,z->", fields[ch], wx, wy, wz))
+    return out
+
+
+@dataclass
+class ParticleGroup:
+    """A WVLagrangianParticles observer: x, y (and z unless xy_only) state
+    blocks; z holds the fixed depths of an xy-only group."""
+
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    xy_only: bool = False
+    spline: bool = False
+    horizontal_tolerance: float = 1e-5
+    vertical_tolerance: float = 1e-6
+
+
+@dataclass
+class Tracer:
+    """A three-dimensional WVTracer observer."""
+
+    antialias: bool = True
+    tolerance: float = 1e-8
+
+
+def system_state(desc, Ap, Am, A0, groups, tracers):
+    """Initial integration state [Ap, Am, A0, blocks...] with the particle
+    positions of each group (x, y[, z]) and one (Nz, Ny, Nx) field per tracer."""
+    y = [Ap, Am, A0]
+    for g in groups:
+        y += [np.array(g.x, float), np.array(g.y, float)] + ([] if g.xy_only else [np.array(g.z, float)])
+    for tr, field in tracers:
+        y.append(np.array(field, float))
+    return y
+
+
+def system_rhs(desc, y, t, t0, groups, tracers, damping=None):
+    """WVConstantStratificationIntegrationSystem::evaluateRightHandSide
+    (PortableRuntime/src/WVConstantStratificationIntegrationSystem.cpp:295-400):
+    the scheduled flux, then each particle group's velocity at its positions and
+    each tracer's F-grid advection, all from the advection fields (u, v, w) of
+    the state.  `tracers` is a list of Tracer (their fields are in y)."""
+    Ap, Am, A0 = y[0], y[1], y[2]
+    out = list(rhs(desc, Ap, Am, A0, t, t0, damping))
+    adv = velocity_fields(desc, Ap, Am, A0, t, t0)
+    i = 3
+    for g in groups:
+        px, py = y[i], y[i + 1]
+        pz = np.asarray(g.z, float) if g.xy_only else y[i + 2]
+        nch = 2 if g.xy_only else 3
+        vel = (particle_velocity_spline if g.spline else particle_velocity_linear)(desc, adv, px, py, pz, nch)
+        out += [vel[c] for c in range(nch)]
+        i += nch
+    for tr in tracers:
+        out.append(advect_fgrid_scalar(desc, y[i], adv, tr.antialias))
+        i += 1
+    return out
+
+
+def system_rk4(desc, y, t, t0, h, steps, groups, tracers, damping=None):
+    """WVFixedStepRK4::step over the extended state (WVRungeKutta.cpp:335-462)."""
+    f = lambda v, tt: system_rhs(desc, v, tt, t0, groups, tracers, damping)
+    for _ in range(steps):
+        k = f(y, t)
+        wsum = [a.copy() for a in k]
+        st = [a + (0.5 * h) * b for a, b in zip(y, k)]
+        k = f(st, t + 0.5 * h)
+        wsum = [a + 2.0 * b for a, b in zip(wsum, k)]
+        st = [a + (0.5 * h) * b for a, b in zip(y, k)]
+        k = f(st, t + 0.5 * h)
+        wsum = [a + 2.0 * b for a, b in zip(wsum, k)]
+        st = [a + h * b for a, b in zip(y, k)]
+        k = f(st, t + h)
+        wsum = [a + 1.0 * b for a, b in zip(wsum, k)]
+        y = [a + (h / 6.0) * b for a, b in zip(y, wsum)]
+        t = t + h
+    return y, t
+
+
+def system_tolerances(desc, abs_scale, groups, tracers):
+    """Absolute tolerances of every state component (UnifiedErrorPolicy,
+    WVConstantStratificationIntegrationSystem.cpp:47-86): the coefficient
+    policy for A+, A-, A0, each block's uniform tolerance after them."""
+    wave, vortex = rk23_tolerances(desc, abs_scale)
+    tol = [wave, wave, vortex]
+    for g in groups:
+        n = len(g.x)
+        tol += [np.full(n, g.horizontal_tolerance)] * 2
+        if not g.xy_only:
+            tol.append(np.full(n, g.vertical_tolerance))
+    c = desc.c
+    for tr in tracers:
+        tol.append(np.full((c.Nz, c.Ny, c.Nx), tr.tolerance))
+    return tol
+
+
+def system_rk23_advance(desc, y, t, t0, final, initial, groups, tracers, damping=None, **options):
+    """Adaptive RK23 over the extended state; returns (y, t, integrator)."""
+    o = {**RK23_DEFAULTS, **options}
+    tol = system_tolerances(desc, o["atol_scale"], groups, tracers)
+    rk = RK23(lambda v, tt: system_rhs(desc, v, tt, t0, groups, tracers, damping), tol, **options)
+    y, t = rk.advance_to_time(y, t, final, initial)
+    return y, t, rk
 
 
 def rk23_advance(desc, Ap, Am, A0, t, t0, final, initial, damping=None, **options):

@@ -60,3 +60,39 @@ def rk23_run(key):
     out = {n: g[f"{key}_{n}"] for n in ("Ap", "Am", "A0", "Kp", "Km", "K0", "diag", "counts", "hashes", "dense")}
     out.update({n: float(g[f"{key}_{n}"]) for n in ("t", "t0", "final", "initial", "tout", "next", "dense_time")})
     return cf, options, out
+
+
+def system_run(key):
+    """Inputs and reference outputs of one integrated-observer fixture run
+    (tests/golden/system.npz): (case config, run spec, arrays)."""
+    with open(os.path.join(GOLDEN, "system_runs.json")) as fh:
+        run = json.load(fh)[key]
+    g = load_golden("system")
+    arrays = {k[len(key) + 1:]: g[k] for k in g.files if k.startswith(key + "_")}
+    return golden_cases()[run["case"]], run, arrays
+
+
+def system_observers(run):
+    """Oracle particle groups and tracers of a fixture run."""
+    groups = [O.ParticleGroup(x=np.array(g["x"]), y=np.array(g["y"]), z=np.array(g["z"]), xy_only=g["xy_only"],
+                              spline=g["spline"], horizontal_tolerance=g["tol_h"], vertical_tolerance=g["tol_v"])
+              for g in run["groups"]]
+    tracers = [O.Tracer(antialias=t["antialias"], tolerance=t["tol"]) for t in run["tracers"]]
+    return groups, tracers
+
+
+def split_extra(desc, groups, tracers, extra):
+    """Packed additional state -> list of blocks (particles 1-D, tracers (Nz, Ny, Nx))."""
+    c = desc.c
+    out, off = [], 0
+    for g in groups:
+        n = len(g.x)
+        for _ in range(2 if g.xy_only else 3):
+            out.append(np.asarray(extra[off:off + n]))
+            off += n
+    R = c.Nx * c.Ny * c.Nz
+    for _ in tracers:
+        out.append(np.asarray(extra[off:off + R]).reshape(c.Nz, c.Ny, c.Nx))
+        off += R
+    assert off == len(extra)
+    return out

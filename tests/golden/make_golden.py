@@ -7,7 +7,8 @@ The outputs are written as .npz files next to this script; tests compare the
 numpy oracle (oracle/wv_oracle.py) and the GPU path against them.
 
 Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT] [--rk23]
-        (--rk23 regenerates only the adaptive RK23 fixture, rk23.npz)
+        (--rk23 regenerates only the adaptive RK23 fixture, rk23.npz;
+         --system only the integrated-observer fixture, system.npz)
 """
 from __future__ import annotations
 
@@ -335,9 +336,128 @@ def make_rk23(lib):
     np.savez_compressed(os.path.join(HERE, "rk23.npz"), **out)
 
 
+# Integration systems with integrated observers (particle groups and tracers)
+# through the reference's WVConstantStratificationIntegrationSystem: one RHS,
+# RK4 steps and an adaptive RK23 interval per case.
+SYSTEM_RUNS = {
+    # the reference's own particle test grid and observers
+    # (PortableRuntime/tests/TestWVLagrangianParticles.cpp:86-205)
+    "obs": dict(case="rk_6x5x7", schedule=0, coeff="fixture", t=0.25, t0=-0.5, dt=20.0, steps=3,
+                groups=[dict(x=[-10.0, 1000.0, 15003.0], y=[20.0, -100.0, 2000.0], z=[-100.0, -300.0, -500.0],
+                             xy_only=True, spline=False, tol_h=1e-5, tol_v=1e-6),
+                        dict(x=[200.0, 3000.0], y=[400.0, 5000.0], z=[-200.0, -900.0], xy_only=False, spline=True,
+                             tol_h=1e-5, tol_v=1e-6)],
+                tracers=[dict(antialias=True, tol=1e-8, scale=1.0), dict(antialias=False, tol=1e-8, scale=0.5)],
+                rk23=dict(final=60.25, initial=30.0, opts=(1e-6, 1e-8, 0.8, 0.5, 5.0, float("inf")))),
+    # hydrostatic with adaptive damping, a linear volume group and a spline xy group
+    "hd": dict(case="hydro_damp_12x10x11", schedule=1, coeff="seeded", t=3.0, t0=1.0, dt=5.0, steps=2,
+               groups=[dict(x=[1000.0, 17000.0, 29500.0, -400.0], y=[300.0, 12000.0, 24900.0, 5000.0],
+                            z=[-100.0, -1000.0, -1999.0, -50.0], xy_only=False, spline=False, tol_h=1e-4, tol_v=1e-5),
+                       dict(x=[2600.0, 14100.0, 31000.0], y=[100.0, 9000.0, -2300.0], z=[-300.0, -700.0, -1500.0],
+                            xy_only=True, spline=True, tol_h=1e-4, tol_v=1e-5)],
+               tracers=[dict(antialias=True, tol=1e-7, scale=2.0)],
+               rk23=dict(final=9.0, initial=10.0, opts=(1e-4, 1e-6, 0.8, 0.5, 5.0, 4.0))),
+}
+
+
+def tracer_field(case, scale):
+    """initializeTracer of TestWVLagrangianParticles.cpp:271-290 as (Nz, Ny, Nx)."""
+    Nx, Ny, Nz = case["Nx"], case["Ny"], case["Nz"]
+    z, y, x = np.meshgrid(np.arange(Nz), np.arange(Ny), np.arange(Nx), indexing="ij")
+    return scale * (np.sin(2.0 * np.pi * x / Nx) + 0.25 * np.cos(2.0 * np.pi * y / Ny) + 0.1 * np.cos(np.pi * z / (Nz - 1)))
+
+
+def fixture_coefficients(M):
+    """The coefficient pattern of the reference's particle test fixture
+    (TestWVLagrangianParticles.cpp:221-231), as three (M,) complex arrays."""
+    v = np.arange(1, M + 1, dtype=float)
+    return (1e-4 * np.sin(0.17 * v) + 1e-4j * np.cos(0.11 * v), 1e-4 * np.cos(0.13 * v) - 1e-4j * np.sin(0.19 * v),
+            1e-4 * np.sin(0.07 * v) + 1e-4j * np.cos(0.23 * v))
+
+
+def make_system(lib):
+    lib.wvref_system_message.restype = ctypes.c_char_p
+    lib.wvref_system_extra.restype = ctypes.c_uint64
+    out = {}
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for key, run in SYSTEM_RUNS.items():
+        case = CASES[run["case"]]
+        r = Ref(lib, case)
+        shape = (r.Nkl, case["Nj"])
+        if run["coeff"] == "fixture":
+            Ap, Am, A0 = (a.reshape(shape) for a in fixture_coefficients(r.M))
+        else:
+            base = sum(ord(ch) for ch in run["case"]) + 200
+            Ap, Am, A0 = (seeded(shape, base + i, 1e-3) for i in (1, 2, 3))
+        lib.wvref_destroy(r.h)
+        v = {**BASE, **{k: case[k] for k in case if k in BASE}}
+        sizes = (ctypes.c_uint64 * 4)(case["Nx"], case["Ny"], case["Nz"], case["Nj"])
+        values = (ctypes.c_double * 9)(case["Lx"], case["Ly"], case["Lz"], v["N0"], v["rho0"], v["g"],
+                                       v["planetaryRadius"], v["rotationRate"], case["latitude"])
+        flags = (ctypes.c_uint8 * 2)(int(case["isHydrostatic"]), int(case["shouldAntialias"]))
+        G = run["groups"]
+        T = run["tracers"]
+        ints = lambda vals: (ctypes.c_int * max(1, len(vals)))(*vals)
+        dbls = lambda vals: (ctypes.c_double * max(1, len(vals)))(*vals)
+        xs = [a for g in G for a in g["x"]]
+        ys = [a for g in G for a in g["y"]]
+        zs = [a for g in G for a in g["z"]]
+        h = ctypes.c_void_p()
+        rc = lib.wvref_system_create(sizes, values, flags, run["schedule"], len(G), ints([len(g["x"]) for g in G]),
+                                     ints([int(g["xy_only"]) for g in G]), ints([int(g["spline"]) for g in G]),
+                                     dbls([g["tol_h"] for g in G]), dbls([g["tol_v"] for g in G]), dbls(xs), dbls(ys),
+                                     dbls(zs), len(T), ints([int(t["antialias"]) for t in T]), dbls([t["tol"] for t in T]),
+                                     ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"system create failed: {rc} {lib.wvref_system_message(h)}")
+        extra = []
+        for g in G:
+            extra += [np.array(g["x"]), np.array(g["y"])] + ([] if g["xy_only"] else [np.array(g["z"])])
+        tracer_fields = [tracer_field(case, t["scale"]) for t in T]
+        extra += [f.ravel() for f in tracer_fields]
+        ex = np.ascontiguousarray(np.concatenate(extra))
+        assert ex.size == lib.wvref_system_extra(h)
+        Ap, Am, A0 = (np.ascontiguousarray(a) for a in (Ap, Am, A0))
+        F = [np.zeros(shape, np.complex128) for _ in range(3)]
+        er = np.zeros_like(ex)
+        chk = lambda rc: (_ for _ in ()).throw(RuntimeError(lib.wvref_system_message(h).decode())) if rc else None
+        chk(lib.wvref_system_rhs(h, ctypes.c_double(run["t"]), ctypes.c_double(run["t0"]), P(Ap), P(Am), P(A0), P(ex),
+                                 P(F[0]), P(F[1]), P(F[2]), P(er)))
+        Kp, Km, K0, kex = Ap.copy(), Am.copy(), A0.copy(), ex.copy()
+        tt = ctypes.c_double(run["t"])
+        chk(lib.wvref_system_rk4(h, P(Kp), P(Km), P(K0), P(kex), ctypes.byref(tt), ctypes.c_double(run["t0"]),
+                                 ctypes.c_double(run["dt"]), ctypes.c_int(run["steps"])))
+        rk = run["rk23"]
+        Rp, Rm, R0, rex = Ap.copy(), Am.copy(), A0.copy(), ex.copy()
+        t23 = ctypes.c_double(run["t"])
+        counts = (ctypes.c_ulonglong * 4)()
+        nxt = ctypes.c_double()
+        steps = np.zeros(4096)
+        chk(lib.wvref_system_rk23(h, (ctypes.c_double * 6)(*rk["opts"]), P(Rp), P(Rm), P(R0), P(rex), ctypes.byref(t23),
+                                  ctypes.c_double(run["t0"]), ctypes.c_double(rk["final"]), ctypes.c_double(rk["initial"]),
+                                  counts, ctypes.byref(nxt), P(steps), ctypes.c_int(4096)))
+        counts = np.array(list(counts), np.uint64)
+        lib.wvref_system_destroy(h)
+        out.update({f"{key}_Ap": Ap, f"{key}_Am": Am, f"{key}_A0": A0, f"{key}_extra": ex, f"{key}_t": run["t"],
+                    f"{key}_t0": run["t0"], f"{key}_Fp": F[0], f"{key}_Fm": F[1], f"{key}_F0": F[2], f"{key}_rhs_extra": er,
+                    f"{key}_dt": run["dt"], f"{key}_steps": run["steps"], f"{key}_Kp": Kp, f"{key}_Km": Km, f"{key}_K0": K0,
+                    f"{key}_k_extra": kex, f"{key}_k_t": tt.value, f"{key}_rk23_final": rk["final"],
+                    f"{key}_rk23_initial": rk["initial"], f"{key}_rk23_opts": np.array(rk["opts"]), f"{key}_Rp": Rp,
+                    f"{key}_Rm": Rm, f"{key}_R0": R0, f"{key}_r_extra": rex, f"{key}_r_t": t23.value,
+                    f"{key}_r_counts": counts, f"{key}_r_next": nxt.value, f"{key}_r_steps": steps[:int(counts[0])].copy()})
+        print(f"system {key}: rk23 counts {counts.tolist()}")
+    with open(os.path.join(HERE, "system_runs.json"), "w") as fh:
+        json.dump(SYSTEM_RUNS, fh, indent=1, sort_keys=True)
+    np.savez_compressed(os.path.join(HERE, "system.npz"), **out)
+
+
 if __name__ == "__main__":
+    root = next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")
     if "--rk23" in sys.argv:
-        make_rk23(load_lib(next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")))
+        make_rk23(load_lib(root))
+    elif "--system" in sys.argv:
+        make_system(load_lib(root))
     else:
         main()
-        make_rk23(load_lib(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+        make_rk23(load_lib(root))
+        make_system(load_lib(root))

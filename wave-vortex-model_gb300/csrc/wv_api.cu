@@ -1118,6 +1118,23 @@ const Descriptor& handle_descriptor(const wv_handle* h) { return h->desc; }
 int handle_device(const wv_handle* h) { return h->device; }
 void* handle_stream(const wv_handle* h) { return h->stream; }
 bool handle_is_single_state(const wv_handle* h) { return h->dd.members == 1; }
+
+int scheduled_rhs_with_fields(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
+                              double* Fp, double* Fm, double* F0, double* fields, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    int rc = check_times(h, t, t0); if (rc) return rc;
+    rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
+    if (!fields) return fail(h, WV_INVALID_POINTER, "Advection fields pointer must be nonnull.");
+    if (!(h->forcing & WV_FORCING_NONLINEAR_ADVECTION))
+        return fail(h, WV_UNSUPPORTED_OPERATION, "Integrated observers need the nonlinear advection schedule.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    cudaSetDevice(h->device);
+    const bool damping = (h->forcing & WV_FORCING_ADAPTIVE_DAMPING) != 0;
+    const cudaError_t e = flux_any(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, static_cast<cudaStream_t>(stream), nullptr, fields);
+    h->metrics.rhs_evaluations++;
+    return finish(h, e, "right-hand side");
+}
 }  // namespace wvgpu
 
 extern "C" {

@@ -111,6 +111,16 @@ class _RK23Metrics(ctypes.Structure):
                                                "next_step_size")] + [("workspace_bytes", ctypes.c_uint64)]
 
 
+class _ParticleGroup(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_uint64), ("xy_only", ctypes.c_int), ("interpolation", ctypes.c_int),
+                ("z_fixed", ctypes.c_void_p), ("horizontal_tolerance", ctypes.c_double),
+                ("vertical_tolerance", ctypes.c_double)]
+
+
+class _Tracer(ctypes.Structure):
+    _fields_ = [("antialias", ctypes.c_int), ("absolute_tolerance", ctypes.c_double)]
+
+
 @dataclass
 class Configuration:
     """WVTransformConstantStratificationConfiguration (WVKernelTypes.hpp:129-146)."""
@@ -223,6 +233,21 @@ def load_library():
     lib.wv_rk23_get_diagnostics.argtypes = [P, ctypes.POINTER(_RK23Diagnostic), ctypes.c_uint64,
                                             ctypes.POINTER(ctypes.c_uint64)]
     lib.wv_rk23_tolerance_hash.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    lib.wv_rk23_create_for_system.argtypes = [P, ctypes.POINTER(_RK23Options), ctypes.POINTER(P)]
+    lib.wv_rk23_system_step_device.argtypes = [P, P, ctypes.POINTER(D), D, D, P]
+    lib.wv_rk23_system_advance_to_time_device.argtypes = [P, P, ctypes.POINTER(D), D, D, D, P]
+    lib.wv_rk23_system_dense_output_device.argtypes = [P, D, P, P]
+    lib.wv_system_create.argtypes = [P, ctypes.POINTER(_ParticleGroup), ctypes.c_int, ctypes.POINTER(_Tracer), ctypes.c_int,
+                                     ctypes.POINTER(P)]
+    lib.wv_system_destroy.argtypes = [P]
+    lib.wv_system_destroy.restype = None
+    lib.wv_system_last_message.argtypes = [P]
+    lib.wv_system_last_message.restype = ctypes.c_char_p
+    lib.wv_system_get_layout.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64), P, P,
+                                         ctypes.c_uint64]
+    lib.wv_system_rhs_device.argtypes = [P, D, D, P, P, P]
+    lib.wv_system_rk4_device.argtypes = [P, P, ctypes.POINTER(D), D, D, ctypes.c_int, P]
+    lib.wv_system_rk4.argtypes = [P, P, ctypes.POINTER(D), D, D, ctypes.c_int]
     _lib = lib
     return lib
 
@@ -244,7 +269,10 @@ def exported_symbols():
             "wv_rk23_default_options", "wv_rk23_create", "wv_rk23_destroy", "wv_rk23_last_message",
             "wv_rk23_prepare_after_restart", "wv_rk23_step_device", "wv_rk23_advance_to_time_device",
             "wv_rk23_advance_to_time", "wv_rk23_dense_output_device", "wv_rk23_next_step_size",
-            "wv_rk23_last_accepted_step", "wv_rk23_get_metrics", "wv_rk23_get_diagnostics", "wv_rk23_tolerance_hash"]
+            "wv_rk23_last_accepted_step", "wv_rk23_get_metrics", "wv_rk23_get_diagnostics", "wv_rk23_tolerance_hash",
+            "wv_rk23_create_for_system", "wv_rk23_system_step_device", "wv_rk23_system_advance_to_time_device",
+            "wv_rk23_system_dense_output_device", "wv_system_create", "wv_system_destroy", "wv_system_last_message",
+            "wv_system_get_layout", "wv_system_rhs_device", "wv_system_rk4_device", "wv_system_rk4"]
 
 
 def describe(configuration: Configuration):
@@ -729,11 +757,19 @@ class WVAdaptiveRK23:
     controllerIdentifier = "matlab-ode23-v1"
 
     def __init__(self, kernel, options: WVAdaptiveRK23Options | None = None):
-        self.kernel = kernel
+        """kernel: a WVTransformConstantStratificationKernel (coefficient state) or a
+        WVConstantStratificationIntegrationSystem (packed state with particles and
+        tracers; step / advanceToTime / evaluateDenseOutput then take and return
+        the packed CUDA state)."""
+        self.system = kernel if isinstance(kernel, WVConstantStratificationIntegrationSystem) else None
+        self.kernel = self.system.kernel if self.system else kernel
         self.options = options or WVAdaptiveRK23Options()
-        self._lib = kernel._lib
+        self._lib = self.kernel._lib
         h = ctypes.c_void_p()
-        rc = self._lib.wv_rk23_create(kernel._h, ctypes.byref(self.options._c()), ctypes.byref(h))
+        if self.system:
+            rc = self._lib.wv_rk23_create_for_system(self.system._h, ctypes.byref(self.options._c()), ctypes.byref(h))
+        else:
+            rc = self._lib.wv_rk23_create(self.kernel._h, ctypes.byref(self.options._c()), ctypes.byref(h))
         if rc != 0:
             raise WVKernelError(rc, "Adaptive RK23 creation failed (options, tolerances or device allocation).")
         self._h = h
@@ -756,17 +792,41 @@ class WVAdaptiveRK23:
     def prepareStateAfterRestart(self):
         self._check(self._lib.wv_rk23_prepare_after_restart(self._h))
 
-    def step(self, Ap, Am, A0, t, t0, proposedStepSize):
-        """One accepted step of the CUDA state (in place); returns the new time."""
+    def step(self, *args):
+        """step(Ap, Am, A0, t, t0, proposedStepSize), or step(state, t, t0,
+        proposedStepSize) for a system: one accepted step of the CUDA state (in
+        place); returns the new time."""
+        if self.system:
+            state, t, t0, h = args
+            self.system._check_state(state)
+            tt = ctypes.c_double(float(t))
+            self._check(self._lib.wv_rk23_system_step_device(self._h, state.data_ptr(), ctypes.byref(tt), float(t0),
+                                                             float(h), self.kernel._stream()))
+            return tt.value
+        return self._step(*args)
+
+    def _step(self, Ap, Am, A0, t, t0, proposedStepSize):
         Ap, Am, A0 = (self.kernel._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
         tt = ctypes.c_double(float(t))
         self._check(self._lib.wv_rk23_step_device(self._h, Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(), ctypes.byref(tt),
                                                   float(t0), float(proposedStepSize), self.kernel._stream()))
         return tt.value
 
-    def advanceToTime(self, Ap, Am, A0, t, t0, finalTime, initialStepSize):
-        """Advances to finalTime.  torch CUDA states in place (returns finalTime);
-        numpy states are copied (returns (Ap, Am, A0, finalTime))."""
+    def advanceToTime(self, *args):
+        """advanceToTime(Ap, Am, A0, t, t0, finalTime, initialStepSize): torch CUDA
+        states in place (returns finalTime); numpy states are copied (returns (Ap,
+        Am, A0, finalTime)).  For a system: advanceToTime(state, t, t0, finalTime,
+        initialStepSize) on the packed CUDA state."""
+        if self.system:
+            state, t, t0, final, h = args
+            self.system._check_state(state)
+            tt = ctypes.c_double(float(t))
+            self._check(self._lib.wv_rk23_system_advance_to_time_device(
+                self._h, state.data_ptr(), ctypes.byref(tt), float(t0), float(final), float(h), self.kernel._stream()))
+            return tt.value
+        return self._advance(*args)
+
+    def _advance(self, Ap, Am, A0, t, t0, finalTime, initialStepSize):
         tt = ctypes.c_double(float(t))
         if _is_torch(Ap):
             Ap, Am, A0 = (self.kernel._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
@@ -781,8 +841,14 @@ class WVAdaptiveRK23:
         return Ap, Am, A0, tt.value
 
     def evaluateDenseOutput(self, time):
-        """State at `time` inside the last accepted step (new CUDA tensors)."""
+        """State at `time` inside the last accepted step (new CUDA tensors; the
+        packed state for a system)."""
         import torch
+        if self.system:
+            out = torch.empty(self.system.state_doubles, dtype=torch.float64, device="cuda")
+            self._check(self._lib.wv_rk23_system_dense_output_device(self._h, float(time), out.data_ptr(),
+                                                                     self.kernel._stream()))
+            return out
         out = tuple(torch.empty(self.kernel.spectral_shape, dtype=torch.complex128, device="cuda") for _ in range(3))
         self._check(self._lib.wv_rk23_dense_output_device(self._h, float(time), *(o.data_ptr() for o in out),
                                                           self.kernel._stream()))
@@ -822,6 +888,135 @@ class WVAdaptiveRK23:
         comp = (ctypes.c_uint64 * 3)()
         self._check(self._lib.wv_rk23_tolerance_hash(self._h, ctypes.byref(h), comp))
         return h.value, list(comp)
+
+
+@dataclass
+class WVParticleGroup:
+    """WVLagrangianParticles (PortableRuntime/include/WaveVortexRuntime/WVLagrangianParticles.hpp):
+    initial positions x, y, z (z is the fixed depth of an xy-only group), the
+    interpolation of the advecting velocity ("linear" or "spline") and the
+    absolute tolerances of the position blocks."""
+
+    x: object
+    y: object
+    z: object
+    isXYOnly: bool = False
+    advectionInterpolation: str = "linear"
+    horizontalAbsoluteTolerance: float = 1e-5
+    verticalAbsoluteTolerance: float = 1e-6
+
+
+@dataclass
+class WVTracerSpec:
+    """A three-dimensional WVTracer (WVTracer.hpp)."""
+
+    shouldAntialias: bool = True
+    absoluteTolerance: float = 1e-8
+
+
+class WVConstantStratificationIntegrationSystem:
+    """Integration system with integrated observers on the GPU
+    (WVConstantStratificationIntegrationSystem,
+    PortableRuntime/src/WVConstantStratificationIntegrationSystem.cpp:112-400).
+    The packed state (float64 CUDA tensor of `state_doubles`) holds Ap, Am, A0
+    as interleaved complex, then for each particle group x, y[, z], then each
+    tracer's (Nz, Ny, Nx) field.  The kernel's forcing schedule applies and the
+    kernel must outlive the system."""
+
+    def __init__(self, kernel, particles=(), tracers=()):
+        self.kernel = kernel
+        self._lib = kernel._lib
+        self.particles = list(particles)
+        self.tracers = list(tracers)
+        self._z = [np.ascontiguousarray(np.asarray(g.z, dtype=np.float64)) for g in self.particles]
+        groups = (_ParticleGroup * max(1, len(self.particles)))()
+        for i, g in enumerate(self.particles):
+            interp = {"linear": 0, "spline": 1}[g.advectionInterpolation]
+            groups[i] = _ParticleGroup(len(np.asarray(g.x)), int(bool(g.isXYOnly)), interp,
+                                       self._z[i].ctypes.data if g.isXYOnly else None, float(g.horizontalAbsoluteTolerance),
+                                       float(g.verticalAbsoluteTolerance))
+        trs = (_Tracer * max(1, len(self.tracers)))()
+        for i, t in enumerate(self.tracers):
+            trs[i] = _Tracer(int(bool(t.shouldAntialias)), float(t.absoluteTolerance))
+        h = ctypes.c_void_p()
+        rc = self._lib.wv_system_create(kernel._h, groups, len(self.particles), trs, len(self.tracers), ctypes.byref(h))
+        if rc != 0:
+            raise WVKernelError(rc, "Integration system creation failed.")
+        self._h = h
+        n = ctypes.c_uint64()
+        nb = ctypes.c_uint64()
+        self._lib.wv_system_get_layout(h, ctypes.byref(n), ctypes.byref(nb), None, None, 0)
+        offs = np.zeros(max(1, nb.value), np.uint64)
+        lens = np.zeros(max(1, nb.value), np.uint64)
+        self._lib.wv_system_get_layout(h, None, None, offs.ctypes.data, lens.ctypes.data, nb.value)
+        self.state_doubles = int(n.value)
+        self.block_offsets = [int(v) for v in offs[:nb.value]]
+        self.block_lengths = [int(v) for v in lens[:nb.value]]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.wv_system_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WVKernelError(rc, self._lib.wv_system_last_message(self._h).decode())
+
+    def _check_state(self, state):
+        import torch
+        if state.dtype != torch.float64 or state.numel() != self.state_doubles or not state.is_contiguous() or not state.is_cuda:
+            raise WVKernelError(2, f"The packed state must be a contiguous float64 CUDA tensor of {self.state_doubles} values.")
+
+    def packState(self, Ap, Am, A0, tracerFields=()):
+        """Packed numpy state from coefficients, the groups' initial positions and
+        the tracers' initial fields (Nz, Ny, Nx)."""
+        parts = [np.ascontiguousarray(a, dtype=np.complex128).view(np.float64).ravel() for a in (Ap, Am, A0)]
+        for g in self.particles:
+            parts += [np.asarray(g.x, np.float64), np.asarray(g.y, np.float64)]
+            if not g.isXYOnly:
+                parts.append(np.asarray(g.z, np.float64))
+        parts += [np.asarray(f, np.float64).ravel() for f in tracerFields]
+        out = np.concatenate(parts)
+        if out.size != self.state_doubles:
+            raise WVKernelError(2, "Packed state does not match the system layout.")
+        return out
+
+    def unpackState(self, state):
+        """(Ap, Am, A0, [blocks]) views of a packed numpy state."""
+        state = np.asarray(state)
+        M2 = 2 * int(np.prod(self.kernel.spectral_shape))
+        coeff = [state[i * M2:(i + 1) * M2].view(np.complex128).reshape(self.kernel.spectral_shape) for i in range(3)]
+        return coeff[0], coeff[1], coeff[2], [state[o:o + n] for o, n in zip(self.block_offsets, self.block_lengths)]
+
+    def evaluateRightHandSide(self, t, t0, state):
+        """Right-hand side of the packed CUDA state (new tensor)."""
+        import torch
+        self._check_state(state)
+        out = torch.empty_like(state)
+        self._check(self._lib.wv_system_rhs_device(self._h, float(t), float(t0), state.data_ptr(), out.data_ptr(),
+                                                   self.kernel._stream()))
+        return out
+
+    def rk4(self, state, t, t0, dt, steps):
+        """WVFixedStepRK4 over the packed state: CUDA tensors in place (returns t),
+        numpy arrays copied (returns (state, t))."""
+        tt = ctypes.c_double(float(t))
+        if _is_torch(state):
+            self._check_state(state)
+            self._check(self._lib.wv_system_rk4_device(self._h, state.data_ptr(), ctypes.byref(tt), float(t0), float(dt),
+                                                       int(steps), self.kernel._stream()))
+            return tt.value
+        state = np.ascontiguousarray(state, dtype=np.float64).copy()
+        if state.size != self.state_doubles:
+            raise WVKernelError(2, "Packed state does not match the system layout.")
+        self._check(self._lib.wv_system_rk4(self._h, state.ctypes.data, ctypes.byref(tt), float(t0), float(dt), int(steps)))
+        return state, tt.value
 
 
 # ---------------------------------------------------------------------------

@@ -23,7 +23,7 @@ LIB = os.path.join(HERE, "libwvgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["wv_descriptor.cpp", "wv_plan.cpp"]
-CUDA_SOURCES = ["wv_api.cu", "wv_rk23.cu"]
+CUDA_SOURCES = ["wv_api.cu", "wv_rk23.cu", "wv_system.cu"]
 
 
 def _nvcc():
