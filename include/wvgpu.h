@@ -55,8 +55,13 @@ typedef struct wv_config {
 
 /* Arithmetic of a handle.  FP64: the plain drop-in, every stage in double.
  * MIXED: FP32 xy transforms and quadratic products, FP64 phases, projections,
- * flux accumulation and RK4 stage accumulation. */
-enum { WV_PRECISION_FP64 = 0, WV_PRECISION_MIXED = 1 };
+ * flux accumulation and RK4 stage accumulation.
+ * FP32X2: the xy transforms, products and vertical contractions in paired FP32
+ * ("float-float", about 48 significand bits) on the FP32 pipe, FP64 phases,
+ * projections and RK4 -- FP64-class flux accuracy without the FP64 pipe.
+ * FP32X2 handles serve the flux, the scheduled RHS, RK4/RK23, forward and inverse
+ * transforms; other entry points return WV_UNSUPPORTED_OPERATION. */
+enum { WV_PRECISION_FP64 = 0, WV_PRECISION_MIXED = 1, WV_PRECISION_FP32X2 = 2 };
 
 /* Forcing schedule of the right-hand side (WVFrozenForcingSchedule entries
  * WVNonlinearAdvection and WVAdaptiveDamping, PortableRuntime/src/WVForcingEngine.cpp). */

@@ -24,6 +24,7 @@
 #include <new>
 #include <string>
 #include <vector>
+#include <type_traits>
 
 using wvgpu::Descriptor;
 using wvgpu::Plan;
@@ -225,7 +226,9 @@ std::vector<float> mixed_flux_projection(const wvgpu::Descriptor& d) {
     return out;
 }
 
-size_t elem_size(int precision) { return precision == WV_PRECISION_FP64 ? sizeof(double) : sizeof(float); }
+size_t elem_size(int precision) {
+    return precision == WV_PRECISION_FP64 ? sizeof(double) : precision == WV_PRECISION_MIXED ? sizeof(float) : sizeof(dev::ff);
+}
 
 // Scratch element counts (complex) of the flux pipeline.
 struct ScratchSizes { size_t z, y, p, f; };
@@ -255,7 +258,7 @@ inline size_t x_len(const Plan& p) { return p.Nx % 2 == 0 ? p.Nx / 2 : p.Nx; }
 template <typename T>
 size_t smem_xflux(const Plan& p) {
     const size_t nt = p.targets.count, L = x_len(p);
-    return (L + p.Nx + (4 + 2 * nt) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (3 + 3 * nt) * p.Nx * sizeof(T);
+    return (L + p.Nx + (4 + 2 * nt) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (3 + nt) * p.Nx * sizeof(T);
 }
 template <typename T>
 size_t smem_xc2r(const Plan& p, int nch) { return (x_len(p) + p.Nx + nch * p.kxColumns + 8 * x_len(p)) * sizeof(dev::cx<T>); }
@@ -308,6 +311,8 @@ inline int warp_ry(const Plan& p) {
     // FP64 stays on the shared-memory radix-4 Stockham kernels: on the FP64 pipe
     // the radix-2 shuffle stages (64-bit shuffles, the twiddle product evaluated
     // in every lane) cost more than the smem round trips they replace.
+    // Paired FP32 (8-byte T) also stays on Stockham: its register rows spill or
+    // lose occupancy (measured slower at 256x256x129).
     if (sizeof(T) == 8 || p.stockhamY || p.Ny % 32 != 0) return 0;
     const int r = static_cast<int>(p.Ny / 32);
     return (r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8 || r == 16) ? r : 0;
@@ -913,7 +918,8 @@ cudaError_t flux_any(wv_handle* h, double t, double t0, const double* Ap, const 
                      const double* advIn = nullptr) {
     return h->precision == WV_PRECISION_FP64
                ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut, advOut, advIn)
-               : launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut, advOut, advIn);
+               : h->precision == WV_PRECISION_MIXED ? launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut, advOut, advIn)
+                                                          : launch_flux<dev::ff>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, damping, s, physOut, advOut, advIn);
 }
 
 // Scheduled RHS on contiguous [3][M] complex state/flux buffers.
@@ -1037,6 +1043,13 @@ int check_state_flux(wv_handle* h, const double* Ap, const double* Am, const dou
 int finish(wv_handle* h, cudaError_t e, const char* where) {
     if (e != cudaSuccess) return cuda_fail(h, e, where);
     return WV_SUCCESS;
+}
+
+// Entry points whose kernels have no paired-FP32 form (adjoint, derivative
+// bundles, F-grid scalars, the static-scratch flux) reject FP32X2 handles.
+int reject_paired(wv_handle* h, const char* what) {
+    if (h->precision != WV_PRECISION_FP32X2) return WV_SUCCESS;
+    return fail(h, WV_UNSUPPORTED_OPERATION, std::string(what) + " is not available on FP32X2 handles.");
 }
 
 // ---- static scratch for callers that cannot allocate ------------------------------
@@ -1196,7 +1209,8 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     if (!out) return WV_INVALID_POINTER;
     *out = nullptr;
     if (!config) return WV_INVALID_POINTER;
-    if (precision != WV_PRECISION_FP64 && precision != WV_PRECISION_MIXED) return WV_INVALID_CONFIGURATION;
+    if (precision != WV_PRECISION_FP64 && precision != WV_PRECISION_MIXED && precision != WV_PRECISION_FP32X2)
+        return WV_INVALID_CONFIGURATION;
     if (members < 1) return WV_INVALID_CONFIGURATION;
     wv_handle* h = new (std::nothrow) wv_handle();
     if (!h) return WV_ALLOCATION_FAILURE;
@@ -1261,6 +1275,14 @@ static int create_handle(const wv_config* config, int precision, int members, wv
         if (e != cudaSuccess) return;
         if (precision == WV_PRECISION_FP64) {
             const double* q = nullptr; e = upload(h, v, &q); *dst = q;
+        } else if (precision == WV_PRECISION_FP32X2) {
+            std::vector<float> f(2 * v.size());  // (hi, lo) pairs
+            for (size_t i = 0; i < v.size(); ++i) {
+                const dev::ff x(v[i]);
+                f[2 * i] = x.hi;
+                f[2 * i + 1] = x.lo;
+            }
+            const float* q = nullptr; e = upload(h, f, &q); *dst = q;
         } else {
             const std::vector<float> f = cast<float>(v);
             const float* q = nullptr; e = upload(h, f, &q); *dst = q;
@@ -1332,8 +1354,12 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->kbuf = static_cast<double*>(tmp); }
     if (e == cudaSuccess) { e = alloc(h, stateBytes, &tmp); h->acc = static_cast<double*>(tmp); }
     if (e == cudaSuccess) { e = alloc(h, 4 * R * sizeof(double), &tmp); h->fields = static_cast<double*>(tmp); }
-    if (e == cudaSuccess) e = precision == WV_PRECISION_FP64 ? set_smem_limits<double>(p) : set_smem_limits<float>(p);
-    if (e == cudaSuccess) e = precision == WV_PRECISION_FP64 ? set_smem_limits_w<double>(p) : set_smem_limits_w<float>(p);
+    if (e == cudaSuccess)
+        e = precision == WV_PRECISION_FP64 ? set_smem_limits<double>(p)
+            : precision == WV_PRECISION_MIXED ? set_smem_limits<float>(p) : set_smem_limits<dev::ff>(p);
+    if (e == cudaSuccess)
+        e = precision == WV_PRECISION_FP64 ? set_smem_limits_w<double>(p)
+            : precision == WV_PRECISION_MIXED ? set_smem_limits_w<float>(p) : set_smem_limits_w<dev::ff>(p);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         const int code = e == cudaErrorMemoryAllocation ? WV_ALLOCATION_FAILURE : WV_FFT_PLAN_FAILURE;
@@ -1455,7 +1481,8 @@ int wv_inverse_device(wv_handle* h, double t, double t0, const double* Ap, const
     cudaSetDevice(h->device);
     const cudaError_t e = h->precision == WV_PRECISION_FP64
                               ? launch_inverse<double>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream))
-                              : launch_inverse<float>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream));
+                              : h->precision == WV_PRECISION_MIXED ? launch_inverse<float>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream))
+                                                                         : launch_inverse<dev::ff>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream));
     h->metrics.inverse_calls++;
     return finish(h, e, "inverse transform");
 }
@@ -1517,7 +1544,8 @@ int wv_inverse_uvw_device(wv_handle* h, double t, double t0, const double* Ap, c
     cudaSetDevice(h->device);
     const cudaError_t e = h->precision == WV_PRECISION_FP64
                               ? launch_inverse<double>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream), 3)
-                              : launch_inverse<float>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream), 3);
+                              : h->precision == WV_PRECISION_MIXED ? launch_inverse<float>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream), 3)
+                                                                         : launch_inverse<dev::ff>(h, t, t0, Ap, Am, A0, fields, static_cast<cudaStream_t>(stream), 3);
     h->metrics.inverse_calls++;
     return finish(h, e, "inverse transform");
 }
@@ -1579,7 +1607,8 @@ int wv_inverse_uvw(wv_handle* h, double t, double t0, const double* Ap, const do
     if (e == cudaSuccess)
         e = h->precision == WV_PRECISION_FP64
                 ? launch_inverse<double>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s, 3)
-                : launch_inverse<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s, 3);
+                : h->precision == WV_PRECISION_MIXED ? launch_inverse<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s, 3)
+                                                           : launch_inverse<dev::ff>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s, 3);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fields, h->fields, fb, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     h->metrics.inverse_calls++;
@@ -1589,6 +1618,7 @@ int wv_inverse_uvw(wv_handle* h, double t, double t0, const double* Ap, const do
 int wv_field_derivatives_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
                                 int field, double* out, void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "State-field derivatives"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (field < 0 || field > 3) return fail(h, WV_INVALID_CONFIGURATION, "Unknown dynamical field derivative target.");
     if (!Ap || !Am || !A0 || !out) return fail(h, WV_INVALID_POINTER, "Field derivatives received a null pointer.");
@@ -1609,6 +1639,7 @@ int wv_field_derivatives_device(wv_handle* h, double t, double t0, const double*
 int wv_family_derivatives_device(wv_handle* h, int ffamily, const double* Apm, const double* A0, double* fields,
                                  void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "Field-family derivatives"); if (rp) return rp; }
     if (!Apm || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Field-family derivatives received a null pointer.");
     if (h->dd.members != 1) return fail(h, WV_UNSUPPORTED_OPERATION, "Field-family derivatives are per single-state handle.");
     const size_t fb = 4 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
@@ -1626,6 +1657,7 @@ int wv_family_derivatives_device(wv_handle* h, int ffamily, const double* Apm, c
 
 int wv_family_derivatives(wv_handle* h, int ffamily, const double* Apm, const double* A0, double* fields) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "Field-family derivatives"); if (rp) return rp; }
     if (!Apm || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Field-family derivatives received a null pointer.");
     Guard g(h->busy);
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
@@ -1656,6 +1688,7 @@ static int scalar_entry_checks(wv_handle* h, const double* scalar, const double*
 int wv_advect_fgrid_scalar_device(wv_handle* h, const double* scalar, const double* fields, int antialias, double* rhs,
                                   void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "F-grid scalar advection"); if (rp) return rp; }
     int rc = scalar_entry_checks(h, scalar, fields, rhs); if (rc) return rc;
     Guard g(h->busy);
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
@@ -1670,6 +1703,7 @@ int wv_advect_fgrid_scalar_device(wv_handle* h, const double* scalar, const doub
 
 int wv_advect_fgrid_scalar(wv_handle* h, const double* scalar, const double* fields, int antialias, double* rhs) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "F-grid scalar advection"); if (rp) return rp; }
     int rc = scalar_entry_checks(h, scalar, fields, rhs); if (rc) return rc;
     Guard g(h->busy);
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
@@ -1694,6 +1728,7 @@ int wv_advect_fgrid_scalar(wv_handle* h, const double* scalar, const double* fie
 int wv_field_derivatives(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, int field,
                          double* out) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "State-field derivatives"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (field < 0 || field > 3) return fail(h, WV_INVALID_CONFIGURATION, "Unknown dynamical field derivative target.");
     if (!Ap || !Am || !A0 || !out) return fail(h, WV_INVALID_POINTER, "Field derivatives received a null pointer.");
@@ -1733,7 +1768,8 @@ int wv_forward_device(wv_handle* h, const double* fields, double t, double t0, d
     cudaSetDevice(h->device);
     const cudaError_t e = h->precision == WV_PRECISION_FP64
                               ? launch_forward<double>(h, fields, t, t0, Ap, Am, A0, static_cast<cudaStream_t>(stream))
-                              : launch_forward<float>(h, fields, t, t0, Ap, Am, A0, static_cast<cudaStream_t>(stream));
+                              : h->precision == WV_PRECISION_MIXED ? launch_forward<float>(h, fields, t, t0, Ap, Am, A0, static_cast<cudaStream_t>(stream))
+                                                                         : launch_forward<dev::ff>(h, fields, t, t0, Ap, Am, A0, static_cast<cudaStream_t>(stream));
     h->metrics.forward_calls++;
     return finish(h, e, "forward transform");
 }
@@ -1821,7 +1857,8 @@ int wv_inverse(wv_handle* h, double t, double t0, const double* Ap, const double
     if (e == cudaSuccess)
         e = h->precision == WV_PRECISION_FP64
                 ? launch_inverse<double>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s)
-                : launch_inverse<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s);
+                : h->precision == WV_PRECISION_MIXED ? launch_inverse<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s)
+                                                           : launch_inverse<dev::ff>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, h->fields, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fields, h->fields, fb, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     h->metrics.inverse_calls++;
@@ -1843,7 +1880,8 @@ int wv_forward(wv_handle* h, const double* fields, double t, double t0, double* 
     if (e == cudaSuccess)
         e = h->precision == WV_PRECISION_FP64
                 ? launch_forward<double>(h, h->fields, t, t0, h->flux, h->flux + M2, h->flux + 2 * M2, s)
-                : launch_forward<float>(h, h->fields, t, t0, h->flux, h->flux + M2, h->flux + 2 * M2, s);
+                : h->precision == WV_PRECISION_MIXED ? launch_forward<float>(h, h->fields, t, t0, h->flux, h->flux + M2, h->flux + 2 * M2, s)
+                                                           : launch_forward<dev::ff>(h, h->fields, t, t0, h->flux, h->flux + M2, h->flux + 2 * M2, s);
     double* out[] = {Ap, Am, A0};
     for (int c = 0; c < 3 && e == cudaSuccess; ++c)
         e = cudaMemcpyAsync(out[c], reinterpret_cast<char*>(h->flux) + c * cb, cb, cudaMemcpyDeviceToHost, s);
@@ -1897,6 +1935,7 @@ int wv_flux_vjp_device(wv_handle* h, double t, double t0, const double* Ap, cons
                        const double* Fpb, const double* Fmb, const double* F0b, double* Apb, double* Amb, double* A0b,
                        void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "The flux adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     const void* ptrs[] = {Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b};
     for (const void* q : ptrs) if (!q) return fail(h, WV_INVALID_POINTER, "Flux VJP received a null pointer.");
@@ -1913,6 +1952,7 @@ int wv_flux_vjp_device(wv_handle* h, double t, double t0, const double* Ap, cons
 int wv_inverse_vjp_device(wv_handle* h, double t, double t0, const double* fb, double* Apb, double* Amb, double* A0b,
                           void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "The inverse-transform adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (!fb || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "Inverse VJP received a null pointer.");
     Guard g(h->busy);
@@ -1945,6 +1985,7 @@ static cudaError_t scatter3(wv_handle* h, const double* src, double* a, double* 
 int wv_rk4_step_vjp_device(wv_handle* h, const double* Ap, const double* Am, const double* A0, double t, double t0, double dt,
                            double* Apb, double* Amb, double* A0b, void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "The RK4 adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (!Ap || !Am || !A0 || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "RK4 VJP received a null pointer.");
     if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
@@ -1962,6 +2003,7 @@ int wv_rk4_step_vjp_device(wv_handle* h, const double* Ap, const double* Am, con
 int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, const double* A0, double t, double t0, double dt,
                           int n, int K, double* Apb, double* Amb, double* A0b, void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "The RK4 adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (!Ap || !Am || !A0 || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "RK4 adjoint received a null pointer.");
     if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
@@ -2092,6 +2134,7 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
 int wv_nonlinear_flux_device_noalloc(wv_handle* h, double t, double t0, const double* Ap, const double* Am,
                                      const double* A0, double* Fp, double* Fm, double* F0, void* stream) {
     if (!h) return WV_INVALID_POINTER;
+    { const int rp = reject_paired(h, "The static-scratch flux"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
     size_t offs[5];
@@ -2238,6 +2281,7 @@ int wv_ensemble_create(const wv_config* configs, const int* members, int n_group
     if (!configs || !members) return WV_INVALID_POINTER;
     if (n_groups < 1 || n_groups > WV_ENSEMBLE_MAX_GROUPS) return WV_INVALID_CONFIGURATION;
     for (int g = 0; g < n_groups; ++g) if (members[g] < 1) return WV_INVALID_CONFIGURATION;
+    if (precision == WV_PRECISION_FP32X2) return WV_UNSUPPORTED_OPERATION;  // ensembles are FP64 or MIXED
     wv_ensemble* e = new (std::nothrow) wv_ensemble();
     if (!e) return WV_ALLOCATION_FAILURE;
     cudaGetDevice(&e->device);

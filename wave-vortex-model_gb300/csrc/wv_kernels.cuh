@@ -14,12 +14,15 @@
 //   vfwd   : per column: forward DCT-I/DST-I contraction, projection onto
 //            Ap/Am/A0 (projectFluxTargetMode, kernel.cpp:396-431), phase,
 //            adaptive damping, written as Fp/Fm/F0.
-// T is the working type of the xy stage (double for FP64 handles, float for
-// MIXED); phases, projections and accumulations are always double.
+// T is the working type of the xy stage and the vertical contractions
+// (double for FP64 handles, float for MIXED, the paired-FP32 ff for FP32X2);
+// phases, projections and accumulations are always double.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <cstdint>
+
+#include "wv_ff.cuh"
 
 namespace wvgpu {
 namespace dev {
@@ -27,7 +30,12 @@ namespace dev {
 template <typename T> struct cxt;
 template <> struct cxt<double> { using type = double2; };
 template <> struct cxt<float> { using type = float2; };
+template <> struct cxt<ff> { using type = ff2; };
 template <typename T> using cx = typename cxt<T>::type;
+// Minimum resident CTAs of the vertical forward kernel: paired FP32 trades a
+// few registers for a third CTA per SM (its FP32-pipe chains need the warps).
+template <typename T> struct VertOcc { static constexpr int value = 1; };
+template <> struct VertOcc<ff> { static constexpr int value = 3; };
 
 template <typename T> __device__ __forceinline__ cx<T> mk(T a, T b) { cx<T> r; r.x = a; r.y = b; return r; }
 template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
@@ -635,7 +643,8 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
     cx<T>* spec = twN + Nx;                           // [nIn][KX]
     cx<T>* bufA = spec + nIn * KX;                    // [8][L]
     cx<T>* bufB = bufA + 8 * L;
-    T* phys = reinterpret_cast<T*>(bufB + 8 * L);    // [nReal][Nx]
+    T* phys = reinterpret_cast<T*>(bufB + 8 * L);    // U, V, W [3][Nx], then S_q [nt][Nx]
+    T* S = phys + 3 * Nx;
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
     const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
     for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = twg[i];
@@ -654,6 +663,11 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
         else if (kind == 1) { ch = 4 + t; useK = false; } // q_y
         else { ch = 4 + nt + t; useK = false; }           // q_z
     };
+    const size_t R3 = (size_t)Nx * Ny * d.Nz;
+    // Rows in batches of 8 lines.  U, V, W stay in shared memory; each derivative
+    // row is folded into its target's product as soon as it is transformed,
+    // S_q = -(u q_x + v q_y + w q_z) accumulated in that order (one thread per x
+    // walks a batch's rows in order, so the order is the same for every x).
     for (int rb = 0; rb < nReal; rb += 8) {
         const int nr = min(8, nReal - rb);
         for (int i = threadIdx.x; i < nr * L; i += blockDim.x) {
@@ -664,41 +678,45 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
         }
         __syncthreads();
         cx<T>* res = fft_lines<T, true>(bufA, bufB, d.fx, nr, L, tw);
-        for (int i = threadIdx.x; i < nr * Nx; i += blockDim.x) {
-            const int li = i / Nx, x = i - li * Nx;
-            phys[(rb + li) * Nx + x] = c2r_sample<T>(d, res + li * L, x);
+        if (rb == 0) {
+            for (int i = threadIdx.x; i < 3 * Nx; i += blockDim.x) {
+                const int c = i / Nx, x = i - c * Nx;
+                const size_t g = (size_t)c * R3 + ((size_t)z * Ny + y) * Nx + x;
+                T v = c2r_sample<T>(d, res + c * L, x);
+                if (advIn) v = T(advIn[g]);
+                else if (advOut) advOut[g] = double(v);
+                phys[i] = v;
+            }
+            __syncthreads();
         }
-        __syncthreads();
-    }
-    if (advIn || advOut) {
-        const size_t R3 = (size_t)Nx * Ny * d.Nz;
-        for (int i = threadIdx.x; i < 3 * Nx; i += blockDim.x) {
-            const int c = i / Nx, x = i - c * Nx;
-            const size_t g = (size_t)c * R3 + ((size_t)z * Ny + y) * Nx + x;
-            if (advIn) phys[i] = T(advIn[g]);
-            else advOut[g] = double(phys[i]);
+        for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+            for (int li = (rb == 0 ? 3 : 0); li < nr; ++li) {
+                const int r = rb + li;
+                const T v = c2r_sample<T>(d, res + li * L, x);
+                if (physOut) physOut[(((size_t)z * nReal + r) * Ny + y) * Nx + x] = v;
+                const int t = (r - 3) / 3, kind = (r - 3) % 3;
+                const T p = phys[kind * Nx + x] * v;
+                S[t * Nx + x] = kind == 0 ? p : S[t * Nx + x] + p;
+            }
         }
         __syncthreads();
     }
     if (physOut)
-        for (int i = threadIdx.x; i < nReal * Nx; i += blockDim.x) {
+        for (int i = threadIdx.x; i < 3 * Nx; i += blockDim.x) {
             const int r = i / Nx, x = i - r * Nx;
             physOut[(((size_t)z * nReal + r) * Ny + y) * Nx + x] = phys[i];
         }
-    // quadratic products S_q = -(u q_x + v q_y + w q_z) and max horizontal speed
-    T* S = reinterpret_cast<T*>(bufA);  // [nt][Nx] reals (bufA holds 16 L >= 4 Nx reals)
     // max |u_h| (only when a consumer asked for it): max of u^2 + v^2, one sqrt
     // at the end -- sqrt is correctly rounded and monotone, so this equals the
     // max over points of sqrt(u^2 + v^2)
     const bool wantSpeed = maxSpeedBits != nullptr;
     double vmax2 = 0.0;
     for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
-        const T U = phys[0 * Nx + x], V = phys[1 * Nx + x], W = phys[2 * Nx + x];
-        for (int t = 0; t < nt; ++t) {
-            const T qx = phys[(3 + 3 * t) * Nx + x], qy = phys[(4 + 3 * t) * Nx + x], qz = phys[(5 + 3 * t) * Nx + x];
-            S[t * Nx + x] = -(U * qx + V * qy + W * qz);
+        for (int t = 0; t < nt; ++t) S[t * Nx + x] = -S[t * Nx + x];
+        if (wantSpeed) {
+            const T U = phys[x], V = phys[Nx + x];
+            vmax2 = fmax(vmax2, double(U) * double(U) + double(V) * double(V));
         }
-        if (wantSpeed) vmax2 = fmax(vmax2, double(U) * double(U) + double(V) * double(V));
     }
     __syncthreads();  // S complete before the forward real transforms read it
     if (wantSpeed) {
@@ -718,8 +736,7 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
         bufB[t * L + n] = r2c_line_entry<T>(d, S + t * Nx, n);
     }
     __syncthreads();
-    cx<T>* scratch = reinterpret_cast<cx<T>*>(phys);  // nReal*Nx reals >= 2*nt*L reals
-    cx<T>* res = fft_lines<T, false>(bufB, scratch, d.fx, nt, L, tw);
+    cx<T>* res = fft_lines<T, false>(bufB, bufA, d.fx, nt, L, tw);
     for (int i = threadIdx.x; i < nt * KX; i += blockDim.x) {
         const int t = i / KX, k = i - t * KX;
         pspec[(((size_t)z * nt + t) * Ny + y) * KX + k] = r2c_value<T>(d, res + t * L, k, twN);
@@ -842,7 +859,7 @@ template <typename T>
 struct cx2t { cx<T> p, q; };
 
 template <typename T, bool FLUX>
-__global__ void __launch_bounds__(256) k_vfwd(DescDev d, const cx<T>* __restrict__ fspec, int nch, double elapsed,
+__global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, const cx<T>* __restrict__ fspec, int nch, double elapsed,
                                              const double* __restrict__ Ap, const double* __restrict__ Am,
                                              const double* __restrict__ A0, const unsigned long long* __restrict__ maxSpeedBits,
                                              int applyDamping, double* __restrict__ Fp, double* __restrict__ Fm,

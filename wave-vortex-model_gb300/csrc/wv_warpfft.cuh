@@ -25,9 +25,15 @@ __host__ __device__ constexpr int brev_bits(int i, int bits) {
 }
 __host__ __device__ constexpr int ilog2c(int r) { return r <= 1 ? 0 : 1 + ilog2c(r >> 1); }
 
+__device__ __forceinline__ float shfl_xor_v(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double shfl_xor_v(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ ff shfl_xor_v(ff v, int m) {
+    return ff(__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m));
+}
+
 template <typename T>
 __device__ __forceinline__ cx<T> shfl_xor_cx(cx<T> v, int m) {
-    return mk<T>(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+    return mk<T>(shfl_xor_v(v.x, m), shfl_xor_v(v.y, m));
 }
 
 // multiply by exp(sigma * i pi / 2): -i (forward) or +i (inverse)
@@ -230,7 +236,7 @@ __device__ __forceinline__ void c2r_row(const DescDev& d, const cx<T>* h, bool u
 // or taken in place of the reconstructed ones (sample pair 2n, 2n+1 of the row
 // sits in register k of lane l with n = k + R brev5(l)).
 template <typename T, int R>
-__global__ void __launch_bounds__(256, 3) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
                                                 unsigned long long* __restrict__ maxSpeedBits, cx<T>* __restrict__ physOut,
                                                 double* __restrict__ advOut, const double* __restrict__ advIn) {
     constexpr int L = 32 * R;

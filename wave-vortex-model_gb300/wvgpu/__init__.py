@@ -29,6 +29,7 @@ LIB_PATH = os.path.join(HERE, "libwvgpu.so")
 CONTRACT_VERSION = 4
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_FP32X2 = 2
 FORCING_NONLINEAR_ADVECTION = 1
 FORCING_ADAPTIVE_DAMPING = 2
 
@@ -315,7 +316,7 @@ class WVTransformConstantStratificationKernel:
         lib = load_library()
         self.configuration = configuration
         self.precision = precision
-        p = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED}[precision]
+        p = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "fp32x2": PRECISION_FP32X2}[precision]
         h = ctypes.c_void_p()
         rc = lib.wv_create(ctypes.byref(configuration._c()), p, ctypes.byref(h))
         if rc != 0:
@@ -649,7 +650,7 @@ class WVEnsemble:
         self.configurations = list(configurations)
         self.members = [int(m) for m in members]
         self.precision = precision
-        p = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED}[precision]
+        p = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "fp32x2": PRECISION_FP32X2}[precision]
         G = len(self.configurations)
         cfgs = (_Config * G)(*(c._c() for c in self.configurations))
         mem = (ctypes.c_int * G)(*self.members)
