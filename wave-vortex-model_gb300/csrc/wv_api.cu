@@ -196,14 +196,14 @@ std::vector<uint16_t> tc_vertical_blob(const Plan& p, int NP, int KE, int K) {
 //   wave = Cu u + Cv v + Cw w,   b = Npm eta - B f0,   cp = wave + b,  cm = wave - b
 // Layout [M][12]: Cu.re Cu.im Cv.re Cv.im | Cw.re Cw.im Du Dv | Dn Npm B 0.
 // The inertial row (mode 0) keeps its own formula in the kernel.
-std::vector<float> mixed_flux_projection(const wvgpu::Descriptor& d) {
-    std::vector<float> out(12 * d.M, 0.0f);
+std::vector<double> mixed_flux_projection(const wvgpu::Descriptor& d) {
+    std::vector<double> out(12 * d.M, 0.0);
     const bool hydro = d.c.is_hydrostatic;
     const size_t Nj = d.c.Nj;
     for (size_t w = 0; w < d.Nkl; ++w) {
         for (size_t j = 0; j < Nj; ++j) {
             const size_t idx = j + Nj * w;
-            float* o = out.data() + 12 * idx;
+            double* o = out.data() + 12 * idx;
             double cu[2] = {0, 0}, cv[2] = {0, 0}, cw[2] = {0, 0};
             if (hydro) {
                 const double ar = d.ApmD[idx].real(), ai = d.ApmD[idx].imag();
@@ -214,13 +214,13 @@ std::vector<float> mixed_flux_projection(const wvgpu::Descriptor& d) {
                 cv[0] = d.sinAlpha[w] * d.ApmDScaled[idx];
                 cw[1] = (d.Kh[w] / 2.0) * d.apmWProjectionPrefactor[j];
             }
-            o[0] = float(cu[0]); o[1] = float(cu[1]); o[2] = float(cv[0]); o[3] = float(cv[1]);
-            o[4] = float(cw[0]); o[5] = float(cw[1]);
-            o[6] = float(-d.l[w] * d.A0FromVorticity[idx]);
-            o[7] = float(d.k[w] * d.A0FromVorticity[idx]);
-            o[8] = float(d.A0FromBuoyancy[idx]);
-            o[9] = float(d.ApmN[idx]);
-            o[10] = float(d.NA0[idx] * d.ApmN[idx]);
+            o[0] = cu[0]; o[1] = cu[1]; o[2] = cv[0]; o[3] = cv[1];
+            o[4] = cw[0]; o[5] = cw[1];
+            o[6] = -d.l[w] * d.A0FromVorticity[idx];
+            o[7] = d.k[w] * d.A0FromVorticity[idx];
+            o[8] = d.A0FromBuoyancy[idx];
+            o[9] = d.ApmN[idx];
+            o[10] = d.NA0[idx] * d.ApmN[idx];
         }
     }
     return out;
@@ -258,7 +258,7 @@ inline size_t x_len(const Plan& p) { return p.Nx % 2 == 0 ? p.Nx / 2 : p.Nx; }
 template <typename T>
 size_t smem_xflux(const Plan& p) {
     const size_t nt = p.targets.count, L = x_len(p);
-    return (L + p.Nx + (4 + 2 * nt) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (3 + nt) * p.Nx * sizeof(T);
+    return (L + p.Nx + 16 * L) * sizeof(dev::cx<T>) + (3 + nt) * p.Nx * sizeof(T);
 }
 template <typename T>
 size_t smem_xc2r(const Plan& p, int nch) { return (x_len(p) + p.Nx + nch * p.kxColumns + 8 * x_len(p)) * sizeof(dev::cx<T>); }
@@ -1262,10 +1262,21 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     WV_UP(p.modeFlags, modeFlags);
     WV_UP(p.rowK, rowK); WV_UP(p.rowL, rowL);
 #undef WV_UP
-    if (precision == WV_PRECISION_MIXED) {
+    // FP32 copies (MIXED) or (hi, lo) pairs (FP32X2) of the arrays the vertical
+    // kernels' reduced-precision branches read
+    auto to_pairs = [](const std::vector<double>& v) {
+        std::vector<float> f(2 * v.size());
+        for (size_t i = 0; i < v.size(); ++i) {
+            const dev::ff x(v[i]);
+            f[2 * i] = x.hi;
+            f[2 * i + 1] = x.lo;
+        }
+        return f;
+    };
+    if (precision == WV_PRECISION_MIXED || precision == WV_PRECISION_FP32X2) {
         auto upf = [&](const std::vector<double>& v, const float** dst) {
             if (e != cudaSuccess) return;
-            const std::vector<float> f = cast<float>(v);
+            const std::vector<float> f = precision == WV_PRECISION_MIXED ? cast<float>(v) : to_pairs(v);
             e = upload(h, f, dst);
         };
         upf(UAp, &dd.fUAp); upf(VAp, &dd.fVAp); upf(WAp, &dd.fWAp); upf(d.NAp, &dd.fNAp);
@@ -1276,12 +1287,7 @@ static int create_handle(const wv_config* config, int precision, int members, wv
         if (precision == WV_PRECISION_FP64) {
             const double* q = nullptr; e = upload(h, v, &q); *dst = q;
         } else if (precision == WV_PRECISION_FP32X2) {
-            std::vector<float> f(2 * v.size());  // (hi, lo) pairs
-            for (size_t i = 0; i < v.size(); ++i) {
-                const dev::ff x(v[i]);
-                f[2 * i] = x.hi;
-                f[2 * i + 1] = x.lo;
-            }
+            const std::vector<float> f = to_pairs(v);
             const float* q = nullptr; e = upload(h, f, &q); *dst = q;
         } else {
             const std::vector<float> f = cast<float>(v);
@@ -1303,8 +1309,9 @@ static int create_handle(const wv_config* config, int precision, int members, wv
         upT(transpose(p.CcosM, Zh, Nj), &dd.CcosMT); upT(transpose(p.CsinM, Zh, Nj), &dd.CsinMT);
         upT(transpose(p.Fcos, Nj, Zh), &dd.FcosT); upT(transpose(p.Fsin, Nj, Zh), &dd.FsinT);
     }
-    if (precision == WV_PRECISION_MIXED && e == cudaSuccess) {
-        const std::vector<float> proj = mixed_flux_projection(d);
+    if ((precision == WV_PRECISION_MIXED || precision == WV_PRECISION_FP32X2) && e == cudaSuccess) {
+        const std::vector<double> proj64 = mixed_flux_projection(d);
+        const std::vector<float> proj = precision == WV_PRECISION_MIXED ? cast<float>(proj64) : to_pairs(proj64);
         const float* q = nullptr;
         e = upload(h, proj, &q);
         dd.fProj = q;

@@ -21,6 +21,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "wv_ff.cuh"
 
@@ -337,6 +338,34 @@ __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restric
             fld[(3 * Nj + j) * kVinvModes + mi] = mk<T>(n.x, n.y);
             continue;
         }
+        if constexpr (std::is_same<T, ff>::value) {
+            // FP32X2: FP64 phase, then paired-FP32 evolution and field spectra with
+            // the coefficient arrays stored as pairs (d.fUAp ... hold ff values)
+            double sd, cd;
+            sincos(d.omega[idx] * elapsed, &sd, &cd);
+            const cx<T> p = mk<T>(T(cd), T(sd));
+            auto ld = [](const double* q) { return mk<T>(T(q[0]), T(q[1])); };
+            const cx<T> ap = cmul<T>(ld(Ap + 2 * idx), p);
+            const cx<T> am = cmul<T>(ld(Am + 2 * idx), cconj<T>(p));
+            const cx<T> a0 = ld(A0 + 2 * idx);
+            const cx<T> uap = reinterpret_cast<const cx<T>*>(d.fUAp)[idx];
+            const cx<T> vap = reinterpret_cast<const cx<T>*>(d.fVAp)[idx];
+            const cx<T> wap = reinterpret_cast<const cx<T>*>(d.fWAp)[idx];
+            const cx<T> ua0 = reinterpret_cast<const cx<T>*>(d.fUA0)[idx];
+            const cx<T> va0 = reinterpret_cast<const cx<T>*>(d.fVA0)[idx];
+            const T nap = reinterpret_cast<const T*>(d.fNAp)[idx], na0 = reinterpret_cast<const T*>(d.fNA0)[idx];
+            cx<T> u = cadd<T>(cadd<T>(cmul<T>(uap, ap), cmul<T>(cconj<T>(uap), am)), cmul<T>(ua0, a0));
+            cx<T> v = cadd<T>(cadd<T>(cmul<T>(vap, ap), cmul<T>(cconj<T>(vap), am)), cmul<T>(va0, a0));
+            cx<T> ww = cadd<T>(cmul<T>(wap, ap), cmul<T>(wap, am));
+            cx<T> n = mk<T>(ap.x * nap - am.x * nap + a0.x * na0, ap.y * nap - am.y * nap + a0.y * na0);
+            if (flags & 1) { u = cconj<T>(u); v = cconj<T>(v); ww = cconj<T>(ww); n = cconj<T>(n); }
+            if (flags & 2) { u.y = T(0); v.y = T(0); ww.y = T(0); n.y = T(0); }
+            fld[(0 * Nj + j) * kVinvModes + mi] = u;
+            fld[(1 * Nj + j) * kVinvModes + mi] = v;
+            fld[(2 * Nj + j) * kVinvModes + mi] = ww;
+            fld[(3 * Nj + j) * kVinvModes + mi] = n;
+            continue;
+        }
         double s, c;
         sincos(d.omega[idx] * elapsed, &s, &c);
         const zd p{c, s};
@@ -640,19 +669,18 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
     const int y = blockIdx.x, z = blockIdx.y;
     cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);  // [L]
     cx<T>* twN = tw + L;                              // [Nx]
-    cx<T>* spec = twN + Nx;                           // [nIn][KX]
-    cx<T>* bufA = spec + nIn * KX;                    // [8][L]
+    cx<T>* bufA = twN + Nx;                           // [8][L]
     cx<T>* bufB = bufA + 8 * L;
     T* phys = reinterpret_cast<T*>(bufB + 8 * L);    // U, V, W [3][Nx], then S_q [nt][Nx]
     T* S = phys + 3 * Nx;
+    // the row's channel spectra are read from L2 where the lines are built (no
+    // staging copy: the smaller footprint fits one more CTA per SM)
+    const cx<T>* yrow = yspec + ((size_t)z * nIn * Ny + y) * KX;
+    const size_t cstride = (size_t)Ny * KX;
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
     const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
     for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = twg[i];
     for (int i = threadIdx.x; i < Nx; i += blockDim.x) twN[i] = twgN[i];
-    for (int i = threadIdx.x; i < nIn * KX; i += blockDim.x) {
-        const int c = i / KX, k = i - c * KX;
-        spec[i] = yspec[(((size_t)z * nIn + c) * Ny + y) * KX + k];
-    }
     __syncthreads();
     // real row r -> (input channel, times i*k)
     auto rowSrc = [&](int r, int& ch, bool& useK) {
@@ -674,7 +702,7 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
             const int li = i / L, k = i - li * L;
             int ch; bool useK;
             rowSrc(rb + li, ch, useK);
-            bufA[li * L + k] = c2r_line_entry<T>(d, spec + ch * KX, k, useK, twN);
+            bufA[li * L + k] = c2r_line_entry<T>(d, yrow + ch * cstride, k, useK, twN);
         }
         __syncthreads();
         cx<T>* res = fft_lines<T, true>(bufA, bufB, d.fx, nr, L, tw);
@@ -932,7 +960,48 @@ __global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, cons
             vr[c] = re;
             vi[c] = conj ? -im : im;
         }
-        if constexpr (FLUX && sizeof(T) == 4) {
+        if constexpr (FLUX && std::is_same<T, ff>::value) {
+            // FP32X2 flux: the folded projection of the mixed form with paired-FP32
+            // coefficients (d.fProj holds 12 ff per (mode, j)) and an FP64 phase.
+            cx<T> ch[4] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (c >= nch) break;
+                ch[d.tq[c]] = mk<T>(vr[c], vi[c]);
+            }
+            const cx<T> U = ch[0], V = ch[1], Wc = ch[2], N = ch[3];
+            const T* pj = reinterpret_cast<const T*>(d.fProj) + 12 * (size_t)idx;
+            const T f0r = -pj[6] * U.y - pj[7] * V.y + pj[8] * N.x;
+            const T f0i = pj[6] * U.x + pj[7] * V.x + pj[8] * N.y;
+            T cpr, cpi, cmr, cmi;
+            if (w == 0) {
+                const T sc = T(d.inertialScale[j]);
+                cpr = sc * (U.x + V.y);
+                cpi = sc * (U.y - V.x);
+                cmr = cpr;
+                cmi = -cpi;
+            } else {
+                const T wr = pj[0] * U.x - pj[1] * U.y + pj[2] * V.x - pj[3] * V.y + pj[4] * Wc.x - pj[5] * Wc.y;
+                const T wi = pj[0] * U.y + pj[1] * U.x + pj[2] * V.y + pj[3] * V.x + pj[4] * Wc.y + pj[5] * Wc.x;
+                const T br = pj[9] * N.x - pj[10] * f0r, bi = pj[9] * N.y - pj[10] * f0i;
+                cpr = wr + br; cpi = wi + bi; cmr = wr - br; cmi = wi - bi;
+            }
+            double sd, cd;
+            sincos(d.omega[idx] * elapsed, &sd, &cd);
+            const T sn = T(sd), cs = T(cd);
+            zd fp{double(cpr * cs + cpi * sn), double(cpi * cs - cpr * sn)};   // (cp) * conj(p)
+            zd fm{double(cmr * cs - cmi * sn), double(cmr * sn + cmi * cs)};   // (cm) * p
+            zd f0{double(f0r), double(f0i)};
+            if (applyDamping) {
+                const double sdmp = __dmul_rn(maxSpeed, d.damping[idx]);
+                fp = zadd(fp, zscale(zload(Ap + 2 * idx), sdmp));
+                fm = zadd(fm, zscale(zload(Am + 2 * idx), sdmp));
+                f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sdmp));
+            }
+            zstore(Fp + 2 * idx, fp);
+            zstore(Fm + 2 * idx, fm);
+            zstore(F0 + 2 * idx, f0);
+        } else if constexpr (FLUX && sizeof(T) == 4) {
             // MIXED flux: projection with the folded FP32 coefficients and an FP32
             // phase after FP64 angle reduction; FP64 only for the angle and the stores.
             float2 ch[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
