@@ -1,0 +1,150 @@
+"""FP32X2 handles: the xy transforms, quadratic products and vertical
+contractions in paired FP32 (float-float) on the FP32 pipe.  The reference has
+no such form; its accuracy is checked against the reference's own FP64 outputs
+(golden fixtures) and against FP64 handles on the same inputs, with gates far
+below the mixed form's: the flux within 1e-9 of max |F|, field tendencies and
+states after many RK4 steps within 1e-8 (the metric's bound is 1e-6)."""
+import math
+
+import numpy as np
+import pytest
+
+from _cases import config_from_case, golden_cases, load_golden, rel_err, rk23_run
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+FP32X2_TOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def wv():
+    import torch
+    import wvgpu
+    from wvgpu import build
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    build.build()
+    wvgpu.load_library()
+    return wvgpu
+
+
+def _conf(wv, c):
+    return wv.Configuration(Nx=c.Nx, Ny=c.Ny, Nz=c.Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, N0=c.N0, rho0=c.rho0, g=c.g,
+                            planetaryRadius=c.planetaryRadius, rotationRate=c.rotationRate, latitude=c.latitude,
+                            isHydrostatic=c.isHydrostatic, shouldAntialias=c.shouldAntialias)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp32x2_flux_rhs_transforms_and_rk4_match_reference(wv, name):
+    cf = CASES[name]
+    g = load_golden(name)
+    k = wv.WVTransformConstantStratificationKernel(_conf(wv, config_from_case(cf)), precision="fp32x2")
+    t, t0 = float(g["t"]), float(g["t0"])
+    F = k.nonlinearFlux(t, t0, g["Ap"], g["Am"], g["A0"])
+    for got, key in zip(F, ("Fp", "Fm", "F0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key, rel_err(got, g[key]))
+    k.set_forcing(nonlinear=True, adaptive_damping=bool(cf["damping"]))
+    R = k.evaluateRightHandSide(t, t0, g["Ap"], g["Am"], g["A0"])
+    for got, key in zip(R, ("Rp", "Rm", "R0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    inv = k.transformWaveVortexToUVWEta(t, t0, g["Ap"], g["Am"], g["A0"])
+    assert rel_err(inv, g["inverse"]) <= FP32X2_TOL
+    if cf["isHydrostatic"]:
+        B = k.transformUVEtaToWaveVortex(g["fields"], t, t0)
+    else:
+        B = k.transformUVWEtaToWaveVortex(g["fields"], t, t0)
+    for got, key in zip(B, ("Bp", "Bm", "B0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    Kp, Km, K0, tK = k.rk4(g["rk_Ap"], g["rk_Am"], g["rk_A0"], float(g["rk_t"]), float(g["rk_t0"]), float(g["rk_dt"]),
+                           int(g["rk_steps"]))
+    assert tK == float(g["rk_tout"])
+    for got, key in zip((Kp, Km, K0), ("Kp", "Km", "K0")):
+        if np.any(g[key]):
+            assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    k.close()
+
+
+def test_fp32x2_configs0_to_t600(wv):
+    """The configs[0] single wave with adaptive damping, 60 RK4 steps to t = 600 s,
+    against the reference's own run."""
+    import os
+    c = config_from_case(CASES["c0_16x16x9"])
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "c0_t600.npz"))
+    k = wv.WVTransformConstantStratificationKernel(_conf(wv, c), precision="fp32x2")
+    k.set_forcing(nonlinear=True, adaptive_damping=True)
+    Ap, Am, A0, t = k.rk4(g["Ap"], g["Am"], g["A0"], 0.0, 0.0, float(g["dt"]), int(g["steps"]))
+    assert t == float(g["t"])
+    for a, b in zip((Ap, Am, A0), (g["Kp"], g["Km"], g["K0"])):
+        if np.any(b):
+            assert rel_err(a, b) <= FP32X2_TOL
+    assert rel_err(k.transformWaveVortexToUVWEta(t, 0.0, Ap, Am, A0), g["fields"]) <= FP32X2_TOL
+    k.close()
+
+
+@pytest.mark.parametrize("N,Nz,hydro", [(64, 33, False), (128, 65, False), (96, 49, True)])
+def test_fp32x2_fields_after_rk4_steps_match_fp64(wv, N, Nz, hydro):
+    """Steep-spectrum turbulent state, 20 RK4 steps at 0.5 x CFL: every field of
+    the FP32X2 run within 1e-8 of the FP64 run (relative L2); the flux's field
+    tendencies within 1e-8."""
+    import torch
+    cfg = wv.Configuration(Nx=N, Ny=N, Nz=Nz, Nj=(2 * (Nz - 1)) // 3, Lx=3125.0 * N, Ly=3125.0 * N, Lz=4000.0,
+                           latitude=33.0, isHydrostatic=hydro)
+    k64 = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
+    A = wv.synthetic_state(k64, seed=5, urms=0.1)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+    fields = [0, 1, 3] if hydro else [0, 1, 2, 3]
+    F64 = [x.cpu().numpy() for x in k64.nonlinearFlux(300.0, 0.0, *dev)]
+    Fx = [x.cpu().numpy() for x in k.nonlinearFlux(300.0, 0.0, *dev)]
+    e64 = k64.transformWaveVortexToUVWEta(0.0, 0.0, *F64)
+    ex = k64.transformWaveVortexToUVWEta(0.0, 0.0, *Fx)
+    terr = [float(np.linalg.norm(ex[i] - e64[i]) / np.linalg.norm(e64[i])) for i in fields]
+    dt = wv.cfl_time_step(k64, *A)
+    y64 = [x.clone() for x in dev]
+    yx = [x.clone() for x in dev]
+    k64.rk4(*y64, 0.0, 0.0, dt, 20)
+    k.rk4(*yx, 0.0, 0.0, dt, 20)
+    f64 = k64.transformWaveVortexToUVWEta(20 * dt, 0.0, *(x.cpu().numpy() for x in y64))
+    fx = k64.transformWaveVortexToUVWEta(20 * dt, 0.0, *(x.cpu().numpy() for x in yx))
+    ferr = [float(np.linalg.norm(fx[i] - f64[i]) / np.linalg.norm(f64[i])) for i in fields]
+    print(f"{N}x{N}x{Nz} hydro={hydro}: tendency err {terr}, field err after 20 steps {ferr}")
+    assert max(terr) <= 1e-8 and max(ferr) <= 1e-8
+    k.close()
+    k64.close()
+
+
+def test_fp32x2_rk23_matches_reference_run(wv):
+    import torch
+    cf, o, ref = rk23_run("odd")
+    k = wv.WVTransformConstantStratificationKernel(_conf(wv, config_from_case(cf)), precision="fp32x2")
+    rk = wv.WVAdaptiveRK23(k, wv.WVAdaptiveRK23Options(relativeTolerance=o["rtol"], absoluteToleranceScale=o["atol_scale"],
+                                                      safetyFactor=o["safety"], rejectionFloorFactor=o["floor"],
+                                                      maximumStepFactor=o["max_factor"], maximumStepSize=o["max_step"]))
+    y = [torch.from_numpy(np.ascontiguousarray(ref[n])).cuda() for n in ("Ap", "Am", "A0")]
+    rk.advanceToTime(*y, ref["t"], ref["t0"], ref["final"], ref["initial"])
+    m = rk.metrics()
+    assert [m["accepted_steps"], m["rejected_steps"], m["rhs_evaluations"]] == ref["counts"].tolist()[:3]
+    for got, want in zip(y, (ref["Kp"], ref["Km"], ref["K0"])):
+        assert rel_err(got.cpu().numpy(), want) <= FP32X2_TOL
+    rk.close()
+    k.close()
+
+
+def test_fp32x2_rejects_entry_points_without_a_paired_form(wv):
+    import torch
+    c = config_from_case(CASES["odd_15x13x9"])
+    k = wv.WVTransformConstantStratificationKernel(_conf(wv, c), precision="fp32x2")
+    g = load_golden("odd_15x13x9")
+    dev = [torch.from_numpy(np.ascontiguousarray(g[n])).cuda() for n in ("Ap", "Am", "A0")]
+    with pytest.raises(wv.WVKernelError) as e:
+        k.flux_vjp(0.0, 0.0, *dev, *dev)
+    assert e.value.code == 10
+    with pytest.raises(wv.WVKernelError) as e:
+        k.set_vertical_kernel("tensor")
+    assert e.value.code == 10
+    with pytest.raises(wv.WVKernelError) as e:
+        k.advectFGridScalar(np.zeros((c.Nz, c.Ny, c.Nx)), np.zeros((3, c.Nz, c.Ny, c.Nx)), True)
+    assert e.value.code == 10
+    k.close()
+    with pytest.raises((wv.WVKernelError, ValueError, KeyError)):
+        wv.WVEnsemble([_conf(wv, c)], [2], precision="fp32x2", autotune=False)
