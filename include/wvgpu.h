@@ -303,6 +303,19 @@ int wv_advect_fgrid_scalar_device(wv_handle* handle, const double* scalar, const
  * (t in/out) exactly as WVFixedStepRK4 advances it (t <- t + dt per step). */
 int wv_rk4_steps_device(wv_handle* handle, double* Ap, double* Am, double* A0,
                         double* t, double t0, double dt, int n_steps, void* stream);
+/* WVFixedStepRK4Options::retainDenseOutput (PortableRuntime/include/WaveVortexRuntime/
+ * WVRungeKutta.hpp:52-54): when enabled, every RK4 entry keeps the last step's end
+ * states and first and fourth stage derivatives on the device. */
+int wv_rk4_set_dense_output(wv_handle* handle, int enabled);
+/* WVFixedStepRK4::advanceToTime (PortableRuntime/src/WVRungeKutta.cpp:464-480): steps of
+ * min(dt, final_time - t) until final_time; *t ends at final_time. */
+int wv_rk4_advance_to_time_device(wv_handle* handle, double* Ap, double* Am, double* A0, double* t, double t0,
+                                  double final_time, double dt, void* stream);
+int wv_rk4_advance_to_time(wv_handle* handle, double* Ap, double* Am, double* A0, double* t, double t0,
+                           double final_time, double dt);
+/* WVFixedStepRK4::evaluateDenseOutput (WVRungeKutta.cpp:482-541): the state at `time`
+ * inside the last step (cubic Hermite), written to device arrays. */
+int wv_rk4_dense_output_device(wv_handle* handle, double time, double* Ap, double* Am, double* A0, void* stream);
 
 /* ---- ensembles ------------------------------------------------------------------------
  * No counterpart in the reference, which steps one state per kernel object

@@ -491,4 +491,26 @@ int wvref_system_rk23(void* sp, const double* opts, double* Ap, double* Am, doub
     return 0;
 }
 
+// WVFixedStepRK4 with retained dense output: advanceToTime(finalTime, dt) from
+// *t, then the interpolant of the last step at denseTime into dense ([3][M]).
+int wvref_rk4_dense(void* handle, double* Ap, double* Am, double* A0, double* t, double t0, double finalTime, double dt,
+                    double denseTime, double* dense, double* lastInterval) {
+    auto* h = static_cast<RefHandle*>(handle);
+    const auto s = h->kernel->descriptor().spectralShape();
+    WVFixedStepRK4Options o;
+    o.retainDenseOutput = true;
+    WVFixedStepRK4 rk(*h->system, o);
+    WVMutableIntegrationState state{{*t, t0, {mview(Ap, s), mview(Am, s), mview(A0, s)}}, nullptr, 0};
+    auto status = rk.prepareStateAfterRestart(state);
+    if (status) status = rk.advanceToTime(state, finalTime, dt);
+    if (!status) return fail(h, status);
+    *t = state.waveVortex.t;
+    lastInterval[0] = rk.initialTime();
+    lastInterval[1] = rk.finalTime();
+    const std::size_t M = s.elementCount();
+    WVMutableIntegrationState out{{0.0, t0, {mview(dense, s), mview(dense + 2 * M, s), mview(dense + 4 * M, s)}}, nullptr, 0};
+    status = rk.evaluateDenseOutput(denseTime, out);
+    return status ? 0 : fail(h, status);
+}
+
 } // extern "C"

@@ -817,6 +817,51 @@ def rk4(desc, Ap, Am, A0, t, t0, h, steps, damping=None):
     return Ap, Am, A0, t
 
 
+def rk4_advance_to_time(desc, Ap, Am, A0, t, t0, final, h, damping=None):
+    """WVFixedStepRK4::advanceToTime (WVRungeKutta.cpp:464-480) with retained
+    dense output: steps of min(h, final - t) until final.  Returns (Ap, Am, A0,
+    final, dense) where dense = (t_i, t_f, y_i, y_f, k1, k4) of the last step:
+    the state before and after it, its first stage derivative and its fourth
+    (f at t_i + h of y_i + h k3)."""
+    y = [Ap, Am, A0]
+    dense = None
+    while t < final:
+        step = min(h, final - t)
+        if not step > 0.0:
+            break
+        k1 = rhs(desc, *y, t, t0, damping)
+        wsum = [x.copy() for x in k1]
+        st = [y[i] + (0.5 * step) * k1[i] for i in range(3)]
+        k = rhs(desc, *st, t + 0.5 * step, t0, damping)
+        wsum = [wsum[i] + 2.0 * k[i] for i in range(3)]
+        st = [y[i] + (0.5 * step) * k[i] for i in range(3)]
+        k = rhs(desc, *st, t + 0.5 * step, t0, damping)
+        wsum = [wsum[i] + 2.0 * k[i] for i in range(3)]
+        st = [y[i] + step * k[i] for i in range(3)]
+        k4 = rhs(desc, *st, t + step, t0, damping)
+        wsum = [wsum[i] + 1.0 * k4[i] for i in range(3)]
+        y1 = [y[i] + (step / 6.0) * wsum[i] for i in range(3)]
+        dense = (t, t + step, y, y1, k1, k4)
+        y, t = y1, t + step
+    return y[0], y[1], y[2], final, dense
+
+
+def rk4_dense_output(dense, time):
+    """WVFixedStepRK4::evaluateDenseOutput (WVRungeKutta.cpp:482-541): the cubic
+    Hermite interpolant through the step's end states with the first and the
+    fourth stage derivatives as end slopes."""
+    ti, tf, y0, y1, k1, k4 = dense
+    h = tf - ti
+    theta = 0.0 if h == 0.0 else (time - ti) / h
+    theta = max(0.0, min(1.0, theta))
+    t2, t3 = theta * theta, theta * theta * theta
+    ew = 3 * t2 - 2 * t3
+    iw = 1 - ew
+    isw = h * (theta - 2 * t2 + t3)
+    esw = h * (t3 - t2)
+    return [iw * a + ew * b + isw * c + esw * e for a, b, c, e in zip(y0, y1, k1, k4)]
+
+
 # ---------------------------------------------------------------------------
 # Adaptive RK23 (WVAdaptiveRK23, PortableRuntime/src/WVRungeKutta.cpp:554-983)
 

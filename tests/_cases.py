@@ -96,3 +96,11 @@ def split_extra(desc, groups, tracers, extra):
         off += R
     assert off == len(extra)
     return out
+
+
+def rk4_dense_run(key):
+    """Inputs and reference outputs of one RK4 advanceToTime / dense-output run
+    (tests/golden/rk4_dense.npz)."""
+    g = load_golden("rk4_dense")
+    cfg = {"odd": "odd_15x13x9", "hd": "hydro_damp_12x10x11"}[key]
+    return golden_cases()[cfg], {k[len(key) + 1:]: g[k] for k in g.files if k.startswith(key + "_")}

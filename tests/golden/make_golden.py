@@ -8,7 +8,8 @@ numpy oracle (oracle/wv_oracle.py) and the GPU path against them.
 
 Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT] [--rk23]
         (--rk23 regenerates only the adaptive RK23 fixture, rk23.npz;
-         --system only the integrated-observer fixture, system.npz)
+         --system only the integrated-observer fixture, system.npz;
+         --rk4-dense only the RK4 advanceToTime / dense-output fixture, rk4_dense.npz)
 """
 from __future__ import annotations
 
@@ -451,13 +452,55 @@ def make_system(lib):
     np.savez_compressed(os.path.join(HERE, "system.npz"), **out)
 
 
+# Fixed-step RK4 advanceToTime with a final partial step and retained dense
+# output, through the reference's WVFixedStepRK4 ({retainDenseOutput = true}).
+RK4_DENSE_RUNS = {
+    "odd": dict(case="odd_15x13x9", damping=False, t=100.0, t0=3.0, final=165.0, dt=20.0, theta=0.37),
+    "hd": dict(case="hydro_damp_12x10x11", damping=True, t=10.0, t0=1.0, final=40.0, dt=12.5, theta=0.81),
+}
+
+
+def make_rk4_dense(lib):
+    out = {}
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for key, run in RK4_DENSE_RUNS.items():
+        case = CASES[run["case"]]
+        r = Ref(lib, case)
+        shape = (r.Nkl, case["Nj"])
+        base = sum(ord(ch) for ch in run["case"]) + 300
+        Ap, Am, A0 = (seeded(shape, base + i, 1e-3) for i in (1, 2, 3))
+        Kp, Km, K0 = Ap.copy(), Am.copy(), A0.copy()
+        tt = ctypes.c_double(run["t"])
+        dense = np.zeros((3,) + shape, np.complex128)
+        interval = np.zeros(2)
+        # the last step runs from the largest multiple of dt below final (here a partial step)
+        n_full = int((run["final"] - run["t"]) // run["dt"])
+        t_last = run["t"] + n_full * run["dt"]
+        if t_last >= run["final"]:
+            t_last -= run["dt"]
+        dense_time = t_last + run["theta"] * (run["final"] - t_last)
+        r.check(lib.wvref_rk4_dense(r.h, P(Kp), P(Km), P(K0), ctypes.byref(tt), ctypes.c_double(run["t0"]),
+                                    ctypes.c_double(run["final"]), ctypes.c_double(run["dt"]), ctypes.c_double(dense_time),
+                                    P(dense), P(interval)))
+        out.update({f"{key}_Ap": Ap, f"{key}_Am": Am, f"{key}_A0": A0, f"{key}_t": run["t"], f"{key}_t0": run["t0"],
+                    f"{key}_final": run["final"], f"{key}_dt": run["dt"], f"{key}_damping": run["damping"],
+                    f"{key}_Kp": Kp, f"{key}_Km": Km, f"{key}_K0": K0, f"{key}_tout": tt.value,
+                    f"{key}_dense_time": dense_time, f"{key}_dense": dense, f"{key}_interval": interval})
+        lib.wvref_destroy(r.h)
+        print(f"rk4 dense {key}: interval {interval.tolist()} t = {tt.value}")
+    np.savez_compressed(os.path.join(HERE, "rk4_dense.npz"), **out)
+
+
 if __name__ == "__main__":
     root = next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")
     if "--rk23" in sys.argv:
         make_rk23(load_lib(root))
     elif "--system" in sys.argv:
         make_system(load_lib(root))
+    elif "--rk4-dense" in sys.argv:
+        make_rk4_dense(load_lib(root))
     else:
         main()
         make_rk23(load_lib(root))
         make_system(load_lib(root))
+        make_rk4_dense(load_lib(root))

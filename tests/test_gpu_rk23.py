@@ -161,3 +161,36 @@ def test_mixed_precision_rk23_tracks_fp64(wv):
         assert err <= 1e-2
     rk.close()
     k.close()
+
+
+@pytest.mark.parametrize("key", ["odd", "hd"])
+def test_rk4_advance_to_time_and_dense_output(wv, key):
+    """WVFixedStepRK4::advanceToTime with a final partial step and the retained
+    dense output, against the reference integrator (tests/golden/rk4_dense.npz)."""
+    import torch
+    from _cases import rk4_dense_run
+    cf, g = rk4_dense_run(key)
+    k = _kernel(wv, cf)
+    k.set_forcing(nonlinear=True, adaptive_damping=bool(g["damping"]))
+    with pytest.raises(wv.WVKernelError) as e:
+        k.rk4DenseOutput(float(g["dense_time"]))
+    assert e.value.code == 10
+    k.setRK4DenseOutput(True)
+    y = [torch.from_numpy(np.ascontiguousarray(g[n])).cuda() for n in ("Ap", "Am", "A0")]
+    t = k.rk4AdvanceToTime(*y, float(g["t"]), float(g["t0"]), float(g["final"]), float(g["dt"]))
+    assert t == float(g["tout"])
+    for got, want in zip(y, (g["Kp"], g["Km"], g["K0"])):
+        assert rel_err(got.cpu().numpy(), want) <= FP64_REL_TOL
+    dense = k.rk4DenseOutput(float(g["dense_time"]))
+    for got, want in zip(dense, g["dense"]):
+        assert rel_err(got.cpu().numpy(), want) <= FP64_REL_TOL
+    with pytest.raises(wv.WVKernelError) as e:
+        k.rk4DenseOutput(float(g["final"]) + 1.0)
+    assert e.value.code == 1
+    # host-pointer form: the same result
+    Hp, Hm, H0, th = k.rk4AdvanceToTime(g["Ap"], g["Am"], g["A0"], float(g["t"]), float(g["t0"]), float(g["final"]),
+                                        float(g["dt"]))
+    assert th == t
+    for a, b in zip((Hp, Hm, H0), y):
+        assert np.array_equal(a, b.cpu().numpy())
+    k.close()

@@ -90,3 +90,22 @@ def test_wave_vortex_run_matches_reference_integrator(key):
     for got, want in zip(dense, ref["dense"]):
         if np.any(want):
             assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-11
+
+
+@pytest.mark.parametrize("key", ["odd", "hd"])
+def test_rk4_advance_and_dense_output_match_reference(key):
+    """WVFixedStepRK4::advanceToTime with a final partial step and the retained
+    cubic Hermite dense output, against the reference integrator."""
+    from _cases import rk4_dense_run
+    cf, g = rk4_dense_run(key)
+    d = O.build_descriptor(config_from_case(cf))
+    damping = O.adaptive_damping_operator(d) if bool(g["damping"]) else None
+    Ap, Am, A0, t, dense = O.rk4_advance_to_time(d, g["Ap"], g["Am"], g["A0"], float(g["t"]), float(g["t0"]),
+                                                 float(g["final"]), float(g["dt"]), damping)
+    assert t == float(g["tout"])
+    assert (dense[0], dense[1]) == tuple(g["interval"].tolist())
+    for got, want in zip((Ap, Am, A0), (g["Kp"], g["Km"], g["K0"])):
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-12
+    out = O.rk4_dense_output(dense, float(g["dense_time"]))
+    for got, want in zip(out, g["dense"]):
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-12

@@ -20,6 +20,8 @@
 #include <atomic>
 #include <mutex>
 #include <cmath>
+#include <limits>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -75,6 +77,12 @@ struct wv_handle {
     cudaStream_t adjStream = nullptr;  // multi-step adjoint: recomputation of the next segment
     double* ybAlt = nullptr;           // multi-step adjoint: second cotangent buffer
     cudaEvent_t slotReady[2] = {}, slotFree[2] = {}, fwdDone = nullptr;
+    // RK4 dense output (WVFixedStepRK4Options::retainDenseOutput): state before
+    // and after the last step, its first and fourth stage derivatives, [4][3][M]
+    bool rk4Dense = false;
+    double* denseBuf = nullptr;
+    bool denseValid = false;
+    double denseTi = 0.0, denseTf = 0.0;
     bool instrument = false;
     bool tcAvailable = false;  // tensor-core vertical transform built for this handle
     bool verticalTC = false;   // ... and selected (default: on where built)
@@ -938,16 +946,22 @@ cudaError_t rhs_contiguous(wv_handle* h, double t, double t0, const double* y, d
 cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t s) {
     const size_t n = 6 * h->plan.M * h->dd.members;
     const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
+    const bool dense = h->rk4Dense && h->denseBuf;
+    const size_t nb = n * sizeof(double);
     cudaError_t e;
+    if (dense) { e = cudaMemcpyAsync(h->denseBuf, h->state, nb, cudaMemcpyDeviceToDevice, s); if (e != cudaSuccess) return e; }
     e = rhs_contiguous(h, t, t0, h->state, h->kbuf, s); if (e != cudaSuccess) return e;
+    if (dense) { e = cudaMemcpyAsync(h->denseBuf + 2 * n, h->kbuf, nb, cudaMemcpyDeviceToDevice, s); if (e != cudaSuccess) return e; }
     dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, h->state, 0.5 * dt, h->stage, 1, n);
     e = rhs_contiguous(h, t + 0.5 * dt, t0, h->stage, h->kbuf, s); if (e != cudaSuccess) return e;
     dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, h->state, 0.5 * dt, h->stage, 0, n);
     e = rhs_contiguous(h, t + 0.5 * dt, t0, h->stage, h->kbuf, s); if (e != cudaSuccess) return e;
     dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, h->state, dt, h->stage, 0, n);
     e = rhs_contiguous(h, t + dt, t0, h->stage, h->kbuf, s); if (e != cudaSuccess) return e;
+    if (dense) { e = cudaMemcpyAsync(h->denseBuf + 3 * n, h->kbuf, nb, cudaMemcpyDeviceToDevice, s); if (e != cudaSuccess) return e; }
     dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, nullptr, 0.0, nullptr, 0, n);
     dev::k_affine<<<grid, 256, 0, s>>>(h->state, h->acc, dt / 6.0, h->state, n);
+    if (dense) { e = cudaMemcpyAsync(h->denseBuf + n, h->state, nb, cudaMemcpyDeviceToDevice, s); if (e != cudaSuccess) return e; }
     h->metrics.kernel_launches += 5;
     h->metrics.rk4_steps += 1;
     h->metrics.rhs_evaluations += 4;
@@ -1799,6 +1813,7 @@ int wv_rk4_steps_device(wv_handle* h, double* Ap, double* Am, double* A0, double
     double tt = *t;
     for (int i = 0; i < n && e == cudaSuccess; ++i) {
         e = rk4_step(h, tt, t0, dt, s);
+        if (e == cudaSuccess && h->rk4Dense) { h->denseValid = true; h->denseTi = tt; h->denseTf = tt + dt; }
         tt = tt + dt;
     }
     double* dst[] = {Ap, Am, A0};
@@ -1807,6 +1822,108 @@ int wv_rk4_steps_device(wv_handle* h, double* Ap, double* Am, double* A0, double
     if (e != cudaSuccess) return cuda_fail(h, e, "RK4");
     *t = tt;
     return WV_SUCCESS;
+}
+
+// WVFixedStepRK4Options::retainDenseOutput (PortableRuntime/include/WaveVortexRuntime/
+// WVRungeKutta.hpp:52-54): keeps the last step's end states and first and
+// fourth stage derivatives on the device (4 state-sized buffers, allocated on
+// first use) for wv_rk4_dense_output_device.
+int wv_rk4_set_dense_output(wv_handle* h, int enabled) {
+    if (!h) return WV_INVALID_POINTER;
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
+    if (enabled && !h->denseBuf) {
+        cudaSetDevice(h->device);
+        void* p = nullptr;
+        const cudaError_t e = alloc(h, 4 * 6 * h->plan.M * h->dd.members * sizeof(double), &p);
+        if (e != cudaSuccess) return cuda_fail(h, e, "RK4 dense-output buffers");
+        h->denseBuf = static_cast<double*>(p);
+    }
+    h->rk4Dense = enabled != 0;
+    h->denseValid = false;
+    return WV_SUCCESS;
+}
+
+// WVFixedStepRK4::advanceToTime (PortableRuntime/src/WVRungeKutta.cpp:464-480):
+// steps of min(dt, final_time - t) until final_time; *t ends at final_time.
+int wv_rk4_advance_to_time_device(wv_handle* h, double* Ap, double* Am, double* A0, double* t, double t0,
+                                  double final_time, double dt, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!Ap || !Am || !A0 || !t) return fail(h, WV_INVALID_POINTER, "RK4 received a null pointer.");
+    int rc = check_times(h, *t, t0); if (rc) return rc;
+    if (final_time < *t || !std::isfinite(final_time))
+        return fail(h, WV_INVALID_CONFIGURATION, "RK4 cannot advance backward or to a nonfinite time.");
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "RK4 stepping is not reentrant.");
+    cudaSetDevice(h->device);
+    auto s = static_cast<cudaStream_t>(stream);
+    const size_t cb = h->plan.M * 16;
+    cudaError_t e = cudaSuccess;
+    const double* src[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, src[c], cb, cudaMemcpyDeviceToDevice, s);
+    double tt = *t;
+    while (tt < final_time && e == cudaSuccess) {
+        const double step = std::min(dt, final_time - tt);
+        if (!(step > 0.0)) break;
+        e = rk4_step(h, tt, t0, step, s);
+        if (e == cudaSuccess && h->rk4Dense) { h->denseValid = true; h->denseTi = tt; h->denseTf = tt + step; }
+        tt = tt + step;
+    }
+    double* dst[] = {Ap, Am, A0};
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(dst[c], reinterpret_cast<char*>(h->state) + c * cb, cb, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "RK4");
+    *t = final_time;
+    return WV_SUCCESS;
+}
+
+// WVFixedStepRK4::evaluateDenseOutput (WVRungeKutta.cpp:482-541): the cubic
+// Hermite interpolant of the last step through its end states, with the first
+// and fourth stage derivatives as end slopes.
+int wv_rk4_dense_output_device(wv_handle* h, double time, double* Ap, double* Am, double* A0, void* stream) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!Ap || !Am || !A0) return fail(h, WV_INVALID_POINTER, "Dense output received a null pointer.");
+    if (!h->rk4Dense || !h->denseValid) return fail(h, WV_UNSUPPORTED_OPERATION, "RK4 dense output is unavailable.");
+    const double tol = 8.0 * std::numeric_limits<double>::epsilon() *
+                       std::max({1.0, std::abs(h->denseTi), std::abs(h->denseTf)});
+    if (time < h->denseTi - tol || time > h->denseTf + tol)
+        return fail(h, WV_INVALID_CONFIGURATION, "Dense-output time is outside the accepted interval.");
+    Guard g(h->busy);
+    if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "RK4 dense-output evaluation is not reentrant.");
+    cudaSetDevice(h->device);
+    const double hstep = h->denseTf - h->denseTi;
+    double theta = hstep == 0.0 ? 0.0 : (time - h->denseTi) / hstep;
+    theta = std::max(0.0, std::min(1.0, theta));
+    const double t2 = theta * theta, t3 = t2 * theta, ew = 3 * t2 - 2 * t3, iw = 1 - ew,
+                 isw = hstep * (theta - 2 * t2 + t3), esw = hstep * (t3 - t2);
+    const size_t n = 6 * h->plan.M, M2 = 2 * h->plan.M;
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((M2 + 255) / 256, 152 * 16));
+    const double* b = h->denseBuf;
+    dev::k_rk4_dense<<<dim3(grid, 3), 256, 0, static_cast<cudaStream_t>(stream)>>>(b, b + n, b + 2 * n, b + 3 * n, iw, ew, isw,
+                                                                                   esw, Ap, Am, A0, M2);
+    h->metrics.kernel_launches += 1;
+    return finish(h, cudaGetLastError(), "RK4 dense output");
+}
+
+int wv_rk4_advance_to_time(wv_handle* h, double* Ap, double* Am, double* A0, double* t, double t0, double final_time,
+                           double dt) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!Ap || !Am || !A0 || !t) return fail(h, WV_INVALID_POINTER, "RK4 received a null pointer.");
+    cudaSetDevice(h->device);
+    const size_t cb = h->plan.M * 16;
+    auto s = h->stream;
+    double* hostPtr[] = {Ap, Am, A0};
+    double* devPtr[] = {h->flux, h->flux + 2 * h->plan.M, h->flux + 4 * h->plan.M};
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c) e = cudaMemcpyAsync(devPtr[c], hostPtr[c], cb, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "RK4 state upload");
+    const int rc = wv_rk4_advance_to_time_device(h, devPtr[0], devPtr[1], devPtr[2], t, t0, final_time, dt, s);
+    if (rc) return rc;
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c) e = cudaMemcpyAsync(hostPtr[c], devPtr[c], cb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return finish(h, e, "RK4 state download");
 }
 
 // ---- host-pointer entries ------------------------------------------------------------
@@ -1915,6 +2032,7 @@ int wv_rk4_steps(wv_handle* h, double* Ap, double* Am, double* A0, double* t, do
     double tt = *t;
     for (int i = 0; i < n && e == cudaSuccess; ++i) {
         e = rk4_step(h, tt, t0, dt, s);
+        if (e == cudaSuccess && h->rk4Dense) { h->denseValid = true; h->denseTi = tt; h->denseTf = tt + dt; }
         tt = tt + dt;
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

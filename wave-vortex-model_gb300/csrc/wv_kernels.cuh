@@ -1175,5 +1175,19 @@ __global__ void k_accumulate(double* __restrict__ out, const double* __restrict_
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         out[i] += x[i];
 }
+// RK4 dense output: out = iw y0 + ew y1 + isw k1 + esw k4, summed left to right
+// without contraction (WVFixedStepRK4::evaluateDenseOutput); grid.y = component.
+__global__ void k_rk4_dense(const double* __restrict__ y0, const double* __restrict__ y1, const double* __restrict__ k1,
+                            const double* __restrict__ k4, double iw, double ew, double isw, double esw, double* Ap,
+                            double* Am, double* A0, size_t M2) {
+    const int c = blockIdx.y;
+    double* dst = c == 0 ? Ap : (c == 1 ? Am : A0);
+    const size_t o = c * M2;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < M2; i += (size_t)gridDim.x * blockDim.x) {
+        double v = __dadd_rn(__dmul_rn(iw, y0[o + i]), __dmul_rn(ew, y1[o + i]));
+        v = __dadd_rn(v, __dmul_rn(isw, k1[o + i]));
+        dst[i] = __dadd_rn(v, __dmul_rn(esw, k4[o + i]));
+    }
+}
 }  // namespace dev
 }  // namespace wvgpu

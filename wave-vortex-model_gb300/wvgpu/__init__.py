@@ -201,6 +201,10 @@ def load_library():
         getattr(lib, name + "_device").argtypes = [P, D, D, P, P, P, P, P, P, P, P]
     lib.wv_rk4_steps.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int]
     lib.wv_rk4_steps_device.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, ctypes.c_int, P]
+    lib.wv_rk4_set_dense_output.argtypes = [P, ctypes.c_int]
+    lib.wv_rk4_advance_to_time_device.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, D, P]
+    lib.wv_rk4_advance_to_time.argtypes = [P, P, P, P, ctypes.POINTER(D), D, D, D]
+    lib.wv_rk4_dense_output_device.argtypes = [P, D, P, P, P, P]
     lib.wv_flux_vjp_device.argtypes = [P, D, D, P, P, P, P, P, P, P, P, P, P]
     lib.wv_inverse_vjp_device.argtypes = [P, D, D, P, P, P, P, P]
     lib.wv_rk4_step_vjp_device.argtypes = [P, P, P, P, D, D, D, P, P, P, P]
@@ -273,7 +277,9 @@ def exported_symbols():
             "wv_rk23_last_accepted_step", "wv_rk23_get_metrics", "wv_rk23_get_diagnostics", "wv_rk23_tolerance_hash",
             "wv_rk23_create_for_system", "wv_rk23_system_step_device", "wv_rk23_system_advance_to_time_device",
             "wv_rk23_system_dense_output_device", "wv_system_create", "wv_system_destroy", "wv_system_last_message",
-            "wv_system_get_layout", "wv_system_rhs_device", "wv_system_rk4_device", "wv_system_rk4"]
+            "wv_system_get_layout", "wv_system_rhs_device", "wv_system_rk4_device", "wv_system_rk4",
+            "wv_rk4_set_dense_output", "wv_rk4_advance_to_time_device", "wv_rk4_advance_to_time",
+            "wv_rk4_dense_output_device"]
 
 
 def describe(configuration: Configuration):
@@ -575,6 +581,33 @@ class WVTransformConstantStratificationKernel:
         self._check(self._lib.wv_rk4_steps(self._h, Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data, ctypes.byref(tt),
                                            float(t0), float(dt), int(steps)))
         return Ap, Am, A0, tt.value
+
+    def setRK4DenseOutput(self, enabled=True):
+        """WVFixedStepRK4Options::retainDenseOutput for the RK4 entries of this handle."""
+        self._check(self._lib.wv_rk4_set_dense_output(self._h, int(bool(enabled))))
+
+    def rk4AdvanceToTime(self, Ap, Am, A0, t, t0, finalTime, dt):
+        """WVFixedStepRK4::advanceToTime: steps of min(dt, finalTime - t).  torch CUDA
+        inputs advance in place (returns finalTime); numpy inputs are copied
+        (returns (Ap, Am, A0, finalTime))."""
+        tt = ctypes.c_double(float(t))
+        if _is_torch(Ap):
+            Ap, Am, A0 = (self._dev_coeff(a, n) for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+            self._check(self._lib.wv_rk4_advance_to_time_device(self._h, Ap.data_ptr(), Am.data_ptr(), A0.data_ptr(),
+                                                                ctypes.byref(tt), float(t0), float(finalTime), float(dt),
+                                                                self._stream()))
+            return tt.value
+        Ap, Am, A0 = (self._host_coeff(a, n).copy() for a, n in zip((Ap, Am, A0), ("Ap", "Am", "A0")))
+        self._check(self._lib.wv_rk4_advance_to_time(self._h, Ap.ctypes.data, Am.ctypes.data, A0.ctypes.data,
+                                                     ctypes.byref(tt), float(t0), float(finalTime), float(dt)))
+        return Ap, Am, A0, tt.value
+
+    def rk4DenseOutput(self, time):
+        """WVFixedStepRK4::evaluateDenseOutput of the last RK4 step (new CUDA tensors)."""
+        import torch
+        out = tuple(torch.empty(self.spectral_shape, dtype=torch.complex128, device="cuda") for _ in range(3))
+        self._check(self._lib.wv_rk4_dense_output_device(self._h, float(time), *(o.data_ptr() for o in out), self._stream()))
+        return out
 
     # -- adjoint (torch CUDA tensors) ---------------------------------------------------
     def flux_vjp(self, t, t0, Ap, Am, A0, Fpb, Fmb, F0b):
