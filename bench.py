@@ -133,6 +133,19 @@ def dist_setup():
     return world, rank, local
 
 
+def replica_value(local_seconds, steps, world, dist=None, device="cpu"):
+    """Whole-job throughput of `world` replicas that each ran `steps` steps:
+    world * steps / (max over ranks of the local time), the max taken with an
+    all-reduce (NCCL on the GPU ranks, gloo in the CPU tests)."""
+    import torch
+    t = float(local_seconds)
+    if world > 1 and dist is not None:
+        tt = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return world * steps / t, t
+
+
 def configuration(wvgpu):
     return wvgpu.Configuration(Nx=GRID["Nx"], Ny=GRID["Ny"], Nz=GRID["Nz"], Nj=GRID["Nj"], Lx=GRID["Lx"], Ly=GRID["Ly"],
                                Lz=GRID["Lz"], N0=GRID["N0"], latitude=GRID["latitude"])
@@ -402,11 +415,7 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     def max_over_ranks(x):
-        if world > 1:
-            tt = torch.tensor([x], device="cuda", dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            return float(tt.item())
-        return x
+        return replica_value(x, 1, 1 if world == 1 else world, dist if world > 1 else None, "cuda")[1]
 
     t0 = 0.0
     dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
