@@ -255,7 +255,19 @@ def _stage_profile(k, dev, t, t0, dt, precision, torch):
     flux_ms = sum(per_launch.values())
     M, P = k.sizes["M"], k.sizes["active_rows"]
     b_flux = 104 * M + 24 * s * P * GRID["Nz"]
+    # arithmetic of the x pass (the dominant stage): per (y, z) row, 15 inverse and 4
+    # forward real transforms as complex lines of L = Nx/2 (5 L log2 L flops per line
+    # plus ~10 flops per entry for the real-transform pre/post twiddles) and the
+    # products (6 flops per point and target)
+    import math
+    L = GRID["Nx"] // 2
+    rows = GRID["Ny"] * GRID["Nz"]
+    x_flops = rows * (19 * (5 * L * math.log2(L) + 10 * L) + 4 * GRID["Nx"] * 6)
+    x_ms = per_launch["x_products"]
+    compute = {"stage": "x_products", "flops_per_launch": x_flops, "achieved_tflops": x_flops / (x_ms * 1e-3) / 1e12,
+               "pipe": "fp64" if precision == "fp64" else "fp32"}
     return {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "compute": compute,
             "frac": achieved / peaks["hbm_gbs"], "traffic": traffic_from_profile(dominant, precision),
             "peak_source": peak_kind, "algorithmic_bytes_per_launch": sbytes[dominant],
             "avg_launch_ms": per_launch[dominant], "stage_ms_per_flux": per_launch,
@@ -428,6 +440,8 @@ def run_ours(args):
     roofline = _stage_profile(k, dev, t, t0, dt, "fp64", torch)
     try:
         roofline["fp64_gemm_peak_tflops_measured"] = fp64_peak_tflops(torch)
+        roofline["compute"]["frac_of_fp64_gemm_peak"] = (roofline["compute"]["achieved_tflops"] /
+                                                         roofline["fp64_gemm_peak_tflops_measured"])
     except Exception:  # pragma: no cover
         roofline["fp64_gemm_peak_tflops_measured"] = None
 
