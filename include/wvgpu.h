@@ -1,7 +1,13 @@
 /*
  * wvgpu.h — C ABI of the GB300 (sm_103a) constant-stratification spectral
  * time step of WaveVortexModel: wave-vortex transforms, the nonlinear flux
- * with 2/3 antialiasing, adaptive damping and fixed-step RK4.
+ * with 2/3 antialiasing, adaptive damping, fixed-step RK4 (with advanceToTime
+ * and dense output) and adaptive RK23; the advection-field flux entries, field
+ * and field-family derivatives and F-grid scalar advection; integration
+ * systems with Lagrangian particles and tracers; vector-Jacobian products of
+ * the flux, the inverse transform and RK4; ensembles of uneven grids in one
+ * CUDA graph; FP64, mixed (FP32 + split-BF16 tensor cores) and paired-FP32
+ * (FP32X2) arithmetic.
  *
  * Plain pointers and sizes only.  Coefficient arrays are column-major
  * [Nj, Nkl] complex doubles stored as interleaved (re, im) pairs (the
