@@ -327,7 +327,7 @@ int wv_rk4_dense_output_device(wv_handle* handle, double time, double* Ap, doubl
  * No counterpart in the reference, which steps one state per kernel object
  * (a caller would hold one WVTransformConstantStratificationKernel per member).
  * An ensemble holds n_groups grids; group g steps members[g] states of
- * configs[g] side by side (each stage kernel covers all members of the group in
+ * group_configs[g] side by side (each stage kernel covers all members of the group in
  * one launch).  wv_ensemble_rk4_device captures the n-step RK4 integration of
  * every group (one stream per group) into one CUDA graph and launches it once;
  * a later call with the same groups and step count updates the graph's
@@ -351,7 +351,7 @@ typedef struct wv_ensemble_metrics {
     uint64_t member_steps;
     uint64_t device_bytes;
 } wv_ensemble_metrics;
-int wv_ensemble_create(const wv_config* configs, const int* members, int n_groups, int precision, int autotune,
+int wv_ensemble_create(const wv_config* group_configs, const int* members, int n_groups, int precision, int autotune,
                        wv_ensemble** ensemble);
 void wv_ensemble_destroy(wv_ensemble* ensemble);
 const char* wv_ensemble_last_message(const wv_ensemble* ensemble);

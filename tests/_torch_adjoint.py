@@ -1,5 +1,5 @@
 """torch.autograd.Function wrappers of the GPU adjoint entry points.  Test
-harness only: they let a test write the configs[3] misfit as an ordinary torch
+harness only: they let a test write the final-state misfit as an ordinary torch
 expression and differentiate it with loss.backward(); the shipped library
 exposes the VJPs through the C ABI (wv_rk4_adjoint_device, wv_inverse_vjp_device)
 and never depends on torch autograd.

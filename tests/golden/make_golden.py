@@ -29,7 +29,7 @@ LIB = os.path.join(ROOT, "oracle", "_ref", "libwvref.so")
 BASE = dict(N0=5.2e-3, rho0=1025.0, g=9.81, planetaryRadius=6.371e6, rotationRate=7.2921e-5)
 
 CASES = {
-    # BASELINE configs[0]: 40 km x 40 km x 1 km, 16x16x9, lat 45, single wave + damping
+    # 40 km x 40 km x 1 km, 16x16x9, lat 45: single internal wave + adaptive damping
     "c0_16x16x9": dict(Nx=16, Ny=16, Nz=9, Nj=5, Lx=40e3, Ly=40e3, Lz=1000.0, latitude=45.0,
                        isHydrostatic=False, shouldAntialias=True, damping=True, dt=10.0, steps=3),
     # odd grid (the survey's 15x13x9 parity case)
@@ -226,7 +226,7 @@ def main():
         fields = rng.standard_normal((nch, case["Nz"], case["Ny"], case["Nx"])) * 0.05
         Bp, Bm, B0 = r.forward(fields, t, t0)
         inv = r.inverse(Ap, Am, A0, t, t0)
-        # single internal wave state (configs[0] style) for the c0 case
+        # single internal wave state (kMode 1, lMode 0, j 1) for the c0 case
         if name.startswith("c0"):
             Sp = np.zeros(shape, np.complex128)
             Sm = np.zeros(shape, np.complex128)
@@ -272,7 +272,7 @@ def main():
         print(f"{name}: Nkl={r.Nkl} M={r.M}")
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
-    # configs[0] end to end: the single internal wave (kMode=1, lMode=0, j=1, u = 0.05 m/s)
+    # 16x16x9 end to end: the single internal wave (kMode=1, lMode=0, j=1, u = 0.05 m/s)
     # under {nonlinear advection, adaptive damping}, 60 RK4 steps of dt = 10 s to t = 600 s
     case = CASES["c0_16x16x9"]
     r = Ref(lib, case)

@@ -147,7 +147,7 @@ def test_checkpointed_adjoint_equals_chained_step_vjps(wv):
 
 
 def test_misfit_gradient_finite_differences(wv):
-    """configs[3]-style gradient: J = 0.5 ||(u, v, eta)(T) - target||^2 after n RK4
+    """Final-state misfit gradient: J = 0.5 ||(u, v, eta)(T) - target||^2 after n RK4
     steps, adjoint gradient vs Richardson-extrapolated central differences along
     random directions (step 1e-6 x rms of the state)."""
     import torch
@@ -212,7 +212,7 @@ def test_mixed_adjoint_close_to_fp64(wv, Nx, Nz, hydro):
 
 
 def test_autograd_misfit_gradient(wv):
-    """The configs[3] misfit written as a torch expression over the autograd
+    """The final-state misfit written as a torch expression over the autograd
     wrappers (tests/_torch_adjoint.py) and differentiated with backward(): the
     gradient equals the direct adjoint call and central differences along
     random directions."""

@@ -65,7 +65,7 @@ def test_fp32x2_flux_rhs_transforms_and_rk4_match_reference(wv, name):
 
 
 def test_fp32x2_configs0_to_t600(wv):
-    """The configs[0] single wave with adaptive damping, 60 RK4 steps to t = 600 s,
+    """The 16x16x9 single internal wave with adaptive damping, 60 RK4 steps to t = 600 s,
     against the reference's own run."""
     import os
     c = config_from_case(CASES["c0_16x16x9"])

@@ -221,7 +221,7 @@ def test_stage_instrumentation(wv):
 
 
 def test_configs0_single_wave_to_t600_matches_reference(wv):
-    """configs[0] end to end: 16x16x9, single internal wave (kMode=1, lMode=0, j=1,
+    """16x16x9 end to end: single internal wave (kMode=1, lMode=0, j=1,
     u = 0.05 m/s) under {nonlinear advection, adaptive damping}, 60 RK4 steps of
     10 s to t = 600 s, field by field against the reference FP64 path (its own
     run, tests/golden/c0_t600.npz)."""

@@ -142,7 +142,7 @@ def test_oracle_family_derivatives(name):
 
 
 def test_oracle_configs0_to_t600():
-    """configs[0]: single internal wave under {nonlinear advection, adaptive damping},
+    """16x16x9: single internal wave under {nonlinear advection, adaptive damping},
     60 RK4 steps of 10 s, against the reference's own run (coefficients and fields)."""
     c = config_from_case(golden_cases()["c0_16x16x9"])
     d = O.build_descriptor(c)

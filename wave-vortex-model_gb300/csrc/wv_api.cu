@@ -2399,11 +2399,11 @@ void wv_ensemble_destroy(wv_ensemble* e) {
     delete e;
 }
 
-int wv_ensemble_create(const wv_config* configs, const int* members, int n_groups, int precision, int autotune,
+int wv_ensemble_create(const wv_config* group_configs, const int* members, int n_groups, int precision, int autotune,
                        wv_ensemble** out) {
     if (!out) return WV_INVALID_POINTER;
     *out = nullptr;
-    if (!configs || !members) return WV_INVALID_POINTER;
+    if (!group_configs || !members) return WV_INVALID_POINTER;
     if (n_groups < 1 || n_groups > WV_ENSEMBLE_MAX_GROUPS) return WV_INVALID_CONFIGURATION;
     for (int g = 0; g < n_groups; ++g) if (members[g] < 1) return WV_INVALID_CONFIGURATION;
     if (precision == WV_PRECISION_FP32X2) return WV_UNSUPPORTED_OPERATION;  // ensembles are FP64 or MIXED
@@ -2412,7 +2412,7 @@ int wv_ensemble_create(const wv_config* configs, const int* members, int n_group
     cudaGetDevice(&e->device);
     for (int g = 0; g < n_groups; ++g) {
         wv_handle* h = nullptr;
-        const int rc = create_handle(&configs[g], precision, members[g], &h);
+        const int rc = create_handle(&group_configs[g], precision, members[g], &h);
         if (rc) { wv_ensemble_destroy(e); return rc; }
         e->groups.push_back(h);
         e->members.push_back(members[g]);
