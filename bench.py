@@ -525,7 +525,8 @@ def run_ours(args):
         fp32x2["rel_field_err_vs_fp64_after_100_steps"] = err
         fp32x2["meets_target_3x_and_1e-6"] = bool(fp32x2["speedup_vs_fp64"] >= 3.0 and max(err) <= 1e-6)
     kx.close()
-    adjoint = {p: _adjoint_timing(wvgpu, p, stream, torch, np) for p in ("fp64", "mixed")} if rank == 0 else None
+    adjoint = ({p: _adjoint_timing(wvgpu, p, stream, torch, np) for p in ("fp64", "mixed", "fp32x2")}
+               if rank == 0 else None)
     ensemble = _ensemble_timing(wvgpu, stream, torch, np) if rank == 0 and not args.no_ensemble else None
     published = _published_flux_comparison(wvgpu, torch, np) if rank == 0 else None
 

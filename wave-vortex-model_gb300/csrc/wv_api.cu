@@ -798,7 +798,9 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
 int ensure_adjoint(wv_handle* h) {
     if (h->adjointReady) return WV_SUCCESS;
     const Plan& p = h->plan;
-    const cudaError_t lim = h->precision == WV_PRECISION_FP64 ? set_smem_limits_adj<double>(p) : set_smem_limits_adj<float>(p);
+    const cudaError_t lim = h->precision == WV_PRECISION_FP64    ? set_smem_limits_adj<double>(p)
+                            : h->precision == WV_PRECISION_MIXED ? set_smem_limits_adj<float>(p)
+                                                                 : set_smem_limits_adj<dev::ff>(p);
     if (lim == cudaErrorInvalidConfiguration)
         return fail(h, WV_UNSUPPORTED_OPERATION, "The adjoint kernels need more shared memory than one CTA has for this grid.");
     if (lim != cudaSuccess) return cuda_fail(h, lim, "adjoint set-up");
@@ -918,7 +920,8 @@ cudaError_t flux_vjp_any(wv_handle* h, double t, double t0, const double* y, con
     const size_t M2 = 2 * h->plan.M;
     return h->precision == WV_PRECISION_FP64
                ? launch_flux_vjp<double>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, physIn)
-               : launch_flux_vjp<float>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, physIn);
+               : h->precision == WV_PRECISION_MIXED ? launch_flux_vjp<float>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, physIn)
+                                                          : launch_flux_vjp<dev::ff>(h, t, t0, y, y + M2, y + 2 * M2, yb, yb + M2, yb + 2 * M2, out, out + M2, out + 2 * M2, s, physIn);
 }
 
 cudaError_t flux_any(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, double* Fp,
@@ -2060,7 +2063,6 @@ int wv_flux_vjp_device(wv_handle* h, double t, double t0, const double* Ap, cons
                        const double* Fpb, const double* Fmb, const double* F0b, double* Apb, double* Amb, double* A0b,
                        void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "The flux adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     const void* ptrs[] = {Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b};
     for (const void* q : ptrs) if (!q) return fail(h, WV_INVALID_POINTER, "Flux VJP received a null pointer.");
@@ -2070,14 +2072,14 @@ int wv_flux_vjp_device(wv_handle* h, double t, double t0, const double* Ap, cons
     auto s = static_cast<cudaStream_t>(stream);
     const cudaError_t e = h->precision == WV_PRECISION_FP64
         ? launch_flux_vjp<double>(h, t, t0, Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b, s)
-        : launch_flux_vjp<float>(h, t, t0, Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b, s);
+        : h->precision == WV_PRECISION_MIXED ? launch_flux_vjp<float>(h, t, t0, Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b, s)
+                                                   : launch_flux_vjp<dev::ff>(h, t, t0, Ap, Am, A0, Fpb, Fmb, F0b, Apb, Amb, A0b, s);
     return finish(h, e, "flux VJP");
 }
 
 int wv_inverse_vjp_device(wv_handle* h, double t, double t0, const double* fb, double* Apb, double* Amb, double* A0b,
                           void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "The inverse-transform adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (!fb || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "Inverse VJP received a null pointer.");
     Guard g(h->busy);
@@ -2085,8 +2087,9 @@ int wv_inverse_vjp_device(wv_handle* h, double t, double t0, const double* fb, d
     cudaSetDevice(h->device);
     rc = ensure_adjoint(h); if (rc) return rc;
     auto s = static_cast<cudaStream_t>(stream);
-    const cudaError_t e = h->precision == WV_PRECISION_FP64 ? launch_inverse_vjp<double>(h, t, t0, fb, Apb, Amb, A0b, s)
-                                                            : launch_inverse_vjp<float>(h, t, t0, fb, Apb, Amb, A0b, s);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64    ? launch_inverse_vjp<double>(h, t, t0, fb, Apb, Amb, A0b, s)
+                          : h->precision == WV_PRECISION_MIXED ? launch_inverse_vjp<float>(h, t, t0, fb, Apb, Amb, A0b, s)
+                                                               : launch_inverse_vjp<dev::ff>(h, t, t0, fb, Apb, Amb, A0b, s);
     return finish(h, e, "inverse VJP");
 }
 
@@ -2110,7 +2113,6 @@ static cudaError_t scatter3(wv_handle* h, const double* src, double* a, double* 
 int wv_rk4_step_vjp_device(wv_handle* h, const double* Ap, const double* Am, const double* A0, double t, double t0, double dt,
                            double* Apb, double* Amb, double* A0b, void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "The RK4 adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (!Ap || !Am || !A0 || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "RK4 VJP received a null pointer.");
     if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
@@ -2128,7 +2130,6 @@ int wv_rk4_step_vjp_device(wv_handle* h, const double* Ap, const double* Am, con
 int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, const double* A0, double t, double t0, double dt,
                           int n, int K, double* Apb, double* Amb, double* A0b, void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "The RK4 adjoint"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (!Ap || !Am || !A0 || !Apb || !Amb || !A0b) return fail(h, WV_INVALID_POINTER, "RK4 adjoint received a null pointer.");
     if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, WV_INVALID_CONFIGURATION, "RK4 step size must be finite and positive.");
