@@ -55,6 +55,22 @@ def test_fp32x2_flux_rhs_transforms_and_rk4_match_reference(wv, name):
         B = k.transformUVWEtaToWaveVortex(g["fields"], t, t0)
     for got, key in zip(B, ("Bp", "Bm", "B0")):
         assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    # advection-field entries, derivative bundles and F-grid scalar advection
+    args = (t, t0, g["Ap"], g["Am"], g["A0"])
+    Fw, adv = k.nonlinearFluxWithAdvectionFields(*args)
+    for got, key in zip(Fw, ("with_Fp", "with_Fm", "with_F0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    assert rel_err(adv, g["with_fields"]) <= FP32X2_TOL
+    Fu = k.nonlinearFluxUsingAdvectionFields(*args, g["given_fields"])
+    for got, key in zip(Fu, ("using_Fp", "using_Fm", "using_F0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    assert rel_err(k.transformWaveVortexToUVW(*args), g["uvw"]) <= FP32X2_TOL
+    for q in ((0, 1, 3) if cf["isHydrostatic"] else (0, 1, 2, 3)):
+        assert rel_err(k.transformStateFieldDerivatives(*args, q), g[f"deriv_{q}"]) <= FP32X2_TOL, (name, q)
+    assert rel_err(k.transformToSpatialDomainWithFAllDerivatives(g["Apm"], g["A0"]), g["fall"]) <= FP32X2_TOL
+    assert rel_err(k.transformToSpatialDomainWithGAllDerivatives(g["Apm"], g["A0"]), g["gall"]) <= FP32X2_TOL
+    for aa, key in ((False, "scalar_rhs"), (True, "scalar_rhs_aa")):
+        assert rel_err(k.advectFGridScalar(g["scalar"], g["given_fields"], aa), g[key]) <= FP32X2_TOL, (name, key)
     Kp, Km, K0, tK = k.rk4(g["rk_Ap"], g["rk_Am"], g["rk_A0"], float(g["rk_t"]), float(g["rk_t0"]), float(g["rk_dt"]),
                            int(g["rk_steps"]))
     assert tK == float(g["rk_tout"])
@@ -164,9 +180,6 @@ def test_fp32x2_rejects_entry_points_without_a_paired_form(wv):
     dev = [torch.from_numpy(np.ascontiguousarray(g[n])).cuda() for n in ("Ap", "Am", "A0")]
     with pytest.raises(wv.WVKernelError) as e:
         k.set_vertical_kernel("tensor")
-    assert e.value.code == 10
-    with pytest.raises(wv.WVKernelError) as e:
-        k.advectFGridScalar(np.zeros((c.Nz, c.Ny, c.Nx)), np.zeros((3, c.Nz, c.Ny, c.Nx)), True)
     assert e.value.code == 10
     k.close()
     with pytest.raises((wv.WVKernelError, ValueError, KeyError)):

@@ -582,7 +582,15 @@ int ensure_scalar(wv_handle* h) {
     auto upT = [&](const std::vector<double>& v, const void** dst) {
         if (e != cudaSuccess) return;
         if (h->precision == WV_PRECISION_FP64) { const double* q = nullptr; e = upload(h, v, &q); *dst = q; }
-        else { const std::vector<float> f = cast<float>(v); const float* q = nullptr; e = upload(h, f, &q); *dst = q; }
+        else if (h->precision == WV_PRECISION_FP32X2) {
+            std::vector<float> f(2 * v.size());  // (hi, lo) pairs
+            for (size_t i = 0; i < v.size(); ++i) {
+                const dev::ff x(v[i]);
+                f[2 * i] = x.hi;
+                f[2 * i + 1] = x.lo;
+            }
+            const float* q = nullptr; e = upload(h, f, &q); *dst = q;
+        } else { const std::vector<float> f = cast<float>(v); const float* q = nullptr; e = upload(h, f, &q); *dst = q; }
     };
     upT(rowK, &sd.tRowK);
     upT(rowL, &sd.tRowL);
@@ -597,12 +605,14 @@ int ensure_scalar(wv_handle* h) {
     const size_t L = x_len(p);
     const size_t smC2R = (L + Nx + 3 * NxHalf + 8 * L) * cb;
     if (e == cudaSuccess)
-        e = h->precision == WV_PRECISION_FP64 ? raise_smem_limit(dev::k_xc2r_fields<double>, static_cast<int>(smC2R))
-                                              : raise_smem_limit(dev::k_xc2r_fields<float>, static_cast<int>(smC2R));
+        e = h->precision == WV_PRECISION_FP64    ? raise_smem_limit(dev::k_xc2r_fields<double>, static_cast<int>(smC2R))
+            : h->precision == WV_PRECISION_MIXED ? raise_smem_limit(dev::k_xc2r_fields<float>, static_cast<int>(smC2R))
+                                                 : raise_smem_limit(dev::k_xc2r_fields<dev::ff>, static_cast<int>(smC2R));
     const size_t smD = Nz * dev::kScalarCols * cb;
     if (e == cudaSuccess)
-        e = h->precision == WV_PRECISION_FP64 ? raise_smem_limit(dev::k_scalar_derivs<double>, static_cast<int>(smD))
-                                              : raise_smem_limit(dev::k_scalar_derivs<float>, static_cast<int>(smD));
+        e = h->precision == WV_PRECISION_FP64    ? raise_smem_limit(dev::k_scalar_derivs<double>, static_cast<int>(smD))
+            : h->precision == WV_PRECISION_MIXED ? raise_smem_limit(dev::k_scalar_derivs<float>, static_cast<int>(smD))
+                                                 : raise_smem_limit(dev::k_scalar_derivs<dev::ff>, static_cast<int>(smD));
     if (e != cudaSuccess) return cuda_fail(h, e, "scalar advection set-up");
     h->sd = sd;
     h->scalarReady = true;
@@ -1642,7 +1652,6 @@ int wv_inverse_uvw(wv_handle* h, double t, double t0, const double* Ap, const do
 int wv_field_derivatives_device(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
                                 int field, double* out, void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "State-field derivatives"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (field < 0 || field > 3) return fail(h, WV_INVALID_CONFIGURATION, "Unknown dynamical field derivative target.");
     if (!Ap || !Am || !A0 || !out) return fail(h, WV_INVALID_POINTER, "Field derivatives received a null pointer.");
@@ -1654,16 +1663,15 @@ int wv_field_derivatives_device(wv_handle* h, double t, double t0, const double*
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
     cudaSetDevice(h->device);
     auto s = static_cast<cudaStream_t>(stream);
-    const cudaError_t e = h->precision == WV_PRECISION_FP64
-                              ? launch_field_derivatives<double>(h, t, t0, Ap, Am, A0, field, out, s)
-                              : launch_field_derivatives<float>(h, t, t0, Ap, Am, A0, field, out, s);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64 ? launch_field_derivatives<double>(h, t, t0, Ap, Am, A0, field, out, s)
+                : h->precision == WV_PRECISION_MIXED ? launch_field_derivatives<float>(h, t, t0, Ap, Am, A0, field, out, s)
+                                                     : launch_field_derivatives<dev::ff>(h, t, t0, Ap, Am, A0, field, out, s);
     return finish(h, e, "field derivatives");
 }
 
 int wv_family_derivatives_device(wv_handle* h, int ffamily, const double* Apm, const double* A0, double* fields,
                                  void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "Field-family derivatives"); if (rp) return rp; }
     if (!Apm || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Field-family derivatives received a null pointer.");
     if (h->dd.members != 1) return fail(h, WV_UNSUPPORTED_OPERATION, "Field-family derivatives are per single-state handle.");
     const size_t fb = 4 * h->plan.Nx * h->plan.Ny * h->plan.Nz * sizeof(double), cb = h->plan.M * 16;
@@ -1673,15 +1681,14 @@ int wv_family_derivatives_device(wv_handle* h, int ffamily, const double* Apm, c
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
     cudaSetDevice(h->device);
     auto s = static_cast<cudaStream_t>(stream);
-    const cudaError_t e = h->precision == WV_PRECISION_FP64
-                              ? launch_family_derivatives<double>(h, ffamily != 0, Apm, A0, fields, s)
-                              : launch_family_derivatives<float>(h, ffamily != 0, Apm, A0, fields, s);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64 ? launch_family_derivatives<double>(h, ffamily != 0, Apm, A0, fields, s)
+                : h->precision == WV_PRECISION_MIXED ? launch_family_derivatives<float>(h, ffamily != 0, Apm, A0, fields, s)
+                                                     : launch_family_derivatives<dev::ff>(h, ffamily != 0, Apm, A0, fields, s);
     return finish(h, e, "field-family derivatives");
 }
 
 int wv_family_derivatives(wv_handle* h, int ffamily, const double* Apm, const double* A0, double* fields) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "Field-family derivatives"); if (rp) return rp; }
     if (!Apm || !A0 || !fields) return fail(h, WV_INVALID_POINTER, "Field-family derivatives received a null pointer.");
     Guard g(h->busy);
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
@@ -1693,7 +1700,8 @@ int wv_family_derivatives(wv_handle* h, int ffamily, const double* Apm, const do
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->state + M2, A0, cb, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = h->precision == WV_PRECISION_FP64 ? launch_family_derivatives<double>(h, ffamily != 0, h->state, h->state + M2, h->fields, s)
-                                              : launch_family_derivatives<float>(h, ffamily != 0, h->state, h->state + M2, h->fields, s);
+                : h->precision == WV_PRECISION_MIXED ? launch_family_derivatives<float>(h, ffamily != 0, h->state, h->state + M2, h->fields, s)
+                                                     : launch_family_derivatives<dev::ff>(h, ffamily != 0, h->state, h->state + M2, h->fields, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fields, h->fields, fb, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     return finish(h, e, "field-family derivatives");
@@ -1712,22 +1720,20 @@ static int scalar_entry_checks(wv_handle* h, const double* scalar, const double*
 int wv_advect_fgrid_scalar_device(wv_handle* h, const double* scalar, const double* fields, int antialias, double* rhs,
                                   void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "F-grid scalar advection"); if (rp) return rp; }
     int rc = scalar_entry_checks(h, scalar, fields, rhs); if (rc) return rc;
     Guard g(h->busy);
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
     cudaSetDevice(h->device);
     rc = ensure_scalar(h); if (rc) return rc;
     auto s = static_cast<cudaStream_t>(stream);
-    const cudaError_t e = h->precision == WV_PRECISION_FP64
-                              ? launch_scalar_advection<double>(h, scalar, fields, antialias != 0, rhs, s)
-                              : launch_scalar_advection<float>(h, scalar, fields, antialias != 0, rhs, s);
+    const cudaError_t e = h->precision == WV_PRECISION_FP64 ? launch_scalar_advection<double>(h, scalar, fields, antialias != 0, rhs, s)
+                : h->precision == WV_PRECISION_MIXED ? launch_scalar_advection<float>(h, scalar, fields, antialias != 0, rhs, s)
+                                                     : launch_scalar_advection<dev::ff>(h, scalar, fields, antialias != 0, rhs, s);
     return finish(h, e, "scalar advection");
 }
 
 int wv_advect_fgrid_scalar(wv_handle* h, const double* scalar, const double* fields, int antialias, double* rhs) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "F-grid scalar advection"); if (rp) return rp; }
     int rc = scalar_entry_checks(h, scalar, fields, rhs); if (rc) return rc;
     Guard g(h->busy);
     if (!g.entered) return fail(h, WV_REENTRANT_EXECUTION, "Kernel operations are not reentrant.");
@@ -1743,7 +1749,8 @@ int wv_advect_fgrid_scalar(wv_handle* h, const double* scalar, const double* fie
     if (e == cudaSuccess) e = cudaMemcpyAsync(dAdv, fields, 3 * bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = h->precision == WV_PRECISION_FP64 ? launch_scalar_advection<double>(h, dScalar, dAdv, antialias != 0, dRhs, s)
-                                              : launch_scalar_advection<float>(h, dScalar, dAdv, antialias != 0, dRhs, s);
+                : h->precision == WV_PRECISION_MIXED ? launch_scalar_advection<float>(h, dScalar, dAdv, antialias != 0, dRhs, s)
+                                                     : launch_scalar_advection<dev::ff>(h, dScalar, dAdv, antialias != 0, dRhs, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(rhs, dRhs, bytes, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     return finish(h, e, "scalar advection");
@@ -1752,7 +1759,6 @@ int wv_advect_fgrid_scalar(wv_handle* h, const double* scalar, const double* fie
 int wv_field_derivatives(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0, int field,
                          double* out) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "State-field derivatives"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     if (field < 0 || field > 3) return fail(h, WV_INVALID_CONFIGURATION, "Unknown dynamical field derivative target.");
     if (!Ap || !Am || !A0 || !out) return fail(h, WV_INVALID_POINTER, "Field derivatives received a null pointer.");
@@ -1767,9 +1773,9 @@ int wv_field_derivatives(wv_handle* h, double t, double t0, const double* Ap, co
     for (int c = 0; c < 3 && e == cudaSuccess; ++c)
         e = cudaMemcpyAsync(reinterpret_cast<char*>(h->state) + c * cb, in[c], cb, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-        e = h->precision == WV_PRECISION_FP64
-                ? launch_field_derivatives<double>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, field, h->fields, s)
-                : launch_field_derivatives<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, field, h->fields, s);
+        e = h->precision == WV_PRECISION_FP64 ? launch_field_derivatives<double>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, field, h->fields, s)
+                : h->precision == WV_PRECISION_MIXED ? launch_field_derivatives<float>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, field, h->fields, s)
+                                                     : launch_field_derivatives<dev::ff>(h, t, t0, h->state, h->state + M2, h->state + 2 * M2, field, h->fields, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, h->fields, fb, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     return finish(h, e, "field derivatives");
