@@ -182,5 +182,31 @@ def test_fp32x2_rejects_entry_points_without_a_paired_form(wv):
         k.set_vertical_kernel("tensor")
     assert e.value.code == 10
     k.close()
-    with pytest.raises((wv.WVKernelError, ValueError, KeyError)):
-        wv.WVEnsemble([_conf(wv, c)], [2], precision="fp32x2", autotune=False)
+
+
+def test_fp32x2_ensemble_members_equal_single_handles(wv):
+    """Member-batched FP32X2 groups in one graph launch step every member exactly
+    as a single FP32X2 handle does."""
+    import torch
+    cfgs = [wv.Configuration(Nx=64, Ny=64, Nz=33, Nj=21, Lx=200e3, Ly=200e3, Lz=4000.0, latitude=33.0),
+            wv.Configuration(Nx=48, Ny=40, Nz=25, Nj=16, Lx=150e3, Ly=125e3, Lz=4000.0, latitude=33.0)]
+    ens = wv.WVEnsemble(cfgs, [2, 3], precision="fp32x2", autotune=True)
+    X, singles = [], []
+    for g, cfg in enumerate(cfgs):
+        k = wv.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
+        B = ens.members[g]
+        X.append(torch.from_numpy(np.stack([np.stack(wv.synthetic_state(k, seed=60 + 7 * g + m, urms=0.1))
+                                            for m in range(B)])).cuda())
+        singles.append(k)
+    Xe = [x.clone() for x in X]
+    ens.rk4(Xe, 0.0, 0.0, [300.0, 250.0], 2)
+    torch.cuda.synchronize()
+    for g, (k, x0, xe) in enumerate(zip(singles, X, Xe)):
+        for m in range(x0.shape[0]):
+            s = [x0[m, c].clone() for c in range(3)]
+            k.rk4(*s, 0.0, 0.0, [300.0, 250.0][g], 2)
+            torch.cuda.synchronize()
+            for c in range(3):
+                assert torch.equal(s[c], xe[m, c]), (g, m, c)
+        k.close()
+    ens.close()

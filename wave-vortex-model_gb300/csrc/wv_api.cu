@@ -2353,7 +2353,7 @@ float time_group_flux(wv_handle* h, int reps, cudaStream_t s, cudaError_t& err) 
 cudaError_t autotune_group(wv_handle* h, cudaStream_t s, wv_ensemble_tuning& out) {
     cudaError_t e = cudaMemsetAsync(h->state, 0, 6 * h->plan.M * h->dd.members * sizeof(double), s);
     Plan& p = h->plan;
-    const bool fp32 = h->precision != WV_PRECISION_FP64;
+    const bool fp32 = h->precision == WV_PRECISION_MIXED;  // warp FFT variants exist for FP32 only
     const bool warpY = fp32 && warp_ry<float>(p) != 0, warpX = fp32 && warp_rx<float>(p) != 0;
     float best = -1.0f;
     bool bestY = false, bestX = false, bestTC = false;
@@ -2413,7 +2413,6 @@ int wv_ensemble_create(const wv_config* group_configs, const int* members, int n
     if (!group_configs || !members) return WV_INVALID_POINTER;
     if (n_groups < 1 || n_groups > WV_ENSEMBLE_MAX_GROUPS) return WV_INVALID_CONFIGURATION;
     for (int g = 0; g < n_groups; ++g) if (members[g] < 1) return WV_INVALID_CONFIGURATION;
-    if (precision == WV_PRECISION_FP32X2) return WV_UNSUPPORTED_OPERATION;  // ensembles are FP64 or MIXED
     wv_ensemble* e = new (std::nothrow) wv_ensemble();
     if (!e) return WV_ALLOCATION_FAILURE;
     cudaGetDevice(&e->device);
@@ -2443,8 +2442,8 @@ int wv_ensemble_create(const wv_config* group_configs, const int* members, int n
             wv_ensemble_tuning& t = e->tuning[g];
             t.stockham_y = h->plan.stockhamY ? 1 : 0;
             t.stockham_x = h->plan.stockhamX ? 1 : 0;
-            t.warp_y_available = h->precision != WV_PRECISION_FP64 && warp_ry<float>(h->plan) != 0;
-            t.warp_x_available = h->precision != WV_PRECISION_FP64 && warp_rx<float>(h->plan) != 0;
+            t.warp_y_available = h->precision == WV_PRECISION_MIXED && warp_ry<float>(h->plan) != 0;
+            t.warp_x_available = h->precision == WV_PRECISION_MIXED && warp_rx<float>(h->plan) != 0;
             t.tensor_vertical_available = h->tcAvailable ? 1 : 0;
             t.vertical = WV_VERTICAL_CUDA_CORES;
             t.flux_ms = -1.0f;
