@@ -65,8 +65,7 @@ typedef struct wv_config {
  * FP32X2: the xy transforms, products and vertical contractions in paired FP32
  * ("float-float", about 48 significand bits) on the FP32 pipe, FP64 phases,
  * projections and RK4 -- FP64-class flux accuracy without the FP64 pipe.
- * FP32X2 handles serve every kernel operation, the adjoint and ensembles; the
- * static-scratch flux returns WV_UNSUPPORTED_OPERATION for them. */
+ * FP32X2 handles serve every entry point (kernel operations, adjoint, ensembles). */
 enum { WV_PRECISION_FP64 = 0, WV_PRECISION_MIXED = 1, WV_PRECISION_FP32X2 = 2 };
 
 /* Forcing schedule of the right-hand side (WVFrozenForcingSchedule entries

@@ -39,11 +39,12 @@ def _config(wv, Nx, Ny, Nz):
                             latitude=33.0)
 
 
-def test_noalloc_flux_matches_device_entry_on_two_calls(wv):
+@pytest.mark.parametrize("precision", ["fp64", "fp32x2"])
+def test_noalloc_flux_matches_device_entry_on_two_calls(wv, precision):
     import torch
     c = _config(wv, 64, 64, 33)
     d = O.build_descriptor(O.Config(Nx=c.Nx, Ny=c.Ny, Nz=c.Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, latitude=c.latitude))
-    k = wv.WVTransformConstantStratificationKernel(c)
+    k = wv.WVTransformConstantStratificationKernel(c, precision=precision)
     lib = wv.load_library()
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for seed, (t, t0) in ((11, (500.0, 0.0)), (12, (1234.5, 10.0))):

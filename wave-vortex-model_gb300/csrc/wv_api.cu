@@ -1072,12 +1072,6 @@ int finish(wv_handle* h, cudaError_t e, const char* where) {
     return WV_SUCCESS;
 }
 
-// Entry points whose kernels have no paired-FP32 form (adjoint, derivative
-// bundles, F-grid scalars, the static-scratch flux) reject FP32X2 handles.
-int reject_paired(wv_handle* h, const char* what) {
-    if (h->precision != WV_PRECISION_FP32X2) return WV_SUCCESS;
-    return fail(h, WV_UNSUPPORTED_OPERATION, std::string(what) + " is not available on FP32X2 handles.");
-}
 
 // ---- static scratch for callers that cannot allocate ------------------------------
 //
@@ -2266,7 +2260,6 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
 int wv_nonlinear_flux_device_noalloc(wv_handle* h, double t, double t0, const double* Ap, const double* Am,
                                      const double* A0, double* Fp, double* Fm, double* F0, void* stream) {
     if (!h) return WV_INVALID_POINTER;
-    { const int rp = reject_paired(h, "The static-scratch flux"); if (rp) return rp; }
     int rc = check_times(h, t, t0); if (rc) return rc;
     rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
     size_t offs[5];
@@ -2282,9 +2275,10 @@ int wv_nonlinear_flux_device_noalloc(wv_handle* h, double t, double t0, const do
     if (e == cudaSuccess) e = static_scratch_address(h->device, &base);
     if (e != cudaSuccess) return cuda_fail(h, e, "static scratch set-up");
     auto s = static_cast<cudaStream_t>(stream);
-    e = h->precision == WV_PRECISION_FP64
-            ? launch_flux_static<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, static_cast<unsigned char*>(base), offs, s)
-            : launch_flux_static<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, static_cast<unsigned char*>(base), offs, s);
+    unsigned char* sb = static_cast<unsigned char*>(base);
+    e = h->precision == WV_PRECISION_FP64    ? launch_flux_static<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, sb, offs, s)
+        : h->precision == WV_PRECISION_MIXED ? launch_flux_static<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, sb, offs, s)
+                                             : launch_flux_static<dev::ff>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, sb, offs, s);
     h->metrics.nonlinear_flux_calls++;
     h->metrics.kernel_launches += 5;
     return finish(h, e, "nonlinear flux (static scratch)");
