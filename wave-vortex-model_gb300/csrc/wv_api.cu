@@ -13,6 +13,7 @@
 #include "wv_warpfft.cuh"
 #include "wv_adjoint.cuh"
 #include "wv_vinv_tc.cuh"
+#include "wv_vfwd_tc.cuh"
 #include "wv_scalar.cuh"
 
 #include <cuda_runtime.h>
@@ -87,6 +88,8 @@ struct wv_handle {
     bool tcAvailable = false;  // tensor-core vertical transform built for this handle
     bool verticalTC = false;   // ... and selected (default: on where built)
     size_t tcSmem = 0;
+    bool tcFwdAvailable = false;  // tensor-core forward vertical transform built (used with verticalTC)
+    size_t tcFwdSmem = 0;
     // F-grid scalar advection (built on first use): full-spectrum descriptor copy,
     // z-derivative matrix, per-position flags and scratch
     bool scalarReady = false;
@@ -193,6 +196,33 @@ std::vector<uint16_t> tc_vertical_blob(const Plan& p, int NP, int KE, int K) {
                 out[(static_cast<size_t>(m) * 3 + 0) * split + e] = hb;
                 out[(static_cast<size_t>(m) * 3 + 1) * split + e] = mb;
                 out[(static_cast<size_t>(m) * 3 + 2) * split + e] = lb;
+            }
+    return out;
+}
+
+// The forward matrices Fcos, Fsin ([Nj][zHalf], FP64) as three BF16 pieces,
+// laid out for the tensor-core forward transform: [family cos|sin][parity
+// even|odd][piece][NF rows][KF], row c holding output j = 2 c + parity, column
+// k = n < zHalf, canonical no-swizzle K-major core matrices; zeros elsewhere.
+std::vector<uint16_t> tc_forward_blob(const Plan& p, int NF, int KF) {
+    const size_t split = static_cast<size_t>(NF) * KF;
+    std::vector<uint16_t> out(2 * 2 * 3 * split, 0);
+    const std::vector<double>* mats[2] = {&p.Fcos, &p.Fsin};
+    const int Zh = static_cast<int>(p.zHalf), Nj = static_cast<int>(p.Nj);
+    for (int m = 0; m < 2; ++m)
+        for (int j = 0; j < Nj; ++j)
+            for (int n = 0; n < Zh; ++n) {
+                const double c = (*mats[m])[static_cast<size_t>(j) * Zh + n];
+                const uint16_t hb = bf16_rne(static_cast<float>(c));
+                const double r1 = c - bf16_value(hb);
+                const uint16_t mb = bf16_rne(static_cast<float>(r1));
+                const double r2 = r1 - bf16_value(mb);
+                const uint16_t lb = bf16_rne(static_cast<float>(r2));
+                const size_t e = dev::tc_kmajor_offset(j >> 1, n, KF) / 2;
+                const size_t blk = static_cast<size_t>(m) * 2 + (j & 1);
+                out[(blk * 3 + 0) * split + e] = hb;
+                out[(blk * 3 + 1) * split + e] = mb;
+                out[(blk * 3 + 2) * split + e] = lb;
             }
     return out;
 }
@@ -499,9 +529,22 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     if (inst) cudaEventRecord(h->ev[3], s);
     launch_yfwd<T>(h, ps, nt, f, s);
     if (inst) cudaEventRecord(h->ev[4], s);
-    dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
-        d, f, nt, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
-    h->metrics.kernel_launches += 5;
+    bool fwdTC = false;
+    if constexpr (sizeof(T) == 4) {
+        if (h->verticalTC && h->tcFwdAvailable) {
+            // the z-grid spectra are consumed by now: their buffer holds the transformed columns
+            auto* vs = reinterpret_cast<float2*>(z);
+            dev::k_vfwd_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcFwdSmem, s>>>(
+                d, reinterpret_cast<const float2*>(f), vs);
+            const int blocks = static_cast<int>(std::min<size_t>(cdiv(static_cast<size_t>(d.members) * p.M, 256), 65535));
+            dev::k_vfwd_proj<<<blocks, 256, 0, s>>>(d, vs, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
+            fwdTC = true;
+        }
+    }
+    if (!fwdTC)
+        dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
+            d, f, nt, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
+    h->metrics.kernel_launches += fwdTC ? 6 : 5;
     cudaError_t e = cudaGetLastError();
     if (inst && e == cudaSuccess) {
         cudaEventRecord(h->ev[5], s);
@@ -1363,6 +1406,20 @@ static int create_handle(const wv_config* config, int precision, int members, wv
             int sms = 0;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
             h->verticalTC = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
+        }
+        // forward transform: two accumulators of NF <= 128 output rows over K = zHalf
+        const int NF = static_cast<int>(((p.Nj + 1) / 2 + 15) / 16 * 16), KF = static_cast<int>((p.zHalf + 15) / 16 * 16);
+        const size_t smemF = 6 * (256u * KF) + 6 * static_cast<size_t>(NF / 8) * 16u * KF;
+        const size_t vspecBytes = 4 * p.M * sizeof(float2), zBytes = scratch_sizes(p).z * 2 * sizeof(float);
+        if (e == cudaSuccess && h->tcAvailable && NF <= 128 && smemF <= 220 * 1024 && vspecBytes <= zBytes) {
+            const std::vector<uint16_t> blob = tc_forward_blob(p, NF, KF);
+            const uint16_t* q = nullptr;
+            e = upload(h, blob, &q);
+            dd.tcFB = reinterpret_cast<const unsigned short*>(q);
+            dd.tcFN = NF; dd.tcFK = KF;
+            h->tcFwdSmem = smemF;
+            if (e == cudaSuccess) e = raise_smem_limit(dev::k_vfwd_tc, static_cast<int>(smemF));
+            h->tcFwdAvailable = e == cudaSuccess;
         }
     }
     const auto ss = scratch_sizes(p);

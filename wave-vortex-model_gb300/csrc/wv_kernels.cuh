@@ -255,6 +255,10 @@ struct DescDev {
     // 16, K = KE (even j) + odd j, each rounded up to 16.
     const unsigned short* tcB;
     int tcN, tcKE, tcK;
+    // ... and the forward matrices Fcos, Fsin split by output parity:
+    // [family cos|sin][parity even|odd][piece][NF rows j/2][KF = Zh rounded up to 16]
+    const unsigned short* tcFB;
+    int tcFN, tcFK;
     unsigned* status;       // device status word (bit 0: a bounded wait ran out)
     int c2rUseK;            // k_xc2r_fields(_w): bit c set -> channel c is multiplied by i k (x derivative)
     // field-family scales (transformToSpatialDomainWith{F,G}AllDerivatives)
@@ -883,6 +887,51 @@ __global__ void __launch_bounds__(256) k_yfwd(DescDev d, const cx<T>* __restrict
 
 constexpr int kVfwdModes = 8;
 
+// MIXED flux projection of one (mode, j): the folded FP32 map (fProj: Cu, Cv,
+// Cw complex, Du, Dv, Dn, Npm, B) of the target spectra ch[q] = (u, v, w, eta)
+// -> cp, cm, f0, an FP32 phase after FP64 angle reduction, FP64 adaptive
+// damping and FP64 stores (projectFluxTargetMode, kernel.cpp:396-431).
+__device__ __forceinline__ void mixed_project_store(const DescDev& d, int idx, int w, int j, const float2 (&ch)[4],
+                                                    double elapsed, double maxSpeed, int applyDamping,
+                                                    const double* __restrict__ Ap, const double* __restrict__ Am,
+                                                    const double* __restrict__ A0, double* __restrict__ Fp,
+                                                    double* __restrict__ Fm, double* __restrict__ F0) {
+    const float2 U = ch[0], V = ch[1], Wc = ch[2], N = ch[3];
+    const float4* pj = reinterpret_cast<const float4*>(d.fProj + 12 * (size_t)idx);
+    const float4 p0 = pj[0], p1 = pj[1], p2 = pj[2];
+    const float f0r = -p1.z * U.y - p1.w * V.y + p2.x * N.x;
+    const float f0i = p1.z * U.x + p1.w * V.x + p2.x * N.y;
+    float cpr, cpi, cmr, cmi;
+    if (w == 0) {
+        const float sc = float(d.inertialScale[j]);
+        cpr = sc * (U.x + V.y);
+        cpi = sc * (U.y - V.x);
+        cmr = cpr;
+        cmi = -cpi;
+    } else {
+        const float wr = p0.x * U.x - p0.y * U.y + p0.z * V.x - p0.w * V.y + p1.x * Wc.x - p1.y * Wc.y;
+        const float wi = p0.x * U.y + p0.y * U.x + p0.z * V.y + p0.w * V.x + p1.x * Wc.y + p1.y * Wc.x;
+        const float br = p2.y * N.x - p2.z * f0r, bi = p2.y * N.y - p2.z * f0i;
+        cpr = wr + br; cpi = wi + bi; cmr = wr - br; cmi = wi - bi;
+    }
+    const double ang = d.omega[idx] * elapsed;
+    const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+    float sn, cs;
+    sincosf(float(red), &sn, &cs);
+    zd fp{double(cpr * cs + cpi * sn), double(cpi * cs - cpr * sn)};   // (cp) * conj(p)
+    zd fm{double(cmr * cs - cmi * sn), double(cmr * sn + cmi * cs)};   // (cm) * p
+    zd f0{double(f0r), double(f0i)};
+    if (applyDamping) {
+        const double sd = __dmul_rn(maxSpeed, d.damping[idx]);
+        fp = zadd(fp, zscale(zload(Ap + 2 * idx), sd));
+        fm = zadd(fm, zscale(zload(Am + 2 * idx), sd));
+        f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sd));
+    }
+    zstore(Fp + 2 * idx, fp);
+    zstore(Fm + 2 * idx, fm);
+    zstore(F0 + 2 * idx, f0);
+}
+
 template <typename T>
 struct cx2t { cx<T> p, q; };
 
@@ -1002,48 +1051,14 @@ __global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, cons
             zstore(Fm + 2 * idx, fm);
             zstore(F0 + 2 * idx, f0);
         } else if constexpr (FLUX && sizeof(T) == 4) {
-            // MIXED flux: projection with the folded FP32 coefficients and an FP32
-            // phase after FP64 angle reduction; FP64 only for the angle and the stores.
+            // MIXED flux: projection with the folded FP32 coefficients
             float2 ch[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 if (c >= nch) break;
                 ch[d.tq[c]] = make_float2(float(vr[c]), float(vi[c]));
             }
-            const float2 U = ch[0], V = ch[1], Wc = ch[2], N = ch[3];
-            const float4* pj = reinterpret_cast<const float4*>(d.fProj + 12 * (size_t)idx);
-            const float4 p0 = pj[0], p1 = pj[1], p2 = pj[2];
-            const float f0r = -p1.z * U.y - p1.w * V.y + p2.x * N.x;
-            const float f0i = p1.z * U.x + p1.w * V.x + p2.x * N.y;
-            float cpr, cpi, cmr, cmi;
-            if (w == 0) {
-                const float sc = float(d.inertialScale[j]);
-                cpr = sc * (U.x + V.y);
-                cpi = sc * (U.y - V.x);
-                cmr = cpr;
-                cmi = -cpi;
-            } else {
-                const float wr = p0.x * U.x - p0.y * U.y + p0.z * V.x - p0.w * V.y + p1.x * Wc.x - p1.y * Wc.y;
-                const float wi = p0.x * U.y + p0.y * U.x + p0.z * V.y + p0.w * V.x + p1.x * Wc.y + p1.y * Wc.x;
-                const float br = p2.y * N.x - p2.z * f0r, bi = p2.y * N.y - p2.z * f0i;
-                cpr = wr + br; cpi = wi + bi; cmr = wr - br; cmi = wi - bi;
-            }
-            const double ang = d.omega[idx] * elapsed;
-            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
-            float sn, cs;
-            sincosf(float(red), &sn, &cs);
-            zd fp{double(cpr * cs + cpi * sn), double(cpi * cs - cpr * sn)};   // (cp) * conj(p)
-            zd fm{double(cmr * cs - cmi * sn), double(cmr * sn + cmi * cs)};   // (cm) * p
-            zd f0{double(f0r), double(f0i)};
-            if (applyDamping) {
-                const double sd = __dmul_rn(maxSpeed, d.damping[idx]);
-                fp = zadd(fp, zscale(zload(Ap + 2 * idx), sd));
-                fm = zadd(fm, zscale(zload(Am + 2 * idx), sd));
-                f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sd));
-            }
-            zstore(Fp + 2 * idx, fp);
-            zstore(Fm + 2 * idx, fm);
-            zstore(F0 + 2 * idx, f0);
+            mixed_project_store(d, idx, w, j, ch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
         } else {
         zd val[4];
 #pragma unroll
