@@ -532,19 +532,15 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     bool fwdTC = false;
     if constexpr (sizeof(T) == 4) {
         if (h->verticalTC && h->tcFwdAvailable) {
-            // the z-grid spectra are consumed by now: their buffer holds the transformed columns
-            auto* vs = reinterpret_cast<float2*>(z);
             dev::k_vfwd_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcFwdSmem, s>>>(
-                d, reinterpret_cast<const float2*>(f), vs);
-            const int blocks = static_cast<int>(std::min<size_t>(cdiv(static_cast<size_t>(d.members) * p.M, 256), 65535));
-            dev::k_vfwd_proj<<<blocks, 256, 0, s>>>(d, vs, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
+                d, reinterpret_cast<const float2*>(f), elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
             fwdTC = true;
         }
     }
     if (!fwdTC)
         dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
             d, f, nt, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
-    h->metrics.kernel_launches += fwdTC ? 6 : 5;
+    h->metrics.kernel_launches += 5;
     cudaError_t e = cudaGetLastError();
     if (inst && e == cudaSuccess) {
         cudaEventRecord(h->ev[5], s);
@@ -1407,11 +1403,10 @@ static int create_handle(const wv_config* config, int precision, int members, wv
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
             h->verticalTC = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
         }
-        // forward transform: two accumulators of NF <= 128 output rows over K = zHalf
+        // forward transform: four accumulators of NF <= 128 output rows over K = zHalf
         const int NF = static_cast<int>(((p.Nj + 1) / 2 + 15) / 16 * 16), KF = static_cast<int>((p.zHalf + 15) / 16 * 16);
         const size_t smemF = 6 * (256u * KF) + 6 * static_cast<size_t>(NF / 8) * 16u * KF;
-        const size_t vspecBytes = 4 * p.M * sizeof(float2), zBytes = scratch_sizes(p).z * 2 * sizeof(float);
-        if (e == cudaSuccess && h->tcAvailable && NF <= 128 && smemF <= 220 * 1024 && vspecBytes <= zBytes) {
+        if (e == cudaSuccess && h->tcAvailable && NF <= 128 && smemF <= 220 * 1024) {
             const std::vector<uint16_t> blob = tc_forward_blob(p, NF, KF);
             const uint16_t* q = nullptr;
             e = upload(h, blob, &q);

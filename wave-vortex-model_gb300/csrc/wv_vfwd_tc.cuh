@@ -1,8 +1,8 @@
 // Vertical forward transform of the mixed-form flux on the tensor cores
 // (tcgen05.mma, FP32 accumulators in tensor memory): the forward DCT-I / DST-I
 // with its normalization (normalizeForwardDCT / DST, kernel.cpp:176-193) of the
-// product spectra, as split-BF16 GEMMs, then the folded FP32 projection in a
-// second pass (k_vfwd_proj).
+// product spectra, as split-BF16 GEMMs, and the folded FP32 projection of the
+// transformed targets in the tensor-memory drain.
 //
 // One CTA (16 warps) takes 32 retained columns and runs two tiles of M = 128
 // rows (mode, target, re|im): tile 0 the cosine-family targets u, v, tile 1 the
@@ -14,9 +14,9 @@
 //   sine:   D_even = A_Q x Fsin_even^T,  D_odd = A_P x Fsin_odd^T
 // with every FP32 operand split into three BF16 pieces and the six leading
 // cross products accumulated smallest first (FP32 precision, as k_vinv_tc).
-// The transformed values go to vspec[q][member][idx] (FP32 complex, canonical
-// (mode, j) order) and k_vfwd_proj applies the projection of k_vfwd's mixed
-// branch per (mode, j).
+// The four accumulators (two per family) stay in tensor memory until both tiles
+// are done; the drain then projects every (mode, j) with the arithmetic of
+// k_vfwd's mixed branch and stores the flux.
 #pragma once
 
 #include "wv_kernels.cuh"
@@ -26,14 +26,87 @@
 namespace wvgpu {
 namespace dev {
 
-constexpr uint32_t kTcFwdCols = 256;  // tensor-memory columns: two accumulators of NF <= 128
+constexpr uint32_t kTcFwdCols = 512;  // tensor-memory columns: four accumulators of NF <= 128
+
+// Eight consecutive K values of one row as three BF16 pieces: one 16-byte store per piece.
+__device__ __forceinline__ void put_split3_run8(unsigned char* A, uint32_t split, uint32_t off, const float (&x)[8]) {
+    uint32_t h[4], m[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        uint32_t hh[2], mm[2], ll[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            float b0, b1, b2;
+            hh[k] = bf16_bits(x[i + k], b0);
+            const float r1 = x[i + k] - b0;
+            mm[k] = bf16_bits(r1, b1);
+            ll[k] = bf16_bits(r1 - b1, b2);
+        }
+        h[i >> 1] = hh[0] | (hh[1] << 16);
+        m[i >> 1] = mm[0] | (mm[1] << 16);
+        l[i >> 1] = ll[0] | (ll[1] << 16);
+    }
+    *reinterpret_cast<uint4*>(A + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(A + split + off) = make_uint4(m[0], m[1], m[2], m[3]);
+    *reinterpret_cast<uint4*>(A + 2 * split + off) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// Element k of four registers (k in 0..3, lane-dependent) without local memory.
+__device__ __forceinline__ float pick4(const float* v, int k) {
+    const float a = (k & 1) ? v[1] : v[0];
+    const float b = (k & 1) ? v[3] : v[2];
+    return (k & 2) ? b : a;
+}
+
+// Tensor-memory drain of one output parity: lanes 4 m .. 4 m + 3 hold, for
+// mode m and 16 outputs j, the (u.re, u.im, v.re, v.im) rows of the cosine
+// accumulator (a) and the (w.re, w.im, eta.re, eta.im) rows of the sine
+// accumulator (b).  A 4 x 4 transpose per group of four columns (rotating
+// shuffles) hands lane 4 m + s the eight values of column 4 g + s, which it
+// projects and stores.
+__device__ __forceinline__ void vfwd_tc_project(const DescDev& d, const float (&a)[16], const float (&b)[16], int c0,
+                                                int parity, int mode, bool valid, double elapsed, double maxSpeed,
+                                                int applyDamping, const double* Ap, const double* Am, const double* A0,
+                                                double* Fp, double* Fm, double* F0) {
+    const int lane = threadIdx.x & 31, sub = lane & 3, base = lane & ~3;
+    const int Nj = d.Nj;
+    const int w = d.modeWV[mode];
+    const bool conj = d.modeFlags[mode] & 1;
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        float ca[4], cb[4];  // ca[k] / cb[k]: row k of the group at column 4 g + sub
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            // round r: read lane (sub + r) & 3 its value for column 4 g + sub, i.e. every
+            // lane sends its value for column 4 g + ((sub - r) & 3)
+            const int sendCol = (sub - r) & 3;
+            const float va = __shfl_sync(0xffffffffu, pick4(a + 4 * g, sendCol), base + ((sub + r) & 3));
+            const float vb = __shfl_sync(0xffffffffu, pick4(b + 4 * g, sendCol), base + ((sub + r) & 3));
+            const int k = (sub + r) & 3;
+            // static register targets: k is lane-dependent, so select into each slot
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                if (k == t) { ca[t] = va; cb[t] = vb; }
+            }
+        }
+        const int j = 2 * (c0 + 4 * g + sub) + parity;
+        if (valid && j < Nj) {
+            const float sg = conj ? -1.f : 1.f;
+            const float2 ch[4] = {make_float2(ca[0], sg * ca[1]), make_float2(ca[2], sg * ca[3]),
+                                  make_float2(cb[0], sg * cb[1]), make_float2(cb[2], sg * cb[3])};
+            mixed_project_store(d, j + Nj * w, w, j, ch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
+        }
+    }
+}
 
 __global__ void __launch_bounds__(kTcThreads, 1)
-k_vfwd_tc(DescDev d, const float2* __restrict__ fspec, float2* __restrict__ vspec) {
+k_vfwd_tc(DescDev d, const float2* __restrict__ fspec, double elapsed, const double* __restrict__ Ap,
+          const double* __restrict__ Am, const double* __restrict__ A0, const unsigned long long* __restrict__ maxSpeedBits,
+          int applyDamping, double* __restrict__ Fp, double* __restrict__ Fm, double* __restrict__ F0) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[2];  // 0: matrix copies, 1: MMA completion
     __shared__ uint32_t tmemBase;
-    const int Nj = d.Nj, Nz = d.Nz, Zh = d.zHalf, P = d.positions, M = d.M;
+    const int Nz = d.Nz, Zh = d.zHalf, P = d.positions;
     const int NF = d.tcFN, KF = d.tcFK;
     const uint32_t aSplit = 256u * static_cast<uint32_t>(KF);                                  // 128 rows x KF BF16
     const uint32_t bSplit = static_cast<uint32_t>(NF >> 3) * 16u * static_cast<uint32_t>(KF);  // NF rows x KF BF16
@@ -43,7 +116,12 @@ k_vfwd_tc(DescDev d, const float2* __restrict__ fspec, float2* __restrict__ vspe
     const int m0 = blockIdx.x * kTcModes;
     const int nm = min(kTcModes, d.Nkl - m0);
     const int member = blockIdx.y;
-    if (member > 0) fspec += (size_t)member * Nz * P;
+    if (member > 0) {
+        const long long o = member * d.memberStride;
+        Ap += o; Am += o; A0 += o;
+        Fp += o; Fm += o; F0 += o;
+        fspec += (size_t)member * Nz * P;
+    }
     int chanOf[4] = {-1, -1, -1, -1};
     for (int c = 0; c < d.nt; ++c) chanOf[d.tq[c]] = c;
     if (tid == 0) {
@@ -68,30 +146,47 @@ k_vfwd_tc(DescDev d, const float2* __restrict__ fspec, float2* __restrict__ vspe
             mbar_arrive_expect_tx(&bars[0], 6 * bSplit);
             bulk_copy_g2s(B, reinterpret_cast<const unsigned char*>(d.tcFB) + (size_t)tile * 6 * bSplit, 6 * bSplit, &bars[0]);
         }
-        // A operands P and Q of the tile's two targets, split into BF16 pieces
-        for (uint32_t i = tid; i < 6 * aSplit / 16; i += kTcThreads) reinterpret_cast<uint4*>(A)[i] = make_uint4(0u, 0u, 0u, 0u);
-        __syncthreads();
-        for (int it = tid; it < 2 * Zh * nm; it += kTcThreads) {
-            const int mi = it % nm;
-            const int rest = it / nm;
-            const int n = rest % Zh, tp = rest / Zh;
-            const int c = chanOf[2 * tile + tp];
-            if (c < 0) continue;
-            const int pos = d.modePos[m0 + mi];
-            const float2* col = fspec + (size_t)c * d.zTotal * P + pos;
-            const float2 a = col[(size_t)n * P];
-            const int n2 = Nz - 1 - n;
-            float2 vp = a, vq = a;
-            if (n2 != n) {
-                const float2 b = col[(size_t)n2 * P];
-                vp = make_float2(a.x + b.x, a.y + b.y);
-                vq = make_float2(a.x - b.x, a.y - b.y);
+        // A operands P and Q of the tile's two targets, split into BF16 pieces.  One
+        // item = one row r = 4 mi + 2 tp + part and 8 consecutive n (one 16-byte run
+        // of each piece); the low three bits of the item index walk the eight rows
+        // of a core matrix, so the eight lanes of each store phase hit eight
+        // different 16-byte bank groups.  Rows of absent targets or modes and the
+        // K padding are written as zeros.  (For the second tile, every thread has
+        // seen the first tile's MMAs complete, so A is free.)
+        {
+            const int nb8 = KF >> 3;
+            for (int it = tid; it < 128 * nb8; it += kTcThreads) {
+                const int part = it & 1, tp = (it >> 1) & 1, miLo = (it >> 2) & 1;
+                const int rest = it >> 3;
+                const int mi = 2 * (rest & 15) + miLo, nb = rest >> 4;
+                const int c = chanOf[2 * tile + tp];
+                float vp[8], vq[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) { vp[i] = 0.f; vq[i] = 0.f; }
+                if (c >= 0 && mi < nm) {
+                    const int pos = d.modePos[m0 + mi];
+                    const float* col = reinterpret_cast<const float*>(fspec + (size_t)c * d.zTotal * P + pos) + part;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int n = 8 * nb + i;
+                        if (n < Zh) {
+                            const int n2 = Nz - 1 - n;
+                            const float a = col[(size_t)n * P * 2];
+                            if (n2 != n) {
+                                const float b = col[(size_t)n2 * P * 2];
+                                vp[i] = a + b;
+                                vq[i] = a - b;
+                            } else {
+                                vp[i] = a;
+                                vq[i] = a;
+                            }
+                        }
+                    }
+                }
+                const uint32_t off = tc_kmajor_offset(4 * mi + 2 * tp + part, 8 * nb, KF);
+                put_split3_run8(A, aSplit, off, vp);
+                put_split3_run8(A + 3 * aSplit, aSplit, off, vq);
             }
-            const int r = 4 * mi + 2 * tp;
-            put_split3(A, aSplit, tc_kmajor_offset(r, n, KF), vp.x);
-            put_split3(A, aSplit, tc_kmajor_offset(r + 1, n, KF), vp.y);
-            put_split3(A + 3 * aSplit, aSplit, tc_kmajor_offset(r, n, KF), vq.x);
-            put_split3(A + 3 * aSplit, aSplit, tc_kmajor_offset(r + 1, n, KF), vq.y);
         }
         fence_proxy_async_smem();
         __syncthreads();
@@ -105,7 +200,7 @@ k_vfwd_tc(DescDev d, const float2* __restrict__ fspec, float2* __restrict__ vspe
                     const int variant = (tile == 0) ? acc : 1 - acc;
                     const uint32_t sAv = sA + static_cast<uint32_t>(variant) * 3u * aSplit;
                     const uint32_t sBp = sB + static_cast<uint32_t>(acc) * 3u * bSplit;
-                    const uint32_t tcol = tbase + static_cast<uint32_t>(acc * NF);
+                    const uint32_t tcol = tbase + static_cast<uint32_t>((2 * tile + acc) * NF);
                     uint32_t accumulate = 0;
                     for (int k0 = 0; k0 < KF; k0 += 16) {
                         for (int p = 0; p < 6; ++p) {
@@ -122,69 +217,34 @@ k_vfwd_tc(DescDev d, const float2* __restrict__ fspec, float2* __restrict__ vspe
             tc_commit(&bars[1]);
         }
         phaseB ^= 1u;
-        mbar_wait(&bars[1], phaseM, d.status);  // MMAs done: A and B are free, accumulators final
+        mbar_wait(&bars[1], phaseM, d.status);  // MMAs done: A and B are free for the next tile
         phaseM ^= 1u;
         tc_fence_after_sync();
-        // drain: row r = 32 (warp % 4) + lane; the four warps of a lane quarter split the column chunks
-        {
-            const int quarter = warp & 3, cgroup = warp >> 2;
-            const int r = 32 * quarter + lane;
-            const int mi = r >> 2, tp = (r >> 1) & 1, part = r & 1;
-            const int q = 2 * tile + tp;
-            const bool valid = mi < nm && chanOf[q] >= 0;
-            const int mode = m0 + (mi < nm ? mi : 0);
-            const int w = d.modeWV[mode];
-            const bool conj = d.modeFlags[mode] & 1;
-            const uint32_t rowAddr = tbase + (static_cast<uint32_t>(32 * quarter) << 16);
-            float2* out = vspec + ((size_t)q * d.members + member) * M;
-            for (int c0 = 16 * cgroup; c0 < NF; c0 += 64) {
-                float e[16], o[16];
-                tc_ld_32x32b_x16(rowAddr + static_cast<uint32_t>(c0), e);
-                tc_ld_32x32b_x16(rowAddr + static_cast<uint32_t>(NF + c0), o);
+    }
+    // drain: row r = 32 (warp % 4) + lane holds (mode r / 4, target pair, re|im) of both
+    // families; the four warps of a lane quarter split the column chunks
+    {
+        const int quarter = warp & 3, cgroup = warp >> 2;
+        const int r = 32 * quarter + lane;
+        const int mi = r >> 2;
+        const bool valid = mi < nm;
+        const int mode = m0 + (valid ? mi : 0);
+        const double maxSpeed = applyDamping ? __longlong_as_double((long long)maxSpeedBits[member]) : 0.0;
+        const uint32_t rowAddr = tbase + (static_cast<uint32_t>(32 * quarter) << 16);
+        for (int c0 = 16 * cgroup; c0 < NF; c0 += 64) {
+            for (int parity = 0; parity < 2; ++parity) {
+                float a[16], b[16];
+                tc_ld_32x32b_x16(rowAddr + static_cast<uint32_t>(parity * NF + c0), a);
+                tc_ld_32x32b_x16(rowAddr + static_cast<uint32_t>((2 + parity) * NF + c0), b);
                 tc_wait_ld();
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const float eP = __shfl_xor_sync(0xffffffffu, e[i], 1);
-                    const float oP = __shfl_xor_sync(0xffffffffu, o[i], 1);
-                    const int je = 2 * (c0 + i), jo = je + 1;
-                    if (part == 0 && valid) {
-                        if (je < Nj) out[je + Nj * w] = make_float2(e[i], conj ? -eP : eP);
-                        if (jo < Nj) out[jo + Nj * w] = make_float2(o[i], conj ? -oP : oP);
-                    }
-                }
+                vfwd_tc_project(d, a, b, c0, parity, mode, valid, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
             }
         }
-        tc_fence_before_sync();
-        __syncthreads();  // all tensor-memory reads done before the next tile's MMAs
-        tc_fence_after_sync();
     }
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
     if (warp == 0) tmem_dealloc(tbase, kTcFwdCols);
-}
-
-// Projection of the tensor-core forward transform's output: one thread per
-// (member, mode, j), the same arithmetic as k_vfwd's mixed branch.
-__global__ void __launch_bounds__(256) k_vfwd_proj(DescDev d, const float2* __restrict__ vspec, double elapsed,
-                                                  const double* __restrict__ Ap, const double* __restrict__ Am,
-                                                  const double* __restrict__ A0,
-                                                  const unsigned long long* __restrict__ maxSpeedBits, int applyDamping,
-                                                  double* __restrict__ Fp, double* __restrict__ Fm, double* __restrict__ F0) {
-    const int M = d.M, Nj = d.Nj;
-    const size_t total = (size_t)d.members * M;
-    for (size_t it = blockIdx.x * (size_t)blockDim.x + threadIdx.x; it < total; it += (size_t)gridDim.x * blockDim.x) {
-        const int member = static_cast<int>(it / M);
-        const int idx = static_cast<int>(it - (size_t)member * M);
-        const int w = idx / Nj, j = idx - w * Nj;
-        const long long o = member * d.memberStride;
-        float2 ch[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) ch[q] = make_float2(0.f, 0.f);
-        for (int c = 0; c < d.nt; ++c) {
-            const int q = d.tq[c];
-            ch[q] = vspec[((size_t)q * d.members + member) * M + idx];
-        }
-        const double maxSpeed = applyDamping ? __longlong_as_double((long long)maxSpeedBits[member]) : 0.0;
-        mixed_project_store(d, idx, w, j, ch, elapsed, maxSpeed, applyDamping, Ap + o, Am + o, A0 + o, Fp + o, Fm + o, F0 + o);
-    }
 }
 
 }  // namespace dev
