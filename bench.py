@@ -493,8 +493,8 @@ def run_ours(args):
     mixed_value = world * args.steps / max_over_ranks(mixed_ms / 1e3)
     mixed = {"value": mixed_value, "unit": UNIT, "ms_per_step": mixed_ms / args.steps,
              "speedup_vs_fp64": mixed_value / value,
-             "dtype": "f32 xy transforms and products; vertical inverse as split-BF16 (3 pieces, 6 products) tcgen05 "
-                      "GEMMs with f32 accumulators; f32 forward contraction and projection; f64 phase angles and RK4",
+             "dtype": "f32 xy transforms and products; vertical inverse and forward transforms as split-BF16 (3 pieces, "
+                      "6 products) tcgen05 GEMMs with f32 accumulators; f32 projection; f64 phase angles and RK4",
              "vertical_kernel": "tensor cores (tcgen05.mma)",
              "roofline": _stage_profile(km, devm, tm, t0, dt, "mixed", torch)}
     if rank == 0:

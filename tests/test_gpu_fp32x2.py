@@ -172,16 +172,80 @@ def test_fp32x2_adjoint_matches_fp64(wv, N, Nz, hydro):
     k64.close()
 
 
-def test_fp32x2_rejects_entry_points_without_a_paired_form(wv):
-    import torch
-    c = config_from_case(CASES["odd_15x13x9"])
-    k = wv.WVTransformConstantStratificationKernel(_conf(wv, c), precision="fp32x2")
-    g = load_golden("odd_15x13x9")
-    dev = [torch.from_numpy(np.ascontiguousarray(g[n])).cuda() for n in ("Ap", "Am", "A0")]
+def test_fp32x2_tensor_vertical_needs_nj_up_to_96(wv):
+    """The digit-sliced tensor-core inverse needs K = Nj / 2 <= 48 per parity
+    (shared memory); larger Nj keeps the CUDA-core contraction."""
+    k = wv.WVTransformConstantStratificationKernel(
+        wv.Configuration(Nx=32, Ny=32, Nz=151, Nj=100, Lx=100e3, Ly=100e3, Lz=4000.0, latitude=33.0), precision="fp32x2")
     with pytest.raises(wv.WVKernelError) as e:
         k.set_vertical_kernel("tensor")
     assert e.value.code == 10
     k.close()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp32x2_tensor_vertical_matches_reference(wv, name):
+    """FP32X2 handles with the vertical inverse on the tensor cores (exact
+    digit-sliced BF16 GEMMs, k_vinv_tcx): flux, right-hand side, the
+    advection-field entries and RK4 against the reference's golden outputs at
+    the FP32X2 tolerance; the device status word stays clear."""
+    cf = CASES[name]
+    g = load_golden(name)
+    k = wv.WVTransformConstantStratificationKernel(_conf(wv, config_from_case(cf)), precision="fp32x2")
+    k.set_vertical_kernel("tensor")
+    t, t0 = float(g["t"]), float(g["t0"])
+    args = (t, t0, g["Ap"], g["Am"], g["A0"])
+    F = k.nonlinearFlux(*args)
+    for got, key in zip(F, ("Fp", "Fm", "F0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key, rel_err(got, g[key]))
+    Fw, adv = k.nonlinearFluxWithAdvectionFields(*args)
+    for got, key in zip(Fw, ("with_Fp", "with_Fm", "with_F0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    k.set_forcing(nonlinear=True, adaptive_damping=bool(cf["damping"]))
+    R = k.evaluateRightHandSide(*args)
+    for got, key in zip(R, ("Rp", "Rm", "R0")):
+        assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    Kp, Km, K0, tK = k.rk4(g["rk_Ap"], g["rk_Am"], g["rk_A0"], float(g["rk_t"]), float(g["rk_t0"]), float(g["rk_dt"]),
+                           int(g["rk_steps"]))
+    for got, key in zip((Kp, Km, K0), ("Kp", "Km", "K0")):
+        if np.any(g[key]):
+            assert rel_err(got, g[key]) <= FP32X2_TOL, (name, key)
+    assert k.device_status() == 0
+    k.close()
+
+
+@pytest.mark.parametrize("Nx,Ny,Nz,hydro", [(64, 64, 33, False), (128, 128, 65, True), (256, 256, 129, False)])
+def test_fp32x2_tensor_vertical_flux_vs_cuda_cores_and_fp64(wv, Nx, Ny, Nz, hydro):
+    """Digit-sliced tensor-core inverse against the CUDA-core paired-FP32
+    contraction on 0.1 m/s spectrum states: flux tendencies (u, v, w, eta
+    through the FP64 inverse) against the FP64 flux within 1e-9 relative L2,
+    and within a small factor of the CUDA-core FP32X2 error."""
+    import torch
+    import wv_oracle as O
+    cfg = wv.Configuration(Nx=Nx, Ny=Ny, Nz=Nz, Nj=O.default_nj(Nz), Lx=3125.0 * Nx, Ly=3125.0 * Ny, Lz=4000.0,
+                           latitude=33.0, isHydrostatic=hydro)
+    k64 = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
+    A = wv.synthetic_state(k64, seed=23, urms=0.1)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+    exact = k64.transformWaveVortexToUVWEta(0.0, 0.0, *(x.cpu().numpy() for x in k64.nonlinearFlux(777.0, 5.0, *dev)))
+    fields = [0, 1, 3] if hydro else [0, 1, 2, 3]
+
+    def tendency_error(F):
+        f = k64.transformWaveVortexToUVWEta(0.0, 0.0, *(x.cpu().numpy() for x in F))
+        return [float(np.linalg.norm(f[i] - exact[i]) / np.linalg.norm(exact[i])) for i in fields]
+
+    k.set_vertical_kernel("cuda")
+    e_cuda = tendency_error(k.nonlinearFlux(777.0, 5.0, *dev))
+    k.set_vertical_kernel("tensor")
+    e_tc = tendency_error(k.nonlinearFlux(777.0, 5.0, *dev))
+    assert k.device_status() == 0
+    print(f"{Nx}x{Ny}x{Nz} hydro={hydro} FP32X2 flux tendency error vs FP64: CUDA cores {e_cuda}, tensor cores {e_tc}")
+    for a, b in zip(e_tc, e_cuda):
+        assert a <= 1e-9
+        assert a <= 20.0 * b + 1e-12
+    k.close()
+    k64.close()
 
 
 def test_fp32x2_ensemble_members_equal_single_handles(wv):

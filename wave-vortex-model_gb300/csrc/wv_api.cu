@@ -14,6 +14,7 @@
 #include "wv_adjoint.cuh"
 #include "wv_vinv_tc.cuh"
 #include "wv_vfwd_tc.cuh"
+#include "wv_vinv_tcx.cuh"
 #include "wv_scalar.cuh"
 
 #include <cuda_runtime.h>
@@ -90,6 +91,7 @@ struct wv_handle {
     size_t tcSmem = 0;
     bool tcFwdAvailable = false;  // tensor-core forward vertical transform built (used with verticalTC)
     size_t tcFwdSmem = 0;
+    size_t tcxSmem = 0;           // FP32X2: shared memory of the digit-sliced tensor-core inverse
     // F-grid scalar advection (built on first use): full-spectrum descriptor copy,
     // z-derivative matrix, per-position flags and scratch
     bool scalarReady = false;
@@ -224,6 +226,58 @@ std::vector<uint16_t> tc_forward_blob(const Plan& p, int NF, int KF) {
                 out[(blk * 3 + 1) * split + e] = mb;
                 out[(blk * 3 + 2) * split + e] = lb;
             }
+    return out;
+}
+
+// The inverse matrices Ccos, Csin, Ccos, -Csin (the z-derivative matrices
+// m_j Ccos and -m_j Csin with m_j moved into the A operand) as six balanced
+// base-256 digit slices per row for the FP32X2 tensor-core inverse
+// (k_vinv_tcx): row n of matrix m is scaled by 2^-F (F = tcxF[m][n], the
+// smallest F with max_j |C[n][j]| < 2^F), rounded to the integer
+// Y = round(C 2^(47-F)) and written as digits D_0 .. D_5 (Y = sum_s D_s
+// 256^(5-s), D_s in [-128, 128]); slice s holds the BF16 value D_s 2^(-7-8s)
+// (exact).  Blocks [matrix][j parity][pass][slice][NP rows][KH] (output row
+// n = pass NP + row; even j = 2 k in parity 0, odd j = 2 k + 1 in parity 1),
+// canonical no-swizzle K-major layout; zeros outside the matrix.
+struct DigitBlob {
+    std::vector<uint16_t> blob;
+    std::vector<int32_t> F;
+};
+DigitBlob tc_digit_blob(const Plan& p, int NP, int KH, int passes) {
+    const size_t split = static_cast<size_t>(NP) * KH;
+    const size_t rows = static_cast<size_t>(NP) * passes;
+    DigitBlob out;
+    out.blob.assign(4 * 2 * rows * dev::kTcxDigits * KH, 0);
+    out.F.assign(4 * rows, 0);
+    const std::vector<double>* mats[4] = {&p.Ccos, &p.Csin, &p.Ccos, &p.Csin};
+    const double sign[4] = {1.0, 1.0, 1.0, -1.0};
+    const int Zh = static_cast<int>(p.zHalf), Nj = static_cast<int>(p.Nj);
+    for (int m = 0; m < 4; ++m)
+        for (int n = 0; n < Zh; ++n) {
+            const double* row = mats[m]->data() + static_cast<size_t>(n) * Nj;
+            double mx = 0.0;
+            for (int j = 0; j < Nj; ++j) mx = std::max(mx, std::fabs(row[j]));
+            int F = 0;
+            if (mx > 0.0) std::frexp(mx, &F);
+            out.F[static_cast<size_t>(m) * rows + n] = F;
+            const int pass = n / NP, rn = n % NP;
+            for (int j = 0; j < Nj; ++j) {
+                long long Y = std::llround(std::ldexp(sign[m] * row[j], 47 - F));
+                int D[dev::kTcxDigits];
+                for (int s2 = dev::kTcxDigits - 1; s2 >= 1; --s2) {
+                    int dd = static_cast<int>(Y & 0xFFll);
+                    dd -= (dd & 0x80) << 1;
+                    D[s2] = dd;
+                    Y = (Y - dd) / 256;
+                }
+                D[0] = static_cast<int>(Y);
+                const size_t e = dev::tc_kmajor_offset(rn, j >> 1, KH) / 2;
+                const size_t blk = (static_cast<size_t>(m) * 2 + (j & 1)) * passes + pass;
+                for (int s2 = 0; s2 < dev::kTcxDigits; ++s2)
+                    out.blob[(blk * dev::kTcxDigits + s2) * split + e] =
+                        bf16_rne(static_cast<float>(std::ldexp(static_cast<double>(D[s2]), -7 - 8 * s2)));
+            }
+        }
     return out;
 }
 
@@ -510,6 +564,12 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
         if (h->verticalTC)
             dev::k_vinv_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcSmem, s>>>(
                 d, Ap, Am, A0, elapsed, reinterpret_cast<float2*>(z), speed);
+        else
+            dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    } else if constexpr (std::is_same<T, dev::ff>::value) {
+        if (h->verticalTC)
+            dev::k_vinv_tcx<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcxSmem, s>>>(
+                d, Ap, Am, A0, elapsed, z, speed, reinterpret_cast<dev::ff*>(y));
         else
             dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
     } else {
@@ -1417,6 +1477,38 @@ static int create_handle(const wv_config* config, int precision, int members, wv
             h->tcFwdAvailable = e == cudaSuccess;
         }
     }
+    if (precision == WV_PRECISION_FP32X2 && e == cudaSuccess) {
+        // digit-sliced tensor-core inverse: 2 parities x 4 accumulators of NP <= 64 columns,
+        // the zHalf output rows in passes of NP; pass-1 spectra in the y-spectra scratch
+        // (free while the vertical inverse runs)
+        const int passes = static_cast<int>((p.zHalf + 63) / 64);
+        const int NP = static_cast<int>(((p.zHalf + passes - 1) / passes + 15) / 16 * 16);
+        const int KH = static_cast<int>(((p.Nj + 1) / 2 + 15) / 16 * 16);
+        // A slices + two matrix-block buffers (even and odd j)
+        const size_t smem = dev::kTcxDigits * (256u * 2 * KH) + 2 * dev::kTcxDigits * static_cast<size_t>(NP / 8) * 16u * KH;
+        const size_t scratchBytes = static_cast<size_t>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) * dev::kTcModes * p.Nj * 64;
+        const size_t yBytes = scratch_sizes(p).y * 2 * elem_size(precision);
+        if (8 * NP <= 512 && passes <= 8 && smem <= 220 * 1024 && scratchBytes <= yBytes) {
+            const DigitBlob db = tc_digit_blob(p, NP, KH, passes);
+            const uint16_t* q = nullptr;
+            e = upload(h, db.blob, &q);
+            dd.tcxB = reinterpret_cast<const unsigned short*>(q);
+            const int32_t* fq = nullptr;
+            if (e == cudaSuccess) e = upload(h, db.F, &fq);
+            dd.tcxF = fq;
+            const std::vector<float> mPairs = to_pairs(d.m);
+            const float* mq = nullptr;
+            if (e == cudaSuccess) e = upload(h, mPairs, &mq);
+            dd.tcxM = mq;
+            dd.tcxN = NP; dd.tcxKH = KH; dd.tcxPasses = passes;
+            h->tcxSmem = smem;
+            if (e == cudaSuccess) e = raise_smem_limit(dev::k_vinv_tcx, static_cast<int>(smem));
+            h->tcAvailable = e == cudaSuccess;
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+            h->verticalTC = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
+        }
+    }
     const auto ss = scratch_sizes(p);
     const size_t cb = 2 * elem_size(precision);
     const size_t R = p.Nx * p.Ny * p.Nz;
@@ -1475,7 +1567,7 @@ int wv_set_vertical_kernel(wv_handle* h, int kind) {
         return fail(h, WV_INVALID_CONFIGURATION, "Unknown vertical-transform kernel.");
     if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
         return fail(h, WV_UNSUPPORTED_OPERATION,
-                    "The tensor-core vertical transform needs a mixed-precision handle with Nz <= 255.");
+                    "The tensor-core vertical transform needs a mixed-precision (Nz <= 255) or FP32X2 (Nj <= 96) handle.");
     h->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
     return WV_SUCCESS;
 }
@@ -2404,7 +2496,11 @@ cudaError_t autotune_group(wv_handle* h, cudaStream_t s, wv_ensemble_tuning& out
     float best = -1.0f;
     bool bestY = false, bestX = false, bestTC = false;
     out.candidates = 0;
-    for (int vt = 0; vt < (h->tcAvailable ? 2 : 1) && e == cudaSuccess; ++vt) {
+    // The tuner chooses the vertical kernel of mixed groups; FP32X2 groups keep the
+    // handle's default, so that members stay bit-identical to single FP32X2 handles.
+    const bool tuneTC = h->tcAvailable && h->precision == WV_PRECISION_MIXED;
+    const bool defaultTC = h->verticalTC;
+    for (int vt = (tuneTC || !defaultTC) ? 0 : 1; vt < (tuneTC || defaultTC ? 2 : 1) && e == cudaSuccess; ++vt) {
         for (int vy = 0; vy < (warpY ? 2 : 1) && e == cudaSuccess; ++vy) {
             for (int vx = 0; vx < (warpX ? 2 : 1) && e == cudaSuccess; ++vx) {
                 h->verticalTC = vt == 1;
@@ -2530,7 +2626,7 @@ int wv_ensemble_set_vertical_kernel(wv_ensemble* e, int kind) {
     for (wv_handle* h : e->groups)
         if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
             return efail(e, WV_UNSUPPORTED_OPERATION,
-                         "The tensor-core vertical transform needs mixed-precision groups with Nz <= 255.");
+                         "The tensor-core vertical transform needs mixed-precision (Nz <= 255) or FP32X2 (Nj <= 96) groups.");
     for (size_t g = 0; g < e->groups.size(); ++g) {
         e->groups[g]->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
         e->tuning[g].vertical = kind;

@@ -55,6 +55,66 @@ __device__ __forceinline__ ff& operator*=(ff& x, ff y) { x = x * y; return x; }
 struct __align__(16) ff2 {
     ff x, y;
 };
+
+// x 2^e for e in [-252, 254] by two exact multiplications by powers of two.
+__device__ __forceinline__ float ff_scale_pow2(float x, int e) {
+    const int h = e / 2;
+    return __fmul_rn(__fmul_rn(x, __int_as_float((h + 127) << 23)), __int_as_float((e - h + 127) << 23));
+}
+
+// A double as an unevaluated pair with integer operations only (GB300 runs
+// FP64 conversions at the FP64 rate): hi = the double truncated to 24
+// significant bits, lo = the remaining 29 bits rounded to FP32 (pair error
+// <= 2^-48 relative).  Zero and values outside the normal FP32 range take the
+// FP64 conversion.
+__device__ __forceinline__ ff ff_from_double(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    const unsigned hw = static_cast<unsigned>(b >> 32), lw = static_cast<unsigned>(b);
+    const int ex = static_cast<int>((hw >> 20) & 0x7FFu);
+    const int fe = ex - 1023 + 127;
+    if (fe <= 24 || fe >= 255) return ff(v);
+    const unsigned sign = hw & 0x80000000u;
+    const float hi = __uint_as_float(sign | (static_cast<unsigned>(fe) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+    const float lo = ff_scale_pow2(__uint2float_rn(lw & 0x1FFFFFFFu), ex - 1075);
+    return ff(hi, sign ? -lo : lo);
+}
+
+// sin and cos of an FP64 angle as pairs, with six FP64 operations: the
+// angle is reduced by the nearest multiple k of pi/2 (Cody and Waite: pi/2 as
+// a double plus its remainder, two fused multiply-adds), and the reduced
+// |r| <= pi/4 goes through the Taylor series of sin and cos to degree 15 and
+// 14 in paired FP32 (truncation below 1e-15; coefficients (-1)^i/(2i+1)! and
+// (-1)^i/(2i)! rounded to pairs), then the quadrant k mod 4 swaps and signs.
+__device__ __forceinline__ void ff_sincos(double a, ff& s, ff& c) {
+    const double k = rint(a * 0.63661977236758134308);
+    double r = fma(-k, 1.5707963267948966192, a);
+    r = fma(-k, 6.123233995736766036e-17, r);
+    const int q = __double2int_rn(k) & 3;
+    const ff x = ff_from_double(r);
+    const ff z = x * x;
+    ff ps = ff(-7.647163609812713e-13f, -1.2200710471178288e-20f);
+    ps = ps * z + ff(1.6059044372074283e-10f, -5.352526511562726e-18f);
+    ps = ps * z + ff(-2.5052107943679403e-08f, -4.4176230446483665e-16f);
+    ps = ps * z + ff(2.7557318844628753e-06f, 3.793571224297229e-14f);
+    ps = ps * z + ff(-0.00019841270113829523f, 2.725596874933456e-12f);
+    ps = ps * z + ff(0.008333333767950535f, -4.34617203337595e-10f);
+    ps = ps * z + ff(-0.1666666716337204f, 4.967053879312289e-09f);
+    ps = ps * z + ff(1.0f, 0.0f);
+    ff pc = ff(-1.147074536050896e-11f, -2.372207689231238e-19f);
+    pc = pc * z + ff(2.0876755879584152e-09f, 1.1082839147459852e-16f);
+    pc = pc * z + ff(-2.755731998149713e-07f, 7.575112209051195e-15f);
+    pc = pc * z + ff(2.4801587642286904e-05f, -3.40699609366682e-13f);
+    pc = pc * z + ff(-0.0013888889225199819f, 3.3631094437103215e-11f);
+    pc = pc * z + ff(0.0416666679084301f, -1.2417634698280722e-09f);
+    pc = pc * z + ff(-0.5f, 0.0f);
+    pc = pc * z + ff(1.0f, 0.0f);
+    const ff sn = x * ps;
+    const ff cs = pc;
+    // a = k pi/2 + r:  q = 0: (sin r, cos r); 1: (cos r, -sin r); 2: (-sin r, -cos r); 3: (-cos r, sin r)
+    const ff s0 = (q & 1) ? cs : sn, c0 = (q & 1) ? sn : cs;
+    s = (q & 2) ? -s0 : s0;
+    c = ((q + 1) & 2) ? -c0 : c0;
+}
 #endif
 
 }  // namespace dev

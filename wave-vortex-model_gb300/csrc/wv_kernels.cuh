@@ -259,6 +259,15 @@ struct DescDev {
     // [family cos|sin][parity even|odd][piece][NF rows j/2][KF = Zh rounded up to 16]
     const unsigned short* tcFB;
     int tcFN, tcFK;
+    // FP32X2 handles with the tensor-core vertical inverse: the matrices Ccos,
+    // Csin, Ccos, -Csin (the last two are the z-derivative matrices with m_j moved
+    // into the A operand) as six signed 8-bit digit slices per row (BF16, slice t
+    // scaled by 2^(-7-8t), row n scaled by 2^-tcxF[m][n]), blocks [matrix][j parity]
+    // [pass][slice][tcxN rows][tcxKH], output rows n = pass tcxN + row
+    const unsigned short* tcxB;
+    const int* tcxF;        // [4][tcxPasses tcxN] row exponents
+    const void* tcxM;       // ff[Nj]: m_j
+    int tcxN, tcxKH, tcxPasses;
     unsigned* status;       // device status word (bit 0: a bounded wait ran out)
     int c2rUseK;            // k_xc2r_fields(_w): bit c set -> channel c is multiplied by i k (x derivative)
     // field-family scales (transformToSpatialDomainWith{F,G}AllDerivatives)
@@ -343,12 +352,13 @@ __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restric
             continue;
         }
         if constexpr (std::is_same<T, ff>::value) {
-            // FP32X2: FP64 phase, then paired-FP32 evolution and field spectra with
-            // the coefficient arrays stored as pairs (d.fUAp ... hold ff values)
-            double sd, cd;
-            sincos(d.omega[idx] * elapsed, &sd, &cd);
-            const cx<T> p = mk<T>(T(cd), T(sd));
-            auto ld = [](const double* q) { return mk<T>(T(q[0]), T(q[1])); };
+            // FP32X2: FP64 angle, paired-FP32 phase (ff_sincos), then paired-FP32
+            // evolution and field spectra with the coefficient arrays stored as
+            // pairs (d.fUAp ... hold ff values)
+            T sf, cf;
+            ff_sincos(d.omega[idx] * elapsed, sf, cf);
+            const cx<T> p = mk<T>(cf, sf);
+            auto ld = [](const double* q) { return mk<T>(ff_from_double(q[0]), ff_from_double(q[1])); };
             const cx<T> ap = cmul<T>(ld(Ap + 2 * idx), p);
             const cx<T> am = cmul<T>(ld(Am + 2 * idx), cconj<T>(p));
             const cx<T> a0 = ld(A0 + 2 * idx);
@@ -1035,9 +1045,8 @@ __global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, cons
                 const T br = pj[9] * N.x - pj[10] * f0r, bi = pj[9] * N.y - pj[10] * f0i;
                 cpr = wr + br; cpi = wi + bi; cmr = wr - br; cmi = wi - bi;
             }
-            double sd, cd;
-            sincos(d.omega[idx] * elapsed, &sd, &cd);
-            const T sn = T(sd), cs = T(cd);
+            T sn, cs;
+            ff_sincos(d.omega[idx] * elapsed, sn, cs);
             zd fp{double(cpr * cs + cpi * sn), double(cpi * cs - cpr * sn)};   // (cp) * conj(p)
             zd fm{double(cmr * cs - cmi * sn), double(cmr * sn + cmi * cs)};   // (cm) * p
             zd f0{double(f0r), double(f0i)};
