@@ -149,13 +149,16 @@ typedef struct wv_stage_times {
  * the elapsed device time to the handle's stage times (reset on enable). */
 int wv_set_stage_instrumentation(wv_handle* handle, int enabled);
 
-/* Kernel of the flux's vertical inverse transform in the mixed form.  No
- * counterpart in the reference.  WV_VERTICAL_TENSOR_CORES runs the dense
- * contraction as split-BF16 GEMMs on the tensor cores (tcgen05.mma, three BF16
- * pieces per operand, six cross products, FP32 accumulators in tensor memory);
- * available on mixed-precision handles with Nz <= 255 (else
- * WV_UNSUPPORTED_OPERATION) and the default there when its blocks of 32 retained
- * columns (one per SM) fill the GPU; WV_VERTICAL_CUDA_CORES otherwise. */
+/* Kernels of the flux's vertical transforms in the reduced-precision forms.
+ * No counterpart in the reference.  WV_VERTICAL_TENSOR_CORES runs the dense
+ * contractions on the tensor cores (tcgen05.mma, FP32 accumulators in tensor
+ * memory): on mixed-precision handles (Nz <= 255) both vertical transforms as
+ * split-BF16 GEMMs (three BF16 pieces per operand, six cross products), the
+ * forward one with the flux projection fused into its drain; on FP32X2 handles
+ * (Nj <= 96) the vertical inverse as exact GEMMs of six 8-bit digit slices per
+ * operand (paired-FP32 accuracy).  Other handles return
+ * WV_UNSUPPORTED_OPERATION.  The default where available when blocks of 32
+ * retained columns (one per SM) fill the GPU; WV_VERTICAL_CUDA_CORES otherwise. */
 #define WV_VERTICAL_CUDA_CORES 0
 #define WV_VERTICAL_TENSOR_CORES 1
 int wv_set_vertical_kernel(wv_handle* handle, int kind);

@@ -645,7 +645,8 @@ class WVTransformConstantStratificationKernel:
         return tuple(out)
 
     def set_vertical_kernel(self, kind):
-        """'cuda' (CUDA-core contraction) or 'tensor' (tcgen05 split-BF16 GEMMs; mixed handles)."""
+        """'cuda' (CUDA-core contractions) or 'tensor' (tcgen05 GEMMs: split-BF16 for both vertical
+        transforms on mixed handles, exact digit slices for the vertical inverse on FP32X2 handles)."""
         self._check(self._lib.wv_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1}[kind]))
 
     def device_status(self):
