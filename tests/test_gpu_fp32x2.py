@@ -214,7 +214,8 @@ def test_fp32x2_tensor_vertical_matches_reference(wv, name):
     k.close()
 
 
-@pytest.mark.parametrize("Nx,Ny,Nz,hydro", [(64, 64, 33, False), (128, 128, 65, True), (256, 256, 129, False)])
+@pytest.mark.parametrize("Nx,Ny,Nz,hydro", [(64, 64, 33, False), (48, 40, 24, False), (64, 64, 64, True),
+                                            (128, 128, 65, True), (96, 96, 97, False), (256, 256, 129, False)])
 def test_fp32x2_tensor_vertical_flux_vs_cuda_cores_and_fp64(wv, Nx, Ny, Nz, hydro):
     """Digit-sliced tensor-core inverse against the CUDA-core paired-FP32
     contraction on 0.1 m/s spectrum states: flux tendencies (u, v, w, eta
@@ -272,5 +273,37 @@ def test_fp32x2_ensemble_members_equal_single_handles(wv):
             torch.cuda.synchronize()
             for c in range(3):
                 assert torch.equal(s[c], xe[m, c]), (g, m, c)
+        k.close()
+    ens.close()
+
+
+def test_fp32x2_tensor_vertical_members_equal_single_handles(wv):
+    """Member-batched FP32X2 groups on the digit-sliced tensor-core inverse (one
+    CTA row per member, per-member scratch rows) step every member exactly as a
+    single FP32X2 handle on the same kernel does."""
+    import torch
+    cfgs = [wv.Configuration(Nx=64, Ny=64, Nz=33, Nj=21, Lx=200e3, Ly=200e3, Lz=4000.0, latitude=33.0),
+            wv.Configuration(Nx=48, Ny=40, Nz=24, Nj=15, Lx=150e3, Ly=125e3, Lz=4000.0, latitude=33.0)]
+    ens = wv.WVEnsemble(cfgs, [3, 2], precision="fp32x2", autotune=False)
+    ens.set_vertical_kernel("tensor")
+    X, singles = [], []
+    for g, cfg in enumerate(cfgs):
+        k = wv.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
+        k.set_vertical_kernel("tensor")
+        B = ens.members[g]
+        X.append(torch.from_numpy(np.stack([np.stack(wv.synthetic_state(k, seed=80 + 7 * g + m, urms=0.1))
+                                            for m in range(B)])).cuda())
+        singles.append(k)
+    Xe = [x.clone() for x in X]
+    ens.rk4(Xe, 0.0, 0.0, [300.0, 250.0], 2)
+    torch.cuda.synchronize()
+    for g, (k, x0, xe) in enumerate(zip(singles, X, Xe)):
+        for m in range(x0.shape[0]):
+            s = [x0[m, c].clone() for c in range(3)]
+            k.rk4(*s, 0.0, 0.0, [300.0, 250.0][g], 2)
+            torch.cuda.synchronize()
+            for c in range(3):
+                assert torch.equal(s[c], xe[m, c]), (g, m, c)
+        assert k.device_status() == 0
         k.close()
     ens.close()

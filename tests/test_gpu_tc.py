@@ -29,7 +29,8 @@ def _cfg(wv, Nx, Ny, Nz, hydro=False):
 
 
 @pytest.mark.parametrize("Nx,Ny,Nz,hydro", [(32, 32, 17, False), (48, 40, 25, False), (64, 64, 33, False),
-                                            (128, 128, 65, True), (96, 96, 97, False), (256, 256, 129, False)])
+                                            (48, 40, 24, False), (64, 64, 64, True), (128, 128, 65, True),
+                                            (96, 96, 97, False), (256, 256, 129, False)])
 def test_tensor_core_vertical_matches_cuda_cores(wv, Nx, Ny, Nz, hydro):
     import torch
     cfg = _cfg(wv, Nx, Ny, Nz, hydro)

@@ -1,6 +1,8 @@
 // Vertical inverse transform of the paired-FP32 (FP32X2) flux on the tensor
-// cores: the same result as k_vinv<ff, true> (phase, field spectra, folded
-// vertical inverse DCT-I / DST-I, z-derivatives of the flux targets) with the
+// cores: the same result as k_vinv<ff, true> (phase kernel.cpp:1186-1191, field
+// spectra kernel.cpp:218-291 and WVCoefficientFormulas.hpp:23-58, Hermitian
+// completion kernel.cpp:433-438, folded vertical inverse DCT-I / DST-I
+// kernel.cpp:161-174, z-derivatives of the flux targets) with the
 // dense contraction done as BF16 GEMMs of exact integer digit slices (the
 // error-free splitting of Ozaki, Ogita, Oishi and Rump, "Error-free
 // transformations of matrix multiplication by using fast routines of matrix
