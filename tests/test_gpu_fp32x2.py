@@ -307,3 +307,26 @@ def test_fp32x2_tensor_vertical_members_equal_single_handles(wv):
         assert k.device_status() == 0
         k.close()
     ens.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32x2", 1e-9), ("mixed", 2e-3)])
+def test_adjoint_with_tensor_vertical_matches_cuda_cores(wv, precision, tol):
+    """The flux VJP and the checkpointed RK4 adjoint (whose forward fluxes keep
+    their y spectra for the adjoint x pass) with the tensor-core vertical
+    transforms against the same handle on the CUDA-core kernels."""
+    import torch
+    cfg = wv.Configuration(Nx=64, Ny=64, Nz=33, Nj=21, Lx=200e3, Ly=200e3, Lz=4000.0, latitude=33.0)
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision=precision)
+    A = wv.synthetic_state(k, seed=31, urms=0.1)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+    rng = np.random.default_rng(6)
+    cot = [torch.from_numpy(rng.standard_normal(A[0].shape) + 1j * rng.standard_normal(A[0].shape)).cuda() for _ in range(3)]
+    dt = wv.cfl_time_step(k, *A)
+    out = {}
+    for kind in ("cuda", "tensor"):
+        k.set_vertical_kernel(kind)
+        out[kind] = (k.flux_vjp(300.0, 0.0, *dev, *cot), k.rk4_adjoint(*dev, 0.0, 0.0, dt, 6, 3, *cot))
+    for a, b in zip(out["tensor"][0] + out["tensor"][1], out["cuda"][0] + out["cuda"][1]):
+        assert float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) <= tol
+    assert k.device_status() == 0
+    k.close()
