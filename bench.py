@@ -246,16 +246,6 @@ def _time_steps(k, dev, t, t0, dt, steps, warmup, stream, barrier, flush, torch)
     return total, t
 
 
-def _select_tensor_vertical(k, wvgpu):
-    """Selects the tensor-core vertical transform where the handle has one;
-    True if selected."""
-    try:
-        k.set_vertical_kernel("tensor")
-        return True
-    except wvgpu.WVKernelError:
-        return False
-
-
 def _stage_profile(k, dev, t, t0, dt, precision, torch):
     k.setStageInstrumentation(True)
     k.rk4(*dev, t, t0, dt, 1)
@@ -523,15 +513,14 @@ def run_ours(args):
     km.close()
     # paired-FP32 form (FP32X2): FP64-class accuracy on the FP32 pipe
     kx = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
-    x_tc = _select_tensor_vertical(kx, wvgpu)
     devx = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
     x_ms, tx = _time_steps(kx, devx, 0.0, t0, dt, args.steps, args.warmup, stream, barrier, flush, torch)
     x_value = world * args.steps / max_over_ranks(x_ms / 1e3)
     fp32x2 = {"value": x_value, "unit": UNIT, "ms_per_step": x_ms / args.steps, "speedup_vs_fp64": x_value / value,
               "dtype": "paired f32 (float-float, ~45-48 significand bits on the FP32 pipe) for the xy transforms, "
-                       "products, phases and the forward vertical contraction; vertical inverse as exact digit-sliced "
-                       "BF16 tcgen05 GEMMs (six 8-bit slices per operand, ~2^-46); f64 angles, stores and RK4",
-              "vertical_inverse_kernel": "tensor cores (tcgen05.mma, digit slices)" if x_tc else "cuda cores",
+                       "products, phases and the vertical transforms (FFTs of the even / odd extension over z); "
+                       "f64 angles, stores and RK4",
+              "vertical_kernel": kx.vertical_kernel(),
               "roofline": _stage_profile(kx, devx, tx, t0, dt, "fp32x2", torch)}
     if rank == 0:
         err = _field_error_after(k, kx, state, dt, 100, torch, np)
@@ -570,6 +559,7 @@ def run_ours(args):
             "grid": [GRID["Nx"], GRID["Ny"], GRID["Nz"]], "Nj": GRID["Nj"], "Nkl": k.sizes["Nkl"], "dt_s": dt,
             "precision": "fp64 (plain drop-in); the reduced-precision forms are reported under 'mixed' (f32 + "
                          "split-BF16 tensor cores) and 'fp32x2' (paired f32)",
+            "vertical_kernel": k.vertical_kernel(),
             "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MB write)"},
         "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": coeff_bytes,
                 "d2h_bytes_per_step": coeff_bytes},

@@ -161,7 +161,15 @@ int wv_set_stage_instrumentation(wv_handle* handle, int enabled);
  * retained columns (one per SM) fill the GPU; WV_VERTICAL_CUDA_CORES otherwise. */
 #define WV_VERTICAL_CUDA_CORES 0
 #define WV_VERTICAL_TENSOR_CORES 1
+/* FP64 and FP32X2 handles (3 <= Nz <= 513; the default there): the flux's
+ * vertical inverse and forward transforms as complex FFTs of length 2 (Nz - 1)
+ * of the even / odd extension over z, one per pair of a cosine-family and a
+ * sine-family channel (the reference's own REDFT00 / RODFT00 route), in the
+ * handle's arithmetic. */
+#define WV_VERTICAL_FFT 2
 int wv_set_vertical_kernel(wv_handle* handle, int kind);
+/* The vertical-transform kernel the handle's flux runs (WV_VERTICAL_*). */
+int wv_get_vertical_kernel(const wv_handle* handle, int* kind);
 /* Device status word of the handle (synchronous read): bit 0 is set when a
  * bounded wait inside a kernel ran out (the kernel returned without hanging). */
 int wv_get_device_status(wv_handle* handle, unsigned* status);

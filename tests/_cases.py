@@ -39,6 +39,27 @@ def rel_err(a, b):
     return num / den if den > 0 else num
 
 
+def state_components_close(got, golden, keys, tol):
+    """Per-component parity of a state (Kp, Km, K0, ...) against golden arrays:
+    a component whose golden values stay below 1e-6 of the state's largest
+    coefficient is accumulated rounding (the single-wave case's A0 starts at
+    zero and ends at 3e-10 of Ap, its digits set by the summation order) and is
+    gated relative to the state; every other component relative to itself.
+    Returns the failing keys."""
+    scale = max(float(np.max(np.abs(golden[k]))) for k in keys)
+    bad = []
+    for a, k in zip(got, keys):
+        ref = golden[k]
+        if not np.any(ref):
+            continue
+        if float(np.max(np.abs(ref))) < 1e-6 * scale:
+            if float(np.max(np.abs(np.asarray(a) - ref))) > tol * scale:
+                bad.append(k)
+        elif rel_err(a, ref) > tol:
+            bad.append(k)
+    return bad
+
+
 def parity_tolerance(floor):
     """Parity gate for states where the FP64 noise floor of the computation
     (two valid orderings of the oracle) exceeds the reference's 1e-12 gate:

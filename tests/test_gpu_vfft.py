@@ -1,0 +1,135 @@
+"""Vertical transforms of the flux as FFTs of the even / odd extension over z
+(WV_VERTICAL_FFT: k_vinv_fft, k_vfwd_fft; the default of FP64 and FP32X2
+handles): every
+reference golden case at the FP64 (1e-12) and FP32X2 (1e-9) tolerances (RK4
+components that are pure accumulated rounding gated against the state), and
+the flux against the dense folded contraction of the same handle on 0.1 m/s
+spectrum states (odd and even Nz, hydrostatic)."""
+import numpy as np
+import pytest
+
+import wv_oracle as O
+from _cases import config_from_case, golden_cases, load_golden, rel_err, state_components_close
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+TOL = {"fp64": 1e-12, "fp32x2": 1e-9}
+
+
+@pytest.fixture(scope="module")
+def wv():
+    import torch
+    import wvgpu
+    from wvgpu import build
+    assert torch.cuda.is_available()
+    build.build()
+    return wvgpu
+
+
+def _conf(wv, c):
+    return wv.Configuration(Nx=c.Nx, Ny=c.Ny, Nz=c.Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, N0=c.N0, rho0=c.rho0, g=c.g,
+                            planetaryRadius=c.planetaryRadius, rotationRate=c.rotationRate, latitude=c.latitude,
+                            isHydrostatic=c.isHydrostatic, shouldAntialias=c.shouldAntialias)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32x2"])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fft_vertical_matches_reference(wv, name, precision):
+    cf = CASES[name]
+    g = load_golden(name)
+    tol = TOL[precision]
+    k = wv.WVTransformConstantStratificationKernel(_conf(wv, config_from_case(cf)), precision=precision)
+    k.set_vertical_kernel("fft")
+    t, t0 = float(g["t"]), float(g["t0"])
+    args = (t, t0, g["Ap"], g["Am"], g["A0"])
+    for got, key in zip(k.nonlinearFlux(*args), ("Fp", "Fm", "F0")):
+        assert rel_err(got, g[key]) <= tol, (name, key, rel_err(got, g[key]))
+    Fw, adv = k.nonlinearFluxWithAdvectionFields(*args)
+    for got, key in zip(Fw, ("with_Fp", "with_Fm", "with_F0")):
+        assert rel_err(got, g[key]) <= tol, (name, key)
+    assert rel_err(adv, g["with_fields"]) <= tol
+    k.set_forcing(nonlinear=True, adaptive_damping=bool(cf["damping"]))
+    for got, key in zip(k.evaluateRightHandSide(*args), ("Rp", "Rm", "R0")):
+        assert rel_err(got, g[key]) <= tol, (name, key)
+    Kp, Km, K0, tK = k.rk4(g["rk_Ap"], g["rk_Am"], g["rk_A0"], float(g["rk_t"]), float(g["rk_t0"]), float(g["rk_dt"]),
+                           int(g["rk_steps"]))
+    assert not state_components_close((Kp, Km, K0), g, ("Kp", "Km", "K0"), tol), name
+    k.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32x2"])
+@pytest.mark.parametrize("Nx,Ny,Nz,hydro", [(32, 32, 17, False), (48, 40, 24, False), (64, 64, 33, True),
+                                            (64, 64, 64, False), (128, 128, 65, False)])
+def test_fft_vertical_flux_matches_dense_contraction(wv, Nx, Ny, Nz, hydro, precision):
+    """The flux with the FFT vertical transforms against the dense folded
+    contraction of the same handle, on the oracle's 0.1 m/s spectrum state.
+    The max-norm relative difference of two valid FP64 orderings of the flux is
+    set by its ill-conditioned coefficients (high j, small K_h) and grows with
+    the grid: the oracle measures it on the same state (its FFT against its
+    dense vertical transforms, O.noise_floor: 1.1e-12 at 32x32x17, 1.3e-11 at
+    64x64x64, 2e-11 at 128x128x65, 3e-10 at 256x256x129), and the GPU
+    difference must stay within 3x that floor (FP64) or 300x (paired FP32,
+    2^8 times FP64's unit roundoff)."""
+    import torch
+    c = O.Config(Nx=Nx, Ny=Ny, Nz=Nz, Nj=O.default_nj(Nz), Lx=3125.0 * Nx, Ly=3125.0 * Ny, Lz=4000.0, latitude=33.0,
+                 isHydrostatic=hydro)
+    d = O.build_descriptor(c)
+    A = O.spectrum_state(d, seed=29, urms=0.1)
+    _, floors = O.noise_floor(O.nonlinear_flux, d, *A, 777.0, 5.0)
+    cfg = wv.Configuration(Nx=Nx, Ny=Ny, Nz=Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, latitude=33.0, isHydrostatic=hydro)
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision=precision)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+    k.set_vertical_kernel("cuda")
+    ref = [x.cpu().numpy() for x in k.nonlinearFlux(777.0, 5.0, *dev)]
+    k.set_vertical_kernel("fft")
+    got = [x.cpu().numpy() for x in k.nonlinearFlux(777.0, 5.0, *dev)]
+    err = [rel_err(a, b) for a, b in zip(got, ref)]
+    print(f"{precision} {Nx}x{Ny}x{Nz} hydro={hydro}: FFT vs dense flux difference {err}, oracle FP64 floor {floors}")
+    factor = 3.0 if precision == "fp64" else 300.0
+    for e, fl in zip(err, floors):
+        assert e <= factor * fl + (1e-14 if precision == "fp64" else 1e-12)
+    k.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("fp32x2", 1e-9)])
+def test_fft_vertical_tendencies_at_256(wv, precision, tol):
+    """At 256x256x129 the flux's field tendencies (u, v, w, eta through the FP64
+    inverse transform; well conditioned, unlike single coefficients) with the
+    FFT vertical transforms against the dense contraction."""
+    import torch
+    cfg = wv.Configuration(Nx=256, Ny=256, Nz=129, Nj=O.default_nj(129), Lx=800e3, Ly=800e3, Lz=4000.0, latitude=33.0)
+    k64 = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    k = k64 if precision == "fp64" else wv.WVTransformConstantStratificationKernel(cfg, precision=precision)
+    A = wv.synthetic_state(k64, seed=23, urms=0.1)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+
+    def tendencies(kind):
+        k.set_vertical_kernel(kind)
+        F = [x.cpu().numpy() for x in k.nonlinearFlux(777.0, 5.0, *dev)]
+        return k64.transformWaveVortexToUVWEta(0.0, 0.0, *F)
+
+    dense, fft = tendencies("cuda"), tendencies("fft")
+    err = [float(np.linalg.norm(fft[i] - dense[i]) / np.linalg.norm(dense[i])) for i in range(4)]
+    print(f"{precision} 256x256x129 FFT vs dense flux tendencies (u, v, w, eta): {err}")
+    assert max(err) <= tol
+    if k is not k64:
+        k.close()
+    k64.close()
+
+
+def test_fft_vertical_is_the_default_for_fp64_and_fp32x2(wv):
+    cfg = wv.Configuration(Nx=32, Ny=32, Nz=17, Nj=10, Lx=100e3, Ly=100e3, Lz=4000.0, latitude=33.0)
+    for precision, kind in (("fp64", "fft"), ("fp32x2", "fft"), ("mixed", "cuda")):
+        k = wv.WVTransformConstantStratificationKernel(cfg, precision=precision)
+        assert k.vertical_kernel() == kind, precision
+        k.close()
+
+
+def test_fft_vertical_rejected_on_mixed(wv):
+    k = wv.WVTransformConstantStratificationKernel(
+        wv.Configuration(Nx=32, Ny=32, Nz=17, Nj=10, Lx=100e3, Ly=100e3, Lz=4000.0, latitude=33.0), precision="mixed")
+    with pytest.raises(wv.WVKernelError) as e:
+        k.set_vertical_kernel("fft")
+    assert e.value.code == 10
+    k.close()

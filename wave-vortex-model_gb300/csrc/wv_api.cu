@@ -15,6 +15,7 @@
 #include "wv_vinv_tc.cuh"
 #include "wv_vfwd_tc.cuh"
 #include "wv_vinv_tcx.cuh"
+#include "wv_vfft.cuh"
 #include "wv_scalar.cuh"
 
 #include <cuda_runtime.h>
@@ -88,6 +89,7 @@ struct wv_handle {
     bool instrument = false;
     bool tcAvailable = false;  // tensor-core vertical transform built for this handle
     bool verticalTC = false;   // ... and selected (default: on where built)
+    bool verticalFFT = false;  // FP64 / FP32X2: vertical inverse as FFTs of the even / odd extension
     size_t tcSmem = 0;
     bool tcFwdAvailable = false;  // tensor-core forward vertical transform built (used with verticalTC)
     size_t tcFwdSmem = 0;
@@ -388,6 +390,13 @@ cudaError_t set_smem_limits(const Plan& p) {
     WV_SET((dev::k_xr2c_fields<T>), smem_xr2c<T>(p));
     WV_SET((dev::k_vfwd<T, true>), smem_vfwd<T>(p, 4));
     WV_SET((dev::k_vfwd<T, false>), smem_vfwd<T>(p, 4));
+    if constexpr (sizeof(dev::cx<T>) == 16) {
+        if (p.fz.N > 0) {
+            WV_SET((dev::k_vinv_fft<T, true>), dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, dev::VzShape<true>::modes));
+            WV_SET((dev::k_vinv_fft<T, false>), dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, dev::VzShape<false>::modes));
+            WV_SET((dev::k_vfwd_fft<T, true>), dev::smem_vfwd_fft<T>(p.fz.N));
+        }
+    }
 #undef WV_SET
     return cudaSuccess;
 }
@@ -541,6 +550,35 @@ void launch_xr2c(wv_handle* h, const double* fields, int nch, dev::cx<T>* ps, cu
     dev::k_xr2c_fields<T><<<dim3(p.Ny, h->dd.zTotal), 256, smem_xr2c<T>(p), s>>>(h->dd, fields, nch, ps);
 }
 
+// The flux's vertical inverse transform with the handle's kernel choice: the
+// tensor-core kernels (mixed: split-BF16; FP32X2: digit slices, with the
+// y-spectra buffer yScratch as its scratch), the FFTs of the even / odd
+// extension (FP64, FP32X2) or the dense folded contraction.
+template <typename T>
+void launch_vinv_flux(wv_handle* h, double elapsed, const double* Ap, const double* Am, const double* A0, dev::cx<T>* z,
+                      unsigned long long* speed, dev::cx<T>* yScratch, cudaStream_t s) {
+    const Plan& p = h->plan;
+    const auto& d = h->dd;
+    auto* y = yScratch;
+    if constexpr (sizeof(T) == 4) {
+        if (h->verticalTC)
+            dev::k_vinv_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcSmem, s>>>(
+                d, Ap, Am, A0, elapsed, reinterpret_cast<float2*>(z), speed);
+        else
+            dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    } else if (std::is_same<T, dev::ff>::value && h->verticalTC) {
+        if constexpr (std::is_same<T, dev::ff>::value)
+            dev::k_vinv_tcx<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcxSmem, s>>>(
+                d, Ap, Am, A0, elapsed, z, speed, reinterpret_cast<dev::ff*>(y));
+    } else if (h->verticalFFT) {
+        constexpr int modes = dev::VzShape<true>::modes;
+        dev::k_vinv_fft<T, true><<<dim3(cdiv(p.Nkl, modes), d.members), 256,
+                                    dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, modes), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    } else {
+        dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    }
+}
+
 // One nonlinear flux (+ adaptive damping when requested) on device buffers.
 // physOut, when given, receives the x pass's real rows (U, V, W and the
 // derivatives of every target) for the adjoint to reuse.
@@ -560,21 +598,7 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     // max |u_h| is reduced only when adaptive damping consumes it
     unsigned long long* speed = damping ? h->maxSpeed : nullptr;
     if (inst) cudaEventRecord(h->ev[0], s);
-    if constexpr (sizeof(T) == 4) {
-        if (h->verticalTC)
-            dev::k_vinv_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcSmem, s>>>(
-                d, Ap, Am, A0, elapsed, reinterpret_cast<float2*>(z), speed);
-        else
-            dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
-    } else if constexpr (std::is_same<T, dev::ff>::value) {
-        if (h->verticalTC)
-            dev::k_vinv_tcx<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcxSmem, s>>>(
-                d, Ap, Am, A0, elapsed, z, speed, reinterpret_cast<dev::ff*>(y));
-        else
-            dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
-    } else {
-        dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
-    }
+    launch_vinv_flux<T>(h, elapsed, Ap, Am, A0, z, speed, y, s);
     if (inst) cudaEventRecord(h->ev[1], s);
     dev::YInvMap map{};
     map.nOut = 4 + 2 * nt;
@@ -589,12 +613,19 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     if (inst) cudaEventRecord(h->ev[3], s);
     launch_yfwd<T>(h, ps, nt, f, s);
     if (inst) cudaEventRecord(h->ev[4], s);
-    bool fwdTC = false;
+    bool fwdTC = false;  // forward transform launched by a specialised kernel
     if constexpr (sizeof(T) == 4) {
         if (h->verticalTC && h->tcFwdAvailable) {
             dev::k_vfwd_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcFwdSmem, s>>>(
                 d, reinterpret_cast<const float2*>(f), elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
             fwdTC = true;
+        }
+    }
+    if constexpr (sizeof(dev::cx<T>) == 16) {
+        if (!fwdTC && h->verticalFFT) {
+            dev::k_vfwd_fft<T, true><<<dim3(cdiv(p.Nkl, dev::kVfModes), d.members), 256, dev::smem_vfwd_fft<T>(p.fz.N), s>>>(
+                d, f, nt, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
+            fwdTC = true;  // forward transform launched
         }
     }
     if (!fwdTC)
@@ -942,7 +973,7 @@ void launch_flux_fields(wv_handle* h, double elapsed, const double* Ap, const do
     const auto& d = h->dd;
     const int nt = p.targets.count;
     auto* z = static_cast<dev::cx<T>*>(h->zspec);
-    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, nullptr);
+    launch_vinv_flux<T>(h, elapsed, Ap, Am, A0, z, nullptr, y, s);
     dev::YInvMap map{};
     map.nOut = 4 + 2 * nt;
     for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
@@ -1228,7 +1259,17 @@ cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* 
     // No damping on this entry, so no max-speed reduction (offs[4] stays reserved).
     unsigned long long* speed = nullptr;
     const int nt = p.targets.count;
-    dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+    bool fft = false;
+    if constexpr (sizeof(dev::cx<T>) == 16) fft = h->verticalFFT;
+    if constexpr (sizeof(dev::cx<T>) == 16) {
+        if (fft) {
+            constexpr int modes = dev::VzShape<true>::modes;
+            dev::k_vinv_fft<T, true><<<dim3(cdiv(p.Nkl, modes), d.members), 256,
+                                        dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, modes), s>>>(d, Ap, Am, A0, elapsed, z, speed);
+        }
+    }
+    if (!fft)
+        dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
     dev::YInvMap map{};
     map.nOut = 4 + 2 * nt;
     for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
@@ -1239,8 +1280,14 @@ cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* 
     launch_yinv<T>(h, map, z, y, s);
     launch_xflux<T>(h, y, ps, speed, s);
     launch_yfwd<T>(h, ps, nt, f, s);
-    dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
-        d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
+    if constexpr (sizeof(dev::cx<T>) == 16) {
+        if (fft)
+            dev::k_vfwd_fft<T, true><<<dim3(cdiv(p.Nkl, dev::kVfModes), d.members), 256, dev::smem_vfwd_fft<T>(p.fz.N), s>>>(
+                d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
+    }
+    if (!fft)
+        dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
+            d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
     return cudaGetLastError();
 }
 
@@ -1362,6 +1409,8 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     dd.xLen = static_cast<int>(x_len(p));
     dd.fx.N = p.fx.N; dd.fx.nstages = p.fx.nstages; dd.fy.N = p.fy.N; dd.fy.nstages = p.fy.nstages;
     for (int i = 0; i < dev::kMaxStages; ++i) { dd.fx.radix[i] = p.fx.radix[i]; dd.fy.radix[i] = p.fy.radix[i]; }
+    dd.fz.N = p.fz.N; dd.fz.nstages = p.fz.nstages;
+    for (int i = 0; i < dev::kMaxStages; ++i) dd.fz.radix[i] = p.fz.radix[i];
     std::vector<int32_t> ymap(p.ymap);
     std::vector<int32_t> posKy(p.posKy), colStart(p.colStart), modeWV(p.modeWV), modePos(p.modePos), modeComp(p.modeCompPos);
     std::vector<double> inertial(d.inertialScale), apmw(d.apmWProjectionPrefactor);
@@ -1416,6 +1465,7 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     };
     upT(p.Ccos, &dd.Ccos); upT(p.Csin, &dd.Csin); upT(p.CcosM, &dd.CcosM); upT(p.CsinM, &dd.CsinM);
     upT(p.Fcos, &dd.Fcos); upT(p.Fsin, &dd.Fsin); upT(p.twx, &dd.twx); upT(p.twxN, &dd.twxN); upT(p.twy, &dd.twy);
+    if (p.fz.N > 0) { upT(p.twz, &dd.twz); upT(std::vector<double>(d.m.begin(), d.m.begin() + p.Nj), &dd.tMz); }
     upT(p.rowK, &dd.tRowK); upT(p.rowL, &dd.tRowL);
     {
         auto transpose = [](const std::vector<double>& a, size_t rows, size_t cols) {
@@ -1509,6 +1559,13 @@ static int create_handle(const wv_config* config, int precision, int members, wv
             h->verticalTC = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
         }
     }
+    // FP64 and FP32X2: the vertical transforms of the flux as FFTs by default (the
+    // reference's own route, fewer operations than the dense contraction); the
+    // tensor-core inverse of FP32X2 stays selectable
+    if (precision != WV_PRECISION_MIXED && p.fz.N > 0) {
+        h->verticalFFT = true;
+        h->verticalTC = false;
+    }
     const auto ss = scratch_sizes(p);
     const size_t cb = 2 * elem_size(precision);
     const size_t R = p.Nx * p.Ny * p.Nz;
@@ -1535,6 +1592,7 @@ static int create_handle(const wv_config* config, int precision, int members, wv
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         const int code = e == cudaErrorMemoryAllocation ? WV_ALLOCATION_FAILURE : WV_FFT_PLAN_FAILURE;
+        cudaGetLastError();  // a failed attribute or allocation call must not surface in a later launch check
         wv_destroy(h);
         return code;
     }
@@ -1563,12 +1621,21 @@ int wv_get_metrics(const wv_handle* h, wv_metrics* m) {
 
 int wv_set_vertical_kernel(wv_handle* h, int kind) {
     if (!h) return WV_INVALID_POINTER;
-    if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES)
+    if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES && kind != WV_VERTICAL_FFT)
         return fail(h, WV_INVALID_CONFIGURATION, "Unknown vertical-transform kernel.");
+    if (kind == WV_VERTICAL_FFT && (h->precision == WV_PRECISION_MIXED || h->plan.fz.N == 0))
+        return fail(h, WV_UNSUPPORTED_OPERATION, "The FFT vertical transform needs an FP64 or FP32X2 handle with 3 <= Nz <= 513.");
     if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
         return fail(h, WV_UNSUPPORTED_OPERATION,
                     "The tensor-core vertical transform needs a mixed-precision (Nz <= 255) or FP32X2 (Nj <= 96) handle.");
     h->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
+    h->verticalFFT = kind == WV_VERTICAL_FFT;
+    return WV_SUCCESS;
+}
+
+int wv_get_vertical_kernel(const wv_handle* h, int* kind) {
+    if (!h || !kind) return WV_INVALID_POINTER;
+    *kind = h->verticalTC ? WV_VERTICAL_TENSOR_CORES : h->verticalFFT ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
     return WV_SUCCESS;
 }
 
@@ -2520,7 +2587,7 @@ cudaError_t autotune_group(wv_handle* h, cudaStream_t s, wv_ensemble_tuning& out
     h->verticalTC = bestTC;
     out.stockham_y = bestY ? 1 : 0;
     out.stockham_x = bestX ? 1 : 0;
-    out.vertical = bestTC ? WV_VERTICAL_TENSOR_CORES : WV_VERTICAL_CUDA_CORES;
+    out.vertical = bestTC ? WV_VERTICAL_TENSOR_CORES : h->verticalFFT ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
     out.warp_y_available = warpY ? 1 : 0;
     out.warp_x_available = warpX ? 1 : 0;
     out.tensor_vertical_available = h->tcAvailable ? 1 : 0;
@@ -2587,7 +2654,7 @@ int wv_ensemble_create(const wv_config* group_configs, const int* members, int n
             t.warp_y_available = h->precision == WV_PRECISION_MIXED && warp_ry<float>(h->plan) != 0;
             t.warp_x_available = h->precision == WV_PRECISION_MIXED && warp_rx<float>(h->plan) != 0;
             t.tensor_vertical_available = h->tcAvailable ? 1 : 0;
-            t.vertical = WV_VERTICAL_CUDA_CORES;
+            t.vertical = h->verticalTC ? WV_VERTICAL_TENSOR_CORES : h->verticalFFT ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
             t.flux_ms = -1.0f;
         }
     }
@@ -2621,14 +2688,18 @@ int wv_ensemble_get_tuning(const wv_ensemble* e, int group, wv_ensemble_tuning* 
 
 int wv_ensemble_set_vertical_kernel(wv_ensemble* e, int kind) {
     if (!e) return WV_INVALID_POINTER;
-    if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES)
+    if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES && kind != WV_VERTICAL_FFT)
         return efail(e, WV_INVALID_CONFIGURATION, "Unknown vertical-transform kernel.");
+    for (wv_handle* h : e->groups)
+        if (kind == WV_VERTICAL_FFT && (h->precision == WV_PRECISION_MIXED || h->plan.fz.N == 0))
+            return efail(e, WV_UNSUPPORTED_OPERATION, "The FFT vertical transform needs FP64 or FP32X2 groups with 3 <= Nz <= 513.");
     for (wv_handle* h : e->groups)
         if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
             return efail(e, WV_UNSUPPORTED_OPERATION,
                          "The tensor-core vertical transform needs mixed-precision (Nz <= 255) or FP32X2 (Nj <= 96) groups.");
     for (size_t g = 0; g < e->groups.size(); ++g) {
         e->groups[g]->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
+        e->groups[g]->verticalFFT = kind == WV_VERTICAL_FFT;
         e->tuning[g].vertical = kind;
     }
     e->keySteps = -1;  // captured kernels changed: capture anew

@@ -278,6 +278,9 @@ struct DescDev {
     int xEven;              // Nx even: real rows go through half-length complex FFTs
     int xLen;               // Nx/2 (even) or Nx (odd)
     FFTDev fx, fy;          // fx factors xLen
+    FFTDev fz;              // 2 (Nz - 1): vertical transforms as FFTs (N = 0: not available)
+    const void* twz;        // cx<T>[2 (Nz - 1)]
+    const void* tMz;        // T[Nj]: m_j in the working type
 };
 
 // Row wavenumbers in the working type T of the xy stage.
@@ -295,6 +298,101 @@ __device__ __forceinline__ const T* row_l(const DescDev& d) { return static_cast
 // imaginary part cleared on self-conjugate rows (kernel.cpp:211-291,433-438).
 
 constexpr int kVinvModes = 8;
+
+// Field spectra u, v, w, eta of one (mode, j) in the stored frame and working
+// precision T (k_vinv's phase 1): phase (kernel.cpp:1186-1191), evolution and
+// coefficient formulas (WVCoefficientFormulas.hpp:23-58), conjugated for
+// kMode < 0 storage, imaginary part cleared on self-conjugate rows.
+template <typename T>
+__device__ __forceinline__ void vinv_field_spectra(const DescDev& d, const double* __restrict__ Ap,
+                                                   const double* __restrict__ Am, const double* __restrict__ A0,
+                                                   double elapsed, int mode, int j, cx<T> (&f)[4]) {
+    const int Nj = d.Nj;
+    const int w = d.modeWV[mode];
+    const unsigned char flags = d.modeFlags[mode];
+    const int idx = j + Nj * w;
+    if constexpr (sizeof(T) == 4) {
+        // MIXED: phase angle in FP64 reduced to [-pi, pi], then FP32 phase and field spectra.
+        const double ang = d.omega[idx] * elapsed;
+        const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+        float sf, cf;
+        sincosf(float(red), &sf, &cf);
+        const float2 ap0 = make_float2(float(Ap[2 * idx]), float(Ap[2 * idx + 1]));
+        const float2 am0 = make_float2(float(Am[2 * idx]), float(Am[2 * idx + 1]));
+        const float2 a0 = make_float2(float(A0[2 * idx]), float(A0[2 * idx + 1]));
+        const float2 ap = make_float2(ap0.x * cf - ap0.y * sf, ap0.x * sf + ap0.y * cf);
+        const float2 am = make_float2(am0.x * cf + am0.y * sf, am0.y * cf - am0.x * sf);
+        const float2 uap = *reinterpret_cast<const float2*>(d.fUAp + 2 * idx);
+        const float2 vap = *reinterpret_cast<const float2*>(d.fVAp + 2 * idx);
+        const float2 wap = *reinterpret_cast<const float2*>(d.fWAp + 2 * idx);
+        const float2 ua0 = *reinterpret_cast<const float2*>(d.fUA0 + 2 * idx);
+        const float2 va0 = *reinterpret_cast<const float2*>(d.fVA0 + 2 * idx);
+        const float nap = d.fNAp[idx], na0 = d.fNA0[idx];
+        auto cm2 = [](float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+        auto cj = [](float2 a) { return make_float2(a.x, -a.y); };
+        auto ca = [](float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); };
+        float2 u = ca(ca(cm2(uap, ap), cm2(cj(uap), am)), cm2(ua0, a0));
+        float2 v = ca(ca(cm2(vap, ap), cm2(cj(vap), am)), cm2(va0, a0));
+        float2 ww = ca(cm2(wap, ap), cm2(wap, am));
+        float2 n = make_float2(ap.x * nap - am.x * nap + a0.x * na0, ap.y * nap - am.y * nap + a0.y * na0);
+        if (flags & 1) { u = cj(u); v = cj(v); ww = cj(ww); n = cj(n); }
+        if (flags & 2) { u.y = 0.f; v.y = 0.f; ww.y = 0.f; n.y = 0.f; }
+        f[0] = mk<T>(u.x, u.y);
+        f[1] = mk<T>(v.x, v.y);
+        f[2] = mk<T>(ww.x, ww.y);
+        f[3] = mk<T>(n.x, n.y);
+        return;
+    }
+    if constexpr (std::is_same<T, ff>::value) {
+        // FP32X2: FP64 angle, paired-FP32 phase (ff_sincos), then paired-FP32
+        // evolution and field spectra with the coefficient arrays stored as
+        // pairs (d.fUAp ... hold ff values)
+        T sf, cf;
+        ff_sincos(d.omega[idx] * elapsed, sf, cf);
+        const cx<T> p = mk<T>(cf, sf);
+        auto ld = [](const double* q) { return mk<T>(ff_from_double(q[0]), ff_from_double(q[1])); };
+        const cx<T> ap = cmul<T>(ld(Ap + 2 * idx), p);
+        const cx<T> am = cmul<T>(ld(Am + 2 * idx), cconj<T>(p));
+        const cx<T> a0 = ld(A0 + 2 * idx);
+        const cx<T> uap = reinterpret_cast<const cx<T>*>(d.fUAp)[idx];
+        const cx<T> vap = reinterpret_cast<const cx<T>*>(d.fVAp)[idx];
+        const cx<T> wap = reinterpret_cast<const cx<T>*>(d.fWAp)[idx];
+        const cx<T> ua0 = reinterpret_cast<const cx<T>*>(d.fUA0)[idx];
+        const cx<T> va0 = reinterpret_cast<const cx<T>*>(d.fVA0)[idx];
+        const T nap = reinterpret_cast<const T*>(d.fNAp)[idx], na0 = reinterpret_cast<const T*>(d.fNA0)[idx];
+        cx<T> u = cadd<T>(cadd<T>(cmul<T>(uap, ap), cmul<T>(cconj<T>(uap), am)), cmul<T>(ua0, a0));
+        cx<T> v = cadd<T>(cadd<T>(cmul<T>(vap, ap), cmul<T>(cconj<T>(vap), am)), cmul<T>(va0, a0));
+        cx<T> ww = cadd<T>(cmul<T>(wap, ap), cmul<T>(wap, am));
+        cx<T> n = mk<T>(ap.x * nap - am.x * nap + a0.x * na0, ap.y * nap - am.y * nap + a0.y * na0);
+        if (flags & 1) { u = cconj<T>(u); v = cconj<T>(v); ww = cconj<T>(ww); n = cconj<T>(n); }
+        if (flags & 2) { u.y = T(0); v.y = T(0); ww.y = T(0); n.y = T(0); }
+        f[0] = u;
+        f[1] = v;
+        f[2] = ww;
+        f[3] = n;
+        return;
+    }
+    double s, c;
+    sincos(d.omega[idx] * elapsed, &s, &c);
+    const zd p{c, s};
+    // evolveWaveVortexCoefficients + coefficientValueForField<0..3> (WVCoefficientFormulas.hpp:23-33)
+    const zd ap = zmul(zload(Ap + 2 * idx), p);
+    const zd am = zmul(zload(Am + 2 * idx), zconj(p));
+    const zd a0 = zload(A0 + 2 * idx);
+    const zd uap = zload(d.UAp + 2 * idx), vap = zload(d.VAp + 2 * idx), wap = zload(d.WAp + 2 * idx);
+    const zd ua0 = zload(d.UA0 + 2 * idx), va0 = zload(d.VA0 + 2 * idx);
+    const double nap = d.NAp[idx], na0 = d.NA0[idx];
+    zd u = zadd(zadd(zmul(uap, ap), zmul(zconj(uap), am)), zmul(ua0, a0));
+    zd v = zadd(zadd(zmul(vap, ap), zmul(zconj(vap), am)), zmul(va0, a0));
+    zd ww = zadd(zmul(wap, ap), zmul(wap, am));
+    zd n = zadd(zadd(zscale(ap, nap), zscale(am, -nap)), zscale(a0, na0));
+    if (flags & 1) { u = zconj(u); v = zconj(v); ww = zconj(ww); n = zconj(n); }
+    if (flags & 2) { u.im = 0.0; v.im = 0.0; ww.im = 0.0; n.im = 0.0; }
+    f[0] = mk<T>(T(u.re), T(u.im));
+    f[1] = mk<T>(T(v.re), T(v.im));
+    f[2] = mk<T>(T(ww.re), T(ww.im));
+    f[3] = mk<T>(T(n.re), T(n.im));
+}
 
 template <typename T, bool FLUX>
 __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restrict__ Ap, const double* __restrict__ Am,
@@ -315,91 +413,10 @@ __global__ void __launch_bounds__(256) k_vinv(DescDev d, const double* __restric
     if (blockIdx.x == 0 && threadIdx.x == 0 && maxSpeedBits) maxSpeedBits[member] = 0ull;
     for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
         const int mi = it / Nj, j = it - mi * Nj;
-        const int mode = m0 + mi;
-        const int w = d.modeWV[mode];
-        const unsigned char flags = d.modeFlags[mode];
-        const int idx = j + Nj * w;
-        if constexpr (sizeof(T) == 4) {
-            // MIXED: phase angle in FP64 reduced to [-pi, pi], then FP32 phase and field spectra.
-            const double ang = d.omega[idx] * elapsed;
-            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
-            float sf, cf;
-            sincosf(float(red), &sf, &cf);
-            const float2 ap0 = make_float2(float(Ap[2 * idx]), float(Ap[2 * idx + 1]));
-            const float2 am0 = make_float2(float(Am[2 * idx]), float(Am[2 * idx + 1]));
-            const float2 a0 = make_float2(float(A0[2 * idx]), float(A0[2 * idx + 1]));
-            const float2 ap = make_float2(ap0.x * cf - ap0.y * sf, ap0.x * sf + ap0.y * cf);
-            const float2 am = make_float2(am0.x * cf + am0.y * sf, am0.y * cf - am0.x * sf);
-            const float2 uap = *reinterpret_cast<const float2*>(d.fUAp + 2 * idx);
-            const float2 vap = *reinterpret_cast<const float2*>(d.fVAp + 2 * idx);
-            const float2 wap = *reinterpret_cast<const float2*>(d.fWAp + 2 * idx);
-            const float2 ua0 = *reinterpret_cast<const float2*>(d.fUA0 + 2 * idx);
-            const float2 va0 = *reinterpret_cast<const float2*>(d.fVA0 + 2 * idx);
-            const float nap = d.fNAp[idx], na0 = d.fNA0[idx];
-            auto cm2 = [](float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
-            auto cj = [](float2 a) { return make_float2(a.x, -a.y); };
-            auto ca = [](float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); };
-            float2 u = ca(ca(cm2(uap, ap), cm2(cj(uap), am)), cm2(ua0, a0));
-            float2 v = ca(ca(cm2(vap, ap), cm2(cj(vap), am)), cm2(va0, a0));
-            float2 ww = ca(cm2(wap, ap), cm2(wap, am));
-            float2 n = make_float2(ap.x * nap - am.x * nap + a0.x * na0, ap.y * nap - am.y * nap + a0.y * na0);
-            if (flags & 1) { u = cj(u); v = cj(v); ww = cj(ww); n = cj(n); }
-            if (flags & 2) { u.y = 0.f; v.y = 0.f; ww.y = 0.f; n.y = 0.f; }
-            fld[(0 * Nj + j) * kVinvModes + mi] = mk<T>(u.x, u.y);
-            fld[(1 * Nj + j) * kVinvModes + mi] = mk<T>(v.x, v.y);
-            fld[(2 * Nj + j) * kVinvModes + mi] = mk<T>(ww.x, ww.y);
-            fld[(3 * Nj + j) * kVinvModes + mi] = mk<T>(n.x, n.y);
-            continue;
-        }
-        if constexpr (std::is_same<T, ff>::value) {
-            // FP32X2: FP64 angle, paired-FP32 phase (ff_sincos), then paired-FP32
-            // evolution and field spectra with the coefficient arrays stored as
-            // pairs (d.fUAp ... hold ff values)
-            T sf, cf;
-            ff_sincos(d.omega[idx] * elapsed, sf, cf);
-            const cx<T> p = mk<T>(cf, sf);
-            auto ld = [](const double* q) { return mk<T>(ff_from_double(q[0]), ff_from_double(q[1])); };
-            const cx<T> ap = cmul<T>(ld(Ap + 2 * idx), p);
-            const cx<T> am = cmul<T>(ld(Am + 2 * idx), cconj<T>(p));
-            const cx<T> a0 = ld(A0 + 2 * idx);
-            const cx<T> uap = reinterpret_cast<const cx<T>*>(d.fUAp)[idx];
-            const cx<T> vap = reinterpret_cast<const cx<T>*>(d.fVAp)[idx];
-            const cx<T> wap = reinterpret_cast<const cx<T>*>(d.fWAp)[idx];
-            const cx<T> ua0 = reinterpret_cast<const cx<T>*>(d.fUA0)[idx];
-            const cx<T> va0 = reinterpret_cast<const cx<T>*>(d.fVA0)[idx];
-            const T nap = reinterpret_cast<const T*>(d.fNAp)[idx], na0 = reinterpret_cast<const T*>(d.fNA0)[idx];
-            cx<T> u = cadd<T>(cadd<T>(cmul<T>(uap, ap), cmul<T>(cconj<T>(uap), am)), cmul<T>(ua0, a0));
-            cx<T> v = cadd<T>(cadd<T>(cmul<T>(vap, ap), cmul<T>(cconj<T>(vap), am)), cmul<T>(va0, a0));
-            cx<T> ww = cadd<T>(cmul<T>(wap, ap), cmul<T>(wap, am));
-            cx<T> n = mk<T>(ap.x * nap - am.x * nap + a0.x * na0, ap.y * nap - am.y * nap + a0.y * na0);
-            if (flags & 1) { u = cconj<T>(u); v = cconj<T>(v); ww = cconj<T>(ww); n = cconj<T>(n); }
-            if (flags & 2) { u.y = T(0); v.y = T(0); ww.y = T(0); n.y = T(0); }
-            fld[(0 * Nj + j) * kVinvModes + mi] = u;
-            fld[(1 * Nj + j) * kVinvModes + mi] = v;
-            fld[(2 * Nj + j) * kVinvModes + mi] = ww;
-            fld[(3 * Nj + j) * kVinvModes + mi] = n;
-            continue;
-        }
-        double s, c;
-        sincos(d.omega[idx] * elapsed, &s, &c);
-        const zd p{c, s};
-        // evolveWaveVortexCoefficients + coefficientValueForField<0..3> (WVCoefficientFormulas.hpp:23-33)
-        const zd ap = zmul(zload(Ap + 2 * idx), p);
-        const zd am = zmul(zload(Am + 2 * idx), zconj(p));
-        const zd a0 = zload(A0 + 2 * idx);
-        const zd uap = zload(d.UAp + 2 * idx), vap = zload(d.VAp + 2 * idx), wap = zload(d.WAp + 2 * idx);
-        const zd ua0 = zload(d.UA0 + 2 * idx), va0 = zload(d.VA0 + 2 * idx);
-        const double nap = d.NAp[idx], na0 = d.NA0[idx];
-        zd u = zadd(zadd(zmul(uap, ap), zmul(zconj(uap), am)), zmul(ua0, a0));
-        zd v = zadd(zadd(zmul(vap, ap), zmul(zconj(vap), am)), zmul(va0, a0));
-        zd ww = zadd(zmul(wap, ap), zmul(wap, am));
-        zd n = zadd(zadd(zscale(ap, nap), zscale(am, -nap)), zscale(a0, na0));
-        if (flags & 1) { u = zconj(u); v = zconj(v); ww = zconj(ww); n = zconj(n); }
-        if (flags & 2) { u.im = 0.0; v.im = 0.0; ww.im = 0.0; n.im = 0.0; }
-        fld[(0 * Nj + j) * kVinvModes + mi] = mk<T>(T(u.re), T(u.im));
-        fld[(1 * Nj + j) * kVinvModes + mi] = mk<T>(T(v.re), T(v.im));
-        fld[(2 * Nj + j) * kVinvModes + mi] = mk<T>(T(ww.re), T(ww.im));
-        fld[(3 * Nj + j) * kVinvModes + mi] = mk<T>(T(n.re), T(n.im));
+        cx<T> f[4];
+        vinv_field_spectra<T>(d, Ap, Am, A0, elapsed, m0 + mi, j, f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) fld[(q * Nj + j) * kVinvModes + mi] = f[q];
     }
     __syncthreads();
     const int Zh = d.zHalf, Nz = d.Nz, P = d.positions;
@@ -945,6 +962,162 @@ __device__ __forceinline__ void mixed_project_store(const DescDev& d, int idx, i
 template <typename T>
 struct cx2t { cx<T> p, q; };
 
+// Projection of one (mode, j) of the forward transform: vr / vi hold the
+// transformed channels (canonical frame).  FLUX: the flux of every target with
+// the phase rotation and optional adaptive damping (projectFluxTargetMode,
+// kernel.cpp:396-431); !FLUX: the forward transform (projectNonhydrostaticMode
+// / projectHydrostaticMode, kernel.cpp:299-370).  Pointers are the member's.
+template <typename T, bool FLUX>
+__device__ __forceinline__ void vfwd_project(const DescDev& d, int w, int j, const T (&vr)[4], const T (&vi)[4], int nch,
+                                             double elapsed, double maxSpeed, int applyDamping,
+                                             const double* __restrict__ Ap, const double* __restrict__ Am,
+                                             const double* __restrict__ A0, double* __restrict__ Fp,
+                                             double* __restrict__ Fm, double* __restrict__ F0) {
+    const int Nj = d.Nj;
+    const int idx = j + Nj * w;
+    if constexpr (FLUX && std::is_same<T, ff>::value) {
+        // FP32X2 flux: the folded projection of the mixed form with paired-FP32
+        // coefficients (d.fProj holds 12 ff per (mode, j)) and an FP64 phase.
+        cx<T> ch[4] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c >= nch) break;
+            ch[d.tq[c]] = mk<T>(vr[c], vi[c]);
+        }
+        const cx<T> U = ch[0], V = ch[1], Wc = ch[2], N = ch[3];
+        const T* pj = reinterpret_cast<const T*>(d.fProj) + 12 * (size_t)idx;
+        const T f0r = -pj[6] * U.y - pj[7] * V.y + pj[8] * N.x;
+        const T f0i = pj[6] * U.x + pj[7] * V.x + pj[8] * N.y;
+        T cpr, cpi, cmr, cmi;
+        if (w == 0) {
+            const T sc = T(d.inertialScale[j]);
+            cpr = sc * (U.x + V.y);
+            cpi = sc * (U.y - V.x);
+            cmr = cpr;
+            cmi = -cpi;
+        } else {
+            const T wr = pj[0] * U.x - pj[1] * U.y + pj[2] * V.x - pj[3] * V.y + pj[4] * Wc.x - pj[5] * Wc.y;
+            const T wi = pj[0] * U.y + pj[1] * U.x + pj[2] * V.y + pj[3] * V.x + pj[4] * Wc.y + pj[5] * Wc.x;
+            const T br = pj[9] * N.x - pj[10] * f0r, bi = pj[9] * N.y - pj[10] * f0i;
+            cpr = wr + br; cpi = wi + bi; cmr = wr - br; cmi = wi - bi;
+        }
+        T sn, cs;
+        ff_sincos(d.omega[idx] * elapsed, sn, cs);
+        zd fp{double(cpr * cs + cpi * sn), double(cpi * cs - cpr * sn)};   // (cp) * conj(p)
+        zd fm{double(cmr * cs - cmi * sn), double(cmr * sn + cmi * cs)};   // (cm) * p
+        zd f0{double(f0r), double(f0i)};
+        if (applyDamping) {
+            const double sdmp = __dmul_rn(maxSpeed, d.damping[idx]);
+            fp = zadd(fp, zscale(zload(Ap + 2 * idx), sdmp));
+            fm = zadd(fm, zscale(zload(Am + 2 * idx), sdmp));
+            f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sdmp));
+        }
+        zstore(Fp + 2 * idx, fp);
+        zstore(Fm + 2 * idx, fm);
+        zstore(F0 + 2 * idx, f0);
+    } else if constexpr (FLUX && sizeof(T) == 4) {
+        // MIXED flux: projection with the folded FP32 coefficients
+        float2 ch[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c >= nch) break;
+            ch[d.tq[c]] = make_float2(float(vr[c]), float(vi[c]));
+        }
+        mixed_project_store(d, idx, w, j, ch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
+    } else {
+    zd val[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) val[c] = zd{double(vr[c]), double(vi[c])};
+const double k = d.k[w], l = d.l[w];
+    double s, cph;
+    sincos(d.omega[idx] * elapsed, &s, &cph);
+    const zd p{cph, s};
+    if (FLUX) {
+        // Contributions of every target are summed first and rotated to the
+        // reference time once: sum_q c_q conj(p) = (sum_q c_q) conj(p).
+        // Per-target formulas of projectFluxTargetMode (kernel.cpp:396-431);
+        // contraction into FMA is allowed here.
+        const double vort = d.A0FromVorticity[idx], buoyF = d.A0FromBuoyancy[idx];
+        const double na0 = d.NA0[idx], apmn = d.ApmN[idx];
+        double cpr = 0.0, cpi = 0.0, cmr = 0.0, cmi = 0.0, f0r = 0.0, f0i = 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c >= nch) break;
+            const int q = d.tq[c];
+            const zd v = val[c];
+            double ar = 0.0, ai = 0.0;  // A0 contribution
+            if (q == 0) { ar = (v.im * l) * vort; ai = (-v.re * l) * vort; }
+            if (q == 1) { ar = (-v.im * k) * vort; ai = (v.re * k) * vort; }
+            if (q == 3) { ar = v.re * buoyF; ai = v.im * buoyF; }
+            double br = -ar * na0, bi = -ai * na0;  // buoyancy value
+            if (q == 3) { br += v.re; bi += v.im; }
+            br *= apmn; bi *= apmn;
+            double wr = 0.0, wi = 0.0;  // wave contribution
+            if (d.hydrostatic) {
+                const zd apmd = zload(d.ApmD + 2 * idx);
+                double xr = 0.0, xi = 0.0;  // value * i*(k or l)
+                if (q == 0) { xr = -v.im * k; xi = v.re * k; }
+                if (q == 1) { xr = -v.im * l; xi = v.re * l; }
+                wr = xr * apmd.re - xi * apmd.im;
+                wi = xr * apmd.im + xi * apmd.re;
+            } else {
+                if (q == 0) { const double sc = d.cosAlpha[w] * d.ApmDScaled[idx]; wr = v.re * sc; wi = v.im * sc; }
+                if (q == 1) { const double sc = d.sinAlpha[w] * d.ApmDScaled[idx]; wr = v.re * sc; wi = v.im * sc; }
+                if (q == 2) { const double sc = (d.Kh[w] / 2.0) * d.apmWPrefactor[j]; wr = -v.im * sc; wi = v.re * sc; }
+            }
+            double pr = wr + br, pi = wi + bi, mr = wr - br, mi = wi - bi;
+            if (w == 0) {
+                const double sc = d.inertialScale[j];
+                pr = 0.0; pi = 0.0;
+                if (q == 0) { pr = v.re * sc; pi = v.im * sc; }
+                if (q == 1) { pr = v.im * sc; pi = -v.re * sc; }
+                mr = pr; mi = -pi;
+            }
+            cpr += pr; cpi += pi; cmr += mr; cmi += mi; f0r += ar; f0i += ai;
+        }
+        zd fp{cpr * p.re + cpi * p.im, cpi * p.re - cpr * p.im};   // (cp) * conj(p)
+        zd fm{cmr * p.re - cmi * p.im, cmr * p.im + cmi * p.re};   // (cm) * p
+        zd f0{f0r, f0i};
+        if (applyDamping) {
+            const double sd = __dmul_rn(maxSpeed, d.damping[idx]);
+            fp = zadd(fp, zscale(zload(Ap + 2 * idx), sd));
+            fm = zadd(fm, zscale(zload(Am + 2 * idx), sd));
+            f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sd));
+        }
+        zstore(Fp + 2 * idx, fp);
+        zstore(Fm + 2 * idx, fm);
+        zstore(F0 + 2 * idx, f0);
+    } else {
+        const zd U = val[0], V = val[1];
+        const zd W = d.hydrostatic ? zd{0.0, 0.0} : val[2];
+        const zd N = d.hydrostatic ? val[2] : val[3];
+        const zd vort = zsub(zmul(V, zd{0.0, k}), zmul(U, zd{0.0, l}));
+        const zd a0 = zadd(zscale(vort, d.A0FromVorticity[idx]), zscale(N, d.A0FromBuoyancy[idx]));
+        zd cp, cm;
+        if (w == 0) {
+            cp = zscale(zsub(U, zmul(V, zd{0.0, 1.0})), d.inertialScale[j]);
+            cm = zconj(cp);
+        } else {
+            const zd buoy = zscale(zsub(N, zscale(a0, d.NA0[idx])), d.ApmN[idx]);
+            zd wave;
+            if (d.hydrostatic) {
+                const zd div = zadd(zmul(U, zd{0.0, k}), zmul(V, zd{0.0, l}));
+                wave = zmul(zload(d.ApmD + 2 * idx), div);
+            } else {
+                const zd delta = zscale(zadd(zscale(U, d.cosAlpha[w]), zscale(V, d.sinAlpha[w])), d.ApmDScaled[idx]);
+                const zd wbar = zmul(zd{0.0, __dmul_rn(d.Kh[w] / 2.0, d.apmWPrefactor[j])}, W);
+                wave = zadd(delta, wbar);
+            }
+            cp = zadd(wave, buoy);
+            cm = zsub(wave, buoy);
+        }
+        zstore(Fp + 2 * idx, zmul(cp, zconj(p)));
+        zstore(Fm + 2 * idx, zmul(cm, p));
+        zstore(F0 + 2 * idx, a0);
+    }
+    }  // FP64 projection
+}
+
 template <typename T, bool FLUX>
 __global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, const cx<T>* __restrict__ fspec, int nch, double elapsed,
                                              const double* __restrict__ Ap, const double* __restrict__ Am,
@@ -992,7 +1165,6 @@ __global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, cons
         const int mode = m0 + mm;
         const int w = d.modeWV[mode];
         const bool conj = d.modeFlags[mode] & 1;
-        const int idx = j + Nj * w;
         const bool evenJ = (j & 1) == 0;
         const T* fc = Fc + (size_t)j * Zh;
         const T* fs = Fs + (size_t)j * Zh;
@@ -1019,147 +1191,7 @@ __global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, cons
             vr[c] = re;
             vi[c] = conj ? -im : im;
         }
-        if constexpr (FLUX && std::is_same<T, ff>::value) {
-            // FP32X2 flux: the folded projection of the mixed form with paired-FP32
-            // coefficients (d.fProj holds 12 ff per (mode, j)) and an FP64 phase.
-            cx<T> ch[4] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (c >= nch) break;
-                ch[d.tq[c]] = mk<T>(vr[c], vi[c]);
-            }
-            const cx<T> U = ch[0], V = ch[1], Wc = ch[2], N = ch[3];
-            const T* pj = reinterpret_cast<const T*>(d.fProj) + 12 * (size_t)idx;
-            const T f0r = -pj[6] * U.y - pj[7] * V.y + pj[8] * N.x;
-            const T f0i = pj[6] * U.x + pj[7] * V.x + pj[8] * N.y;
-            T cpr, cpi, cmr, cmi;
-            if (w == 0) {
-                const T sc = T(d.inertialScale[j]);
-                cpr = sc * (U.x + V.y);
-                cpi = sc * (U.y - V.x);
-                cmr = cpr;
-                cmi = -cpi;
-            } else {
-                const T wr = pj[0] * U.x - pj[1] * U.y + pj[2] * V.x - pj[3] * V.y + pj[4] * Wc.x - pj[5] * Wc.y;
-                const T wi = pj[0] * U.y + pj[1] * U.x + pj[2] * V.y + pj[3] * V.x + pj[4] * Wc.y + pj[5] * Wc.x;
-                const T br = pj[9] * N.x - pj[10] * f0r, bi = pj[9] * N.y - pj[10] * f0i;
-                cpr = wr + br; cpi = wi + bi; cmr = wr - br; cmi = wi - bi;
-            }
-            T sn, cs;
-            ff_sincos(d.omega[idx] * elapsed, sn, cs);
-            zd fp{double(cpr * cs + cpi * sn), double(cpi * cs - cpr * sn)};   // (cp) * conj(p)
-            zd fm{double(cmr * cs - cmi * sn), double(cmr * sn + cmi * cs)};   // (cm) * p
-            zd f0{double(f0r), double(f0i)};
-            if (applyDamping) {
-                const double sdmp = __dmul_rn(maxSpeed, d.damping[idx]);
-                fp = zadd(fp, zscale(zload(Ap + 2 * idx), sdmp));
-                fm = zadd(fm, zscale(zload(Am + 2 * idx), sdmp));
-                f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sdmp));
-            }
-            zstore(Fp + 2 * idx, fp);
-            zstore(Fm + 2 * idx, fm);
-            zstore(F0 + 2 * idx, f0);
-        } else if constexpr (FLUX && sizeof(T) == 4) {
-            // MIXED flux: projection with the folded FP32 coefficients
-            float2 ch[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (c >= nch) break;
-                ch[d.tq[c]] = make_float2(float(vr[c]), float(vi[c]));
-            }
-            mixed_project_store(d, idx, w, j, ch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
-        } else {
-        zd val[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) val[c] = zd{double(vr[c]), double(vi[c])};
-    const double k = d.k[w], l = d.l[w];
-        double s, cph;
-        sincos(d.omega[idx] * elapsed, &s, &cph);
-        const zd p{cph, s};
-        if (FLUX) {
-            // Contributions of every target are summed first and rotated to the
-            // reference time once: sum_q c_q conj(p) = (sum_q c_q) conj(p).
-            // Per-target formulas of projectFluxTargetMode (kernel.cpp:396-431);
-            // contraction into FMA is allowed here.
-            const double vort = d.A0FromVorticity[idx], buoyF = d.A0FromBuoyancy[idx];
-            const double na0 = d.NA0[idx], apmn = d.ApmN[idx];
-            double cpr = 0.0, cpi = 0.0, cmr = 0.0, cmi = 0.0, f0r = 0.0, f0i = 0.0;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (c >= nch) break;
-                const int q = d.tq[c];
-                const zd v = val[c];
-                double ar = 0.0, ai = 0.0;  // A0 contribution
-                if (q == 0) { ar = (v.im * l) * vort; ai = (-v.re * l) * vort; }
-                if (q == 1) { ar = (-v.im * k) * vort; ai = (v.re * k) * vort; }
-                if (q == 3) { ar = v.re * buoyF; ai = v.im * buoyF; }
-                double br = -ar * na0, bi = -ai * na0;  // buoyancy value
-                if (q == 3) { br += v.re; bi += v.im; }
-                br *= apmn; bi *= apmn;
-                double wr = 0.0, wi = 0.0;  // wave contribution
-                if (d.hydrostatic) {
-                    const zd apmd = zload(d.ApmD + 2 * idx);
-                    double xr = 0.0, xi = 0.0;  // value * i*(k or l)
-                    if (q == 0) { xr = -v.im * k; xi = v.re * k; }
-                    if (q == 1) { xr = -v.im * l; xi = v.re * l; }
-                    wr = xr * apmd.re - xi * apmd.im;
-                    wi = xr * apmd.im + xi * apmd.re;
-                } else {
-                    if (q == 0) { const double sc = d.cosAlpha[w] * d.ApmDScaled[idx]; wr = v.re * sc; wi = v.im * sc; }
-                    if (q == 1) { const double sc = d.sinAlpha[w] * d.ApmDScaled[idx]; wr = v.re * sc; wi = v.im * sc; }
-                    if (q == 2) { const double sc = (d.Kh[w] / 2.0) * d.apmWPrefactor[j]; wr = -v.im * sc; wi = v.re * sc; }
-                }
-                double pr = wr + br, pi = wi + bi, mr = wr - br, mi = wi - bi;
-                if (w == 0) {
-                    const double sc = d.inertialScale[j];
-                    pr = 0.0; pi = 0.0;
-                    if (q == 0) { pr = v.re * sc; pi = v.im * sc; }
-                    if (q == 1) { pr = v.im * sc; pi = -v.re * sc; }
-                    mr = pr; mi = -pi;
-                }
-                cpr += pr; cpi += pi; cmr += mr; cmi += mi; f0r += ar; f0i += ai;
-            }
-            zd fp{cpr * p.re + cpi * p.im, cpi * p.re - cpr * p.im};   // (cp) * conj(p)
-            zd fm{cmr * p.re - cmi * p.im, cmr * p.im + cmi * p.re};   // (cm) * p
-            zd f0{f0r, f0i};
-            if (applyDamping) {
-                const double sd = __dmul_rn(maxSpeed, d.damping[idx]);
-                fp = zadd(fp, zscale(zload(Ap + 2 * idx), sd));
-                fm = zadd(fm, zscale(zload(Am + 2 * idx), sd));
-                f0 = zadd(f0, zscale(zload(A0 + 2 * idx), sd));
-            }
-            zstore(Fp + 2 * idx, fp);
-            zstore(Fm + 2 * idx, fm);
-            zstore(F0 + 2 * idx, f0);
-        } else {
-            const zd U = val[0], V = val[1];
-            const zd W = d.hydrostatic ? zd{0.0, 0.0} : val[2];
-            const zd N = d.hydrostatic ? val[2] : val[3];
-            const zd vort = zsub(zmul(V, zd{0.0, k}), zmul(U, zd{0.0, l}));
-            const zd a0 = zadd(zscale(vort, d.A0FromVorticity[idx]), zscale(N, d.A0FromBuoyancy[idx]));
-            zd cp, cm;
-            if (w == 0) {
-                cp = zscale(zsub(U, zmul(V, zd{0.0, 1.0})), d.inertialScale[j]);
-                cm = zconj(cp);
-            } else {
-                const zd buoy = zscale(zsub(N, zscale(a0, d.NA0[idx])), d.ApmN[idx]);
-                zd wave;
-                if (d.hydrostatic) {
-                    const zd div = zadd(zmul(U, zd{0.0, k}), zmul(V, zd{0.0, l}));
-                    wave = zmul(zload(d.ApmD + 2 * idx), div);
-                } else {
-                    const zd delta = zscale(zadd(zscale(U, d.cosAlpha[w]), zscale(V, d.sinAlpha[w])), d.ApmDScaled[idx]);
-                    const zd wbar = zmul(zd{0.0, __dmul_rn(d.Kh[w] / 2.0, d.apmWPrefactor[j])}, W);
-                    wave = zadd(delta, wbar);
-                }
-                cp = zadd(wave, buoy);
-                cm = zsub(wave, buoy);
-            }
-            zstore(Fp + 2 * idx, zmul(cp, zconj(p)));
-            zstore(Fm + 2 * idx, zmul(cm, p));
-            zstore(F0 + 2 * idx, a0);
-        }
-        }  // FP64 projection
+        vfwd_project<T, FLUX>(d, w, j, vr, vi, nch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
     }
 }
 

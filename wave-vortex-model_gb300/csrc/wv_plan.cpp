@@ -161,6 +161,10 @@ Status build_plan(const Descriptor& d, Plan& p) {
     p.twx = twiddles(xLen);
     p.twxN = twiddles(static_cast<int>(p.Nx));
     p.twy = twiddles(static_cast<int>(p.Ny));
+    if (p.Nz >= 3 && 2 * (p.Nz - 1) <= static_cast<size_t>(kMaxFFT)) {
+        p.fz = factor_fft(static_cast<int>(2 * (p.Nz - 1)));
+        p.twz = twiddles(static_cast<int>(2 * (p.Nz - 1)));
+    }
     return {};
 }
 

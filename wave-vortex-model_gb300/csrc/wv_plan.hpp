@@ -59,6 +59,10 @@ struct Plan {
     std::vector<double> Fcos, Fsin;
     FFTFactors fx, fy;                    // fx: x line length (Nx/2 for even Nx, else Nx)
     std::vector<double> twx, twxN, twy;   // interleaved exp(-2 pi i k / N) for the x line, Nx, Ny
+    // Vertical transforms as FFTs of the even / odd extension over z: length
+    // 2 (Nz - 1) (0 when Nz < 3) and its twiddles.
+    FFTFactors fz;
+    std::vector<double> twz;
     // FFT variant per axis: the shared-memory Stockham kernels instead of the
     // register-resident warp FFTs where both exist (set by the ensemble autotuner).
     bool stockhamY = false, stockhamX = false;

@@ -1,0 +1,243 @@
+// Vertical transforms as FFTs of the even / odd extension over z (FP64 and
+// FP32X2 handles), the way the reference computes them (FFTW REDFT00 /
+// RODFT00, WVNativeFFTWEngine.cpp:154; exact definitions
+// WVReferenceFFTEngine.cpp:88-107), instead of the dense folded contraction.
+//
+// With L = Nz - 1 and a line y[0 .. 2L-1] holding a cosine-family channel C_j
+// and a sine-family channel D_j of the same retained column,
+//   y[0] = C_0 / 2,  y[L] = C_L (when j = L is kept),
+//   y[j] = (C_j + i D_j) / 2,  y[2L-j] = (C_j - i D_j) / 2   (1 <= j < L),
+// the forward FFT F[n] = sum_k y[k] exp(-i pi k n / L) splits into a part even
+// in n and a part odd in n:
+//   (F[n] + F[2L-n]) / 2 = C_0 / 2 + sum_{j>=1} C_j cos(pi j n / L)   (Ccos)
+//   (F[n] - F[2L-n]) / 2 = sum_{j>=1} D_j sin(pi j n / L)             (Csin)
+// for n = 0 .. L (the odd part is zero at n = 0 and n = L).  One complex FFT
+// of length 2L per pair of channels: per retained column the values pair
+// (u, w) and (v, eta), the z-derivatives (m_j w, -m_j u) and (m_j eta, -m_j v)
+// (kernel.cpp:246-267; CcosM = m Ccos, CsinM = -m Csin).  At 256x256x129 that
+// is 4 FFTs of 256 points per column (~41 kflop) against ~177 kflop for the
+// dense folded contraction.
+//
+// The forward transform (normalizeForwardDCT / DST, kernel.cpp:176-193) pairs
+// a cosine-family z-grid channel c_z with a sine-family one s_z the same way:
+// y[0] = c_0, y[L] = c_L, y[z] = c_z + s_z, y[2L-z] = c_z - s_z, and
+//   X_cos[j] = (F[j] + F[2L-j]) / 2 / (L Nx Ny)   (halved at j = L)
+//   X_sin[j] = i (F[j] - F[2L-j]) / 2 / (L Nx Ny)
+// (Fcos, Fsin with their endpoint weights and the horizontal scale), then the
+// projection of k_vfwd (vfwd_project) per (mode, j).
+#pragma once
+
+#include "wv_kernels.cuh"
+
+namespace wvgpu {
+namespace dev {
+
+constexpr int kVzLines = 4;  // FFT lines per CTA (256 threads: one radix-4 butterfly each at 2L = 256)
+
+template <bool FLUX>
+struct VzShape {
+    static constexpr int lines = FLUX ? 4 : 2;       // lines per retained column
+    static constexpr int modes = kVzLines / lines;   // retained columns per CTA
+};
+
+// Shared memory of k_vinv_fft: field spectra [4][Nj][modes], two line buffers
+// [kVzLines][2L] and the twiddles [2L].
+template <typename T>
+inline size_t smem_vinv_fft(int Nj, int N2, int modes) {
+    return (static_cast<size_t>(4) * Nj * modes + 2 * static_cast<size_t>(kVzLines) * N2 + N2) * sizeof(cx<T>);
+}
+
+template <typename T, bool FLUX>
+__global__ void __launch_bounds__(256) k_vinv_fft(DescDev d, const double* __restrict__ Ap, const double* __restrict__ Am,
+                                                 const double* __restrict__ A0, double elapsed, cx<T>* __restrict__ zspec,
+                                                 unsigned long long* __restrict__ maxSpeedBits) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kLines = VzShape<FLUX>::lines, kModes = VzShape<FLUX>::modes;
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, L = Nz - 1, N2 = d.fz.N;
+    cx<T>* fld = reinterpret_cast<cx<T>*>(smem_raw);   // [4][Nj][kModes]
+    cx<T>* bufA = fld + 4 * Nj * kModes;               // [kVzLines][N2]
+    cx<T>* bufB = bufA + kVzLines * N2;
+    cx<T>* tw = bufB + kVzLines * N2;                  // [N2]
+    const int m0 = blockIdx.x * kModes;
+    const int nm = min(kModes, d.Nkl - m0);
+    const int member = blockIdx.y;
+    if (member > 0) {
+        const long long o = member * d.memberStride;
+        Ap += o; Am += o; A0 += o;
+        zspec += (size_t)member * Nz * P;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && maxSpeedBits) maxSpeedBits[member] = 0ull;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    for (int i = threadIdx.x; i < kVzLines * N2; i += blockDim.x) bufA[i] = mk<T>(T(0), T(0));
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it / Nj, j = it - mi * Nj;
+        cx<T> f[4];
+        vinv_field_spectra<T>(d, Ap, Am, A0, elapsed, m0 + mi, j, f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) fld[(q * Nj + j) * kModes + mi] = f[q];
+    }
+    __syncthreads();
+    // lines: y[j] = (C_j + i D_j) / 2, y[2L-j] = (C_j - i D_j) / 2, y[0] = C_0 / 2, y[L] = C_L
+    const T* mz = reinterpret_cast<const T*>(d.tMz);
+    const T half = T(0.5f);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it / Nj, j = it - mi * Nj;
+        const cx<T> U = fld[(0 * Nj + j) * kModes + mi], V = fld[(1 * Nj + j) * kModes + mi];
+        const cx<T> W = fld[(2 * Nj + j) * kModes + mi], E = fld[(3 * Nj + j) * kModes + mi];
+        cx<T> C[kLines], D[kLines];
+        C[0] = U; D[0] = W;
+        C[1] = V; D[1] = E;
+        if constexpr (FLUX) {
+            const T m = mz[j];
+            C[2] = mk<T>(m * W.x, m * W.y); D[2] = mk<T>(-(m * U.x), -(m * U.y));
+            C[3] = mk<T>(m * E.x, m * E.y); D[3] = mk<T>(-(m * V.x), -(m * V.y));
+        }
+#pragma unroll
+        for (int l = 0; l < kLines; ++l) {
+            cx<T>* y = bufA + (mi * kLines + l) * N2;
+            if (j == 0) {
+                y[0] = mk<T>(C[l].x * half, C[l].y * half);
+            } else if (j == L) {
+                y[L] = C[l];
+            } else {
+                // (C +/- i D) / 2
+                const cx<T> c = mk<T>(C[l].x * half, C[l].y * half);
+                const cx<T> id = mk<T>(-(D[l].y * half), D[l].x * half);
+                y[j] = cadd<T>(c, id);
+                y[N2 - j] = csub<T>(c, id);
+            }
+        }
+    }
+    __syncthreads();
+    const cx<T>* F = fft_lines<T, false>(bufA, bufB, d.fz, kVzLines, N2, tw);
+    // even part -> cosine channel, odd part -> sine channel, n = 0 .. L
+    int derivChan[4] = {-1, -1, -1, -1};
+    if constexpr (FLUX)
+        for (int t = 0; t < d.nt; ++t) derivChan[d.tq[t]] = 4 + t;
+    for (int it = threadIdx.x; it < nm * kLines * (L + 1); it += blockDim.x) {
+        const int n = it % (L + 1);
+        const int rest = it / (L + 1);
+        const int l = rest % kLines, mi = rest / kLines;
+        const cx<T>* row = F + (mi * kLines + l) * N2;
+        const cx<T> a = row[n];
+        cx<T> ev = a, od = mk<T>(T(0), T(0));
+        if (n != 0 && n != L) {
+            const cx<T> b = row[N2 - n];
+            ev = mk<T>((a.x + b.x) * half, (a.y + b.y) * half);
+            od = mk<T>((a.x - b.x) * half, (a.y - b.y) * half);
+        }
+        int chC, chS;  // channels of the cosine and sine parts
+        if (l == 0) { chC = 0; chS = 2; }
+        else if (l == 1) { chC = 1; chS = 3; }
+        else if (l == 2) { chC = derivChan[2]; chS = derivChan[0]; }
+        else { chC = derivChan[3]; chS = derivChan[1]; }
+        const int mode = m0 + mi;
+        const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
+        if (chC >= 0) {
+            cx<T>* base = zspec + (size_t)chC * d.zTotal * P + (size_t)n * P;
+            base[pos] = ev;
+            if (cpos >= 0) base[cpos] = cconj<T>(ev);
+        }
+        if (chS >= 0) {
+            cx<T>* base = zspec + (size_t)chS * d.zTotal * P + (size_t)n * P;
+            base[pos] = od;
+            if (cpos >= 0) base[cpos] = cconj<T>(od);
+        }
+    }
+}
+
+// Shared memory of k_vfwd_fft: two line buffers [kVzLines][2L] and the twiddles [2L].
+template <typename T>
+inline size_t smem_vfwd_fft(int N2) {
+    return (2 * static_cast<size_t>(kVzLines) * N2 + N2) * sizeof(cx<T>);
+}
+
+constexpr int kVfModes = kVzLines / 2;  // retained columns per CTA: lines (u | w) and (v | eta) each
+
+template <typename T, bool FLUX>
+__global__ void __launch_bounds__(256) k_vfwd_fft(DescDev d, const cx<T>* __restrict__ fspec, int nch, double elapsed,
+                                                 const double* __restrict__ Ap, const double* __restrict__ Am,
+                                                 const double* __restrict__ A0, const unsigned long long* __restrict__ maxSpeedBits,
+                                                 int applyDamping, double* __restrict__ Fp, double* __restrict__ Fm,
+                                                 double* __restrict__ F0) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, L = Nz - 1, N2 = d.fz.N;
+    cx<T>* bufA = reinterpret_cast<cx<T>*>(smem_raw);  // [kVzLines][N2]
+    cx<T>* bufB = bufA + kVzLines * N2;
+    cx<T>* tw = bufB + kVzLines * N2;                 // [N2]
+    const int m0 = blockIdx.x * kVfModes;
+    const int nm = min(kVfModes, d.Nkl - m0);
+    const int member = blockIdx.y;
+    if (member > 0) {
+        const long long o = member * d.memberStride;
+        if (Ap) { Ap += o; Am += o; A0 += o; }
+        Fp += o; Fm += o; F0 += o;
+        fspec += (size_t)member * Nz * P;
+        if (maxSpeedBits) maxSpeedBits += member;
+    }
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    for (int i = threadIdx.x; i < kVzLines * N2; i += blockDim.x) bufA[i] = mk<T>(T(0), T(0));
+    // channel holding each field slot q (0 u, 1 v: cosine family; 2 w, 3 eta: sine family)
+    int chanOfQ[4] = {-1, -1, -1, -1};
+    for (int c = 0; c < nch; ++c) chanOfQ[FLUX ? d.tq[c] : ((d.hydrostatic && c == 2) ? 3 : c)] = c;
+    __syncthreads();
+    for (int it = threadIdx.x; it < nm * 2 * (L + 1); it += blockDim.x) {
+        const int z = it % (L + 1);
+        const int rest = it / (L + 1);
+        const int l = rest & 1, mi = rest >> 1;
+        const int pos = d.modePos[m0 + mi];
+        const int cc = l == 0 ? chanOfQ[0] : chanOfQ[1], cs = l == 0 ? chanOfQ[2] : chanOfQ[3];
+        const cx<T> cv = cc >= 0 ? fspec[(size_t)cc * d.zTotal * P + (size_t)z * P + pos] : mk<T>(T(0), T(0));
+        cx<T>* y = bufA + (mi * 2 + l) * N2;
+        if (z == 0 || z == L) {
+            y[z] = cv;
+        } else {
+            const cx<T> sv = cs >= 0 ? fspec[(size_t)cs * d.zTotal * P + (size_t)z * P + pos] : mk<T>(T(0), T(0));
+            y[z] = cadd<T>(cv, sv);
+            y[N2 - z] = csub<T>(cv, sv);
+        }
+    }
+    __syncthreads();
+    const cx<T>* F = fft_lines<T, false>(bufA, bufB, d.fz, kVzLines, N2, tw);
+    double maxSpeed = 0.0;
+    if (FLUX && applyDamping) maxSpeed = __longlong_as_double((long long)*maxSpeedBits);
+    const T sc = T(1.0 / (static_cast<double>(L) * static_cast<double>(d.Nx) * static_cast<double>(d.Ny)));
+    const T half = T(0.5f);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it % nm, j = it / nm;
+        const int mode = m0 + mi;
+        const int w = d.modeWV[mode];
+        const bool conj = d.modeFlags[mode] & 1;
+        // transformed slots (canonical frame): 0 u, 1 v (cosine), 2 w, 3 eta (sine)
+        cx<T> X[4];
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            const cx<T>* row = F + (mi * 2 + l) * N2;
+            const cx<T> a = row[j];
+            cx<T> ev = a, od = mk<T>(T(0), T(0));
+            if (j != 0 && j != L) {
+                const cx<T> b = row[N2 - j];
+                ev = mk<T>((a.x + b.x) * half, (a.y + b.y) * half);
+                od = mk<T>((a.x - b.x) * half, (a.y - b.y) * half);
+            }
+            const T scC = j == L ? sc * half : sc;
+            X[l] = mk<T>(ev.x * scC, ev.y * scC);
+            X[2 + l] = mk<T>(-(od.y * sc), od.x * sc);  // i * odd part
+        }
+        T vr[4] = {T(0), T(0), T(0), T(0)}, vi[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c >= nch) break;
+            const int q = FLUX ? d.tq[c] : ((d.hydrostatic && c == 2) ? 3 : c);
+            const cx<T> v = q == 0 ? X[0] : q == 1 ? X[1] : q == 2 ? X[2] : X[3];
+            vr[c] = v.x;
+            vi[c] = conj ? -v.y : v.y;
+        }
+        vfwd_project<T, FLUX>(d, w, j, vr, vi, nch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
+    }
+}
+
+}  // namespace dev
+}  // namespace wvgpu

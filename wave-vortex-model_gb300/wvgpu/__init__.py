@@ -178,6 +178,7 @@ def load_library():
     lib.wv_set_forcing.argtypes = [P, ctypes.c_uint32]
     lib.wv_set_stage_instrumentation.argtypes = [P, ctypes.c_int]
     lib.wv_set_vertical_kernel.argtypes = [P, ctypes.c_int]
+    lib.wv_get_vertical_kernel.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     lib.wv_get_device_status.argtypes = [P, ctypes.POINTER(ctypes.c_uint)]
     lib.wv_get_stage_times.argtypes = [P, ctypes.POINTER(_StageTimes)]
     for name in ("wv_nonlinear_flux", "wv_evaluate_rhs"):
@@ -261,7 +262,7 @@ def exported_symbols():
     """Names of the C entry points this binding expects (declared in include/wvgpu.h)."""
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times",
-            "wv_set_vertical_kernel", "wv_get_device_status", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
+            "wv_set_vertical_kernel", "wv_get_vertical_kernel", "wv_get_device_status", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
             "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc", "wv_flux_vjp_device",
             "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device",
@@ -645,9 +646,16 @@ class WVTransformConstantStratificationKernel:
         return tuple(out)
 
     def set_vertical_kernel(self, kind):
-        """'cuda' (CUDA-core contractions) or 'tensor' (tcgen05 GEMMs: split-BF16 for both vertical
-        transforms on mixed handles, exact digit slices for the vertical inverse on FP32X2 handles)."""
-        self._check(self._lib.wv_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1}[kind]))
+        """'cuda' (CUDA-core dense contractions), 'tensor' (tcgen05 GEMMs: split-BF16 for both vertical
+        transforms on mixed handles, exact digit slices for the vertical inverse on FP32X2 handles) or
+        'fft' (FFTs of the even / odd extension over z; FP64 and FP32X2 handles, their default)."""
+        self._check(self._lib.wv_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1, "fft": 2}[kind]))
+
+    def vertical_kernel(self):
+        """The vertical-transform kernel the flux runs: 'cuda', 'tensor' or 'fft'."""
+        v = ctypes.c_int(0)
+        self._check(self._lib.wv_get_vertical_kernel(self._h, ctypes.byref(v)))
+        return {0: "cuda", 1: "tensor", 2: "fft"}[v.value]
 
     def device_status(self):
         """Device status word (bit 0: a bounded in-kernel wait ran out)."""
@@ -727,13 +735,13 @@ class WVEnsemble:
                         "tensor_vertical_available": bool(t.tensor_vertical_available),
                         "y": "stockham" if t.stockham_y or not t.warp_y_available else "warp",
                         "x": "stockham" if t.stockham_x or not t.warp_x_available else "warp",
-                        "vertical": "tensor" if t.vertical == 1 else "cuda",
+                        "vertical": {0: "cuda", 1: "tensor", 2: "fft"}[t.vertical],
                         "candidate_ms": list(t.candidate_ms)[:max(0, min(8, t.candidates))], "flux_ms": t.flux_ms})
         return out
 
     def set_vertical_kernel(self, kind):
-        """'cuda' or 'tensor' for every group (overrides the autotuner's choice)."""
-        self._check(self._lib.wv_ensemble_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1}[kind]))
+        """'cuda', 'tensor' or 'fft' for every group (overrides the autotuner's choice)."""
+        self._check(self._lib.wv_ensemble_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1, "fft": 2}[kind]))
 
     def metrics(self):
         m = _EnsembleMetrics()
