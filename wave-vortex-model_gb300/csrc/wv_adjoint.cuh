@@ -21,6 +21,97 @@ namespace wvgpu {
 namespace dev {
 
 // ---------------------------------------------------------------------------
+// Cotangents of the transformed target channels (canonical frame, index t of
+// the targets) of one (mode, j): the projection and phase of k_vfwd transposed.
+template <typename T>
+__device__ __forceinline__ void vfwd_adj_values(const DescDev& d, const double* __restrict__ Fpb,
+                                                const double* __restrict__ Fmb, const double* __restrict__ F0b,
+                                                double elapsed, int w, int j, cx<T> (&vt)[4]) {
+    const int Nj = d.Nj, nt = d.nt;
+    const int idx = j + Nj * w;
+    if constexpr (sizeof(T) == 4) {
+        // MIXED: transpose of the folded FP32 projection of k_vfwd, FP32 phase
+        // after FP64 angle reduction
+        const double ang = d.omega[idx] * elapsed;
+        const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+        float sn, cs;
+        sincosf(float(red), &sn, &cs);
+        const float2 fpb = make_float2(float(Fpb[2 * idx]), float(Fpb[2 * idx + 1]));
+        const float2 fmb = make_float2(float(Fmb[2 * idx]), float(Fmb[2 * idx + 1]));
+        const float2 a0b = make_float2(float(F0b[2 * idx]), float(F0b[2 * idx + 1]));
+        const float2 cpb = make_float2(fpb.x * cs - fpb.y * sn, fpb.x * sn + fpb.y * cs);  // Fp_bar * p
+        const float2 cmb = make_float2(fmb.x * cs + fmb.y * sn, fmb.y * cs - fmb.x * sn);  // Fm_bar * conj(p)
+        float2 ch[4];
+        if (w == 0) {
+            const float sc = float(d.inertialScale[j]);
+            const float2 tot = make_float2(cpb.x + cmb.x, cpb.y - cmb.y);  // cp_bar + conj(cm_bar)
+            ch[0] = make_float2(sc * tot.x, sc * tot.y);
+            ch[1] = make_float2(-sc * tot.y, sc * tot.x);
+            ch[2] = make_float2(0.f, 0.f);
+            const float dn = d.fProj[12 * (size_t)idx + 8];
+            ch[3] = make_float2(dn * a0b.x, dn * a0b.y);
+        } else {
+            const float4* pj = reinterpret_cast<const float4*>(d.fProj + 12 * (size_t)idx);
+            const float4 p0 = pj[0], p1 = pj[1], p2 = pj[2];
+            const float2 wb = make_float2(cpb.x + cmb.x, cpb.y + cmb.y);
+            const float2 bb = make_float2(cpb.x - cmb.x, cpb.y - cmb.y);
+            const float2 f0b = make_float2(a0b.x - p2.z * bb.x, a0b.y - p2.z * bb.y);
+            // conj(C) * wave_bar - i D * f0_bar
+            ch[0] = make_float2(p0.x * wb.x + p0.y * wb.y + p1.z * f0b.y, p0.x * wb.y - p0.y * wb.x - p1.z * f0b.x);
+            ch[1] = make_float2(p0.z * wb.x + p0.w * wb.y + p1.w * f0b.y, p0.z * wb.y - p0.w * wb.x - p1.w * f0b.x);
+            ch[2] = make_float2(p1.x * wb.x + p1.y * wb.y, p1.x * wb.y - p1.y * wb.x);
+            ch[3] = make_float2(p2.y * bb.x + p2.x * f0b.x, p2.y * bb.y + p2.x * f0b.y);
+        }
+        for (int t = 0; t < nt; ++t) {
+            const float2 v = ch[d.tq[t]];
+            vt[t] = mk<T>(T(v.x), T(v.y));
+        }
+        return;
+    }
+    double s, c;
+    sincos(d.omega[idx] * elapsed, &s, &c);
+    const zd fpb = zload(Fpb + 2 * idx), fmb = zload(Fmb + 2 * idx), a0b = zload(F0b + 2 * idx);
+    // cp_bar = Fp_bar * p ; cm_bar = Fm_bar * conj(p)
+    const zd cpb{fpb.re * c - fpb.im * s, fpb.re * s + fpb.im * c};
+    const zd cmb{fmb.re * c + fmb.im * s, fmb.im * c - fmb.re * s};
+    const double k = d.k[w], l = d.l[w];
+    const double vort = d.A0FromVorticity[idx], buoyF = d.A0FromBuoyancy[idx], na0 = d.NA0[idx], apmn = d.ApmN[idx];
+    const zd waveb{cpb.re + cmb.re, cpb.im + cmb.im};
+    const zd buoyb{cpb.re - cmb.re, cpb.im - cmb.im};
+    const zd bvb{buoyb.re * apmn, buoyb.im * apmn};
+    const zd a0cb{a0b.re - na0 * bvb.re, a0b.im - na0 * bvb.im};
+    for (int t = 0; t < nt; ++t) {
+        const int q = d.tq[t];
+        double vr = 0.0, vi = 0.0;
+        if (w == 0) {
+            // inertial override: cp = f(value), cm = conj(cp)
+            const double sc = d.inertialScale[j];
+            const zd tot{cpb.re + cmb.re, cpb.im - cmb.im};  // cp_bar + conj(cm_bar)
+            if (q == 0) { vr = sc * tot.re; vi = sc * tot.im; }
+            if (q == 1) { vr = -sc * tot.im; vi = sc * tot.re; }  // (i sc) * tot
+            if (q == 3) { vr += buoyF * a0b.re; vi += buoyF * a0b.im; }
+        } else {
+            if (q == 3) { vr += bvb.re; vi += bvb.im; }
+            if (q == 0) { vr += -l * vort * a0cb.im; vi += l * vort * a0cb.re; }   // (i l) vort a0c_bar
+            if (q == 1) { vr += k * vort * a0cb.im; vi += -k * vort * a0cb.re; }   // (-i k) vort a0c_bar
+            if (q == 3) { vr += buoyF * a0cb.re; vi += buoyF * a0cb.im; }
+            if (d.hydrostatic) {
+                const zd apmd = zload(d.ApmD + 2 * idx);
+                // conj(i kk ApmD) * wave_bar, kk = k (u) or l (v)
+                const double kk = q == 0 ? k : (q == 1 ? l : 0.0);
+                const zd cf{-kk * apmd.im, -kk * apmd.re};  // conj(i kk apmd) = -i kk conj(apmd)
+                vr += cf.re * waveb.re - cf.im * waveb.im;
+                vi += cf.re * waveb.im + cf.im * waveb.re;
+            } else {
+                if (q == 0) { const double sc = d.cosAlpha[w] * d.ApmDScaled[idx]; vr += sc * waveb.re; vi += sc * waveb.im; }
+                if (q == 1) { const double sc = d.sinAlpha[w] * d.ApmDScaled[idx]; vr += sc * waveb.re; vi += sc * waveb.im; }
+                if (q == 2) { const double sc = (d.Kh[w] / 2.0) * d.apmWPrefactor[j]; vr += sc * waveb.im; vi += -sc * waveb.re; }
+            }
+        }
+        vt[t] = mk<T>(T(vr), T(vi));
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_vfwd_adj(DescDev d, const double* __restrict__ Fpb, const double* __restrict__ Fmb,
                                                  const double* __restrict__ F0b, double elapsed, cx<T>* __restrict__ zadj) {
@@ -31,89 +122,9 @@ __global__ void __launch_bounds__(256) k_vfwd_adj(DescDev d, const double* __res
     cx<T>* vb = reinterpret_cast<cx<T>*>(smem_raw);  // [nt][Nj][modes]
     for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
         const int mm = it % nm, j = it / nm;
-        const int w = d.modeWV[m0 + mm];
-        const int idx = j + Nj * w;
-        if constexpr (sizeof(T) == 4) {
-            // MIXED: transpose of the folded FP32 projection of k_vfwd, FP32 phase
-            // after FP64 angle reduction
-            const double ang = d.omega[idx] * elapsed;
-            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
-            float sn, cs;
-            sincosf(float(red), &sn, &cs);
-            const float2 fpb = make_float2(float(Fpb[2 * idx]), float(Fpb[2 * idx + 1]));
-            const float2 fmb = make_float2(float(Fmb[2 * idx]), float(Fmb[2 * idx + 1]));
-            const float2 a0b = make_float2(float(F0b[2 * idx]), float(F0b[2 * idx + 1]));
-            const float2 cpb = make_float2(fpb.x * cs - fpb.y * sn, fpb.x * sn + fpb.y * cs);  // Fp_bar * p
-            const float2 cmb = make_float2(fmb.x * cs + fmb.y * sn, fmb.y * cs - fmb.x * sn);  // Fm_bar * conj(p)
-            float2 ch[4];
-            if (w == 0) {
-                const float sc = float(d.inertialScale[j]);
-                const float2 tot = make_float2(cpb.x + cmb.x, cpb.y - cmb.y);  // cp_bar + conj(cm_bar)
-                ch[0] = make_float2(sc * tot.x, sc * tot.y);
-                ch[1] = make_float2(-sc * tot.y, sc * tot.x);
-                ch[2] = make_float2(0.f, 0.f);
-                const float dn = d.fProj[12 * (size_t)idx + 8];
-                ch[3] = make_float2(dn * a0b.x, dn * a0b.y);
-            } else {
-                const float4* pj = reinterpret_cast<const float4*>(d.fProj + 12 * (size_t)idx);
-                const float4 p0 = pj[0], p1 = pj[1], p2 = pj[2];
-                const float2 wb = make_float2(cpb.x + cmb.x, cpb.y + cmb.y);
-                const float2 bb = make_float2(cpb.x - cmb.x, cpb.y - cmb.y);
-                const float2 f0b = make_float2(a0b.x - p2.z * bb.x, a0b.y - p2.z * bb.y);
-                // conj(C) * wave_bar - i D * f0_bar
-                ch[0] = make_float2(p0.x * wb.x + p0.y * wb.y + p1.z * f0b.y, p0.x * wb.y - p0.y * wb.x - p1.z * f0b.x);
-                ch[1] = make_float2(p0.z * wb.x + p0.w * wb.y + p1.w * f0b.y, p0.z * wb.y - p0.w * wb.x - p1.w * f0b.x);
-                ch[2] = make_float2(p1.x * wb.x + p1.y * wb.y, p1.x * wb.y - p1.y * wb.x);
-                ch[3] = make_float2(p2.y * bb.x + p2.x * f0b.x, p2.y * bb.y + p2.x * f0b.y);
-            }
-            for (int t = 0; t < nt; ++t) {
-                const float2 v = ch[d.tq[t]];
-                vb[(t * Nj + j) * kVfwdModes + mm] = mk<T>(T(v.x), T(v.y));
-            }
-            continue;
-        }
-        double s, c;
-        sincos(d.omega[idx] * elapsed, &s, &c);
-        const zd fpb = zload(Fpb + 2 * idx), fmb = zload(Fmb + 2 * idx), a0b = zload(F0b + 2 * idx);
-        // cp_bar = Fp_bar * p ; cm_bar = Fm_bar * conj(p)
-        const zd cpb{fpb.re * c - fpb.im * s, fpb.re * s + fpb.im * c};
-        const zd cmb{fmb.re * c + fmb.im * s, fmb.im * c - fmb.re * s};
-        const double k = d.k[w], l = d.l[w];
-        const double vort = d.A0FromVorticity[idx], buoyF = d.A0FromBuoyancy[idx], na0 = d.NA0[idx], apmn = d.ApmN[idx];
-        const zd waveb{cpb.re + cmb.re, cpb.im + cmb.im};
-        const zd buoyb{cpb.re - cmb.re, cpb.im - cmb.im};
-        const zd bvb{buoyb.re * apmn, buoyb.im * apmn};
-        const zd a0cb{a0b.re - na0 * bvb.re, a0b.im - na0 * bvb.im};
-        for (int t = 0; t < nt; ++t) {
-            const int q = d.tq[t];
-            double vr = 0.0, vi = 0.0;
-            if (w == 0) {
-                // inertial override: cp = f(value), cm = conj(cp)
-                const double sc = d.inertialScale[j];
-                const zd tot{cpb.re + cmb.re, cpb.im - cmb.im};  // cp_bar + conj(cm_bar)
-                if (q == 0) { vr = sc * tot.re; vi = sc * tot.im; }
-                if (q == 1) { vr = -sc * tot.im; vi = sc * tot.re; }  // (i sc) * tot
-                if (q == 3) { vr += buoyF * a0b.re; vi += buoyF * a0b.im; }
-            } else {
-                if (q == 3) { vr += bvb.re; vi += bvb.im; }
-                if (q == 0) { vr += -l * vort * a0cb.im; vi += l * vort * a0cb.re; }   // (i l) vort a0c_bar
-                if (q == 1) { vr += k * vort * a0cb.im; vi += -k * vort * a0cb.re; }   // (-i k) vort a0c_bar
-                if (q == 3) { vr += buoyF * a0cb.re; vi += buoyF * a0cb.im; }
-                if (d.hydrostatic) {
-                    const zd apmd = zload(d.ApmD + 2 * idx);
-                    // conj(i kk ApmD) * wave_bar, kk = k (u) or l (v)
-                    const double kk = q == 0 ? k : (q == 1 ? l : 0.0);
-                    const zd cf{-kk * apmd.im, -kk * apmd.re};  // conj(i kk apmd) = -i kk conj(apmd)
-                    vr += cf.re * waveb.re - cf.im * waveb.im;
-                    vi += cf.re * waveb.im + cf.im * waveb.re;
-                } else {
-                    if (q == 0) { const double sc = d.cosAlpha[w] * d.ApmDScaled[idx]; vr += sc * waveb.re; vi += sc * waveb.im; }
-                    if (q == 1) { const double sc = d.sinAlpha[w] * d.ApmDScaled[idx]; vr += sc * waveb.re; vi += sc * waveb.im; }
-                    if (q == 2) { const double sc = (d.Kh[w] / 2.0) * d.apmWPrefactor[j]; vr += sc * waveb.im; vi += -sc * waveb.re; }
-                }
-            }
-            vb[(t * Nj + j) * kVfwdModes + mm] = mk<T>(T(vr), T(vi));
-        }
+        cx<T> vt[4];
+        vfwd_adj_values<T>(d, Fpb, Fmb, F0b, elapsed, d.modeWV[m0 + mm], j, vt);
+        for (int t = 0; t < nt; ++t) vb[(t * Nj + j) * kVfwdModes + mm] = vt[t];
     }
     __syncthreads();
     const T* Fc = reinterpret_cast<const T*>(d.FcosT);   // [Zh][Nj]
@@ -384,6 +395,57 @@ __global__ void __launch_bounds__(256) k_xr2c_adj(DescDev d, const double* __res
 // per SM, which its latency-bound gathers need.
 constexpr int kVinvAdjModes = 4;
 
+// Assembly and phase of k_vinv transposed for one (mode, j): the field
+// cotangents (ubT, vbT, wbT, nbT) -> (Ap, Am, A0) cotangents at index idx.
+template <typename T>
+__device__ __forceinline__ void vinv_adj_store(const DescDev& d, int idx, double elapsed, cx<T> ubT, cx<T> vbT, cx<T> wbT,
+                                               cx<T> nbT, double* __restrict__ Apb, double* __restrict__ Amb,
+                                               double* __restrict__ A0b) {
+    if constexpr (sizeof(T) == 4) {
+        // MIXED: assembly adjoint with the FP32 field factors, FP32 phase after
+        // FP64 angle reduction
+        const float2 uap = *reinterpret_cast<const float2*>(d.fUAp + 2 * idx);
+        const float2 vap = *reinterpret_cast<const float2*>(d.fVAp + 2 * idx);
+        const float2 wap = *reinterpret_cast<const float2*>(d.fWAp + 2 * idx);
+        const float2 ua0 = *reinterpret_cast<const float2*>(d.fUA0 + 2 * idx);
+        const float2 va0 = *reinterpret_cast<const float2*>(d.fVA0 + 2 * idx);
+        const float nap = d.fNAp[idx], na0 = d.fNA0[idx];
+        auto cm = [](float2 a, cx<T> b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+        auto cjm = [](float2 a, cx<T> b) { return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); };
+        const float2 t1 = cjm(uap, ubT), t2 = cjm(vap, vbT), t3 = cjm(wap, wbT);
+        const float2 ape = make_float2(t1.x + t2.x + t3.x + nap * nbT.x, t1.y + t2.y + t3.y + nap * nbT.y);
+        const float2 s1 = cm(uap, ubT), s2 = cm(vap, vbT);
+        const float2 ame = make_float2(s1.x + s2.x + t3.x - nap * nbT.x, s1.y + s2.y + t3.y - nap * nbT.y);
+        const float2 r1 = cjm(ua0, ubT), r2 = cjm(va0, vbT);
+        const float2 a0 = make_float2(r1.x + r2.x + na0 * nbT.x, r1.y + r2.y + na0 * nbT.y);
+        const double ang = d.omega[idx] * elapsed;
+        const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
+        float sn, cs;
+        sincosf(float(red), &sn, &cs);
+        Apb[2 * idx] = double(ape.x * cs + ape.y * sn);   // ape * conj(p)
+        Apb[2 * idx + 1] = double(ape.y * cs - ape.x * sn);
+        Amb[2 * idx] = double(ame.x * cs - ame.y * sn);   // ame * p
+        Amb[2 * idx + 1] = double(ame.x * sn + ame.y * cs);
+        A0b[2 * idx] = double(a0.x);
+        A0b[2 * idx + 1] = double(a0.y);
+        return;
+    }
+    const zd ub{double(ubT.x), double(ubT.y)}, vbv{double(vbT.x), double(vbT.y)};
+    const zd wb{double(wbT.x), double(wbT.y)}, nb{double(nbT.x), double(nbT.y)};
+    // assembly adjoint (coefficientValueForField on evolved coefficients)
+    const zd uap = zload(d.UAp + 2 * idx), vap = zload(d.VAp + 2 * idx), wap = zload(d.WAp + 2 * idx);
+    const zd ua0 = zload(d.UA0 + 2 * idx), va0 = zload(d.VA0 + 2 * idx);
+    const double nap = d.NAp[idx], na0 = d.NA0[idx];
+    const zd ape = zadd(zadd(zadd(zmul(zconj(uap), ub), zmul(zconj(vap), vbv)), zmul(zconj(wap), wb)), zscale(nb, nap));
+    const zd ame = zsub(zadd(zadd(zmul(uap, ub), zmul(vap, vbv)), zmul(zconj(wap), wb)), zscale(nb, nap));
+    const zd a0 = zadd(zadd(zmul(zconj(ua0), ub), zmul(zconj(va0), vbv)), zscale(nb, na0));
+    double s, c;
+    sincos(d.omega[idx] * elapsed, &s, &c);
+    zstore(Apb + 2 * idx, zmul(ape, zd{c, -s}));
+    zstore(Amb + 2 * idx, zmul(ame, zd{c, s}));
+    zstore(A0b + 2 * idx, a0);
+}
+
 template <typename T, bool FLUX>
 __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __restrict__ fadj, int nchIn, double elapsed,
                                                  double* __restrict__ Apb, double* __restrict__ Amb, double* __restrict__ A0b) {
@@ -455,49 +517,7 @@ __global__ void __launch_bounds__(256) k_vinv_adj(DescDev d, const cx<T>* __rest
                 if (q == 3) nbT = cadd<T>(nbT, zb);
             }
         }
-        if constexpr (sizeof(T) == 4) {
-            // MIXED: assembly adjoint with the FP32 field factors, FP32 phase after
-            // FP64 angle reduction
-            const float2 uap = *reinterpret_cast<const float2*>(d.fUAp + 2 * idx);
-            const float2 vap = *reinterpret_cast<const float2*>(d.fVAp + 2 * idx);
-            const float2 wap = *reinterpret_cast<const float2*>(d.fWAp + 2 * idx);
-            const float2 ua0 = *reinterpret_cast<const float2*>(d.fUA0 + 2 * idx);
-            const float2 va0 = *reinterpret_cast<const float2*>(d.fVA0 + 2 * idx);
-            const float nap = d.fNAp[idx], na0 = d.fNA0[idx];
-            auto cm = [](float2 a, cx<T> b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
-            auto cjm = [](float2 a, cx<T> b) { return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); };
-            const float2 t1 = cjm(uap, ubT), t2 = cjm(vap, vbT), t3 = cjm(wap, wbT);
-            const float2 ape = make_float2(t1.x + t2.x + t3.x + nap * nbT.x, t1.y + t2.y + t3.y + nap * nbT.y);
-            const float2 s1 = cm(uap, ubT), s2 = cm(vap, vbT);
-            const float2 ame = make_float2(s1.x + s2.x + t3.x - nap * nbT.x, s1.y + s2.y + t3.y - nap * nbT.y);
-            const float2 r1 = cjm(ua0, ubT), r2 = cjm(va0, vbT);
-            const float2 a0 = make_float2(r1.x + r2.x + na0 * nbT.x, r1.y + r2.y + na0 * nbT.y);
-            const double ang = d.omega[idx] * elapsed;
-            const double red = ang - 6.283185307179586476925 * rint(ang * 0.15915494309189533577);
-            float sn, cs;
-            sincosf(float(red), &sn, &cs);
-            Apb[2 * idx] = double(ape.x * cs + ape.y * sn);   // ape * conj(p)
-            Apb[2 * idx + 1] = double(ape.y * cs - ape.x * sn);
-            Amb[2 * idx] = double(ame.x * cs - ame.y * sn);   // ame * p
-            Amb[2 * idx + 1] = double(ame.x * sn + ame.y * cs);
-            A0b[2 * idx] = double(a0.x);
-            A0b[2 * idx + 1] = double(a0.y);
-            continue;
-        }
-        const zd ub{double(ubT.x), double(ubT.y)}, vbv{double(vbT.x), double(vbT.y)};
-        const zd wb{double(wbT.x), double(wbT.y)}, nb{double(nbT.x), double(nbT.y)};
-        // assembly adjoint (coefficientValueForField on evolved coefficients)
-        const zd uap = zload(d.UAp + 2 * idx), vap = zload(d.VAp + 2 * idx), wap = zload(d.WAp + 2 * idx);
-        const zd ua0 = zload(d.UA0 + 2 * idx), va0 = zload(d.VA0 + 2 * idx);
-        const double nap = d.NAp[idx], na0 = d.NA0[idx];
-        const zd ape = zadd(zadd(zadd(zmul(zconj(uap), ub), zmul(zconj(vap), vbv)), zmul(zconj(wap), wb)), zscale(nb, nap));
-        const zd ame = zsub(zadd(zadd(zmul(uap, ub), zmul(vap, vbv)), zmul(zconj(wap), wb)), zscale(nb, nap));
-        const zd a0 = zadd(zadd(zmul(zconj(ua0), ub), zmul(zconj(va0), vbv)), zscale(nb, na0));
-        double s, c;
-        sincos(d.omega[idx] * elapsed, &s, &c);
-        zstore(Apb + 2 * idx, zmul(ape, zd{c, -s}));
-        zstore(Amb + 2 * idx, zmul(ame, zd{c, s}));
-        zstore(A0b + 2 * idx, a0);
+        vinv_adj_store<T>(d, idx, elapsed, ubT, vbT, wbT, nbT, Apb, Amb, A0b);
     }
 }
 

@@ -931,6 +931,12 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
     WV_SET((dev::k_xr2c_adj<T>), smem_xr2c_adj<T>(p));
     WV_SET((dev::k_vinv_adj<T, true>), smem_vinv_adj<T>(p, true));
     WV_SET((dev::k_vinv_adj<T, false>), smem_vinv_adj<T>(p, false));
+    if constexpr (sizeof(dev::cx<T>) == 16) {
+        if (p.fz.N > 0) {
+            WV_SET((dev::k_vfwd_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
+            WV_SET((dev::k_vinv_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
+        }
+    }
 #undef WV_SET
     return cudaSuccess;
 }
@@ -970,7 +976,6 @@ template <typename T>
 void launch_flux_fields(wv_handle* h, double elapsed, const double* Ap, const double* Am, const double* A0, dev::cx<T>* y,
                         cudaStream_t s) {
     const Plan& p = h->plan;
-    const auto& d = h->dd;
     const int nt = p.targets.count;
     auto* z = static_cast<dev::cx<T>*>(h->zspec);
     launch_vinv_flux<T>(h, elapsed, Ap, Am, A0, z, nullptr, y, s);
@@ -1003,7 +1008,15 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
     const dev::cx<T>* y = static_cast<const dev::cx<T>*>(h->yspec);
     if (!physIn) launch_flux_fields<T>(h, elapsed, Ap, Am, A0, static_cast<dev::cx<T>*>(h->yspec), s);
     // adjoint of projection and forward vertical transform, then inverse y FFTs
-    dev::k_vfwd_adj<T><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd_adj<T>(p), s>>>(d, Fpb, Fmb, F0b, elapsed, za);
+    bool fftAdj = false;
+    if constexpr (sizeof(dev::cx<T>) == 16) fftAdj = h->verticalFFT;
+    if constexpr (sizeof(dev::cx<T>) == 16) {
+        if (fftAdj)
+            dev::k_vfwd_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::kVfModes), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
+                d, Fpb, Fmb, F0b, elapsed, za);
+    }
+    if (!fftAdj)
+        dev::k_vfwd_adj<T><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd_adj<T>(p), s>>>(d, Fpb, Fmb, F0b, elapsed, za);
     dev::YInvMap amap{};
     amap.nOut = nt;
     for (int c = 0; c < nt; ++c) { amap.src[c] = c; amap.mulL[c] = 0; }
@@ -1035,7 +1048,13 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
                                                                                                               nIn, fa);
         }
     }
-    dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvAdjModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
+    if constexpr (sizeof(dev::cx<T>) == 16) {
+        if (fftAdj)
+            dev::k_vinv_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::kVzLines / 4), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
+                d, fa, elapsed, Apb, Amb, A0b);
+    }
+    if (!fftAdj)
+        dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvAdjModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
     h->metrics.kernel_launches += 5;
     return cudaGetLastError();
 }

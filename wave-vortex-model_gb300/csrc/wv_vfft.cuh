@@ -25,8 +25,17 @@
 //   X_sin[j] = i (F[j] - F[2L-j]) / 2 / (L Nx Ny)
 // (Fcos, Fsin with their endpoint weights and the horizontal scale), then the
 // projection of k_vfwd (vfwd_project) per (mode, j).
+//
+// The adjoints (k_vfwd_adj_fft, k_vinv_adj_fft) are the transposed maps on the
+// same lines: the transposed forward matrices are an inverse-type line
+// (y[0] = X_0, y[L] = X_L / 2, y[j] = (X_j + i Y_j) / 2 ...) scaled by
+// w_z / (L Nx Ny) (w_z = 2 inside, 1 at the ends) or 2 / (L Nx Ny); the
+// transposed inverse matrices a forward-type line (y[0] = o_0, y[L] = o_L,
+// y[z] = (o_z + i s_z) / 2, y[2L-z] = (o_z - i s_z) / 2) with Ccos's 1/2 at
+// j = 0 and +/- m_j for the z-derivative channels.
 #pragma once
 
+#include "wv_adjoint.cuh"
 #include "wv_kernels.cuh"
 
 namespace wvgpu {
@@ -236,6 +245,181 @@ __global__ void __launch_bounds__(256) k_vfwd_fft(DescDev d, const cx<T>* __rest
             vi[c] = conj ? -v.y : v.y;
         }
         vfwd_project<T, FLUX>(d, w, j, vr, vi, nch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
+    }
+}
+
+// Shared memory of the adjoint kernels: two line buffers and the twiddles.
+template <typename T>
+inline size_t smem_vadj_fft(int N2) {
+    return (2 * static_cast<size_t>(kVzLines) * N2 + N2) * sizeof(cx<T>);
+}
+
+// Transpose of the projection + forward vertical transform (k_vfwd_adj) with the
+// transposed forward matrices as FFTs: per retained column the target pairs
+// (u | w) and (v | eta).  Single-state handles, like k_vfwd_adj.
+template <typename T>
+__global__ void __launch_bounds__(256) k_vfwd_adj_fft(DescDev d, const double* __restrict__ Fpb, const double* __restrict__ Fmb,
+                                                     const double* __restrict__ F0b, double elapsed, cx<T>* __restrict__ zadj) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, nt = d.nt, L = Nz - 1, N2 = d.fz.N;
+    cx<T>* bufA = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* bufB = bufA + kVzLines * N2;
+    cx<T>* tw = bufB + kVzLines * N2;
+    const int m0 = blockIdx.x * kVfModes;
+    const int nm = min(kVfModes, d.Nkl - m0);
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    for (int i = threadIdx.x; i < kVzLines * N2; i += blockDim.x) bufA[i] = mk<T>(T(0), T(0));
+    int tOfQ[4] = {-1, -1, -1, -1};
+    for (int t = 0; t < nt; ++t) tOfQ[d.tq[t]] = t;
+    __syncthreads();
+    const T half = T(0.5f);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it % nm, j = it / nm;
+        cx<T> vt[4];
+        vfwd_adj_values<T>(d, Fpb, Fmb, F0b, elapsed, d.modeWV[m0 + mi], j, vt);
+        cx<T> X[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int t = tOfQ[q];
+            X[q] = t < 0 ? mk<T>(T(0), T(0)) : (t == 0 ? vt[0] : t == 1 ? vt[1] : t == 2 ? vt[2] : vt[3]);
+        }
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            const cx<T> C = X[l], D = X[2 + l];  // cosine target, sine target
+            cx<T>* y = bufA + (mi * 2 + l) * N2;
+            if (j == 0) {
+                y[0] = C;
+            } else if (j == L) {
+                y[L] = mk<T>(C.x * half, C.y * half);
+            } else {
+                const cx<T> c = mk<T>(C.x * half, C.y * half);
+                const cx<T> id = mk<T>(-(D.y * half), D.x * half);
+                y[j] = cadd<T>(c, id);
+                y[N2 - j] = csub<T>(c, id);
+            }
+        }
+    }
+    __syncthreads();
+    const cx<T>* F = fft_lines<T, false>(bufA, bufB, d.fz, kVzLines, N2, tw);
+    const T sc = T(1.0 / (static_cast<double>(L) * static_cast<double>(d.Nx) * static_cast<double>(d.Ny)));
+    const T sc2 = sc + sc;
+    for (int it = threadIdx.x; it < nm * 2 * (L + 1); it += blockDim.x) {
+        const int z = it % (L + 1);
+        const int rest = it / (L + 1);
+        const int l = rest & 1, mi = rest >> 1;
+        const int mode = m0 + mi;
+        const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
+        const bool conj = d.modeFlags[mode] & 1;
+        const cx<T>* row = F + (mi * 2 + l) * N2;
+        const cx<T> a = row[z];
+        cx<T> vc, vs;
+        if (z == 0 || z == L) {
+            vc = mk<T>(a.x * sc, a.y * sc);
+            vs = mk<T>(T(0), T(0));
+        } else {
+            const cx<T> b = row[N2 - z];
+            vc = mk<T>((a.x + b.x) * sc, (a.y + b.y) * sc);  // w_z (F[z] + F[2L-z]) / 2 with w_z = 2
+            vs = mk<T>((a.x - b.x) * half * sc2, (a.y - b.y) * half * sc2);
+        }
+        const int tc = l == 0 ? tOfQ[0] : tOfQ[1], ts = l == 0 ? tOfQ[2] : tOfQ[3];
+        if (tc >= 0) {
+            cx<T>* base = zadj + (size_t)tc * Nz * P + (size_t)z * P;
+            base[pos] = conj ? cconj<T>(vc) : vc;
+            if (cpos >= 0) base[cpos] = mk<T>(T(0), T(0));
+        }
+        if (ts >= 0) {
+            cx<T>* base = zadj + (size_t)ts * Nz * P + (size_t)z * P;
+            base[pos] = conj ? cconj<T>(vs) : vs;
+            if (cpos >= 0) base[cpos] = mk<T>(T(0), T(0));
+        }
+    }
+}
+
+// Transpose of the flux's vertical inverse (k_vinv_adj<T, true>) with the
+// transposed inverse matrices as FFTs: per retained column the channel pairs
+// (U | W), (V | N) and the z-derivative channels (w_z | u_z), (eta_z | v_z),
+// then the transposed assembly and phase (vinv_adj_store).  Single-state
+// handles, like k_vinv_adj.
+template <typename T>
+__global__ void __launch_bounds__(256) k_vinv_adj_fft(DescDev d, const cx<T>* __restrict__ fadj, double elapsed,
+                                                     double* __restrict__ Apb, double* __restrict__ Amb,
+                                                     double* __restrict__ A0b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kLines = 4, kModes = kVzLines / kLines;
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, nt = d.nt, L = Nz - 1, N2 = d.fz.N;
+    cx<T>* bufA = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* bufB = bufA + kVzLines * N2;
+    cx<T>* tw = bufB + kVzLines * N2;
+    const int m0 = blockIdx.x * kModes;
+    const int nm = min(kModes, d.Nkl - m0);
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    int derivChan[4] = {-1, -1, -1, -1};
+    for (int t = 0; t < nt; ++t) derivChan[d.tq[t]] = 4 + t;
+    const T half = T(0.5f);
+    // lines: y[0] = o_0, y[L] = o_L, y[z] = (o_z + i s_z) / 2, y[2L-z] = (o_z - i s_z) / 2
+    for (int it = threadIdx.x; it < nm * kLines * (L + 1); it += blockDim.x) {
+        const int z = it % (L + 1);
+        const int rest = it / (L + 1);
+        const int l = rest % kLines, mi = rest / kLines;
+        const int mode = m0 + mi;
+        const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
+        const unsigned char flags = d.modeFlags[mode];
+        int chC, chS;
+        if (l == 0) { chC = 0; chS = 2; }
+        else if (l == 1) { chC = 1; chS = 3; }
+        else if (l == 2) { chC = derivChan[2]; chS = derivChan[0]; }
+        else { chC = derivChan[3]; chS = derivChan[1]; }
+        // stored row + conjugated completion row, frame of k_vinv (as k_vinv_adj's gather)
+        auto colval = [&](int ch) -> cx<T> {
+            if (ch < 0) return mk<T>(T(0), T(0));
+            const cx<T>* r = fadj + ((size_t)ch * Nz + z) * P;
+            cx<T> v = r[pos];
+            if (cpos >= 0) { const cx<T> c = r[cpos]; v = mk<T>(v.x + c.x, v.y - c.y); }
+            if (flags & 2) v.y = T(0);
+            if (flags & 1) v.y = -v.y;
+            return v;
+        };
+        cx<T>* y = bufA + (mi * kLines + l) * N2;
+        const cx<T> o = colval(chC);
+        if (z == 0 || z == L) {
+            y[z] = o;
+        } else {
+            const cx<T> sv = colval(chS);
+            const cx<T> c = mk<T>(o.x * half, o.y * half);
+            const cx<T> id = mk<T>(-(sv.y * half), sv.x * half);
+            y[z] = cadd<T>(c, id);
+            y[N2 - z] = csub<T>(c, id);
+        }
+    }
+    __syncthreads();
+    const cx<T>* F = fft_lines<T, false>(bufA, bufB, d.fz, kVzLines, N2, tw);
+    const T* mz = reinterpret_cast<const T*>(d.tMz);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it % nm, j = it / nm;
+        const int w = d.modeWV[m0 + mi];
+        cx<T> Ev[kLines], Od[kLines];
+#pragma unroll
+        for (int l = 0; l < kLines; ++l) {
+            const cx<T>* row = F + (mi * kLines + l) * N2;
+            const cx<T> a = row[j];
+            if (j == 0 || j == L) {
+                Ev[l] = j == 0 ? mk<T>(a.x * half, a.y * half) : a;  // Ccos's 1/2 at j = 0
+                Od[l] = mk<T>(T(0), T(0));
+            } else {
+                const cx<T> b = row[N2 - j];
+                Ev[l] = mk<T>((a.x + b.x) * half, (a.y + b.y) * half);
+                Od[l] = mk<T>((a.x - b.x) * half, (a.y - b.y) * half);
+            }
+        }
+        const T m = mz[j];
+        // u_bar = Ccos^T U + (-m) Csin^T u_z;  w_bar = Csin^T W + m Ccos^T w_z; likewise v, eta
+        const cx<T> ubT = mk<T>(Ev[0].x - m * Od[2].x, Ev[0].y - m * Od[2].y);
+        const cx<T> wbT = mk<T>(Od[0].x + m * Ev[2].x, Od[0].y + m * Ev[2].y);
+        const cx<T> vbT = mk<T>(Ev[1].x - m * Od[3].x, Ev[1].y - m * Od[3].y);
+        const cx<T> nbT = mk<T>(Od[1].x + m * Ev[3].x, Od[1].y + m * Ev[3].y);
+        vinv_adj_store<T>(d, j + Nj * w, elapsed, ubT, vbT, wbT, nbT, Apb, Amb, A0b);
     }
 }
 
