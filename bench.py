@@ -63,8 +63,9 @@ def parse():
     ap.add_argument("--profile-size", type=int, default=256,
                     help="with --profile-flux: grid N x N x (N/2+1) over 3.125 km x N (256: the benchmark workload)")
     ap.add_argument("--workload", choices=["c1", "c2"], default="c1",
-                    help="c2: 512x512x257 mixed vs FP64 over --c2-steps RK4 steps (field error and energy drift)")
-    ap.add_argument("--c2-steps", type=int, default=200)
+                    help="c2: only the 512x512x257 leg (mixed and paired FP32 vs FP64 over --c2-steps RK4 steps)")
+    ap.add_argument("--c2-steps", type=int, default=200,
+                    help="RK4 steps of the 512x512x257 leg (part of the default run; 0 skips it)")
     return ap.parse_args()
 
 
@@ -209,6 +210,71 @@ def traffic_from_profile(stage, precision="fp64"):
             if len(parts) >= 3 and not line.startswith("#") and parts[0] == stage and parts[1] == precision:
                 return float(parts[2])
     return None
+
+
+REF_WORKLOAD_CASE = dict(Nx=GRID["Nx"], Ny=GRID["Ny"], Nz=GRID["Nz"], Nj=GRID["Nj"], Lx=GRID["Lx"], Ly=GRID["Ly"],
+                         Lz=GRID["Lz"], latitude=GRID["latitude"], isHydrostatic=False, shouldAntialias=True,
+                         damping=False)
+
+
+def _reference_cpp():
+    """The reference's own C++ (CompiledKernel + PortableRuntime fixed-step RK4,
+    built by oracle/ref_build.sh on this host) with the oracle's O(N log N) FFT
+    engine; None when it cannot be built here."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_lib as R
+    if not R.available():
+        return None
+    return R
+
+
+def _host_cpu():
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def reference_cpp_steps(state, dt, steps, warmup, budget_s):
+    """WVFixedStepRK4::step of the reference's C++ on the 256x256x129 state:
+    (seconds per step, steps timed, threads, sample text), or None."""
+    R = _reference_cpp()
+    if R is None:
+        return None
+    lib = R.load_lib()
+    ref = R.Ref(lib, REF_WORKLOAD_CASE, R.ENGINE_ORACLE_FFT)
+    Ap, Am, A0 = state
+    t = 0.0
+    for _ in range(warmup):
+        Ap, Am, A0, t = ref.rk4(Ap, Am, A0, t, 0.0, dt, 1)
+    done, el = 0, 0.0
+    w0 = time.perf_counter()
+    while done < steps:
+        Ap, Am, A0, t = ref.rk4(Ap, Am, A0, t, 0.0, dt, 1)
+        done += 1
+        el = time.perf_counter() - w0
+        if el > budget_s:
+            break
+    threads = int(lib.wvref_oracle_fft_threads())
+    sample = (f"{done} WVFixedStepRK4 steps (4 nonlinear fluxes each) of the 256x256x129 state after {warmup} warm-up "
+              f"step(s): the reference's own C++ (CompiledKernel + PortableRuntime, -O3, 2 coefficient workers as "
+              f"published) with the oracle's O(N log N) FFT engine on {threads} threads standing in for FFTW "
+              f"(absent here); host {_host_cpu()}, {os.cpu_count()} cores")
+    return el / done, done, threads, sample, (Ap, Am, A0, t, warmup + done)
+
+
+def cpu_baseline(state, dt):
+    """Bounded CPU sample of the same workload: 2 RK4 steps of the reference's
+    own C++ (1 warm-up), else 1 step of the numpy restatement."""
+    r = reference_cpp_steps(state, dt, steps=2, warmup=1, budget_s=60.0)
+    if r is not None:
+        per, done, threads, sample, final = r
+        return {"value": 1.0 / per, "unit": UNIT, "cores": threads, "kind": "reference", "sample": sample}, final
+    return cpu_baseline_oracle(state, dt), None
 
 
 def cpu_baseline_oracle(state, dt):
@@ -546,6 +612,12 @@ def run_ours(args):
     e2e_s = max_over_ranks(time.perf_counter() - w0)
     M = k.sizes["M"]
     coeff_bytes = 3 * M * 16
+    c2 = _c2_leg(wvgpu, stream, torch, np, args.c2_steps) if rank == 0 and args.c2_steps > 0 else None
+    cpu, vs_ref = None, None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, final = cpu_baseline(state, dt)
+        if final is not None:
+            vs_ref = _error_vs_reference_cpp(wvgpu, cfg, k, state, dt, final, torch, np)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -553,13 +625,14 @@ def run_ours(args):
         "vs_baseline_source": "published fixed-step RK4 at 256x256x129, standalone C++ (FFTW) on an 18-thread Apple "
                               "M5 Max: 2.20 steps/s (the reference's three-interface record; its run includes an "
                               "observer graph)",
-        "dtype": "f64", "data": "synthetic", "config": {
+        "dtype": "f64", "data": "synthetic",
+        "precision": "fp64 (plain drop-in); the reduced-precision forms are reported under 'mixed' (f32 + "
+                     "split-BF16 tensor cores) and 'fp32x2' (paired f32)",
+        "vertical_kernel": k.vertical_kernel(),
+        "config": {
             "workload": "fixed-step RK4, nonlinear advection, 256x256x129, 800 km x 800 km x 4 km, N0 5.2e-3, lat 33, "
                         "0.1 m/s rms seeded spectrum state, dt = 0.5 x CFL",
             "grid": [GRID["Nx"], GRID["Ny"], GRID["Nz"]], "Nj": GRID["Nj"], "Nkl": k.sizes["Nkl"], "dt_s": dt,
-            "precision": "fp64 (plain drop-in); the reduced-precision forms are reported under 'mixed' (f32 + "
-                         "split-BF16 tensor cores) and 'fp32x2' (paired f32)",
-            "vertical_kernel": k.vertical_kernel(),
             "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MB write)"},
         "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": coeff_bytes,
                 "d2h_bytes_per_step": coeff_bytes},
@@ -570,22 +643,87 @@ def run_ours(args):
         "adjoint": adjoint,
         "ensemble": ensemble,
         "published_flux_comparison": published,
+        "c2_512x512x257": c2,
+        "error_vs_reference_cpp": vs_ref,
         "clocks": clocks.summary(),
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline_oracle(state, dt)
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
     if rank == 0:
+        out["summary"] = _summary(value, mixed, fp32x2, adjoint, ensemble, c2, vs_ref, roofline)
         print(json.dumps(out), flush=True)
     k.close()
     if world > 1:
         dist.destroy_process_group()
 
 
+def _error_vs_reference_cpp(wvgpu, cfg, k64, state, dt, final, torch, np):
+    """Each precision against the reference's own C++ FP64 (WVFixedStepRK4, the
+    oracle FFT engine): relative L2 error per field (u, v, w, eta) after the same
+    RK4 steps from the same state, and max |F - F_ref| / max |F_ref| of the flux
+    at the initial state."""
+    R = _reference_cpp()
+    Rp, Rm, R0, tr, nsteps = final
+    ref_fields = k64.transformWaveVortexToUVWEta(tr, 0.0, Rp, Rm, R0)
+    ref = R.Ref(R.load_lib(), REF_WORKLOAD_CASE, R.ENGINE_ORACLE_FFT)
+    ref_flux = ref.flux(*state, 0.0, 0.0)
+    del ref
+    out = {"steps": nsteps, "norm": "field: ||f - f_ref||_2 / ||f_ref||_2 per (u, v, w, eta); "
+                                    "flux: max|F - F_ref| / max|F_ref| per (Fp, Fm, F0)"}
+    for prec in ("fp64", "fp32x2", "mixed"):
+        kk = k64 if prec == "fp64" else wvgpu.WVTransformConstantStratificationKernel(cfg, precision=prec)
+        dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
+        F = kk.nonlinearFlux(0.0, 0.0, *dev)
+        _, _, _, t1 = kk.rk4(*dev, 0.0, 0.0, dt, nsteps)
+        torch.cuda.synchronize()
+        f = k64.transformWaveVortexToUVWEta(t1, 0.0, *(x.cpu().numpy() for x in dev))
+        out[prec] = {
+            "rel_field_err": [float(np.linalg.norm(f[i] - ref_fields[i]) / np.linalg.norm(ref_fields[i])) for i in range(4)],
+            "rel_flux_err": [float(np.max(np.abs(a.cpu().numpy() - b)) / np.max(np.abs(b))) for a, b in zip(F, ref_flux)]}
+        if kk is not k64:
+            kk.close()
+    return out
+
+
+def _summary(value, mixed, fp32x2, adjoint, ensemble, c2, vs_ref, roofline):
+    """The metric's own figures as flat scalars, last on the line."""
+    ok = [(f, d) for f, d in (("fp32x2", fp32x2), ("mixed", mixed))
+          if d and max(d.get("rel_field_err_vs_fp64_after_100_steps", [1.0])) <= 1e-6]
+    best = max(ok, key=lambda fd: fd[1]["value"]) if ok else None
+    s = {"fp64_steps_s": value,
+         "form_meeting_1e-6": best[0] if best else None,
+         "speedup_at_1e-6_vs_fp64": best[1]["speedup_vs_fp64"] if best else None,
+         "fp32x2_speedup_vs_fp64": fp32x2["speedup_vs_fp64"],
+         "fp32x2_max_field_err_100": max(fp32x2.get("rel_field_err_vs_fp64_after_100_steps", [float("nan")])),
+         "mixed_speedup_vs_fp64": mixed["speedup_vs_fp64"],
+         "mixed_field_err_100": mixed.get("rel_field_err_vs_fp64_after_100_steps"),
+         "flux_hbm_frac_mixed": mixed["roofline"]["flux"]["frac"],
+         "flux_hbm_frac_fp64": roofline["flux"]["frac"]}
+    if adjoint:
+        for p, a in adjoint.items():
+            s[f"adjoint_over_forward_{p}"] = a["adjoint_over_forward"]
+    if ensemble:
+        s["ensemble_speedup_vs_one_at_a_time"] = ensemble["speedup_vs_one_at_a_time"]
+    if c2:
+        s["c2_fp64_steps_s"] = c2["fp64"]["value"]
+        for p in ("fp32x2", "mixed"):
+            s[f"c2_{p}_speedup_vs_fp64"] = c2[p]["speedup_vs_fp64"]
+            s[f"c2_{p}_max_field_err_{c2['steps']}"] = max(c2[p]["rel_field_err_vs_fp64"])
+    if vs_ref:
+        for p in ("fp64", "fp32x2", "mixed"):
+            s[f"{p}_max_field_err_vs_reference_cpp_{vs_ref['steps']}_steps"] = max(vs_ref[p]["rel_field_err"])
+    return s
+
+
 def run_reference(args):
+    """The reference arm: the reference's own CPU implementation of the step on
+    this host's cores -- its C++ CompiledKernel + PortableRuntime WVFixedStepRK4
+    (oracle/ref_build.sh; the oracle's O(N log N) FFT engine in place of FFTW) --
+    on the same 256x256x129 state and dt.  Falls back to the numpy restatement
+    only when the C++ cannot be built on this host.  Rank 0 alone runs."""
     world, rank, local = dist_setup()
     if rank != 0:
         return
-    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import wv_oracle as O
     c = O.Config(Nx=GRID["Nx"], Ny=GRID["Ny"], Nz=GRID["Nz"], Nj=GRID["Nj"], Lx=GRID["Lx"], Ly=GRID["Ly"], Lz=GRID["Lz"],
@@ -593,29 +731,41 @@ def run_reference(args):
     d = O.build_descriptor(c)
     Ap, Am, A0 = O.spectrum_state(d, seed=SEED, urms=URMS)
     dt = O.cfl_time_step(d, Ap, Am, A0)
-    t, t0 = 0.0, 0.0
-    for _ in range(min(args.warmup, 1)):
-        Ap, Am, A0, t = O.rk4_step(d, Ap, Am, A0, t, t0, dt)
     budget = 150.0
-    done, el = 0, 0.0
-    w0 = time.perf_counter()
-    while done < args.steps:
-        Ap, Am, A0, t = O.rk4_step(d, Ap, Am, A0, t, t0, dt)
-        done += 1
-        el = time.perf_counter() - w0
-        if el > budget:
-            break
-    value = done / el
-    sample = (f"{done} of {args.steps} RK4 steps of the 256x256x129 state (4 nonlinear fluxes each) with the "
-              f"numpy/scipy restatement of the reference kernel, {min(args.warmup, 1)} warm-up step; "
-              f"capped at {budget:.0f} s")
+    warm = min(args.warmup, 1)
+    r = reference_cpp_steps((Ap, Am, A0), dt, args.steps, warm, budget)
+    if r is not None:
+        per, done, threads, sample, _ = r
+        kind, cores = "reference", threads
+        sample += f"; {done} of {args.steps} requested steps, capped at {budget:.0f} s"
+    else:
+        t, t0 = 0.0, 0.0
+        for _ in range(warm):
+            Ap, Am, A0, t = O.rk4_step(d, Ap, Am, A0, t, t0, dt)
+        done, el = 0, 0.0
+        w0 = time.perf_counter()
+        while done < args.steps:
+            Ap, Am, A0, t = O.rk4_step(d, Ap, Am, A0, t, t0, dt)
+            done += 1
+            el = time.perf_counter() - w0
+            if el > budget:
+                break
+        per = el / done
+        kind, cores = "port", os.cpu_count()
+        sample = (f"{done} of {args.steps} RK4 steps of the 256x256x129 state (4 nonlinear fluxes each) with the "
+                  f"numpy/scipy restatement of the reference kernel (the reference's C++ could not be built here), "
+                  f"{warm} warm-up step; capped at {budget:.0f} s")
+    value = 1.0 / per
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1e3 * el / done, "higher_is_better": True, "scaling": "weak",
+           "ms_per_step": 1e3 * per, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": value / PUBLISHED_RK4_STEPS_S, "dtype": "f64",
            "data": "synthetic", "impl": "reference",
-           "config": {"workload": "fixed-step RK4, nonlinear advection, 256x256x129 (CPU oracle of the reference kernel)",
-                      "grid": [GRID["Nx"], GRID["Ny"], GRID["Nz"]], "dt_s": dt, "parallelism": "host threads"},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample},
+           "config": {"workload": "fixed-step RK4, nonlinear advection, 256x256x129, 800 km x 800 km x 4 km, N0 5.2e-3, "
+                                  "lat 33, 0.1 m/s rms seeded spectrum state, dt = 0.5 x CFL",
+                      "grid": [GRID["Nx"], GRID["Ny"], GRID["Nz"]], "Nj": GRID["Nj"], "Nkl": d.Nkl, "dt_s": dt,
+                      "parallelism": "host threads", "l2": "not applicable (CPU arm)"},
+           "steps_timed": done, "precision": "fp64",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -631,51 +781,54 @@ def _energy(k, state, t, t0, np):
     return 0.5 * float(np.sum(e * wz[:, None, None]) / (np.sum(wz) * f.shape[2] * f.shape[3]))
 
 
-def run_workload_c2(args):
+def _c2_leg(wvgpu, stream, torch, np, steps):
     """512x512x257 over the 800 km x 800 km x 4 km domain of the 256 workload, seeded
-    spectrum state at 0.1 m/s (seed 2), dt = 0.5 CFL: RK4 steps/s of the FP64 and the
-    mixed form, per-field relative L2 error of the mixed form against FP64 after
-    the run, and the energy drift of both."""
-    import numpy as np
-    import torch
-    import wvgpu
-    from wvgpu import build
-    build.build()
+    spectrum state at 0.1 m/s (seed 2), dt = 0.5 CFL: RK4 steps/s of the FP64, mixed
+    and paired-FP32 forms over `steps` steps, per-field relative L2 error of the
+    reduced forms against FP64 after the run, and the energy drift of each."""
     cfg = wvgpu.Configuration(Nx=512, Ny=512, Nz=257, Nj=170, Lx=800e3, Ly=800e3, Lz=4000.0, N0=5.2e-3, latitude=33.0)
     k = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="fp64")
-    km = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="mixed")
     state = wvgpu.synthetic_state(k, seed=2, urms=URMS)
     dt = wvgpu.cfl_time_step(k, *state)
-    stream = torch.cuda.current_stream()
     out = {"workload": "512x512x257, 800 km x 800 km x 4 km, N0 5.2e-3, lat 33, 0.1 m/s rms seeded spectrum (seed 2), "
-                       "dt = 0.5 x CFL", "steps": args.c2_steps, "dt_s": dt, "unit": UNIT}
+                       "dt = 0.5 x CFL", "steps": steps, "dt_s": dt, "unit": UNIT}
     E0 = _energy(k, state, 0.0, 0.0, np)
-    kx = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
-    for name, kk in (("fp64", k), ("mixed", km), ("fp32x2", kx)):
+    finals = {}
+    for name in ("fp64", "mixed", "fp32x2"):
+        kk = k if name == "fp64" else wvgpu.WVTransformConstantStratificationKernel(cfg, precision=name)
         dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
         kk.rk4(*[x.clone() for x in dev], 0.0, 0.0, dt, 2)  # warm
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        _, _, _, tT = kk.rk4(*dev, 0.0, 0.0, dt, args.c2_steps)
+        _, _, _, tT = kk.rk4(*dev, 0.0, 0.0, dt, steps)
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        final = [x.cpu().numpy() for x in dev]
-        out[name] = {"value": args.c2_steps / (ms * 1e-3), "ms_per_step": ms / args.c2_steps,
-                     "energy_drift": (_energy(k, final, tT, 0.0, np) - E0) / E0}
-        out[name + "_state"] = final
-    f64 = k.transformWaveVortexToUVWEta(tT, 0.0, *out.pop("fp64_state"))
+        finals[name] = [x.cpu().numpy() for x in dev]
+        out[name] = {"value": steps / (ms * 1e-3), "ms_per_step": ms / steps, "vertical_kernel": kk.vertical_kernel(),
+                     "energy_drift": (_energy(k, finals[name], tT, 0.0, np) - E0) / E0}
+        if kk is not k:
+            kk.close()
+        del dev
+    f64 = k.transformWaveVortexToUVWEta(tT, 0.0, *finals["fp64"])
     for name in ("mixed", "fp32x2"):
-        fr = k.transformWaveVortexToUVWEta(tT, 0.0, *out.pop(name + "_state"))
+        fr = k.transformWaveVortexToUVWEta(tT, 0.0, *finals[name])
         out[name]["rel_field_err_vs_fp64"] = [float(np.linalg.norm(fr[i] - f64[i]) / np.linalg.norm(f64[i]))
                                               for i in range(4)]
         out[name]["speedup_vs_fp64"] = out[name]["value"] / out["fp64"]["value"]
-    out["mixed"]["vertical_kernel"] = "cuda cores (the tensor-core transform needs Nz <= 255)"
-    print(json.dumps(out), flush=True)
     k.close()
-    km.close()
-    kx.close()
+    return out
+
+
+def run_workload_c2(args):
+    """The 512x512x257 leg alone (see _c2_leg)."""
+    import numpy as np
+    import torch
+    import wvgpu
+    from wvgpu import build
+    build.build()
+    print(json.dumps(_c2_leg(wvgpu, torch.cuda.current_stream(), torch, np, args.c2_steps)), flush=True)
 
 
 def run_profile_case(args):

@@ -250,19 +250,24 @@ int wv_rk4_adjoint_device(wv_handle* handle, const double* Ap, const double* Am,
 
 /* Nonlinear flux that allocates no device memory.  No counterpart in the
  * reference: the reference's kernel owns a heap scratch arena.  It exists for
- * callers that cannot call cudaMalloc at the point where they need a flux
- * (e.g. code running while a stream is being captured into a CUDA graph, or a
- * host application whose memory manager owns every device allocation and forbids
- * further driver allocations, or latency-sensitive loops where cudaMalloc's
- * implicit device synchronization is not acceptable).  Inputs and outputs are
- * device pointers supplied by the caller, exactly as for
- * wv_nonlinear_flux_device; the handle must already exist (wv_create allocates).
+ * callers that cannot call cudaMalloc at the point where they need a flux: a
+ * host application whose memory manager owns every device allocation and
+ * forbids further driver allocations, or latency-sensitive loops where
+ * cudaMalloc's implicit device synchronization is not acceptable.  Inputs and
+ * outputs are device pointers supplied by the caller, exactly as for
+ * wv_nonlinear_flux_device (no adaptive damping); the handle must already exist
+ * (wv_create allocates) and hold a single state, else WV_UNSUPPORTED_OPERATION.
+ * The launches and the vertical-kernel choice (wv_set_vertical_kernel) are
+ * those of wv_nonlinear_flux_device on the same handle; only the scratch differs.
  * The flux pipeline's scratch lives in one file-scope __device__ array of
  * WV_STATIC_SCRATCH_BYTES, held by every GPU that loads the library until exit.
  * Configurations whose scratch exceeds it are rejected with WV_SIZE_OVERFLOW.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the one array, so
- * calls that overlap on the GPU (other streams, other handles) race. */
+ * The first call on a device looks up the array's device address and keeps it
+ * for the process; make that first call before any stream capture.  A device
+ * reset (cudaDeviceReset) invalidates the kept address: do not call this entry
+ * on a device that was reset after its first call.  All calls share the one
+ * array, which keeps the last call's contents, so calls that overlap on the GPU
+ * (other streams, other handles) race. */
 #define WV_STATIC_SCRATCH_BYTES (32ull << 20)
 int wv_nonlinear_flux_device_noalloc(wv_handle* handle, double t, double t0,
                                      const double* Ap, const double* Am, const double* A0,

@@ -12,9 +12,12 @@
 //     (PortableRuntime/include/WaveVortexRuntime/WVConstantStratificationIntegrationSystem.hpp:40-66)
 //   WVFixedStepRK4::step (PortableRuntime/src/WVRungeKutta.cpp:335-462)
 //   WVReferenceFFTEngine, the exact direct DFT/DCT-I/DST-I engine
-//     (CompiledKernel/adapters/reference/WVReferenceFFTEngine.cpp:47-107)
+//     (CompiledKernel/adapters/reference/WVReferenceFFTEngine.cpp:47-107), or
+//   wvoracle::OracleFFTEngine (oracle/wv_fft_engine.cpp), an O(N log N)
+//     provider of the same contract for grids the direct engine cannot reach
 
 #include "WVReferenceFFTEngine.hpp"
+#include "wv_fft_engine.hpp"
 #include "WaveVortexKernel/WVTransformConstantStratificationKernel.hpp"
 #include "WaveVortexRuntime/WVConstantStratificationIntegrationSystem.hpp"
 #include "WaveVortexRuntime/WVExtensionCatalog.hpp"
@@ -90,15 +93,26 @@ std::vector<WVAdditionalStateBlockView> blockViews(const WVConstantStratificatio
     return v;
 }
 
+// engine: 0 = the reference's direct DFT engine, 1 = the oracle's O(N log N) engine
+std::unique_ptr<WVFFTEngine> makeEngine(int engine) {
+    if (engine == 1) return std::make_unique<wvoracle::OracleFFTEngine>();
+    return std::make_unique<WVReferenceFFTEngine>();
+}
+
 } // namespace
 
 extern "C" {
 
-// schedule: 0 = {nonlinear advection}; 1 = {nonlinear advection, adaptive damping}
-int wvref_create(const std::uint64_t* sizes, const double* values, const std::uint8_t* flags, int schedule, void** out) {
+// Threads the oracle FFT engine uses (WV_ORACLE_FFT_THREADS or every hardware thread).
+unsigned wvref_oracle_fft_threads() { return wvoracle::defaultOracleFFTThreads(); }
+
+// schedule: 0 = {nonlinear advection}; 1 = {nonlinear advection, adaptive damping};
+// engine as makeEngine.  The kernel and the integration system each own an engine.
+int wvref_create_engine(const std::uint64_t* sizes, const double* values, const std::uint8_t* flags, int schedule,
+                        int engine, void** out) {
     auto h = std::make_unique<RefHandle>();
     const auto c = makeConfiguration(sizes, values, flags);
-    auto status = WVTransformConstantStratificationKernel::create(c, std::make_unique<WVReferenceFFTEngine>(), h->kernel);
+    auto status = WVTransformConstantStratificationKernel::create(c, makeEngine(engine), h->kernel);
     if (!status) { *out = nullptr; return static_cast<int>(status.code); }
     WVFrozenForcingSchedule frozen;
     frozen.entries.push_back(forcingEntry("WVNonlinearAdvection", "nonlinear", WVForcingStage::spatial, 127));
@@ -106,11 +120,15 @@ int wvref_create(const std::uint64_t* sizes, const double* values, const std::ui
     std::shared_ptr<const WVExtensionCatalog> catalog;
     status = makeBuiltInExtensionCatalog(catalog);
     if (!status) { *out = nullptr; return static_cast<int>(status.code); }
-    status = WVConstantStratificationIntegrationSystem::create(c, frozen, catalog, std::make_unique<WVReferenceFFTEngine>(), h->system);
+    status = WVConstantStratificationIntegrationSystem::create(c, frozen, catalog, makeEngine(engine), h->system);
     if (!status) { *out = nullptr; return static_cast<int>(status.code); }
     h->rk4 = std::make_unique<WVFixedStepRK4>(*h->system);
     *out = h.release();
     return 0;
+}
+
+int wvref_create(const std::uint64_t* sizes, const double* values, const std::uint8_t* flags, int schedule, void** out) {
+    return wvref_create_engine(sizes, values, flags, schedule, 0, out);
 }
 
 void wvref_destroy(void* handle) { delete static_cast<RefHandle*>(handle); }
@@ -148,6 +166,20 @@ void wvref_descriptor(void* handle, std::int64_t* kMode, std::int64_t* lMode, do
     std::memcpy(ApmNProjection, m.ApmNProjection.data(), M * sizeof(double));
     std::memcpy(UApField, m.UApField.data(), M * 2 * sizeof(double));
     std::memcpy(WApField, m.WApField.data(), M * 2 * sizeof(double));
+}
+
+// Stage instrumentation of the reference kernel (WVKernelMetrics): enable != 0
+// turns it on; out[0..7] = phase, reconstruction, derivative reconstruction,
+// product, projection, coefficient assembly, derivative coefficient assembly and
+// coefficient projection seconds of the last call.
+void wvref_stage_seconds(void* handle, int enable, double* out) {
+    auto* h = static_cast<RefHandle*>(handle);
+    h->kernel->setStageInstrumentation(enable != 0);
+    const auto& m = h->kernel->metrics();
+    const double v[8] = {m.phaseSeconds, m.reconstructionSeconds, m.derivativeReconstructionSeconds, m.productSeconds,
+                         m.projectionSeconds, m.coefficientAssemblySeconds, m.derivativeCoefficientAssemblySeconds,
+                         m.coefficientProjectionSeconds};
+    for (int i = 0; i < 8; ++i) out[i] = v[i];
 }
 
 int wvref_flux(void* handle, double t, double t0, const double* Ap, const double* Am, const double* A0,

@@ -56,4 +56,5 @@ def test_reference_arm_under_torchrun_prints_on_rank0_only():
     assert len(lines) == 1
     out = json.loads(lines[0])
     assert out["impl"] == "reference" and out["n_gpus"] == 2 and out["value"] > 0
-    assert out["e2e"]["h2d_bytes_per_step"] == 0 and out["cpu_baseline"]["kind"] == "port"
+    # the reference's own C++ where it builds on this host, else the numpy restatement
+    assert out["e2e"]["h2d_bytes_per_step"] == 0 and out["cpu_baseline"]["kind"] in ("reference", "port")

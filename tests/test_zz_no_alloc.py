@@ -1,12 +1,13 @@
 """The allocation-free flux entry point (wv_nonlinear_flux_device_noalloc).
 
-Some callers cannot call cudaMalloc where they need a flux: code running while
-a stream is captured into a CUDA graph, host applications whose memory manager
-owns all device memory, or loops that cannot afford cudaMalloc's implicit
-device synchronization.  For them the library keeps the flux scratch in one
-static device array.  This test calls that entry point through the C ABI and
-checks it against the regular device entry point, on two calls in a row with
-different states (the shared array keeps the previous call's contents), and
+Some callers cannot call cudaMalloc where they need a flux: a host application
+whose memory manager owns all device memory and forbids further driver
+allocations, or a loop that cannot afford cudaMalloc's implicit device
+synchronization.  For them the library keeps the flux scratch in one static
+device array.  This test calls that entry point through the C ABI and checks it
+against the regular device entry point of the same handle, on two calls in a
+row with different states (the shared array keeps the previous call's
+contents), for every precision and vertical-kernel choice, on two grids, and
 that configurations too large for the array are rejected with a clear error.
 
 Collected last (file name) so a stop-at-first-failure run has already run
@@ -39,12 +40,23 @@ def _config(wv, Nx, Ny, Nz):
                             latitude=33.0)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32x2"])
-def test_noalloc_flux_matches_device_entry_on_two_calls(wv, precision):
+# (precision, vertical kernel): each precision's default, and the other kernels
+# the handle can be switched to (the entry point follows the handle's choice)
+VARIANTS = [("fp64", None), ("fp64", "cuda"), ("fp32x2", None), ("fp32x2", "tensor"), ("mixed", "tensor"),
+            ("mixed", "cuda")]
+# 64x64x33, and a rectangular odd grid (radix-3 and radix-5 FFTs, Nz = 25)
+GRIDS = [(64, 64, 33), (60, 45, 25)]
+
+
+@pytest.mark.parametrize("grid", GRIDS, ids=lambda g: "x".join(map(str, g)))
+@pytest.mark.parametrize("precision,vertical", VARIANTS, ids=lambda v: str(v))
+def test_noalloc_flux_matches_device_entry_on_two_calls(wv, precision, vertical, grid):
     import torch
-    c = _config(wv, 64, 64, 33)
+    c = _config(wv, *grid)
     d = O.build_descriptor(O.Config(Nx=c.Nx, Ny=c.Ny, Nz=c.Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, latitude=c.latitude))
     k = wv.WVTransformConstantStratificationKernel(c, precision=precision)
+    if vertical is not None:
+        k.set_vertical_kernel(vertical)
     lib = wv.load_library()
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for seed, (t, t0) in ((11, (500.0, 0.0)), (12, (1234.5, 10.0))):
@@ -58,7 +70,9 @@ def test_noalloc_flux_matches_device_entry_on_two_calls(wv, precision):
         for a, b in zip(got, expected):
             a, b = a.cpu().numpy(), b.cpu().numpy()
             assert np.all(np.isfinite(a))
+            # same kernels on the same inputs: within the FP64 gate (in practice bit for bit)
             assert rel_err(a, b) <= FP64_REL_TOL
+    assert k.device_status() == 0
     k.close()
 
 

@@ -579,24 +579,37 @@ void launch_vinv_flux(wv_handle* h, double elapsed, const double* Ap, const doub
     }
 }
 
+// Device scratch of one flux: the z-grid, y-spectra, product and gathered
+// spectra buffers and the max-speed counter.  The handle's own buffers by
+// default; the static array for wv_nonlinear_flux_device_noalloc.
+struct FluxScratch {
+    void* z;
+    void* y;
+    void* p;
+    void* f;
+    unsigned long long* maxSpeed;
+};
+
 // One nonlinear flux (+ adaptive damping when requested) on device buffers.
 // physOut, when given, receives the x pass's real rows (U, V, W and the
-// derivatives of every target) for the adjoint to reuse.
+// derivatives of every target) for the adjoint to reuse.  scratch, when given,
+// replaces the handle's scratch buffers (the kernel choice stays the handle's).
 template <typename T>
 cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
                         double* Fp, double* Fm, double* F0, bool damping, cudaStream_t s, void* physOut = nullptr,
-                        double* advOut = nullptr, const double* advIn = nullptr) {
+                        double* advOut = nullptr, const double* advIn = nullptr, const FluxScratch* scratch = nullptr) {
     const Plan& p = h->plan;
     const auto& d = h->dd;
     const double elapsed = t - t0;
-    auto* z = static_cast<dev::cx<T>*>(h->zspec);
-    auto* y = static_cast<dev::cx<T>*>(h->yspec);
-    auto* ps = static_cast<dev::cx<T>*>(h->pspec);
-    auto* f = static_cast<dev::cx<T>*>(h->fspec);
+    const FluxScratch sc = scratch ? *scratch : FluxScratch{h->zspec, h->yspec, h->pspec, h->fspec, h->maxSpeed};
+    auto* z = static_cast<dev::cx<T>*>(sc.z);
+    auto* y = static_cast<dev::cx<T>*>(sc.y);
+    auto* ps = static_cast<dev::cx<T>*>(sc.p);
+    auto* f = static_cast<dev::cx<T>*>(sc.f);
     const int nt = p.targets.count;
     const bool inst = h->instrument;
     // max |u_h| is reduced only when adaptive damping consumes it
-    unsigned long long* speed = damping ? h->maxSpeed : nullptr;
+    unsigned long long* speed = damping ? sc.maxSpeed : nullptr;
     if (inst) cudaEventRecord(h->ev[0], s);
     launch_vinv_flux<T>(h, elapsed, Ap, Am, A0, z, speed, y, s);
     if (inst) cudaEventRecord(h->ev[1], s);
@@ -1262,52 +1275,6 @@ size_t static_scratch_layout(const Plan& p, size_t complexBytes, size_t offs[5])
     size_t off = 0;
     for (int i = 0; i < 5; ++i) { offs[i] = off; off += round256(sizes[i]); }
     return off;
-}
-
-// The flux of launch_flux on caller-independent scratch pointers (no damping).
-template <typename T>
-cudaError_t launch_flux_static(wv_handle* h, double t, double t0, const double* Ap, const double* Am, const double* A0,
-                               double* Fp, double* Fm, double* F0, unsigned char* base, const size_t offs[5], cudaStream_t s) {
-    const Plan& p = h->plan;
-    const auto& d = h->dd;
-    const double elapsed = t - t0;
-    auto* z = reinterpret_cast<dev::cx<T>*>(base + offs[0]);
-    auto* y = reinterpret_cast<dev::cx<T>*>(base + offs[1]);
-    auto* ps = reinterpret_cast<dev::cx<T>*>(base + offs[2]);
-    auto* f = reinterpret_cast<dev::cx<T>*>(base + offs[3]);
-    // No damping on this entry, so no max-speed reduction (offs[4] stays reserved).
-    unsigned long long* speed = nullptr;
-    const int nt = p.targets.count;
-    bool fft = false;
-    if constexpr (sizeof(dev::cx<T>) == 16) fft = h->verticalFFT;
-    if constexpr (sizeof(dev::cx<T>) == 16) {
-        if (fft) {
-            constexpr int modes = dev::VzShape<true>::modes;
-            dev::k_vinv_fft<T, true><<<dim3(cdiv(p.Nkl, modes), d.members), 256,
-                                        dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, modes), s>>>(d, Ap, Am, A0, elapsed, z, speed);
-        }
-    }
-    if (!fft)
-        dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
-    dev::YInvMap map{};
-    map.nOut = 4 + 2 * nt;
-    for (int c = 0; c < 4; ++c) { map.src[c] = c; map.mulL[c] = 0; }
-    for (int t2 = 0; t2 < nt; ++t2) {
-        map.src[4 + t2] = p.targets.q[t2]; map.mulL[4 + t2] = 1;
-        map.src[4 + nt + t2] = 4 + t2;     map.mulL[4 + nt + t2] = 0;
-    }
-    launch_yinv<T>(h, map, z, y, s);
-    launch_xflux<T>(h, y, ps, speed, s);
-    launch_yfwd<T>(h, ps, nt, f, s);
-    if constexpr (sizeof(dev::cx<T>) == 16) {
-        if (fft)
-            dev::k_vfwd_fft<T, true><<<dim3(cdiv(p.Nkl, dev::kVfModes), d.members), 256, dev::smem_vfwd_fft<T>(p.fz.N), s>>>(
-                d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
-    }
-    if (!fft)
-        dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
-            d, f, nt, elapsed, Ap, Am, A0, speed, 0, Fp, Fm, F0);
-    return cudaGetLastError();
 }
 
 }  // namespace
@@ -2492,6 +2459,9 @@ int wv_nonlinear_flux_device_noalloc(wv_handle* h, double t, double t0, const do
     if (!h) return WV_INVALID_POINTER;
     int rc = check_times(h, t, t0); if (rc) return rc;
     rc = check_state_flux(h, Ap, Am, A0, Fp, Fm, F0); if (rc) return rc;
+    // the static layout holds one state's scratch
+    if (h->dd.members != 1)
+        return fail(h, WV_UNSUPPORTED_OPERATION, "The static-scratch flux serves single-state handles only.");
     size_t offs[5];
     const size_t need = static_scratch_layout(h->plan, 2 * elem_size(h->precision), offs);
     if (need > kStaticScratchBytes)
@@ -2506,11 +2476,15 @@ int wv_nonlinear_flux_device_noalloc(wv_handle* h, double t, double t0, const do
     if (e != cudaSuccess) return cuda_fail(h, e, "static scratch set-up");
     auto s = static_cast<cudaStream_t>(stream);
     unsigned char* sb = static_cast<unsigned char*>(base);
-    e = h->precision == WV_PRECISION_FP64    ? launch_flux_static<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, sb, offs, s)
-        : h->precision == WV_PRECISION_MIXED ? launch_flux_static<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, sb, offs, s)
-                                             : launch_flux_static<dev::ff>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, sb, offs, s);
+    const FluxScratch sc{sb + offs[0], sb + offs[1], sb + offs[2], sb + offs[3],
+                         reinterpret_cast<unsigned long long*>(sb + offs[4])};
+    // the same launch sequence (and kernel choice) as wv_nonlinear_flux_device, without damping
+    e = h->precision == WV_PRECISION_FP64
+            ? launch_flux<double>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, false, s, nullptr, nullptr, nullptr, &sc)
+        : h->precision == WV_PRECISION_MIXED
+            ? launch_flux<float>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, false, s, nullptr, nullptr, nullptr, &sc)
+            : launch_flux<dev::ff>(h, t, t0, Ap, Am, A0, Fp, Fm, F0, false, s, nullptr, nullptr, nullptr, &sc);
     h->metrics.nonlinear_flux_calls++;
-    h->metrics.kernel_launches += 5;
     return finish(h, e, "nonlinear flux (static scratch)");
 }
 
