@@ -173,6 +173,8 @@ int wv_get_vertical_kernel(const wv_handle* handle, int* kind);
 /* Device status word of the handle (synchronous read): bit 0 is set when a
  * bounded wait inside a kernel ran out (the kernel returned without hanging). */
 int wv_get_device_status(wv_handle* handle, unsigned* status);
+/* Clears the device status word. */
+int wv_reset_device_status(wv_handle* handle);
 int wv_get_stage_times(const wv_handle* handle, wv_stage_times* times);
 
 /* ---- operators (host pointers) ------------------------------------------------------ */
@@ -505,6 +507,31 @@ int wv_rk23_system_step_device(wv_rk23* integrator, double* state, double* t, do
 int wv_rk23_system_advance_to_time_device(wv_rk23* integrator, double* state, double* t, double t0, double final_time,
                                           double initial_step, void* stream);
 int wv_rk23_system_dense_output_device(wv_rk23* integrator, double time, double* state, void* stream);
+
+/* ---- test hooks ----------------------------------------------------------------------
+ * No counterpart in the reference's C ABI.  The reference's contract tests
+ * inject plan, allocation and execution failures through a failing FFT engine
+ * (tools/compiled-kernel/tests/TestWVKernelContract.cpp:153-175,331-355); these
+ * hooks give the GPU library's tests the same reach, on the host, without a
+ * GPU fault.  Not for production use. */
+/* The library's next n device allocations for handles succeed and the one after
+ * fails as cudaErrorMemoryAllocation would (n < 0: off; one-shot). */
+int wv_test_fail_allocation_after(long long n);
+/* Device bytes held by all live handles of this process. */
+long long wv_test_live_device_bytes(void);
+/* The handle's next n flux launch sequences run and the one after fails before
+ * launching anything, reported as WV_FFT_EXECUTION_FAILURE with the message
+ * "...: injected execution failure" (n < 0: off; one-shot). */
+int wv_test_fail_launch_after(wv_handle* handle, long long n);
+/* hold != 0 marks the handle as inside an operation, so every entry returns
+ * WV_REENTRANT_EXECUTION until it is released with hold = 0. */
+int wv_test_hold_busy(wv_handle* handle, int hold);
+/* polls != 0: the tensor-core vertical inverse (k_vinv_tc) waits for its first
+ * matrix operand without the copy being issued, at most `polls` times; the wait
+ * runs out before any MMA, the kernel sets bit 0 of the device status word,
+ * frees its tensor memory and returns (the flux's output is then undefined).
+ * polls = 0 restores normal operation. */
+int wv_test_inject_wait_timeout(wv_handle* handle, unsigned polls);
 
 #ifdef __cplusplus
 }

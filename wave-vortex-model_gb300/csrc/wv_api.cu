@@ -106,9 +106,23 @@ struct wv_handle {
     double* scalarRhs = nullptr;  // [R] doubles (host-pointer entry)
     cudaEvent_t ev[6] = {};
     wv_stage_times stages{};
+    // test hooks (wv_test_*): flux launch sequences to let through before one
+    // fails (-1: off), and whether the last failure was the injected one
+    long long failLaunchAfter = -1;
+    bool injectedFailure = false;
 };
 
 namespace {
+
+// Test hooks: device allocations of the handles to let through before one
+// fails (-1: off), and the device bytes the handles hold right now.
+std::atomic<long long> g_failAllocationAfter{-1};
+std::atomic<long long> g_liveDeviceBytes{0};
+
+bool injected_allocation_failure() {
+    if (g_failAllocationAfter.load() < 0) return false;
+    return g_failAllocationAfter.fetch_sub(1) == 0;
+}
 
 struct Guard {
     std::atomic<bool>& flag;
@@ -124,6 +138,10 @@ int fail(wv_handle* h, int code, const std::string& message) {
 
 int cuda_fail(wv_handle* h, cudaError_t e, const char* where) {
     const int code = e == cudaErrorMemoryAllocation ? WV_ALLOCATION_FAILURE : WV_FFT_EXECUTION_FAILURE;
+    if (h && h->injectedFailure) {
+        h->injectedFailure = false;
+        return fail(h, code, std::string(where) + ": injected execution failure");
+    }
     return fail(h, code, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
@@ -131,10 +149,12 @@ template <typename V>
 cudaError_t upload(wv_handle* h, const std::vector<V>& host, const V** out) {
     void* p = nullptr;
     const size_t bytes = std::max<size_t>(host.size() * sizeof(V), 16);
+    if (injected_allocation_failure()) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) return e;
     h->allocations.push_back(p);
     h->deviceBytes += bytes;
+    g_liveDeviceBytes += static_cast<long long>(bytes);
     if (!host.empty()) e = cudaMemcpy(p, host.data(), host.size() * sizeof(V), cudaMemcpyHostToDevice);
     *out = static_cast<const V*>(p);
     return e;
@@ -143,10 +163,12 @@ cudaError_t upload(wv_handle* h, const std::vector<V>& host, const V** out) {
 cudaError_t alloc(wv_handle* h, size_t bytes, void** out) {
     void* p = nullptr;
     bytes = std::max<size_t>(bytes, 16);
+    if (injected_allocation_failure()) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) return e;
     h->allocations.push_back(p);
     h->deviceBytes += bytes;
+    g_liveDeviceBytes += static_cast<long long>(bytes);
     *out = p;
     return cudaMemset(p, 0, bytes);
 }
@@ -601,6 +623,10 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     const Plan& p = h->plan;
     const auto& d = h->dd;
     const double elapsed = t - t0;
+    if (h->failLaunchAfter >= 0 && h->failLaunchAfter-- == 0) {  // test hook: fail before any launch
+        h->injectedFailure = true;
+        return cudaErrorLaunchFailure;
+    }
     const FluxScratch sc = scratch ? *scratch : FluxScratch{h->zspec, h->yspec, h->pspec, h->fspec, h->maxSpeed};
     auto* z = static_cast<dev::cx<T>*>(sc.z);
     auto* y = static_cast<dev::cx<T>*>(sc.y);
@@ -1352,6 +1378,7 @@ void wv_destroy(wv_handle* h) {
     for (cudaEvent_t ev : {h->slotReady[0], h->slotReady[1], h->slotFree[0], h->slotFree[1], h->fwdDone})
         if (ev) cudaEventDestroy(ev);
     for (void* p : h->allocations) cudaFree(p);
+    g_liveDeviceBytes -= static_cast<long long>(h->deviceBytes);
     cudaSetDevice(prev);
     delete h;
 }
@@ -1630,6 +1657,42 @@ int wv_get_device_status(wv_handle* h, unsigned* status) {
     cudaSetDevice(h->device);
     const cudaError_t e = cudaMemcpy(status, h->dd.status, sizeof(unsigned), cudaMemcpyDeviceToHost);
     return finish(h, e, "device status");
+}
+
+int wv_reset_device_status(wv_handle* h) {
+    if (!h) return WV_INVALID_POINTER;
+    cudaSetDevice(h->device);
+    return finish(h, cudaMemset(h->dd.status, 0, sizeof(unsigned)), "device status");
+}
+
+// ---- test hooks ----------------------------------------------------------------------
+// Failure injection on the host (and one bounded in-kernel wait made to run
+// out): how the contract tests reach the error paths without a GPU fault.
+
+int wv_test_fail_allocation_after(long long n) {
+    g_failAllocationAfter.store(n < 0 ? -1 : n);
+    return WV_SUCCESS;
+}
+
+long long wv_test_live_device_bytes(void) { return g_liveDeviceBytes.load(); }
+
+int wv_test_fail_launch_after(wv_handle* h, long long n) {
+    if (!h) return WV_INVALID_POINTER;
+    h->failLaunchAfter = n < 0 ? -1 : n;
+    h->injectedFailure = false;
+    return WV_SUCCESS;
+}
+
+int wv_test_hold_busy(wv_handle* h, int hold) {
+    if (!h) return WV_INVALID_POINTER;
+    h->busy.store(hold != 0);
+    return WV_SUCCESS;
+}
+
+int wv_test_inject_wait_timeout(wv_handle* h, unsigned polls) {
+    if (!h) return WV_INVALID_POINTER;
+    h->dd.injectWaitPolls = polls;
+    return WV_SUCCESS;
 }
 
 int wv_set_stage_instrumentation(wv_handle* h, int enabled) {

@@ -269,6 +269,7 @@ struct DescDev {
     const void* tcxM;       // ff[Nj]: m_j
     int tcxN, tcxKH, tcxPasses;
     unsigned* status;       // device status word (bit 0: a bounded wait ran out)
+    unsigned injectWaitPolls;  // test hook (0: off): k_vinv_tc's first operand wait gets no copy and this poll limit
     int c2rUseK;            // k_xc2r_fields(_w): bit c set -> channel c is multiplied by i k (x derivative)
     // field-family scales (transformToSpatialDomainWith{F,G}AllDerivatives)
     const double* fWaveScale;   // [M]

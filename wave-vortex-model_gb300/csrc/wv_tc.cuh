@@ -34,13 +34,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the phase with the given parity; false (and the status bit
-// set) if it did not complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* status) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
+// Bounded wait for the phase with the given parity: at most `polls` try_waits;
+// false (and the status bit set) if it did not complete.
+__device__ __forceinline__ bool mbar_wait_polls(uint64_t* bar, uint32_t parity, unsigned* status, uint32_t polls) {
+    for (uint32_t i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     if (status) atomicOr(status, kDeviceTimeout);
     return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* status) {
+    return mbar_wait_polls(bar, parity, status, kWaitLimit);
+}
+// One plain arrival (count 1) on bar.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // ---- bulk async copy (global -> shared), completes on an mbarrier --------------------------

@@ -57,6 +57,7 @@ k_vinv_tc(DescDev d, const double* __restrict__ Ap, const double* __restrict__ A
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[2];  // 0: matrix copies, 1: MMA completion
     __shared__ uint32_t tmemBase;
+    __shared__ int aborted;  // a bounded operand wait ran out: no further MMA, no drain
     const int Nj = d.Nj, Nz = d.Nz, Zh = d.zHalf, P = d.positions, nt = d.nt;
     const int NP = d.tcN, KE = d.tcKE, K = d.tcK;
     const uint32_t aSplit = 256u * static_cast<uint32_t>(K);                                  // 128 rows x K BF16
@@ -79,6 +80,7 @@ k_vinv_tc(DescDev d, const double* __restrict__ Ap, const double* __restrict__ A
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         mbar_init_fence();
+        aborted = 0;
     }
     if (warp == 0) {
         tmem_alloc(&tmemBase, kTcCols);
@@ -139,15 +141,27 @@ k_vinv_tc(DescDev d, const double* __restrict__ Ap, const double* __restrict__ A
     __syncthreads();
 
     uint32_t phaseB = 0, phaseM = 0;
-    for (int tile = 0; tile < 2; ++tile) {
+    for (int tile = 0; tile < 2 && !aborted; ++tile) {
         const uint32_t sAt = sA + static_cast<uint32_t>(tile) * 3u * aSplit;
         // ---- value matrix (half 0), then z-derivative matrix (half 1)
         for (int half = 0; half < 2; ++half) {
             const int mat = tile == 0 ? (half == 0 ? 0 : 3) : (half == 0 ? 1 : 2);  // Ccos, CsinM | Csin, CcosM
             if (tid == 0) {
-                mbar_arrive_expect_tx(&bars[0], 3 * bSplit);
-                bulk_copy_g2s(B, reinterpret_cast<const unsigned char*>(d.tcB) + (size_t)mat * 3 * bSplit, 3 * bSplit, &bars[0]);
-                if (mbar_wait(&bars[0], phaseB, d.status)) {
+                // test hook: the first operand wait gets no copy, so it runs out before any MMA
+                const bool inject = d.injectWaitPolls != 0 && tile == 0 && half == 0;
+                if (!inject) {
+                    mbar_arrive_expect_tx(&bars[0], 3 * bSplit);
+                    bulk_copy_g2s(B, reinterpret_cast<const unsigned char*>(d.tcB) + (size_t)mat * 3 * bSplit, 3 * bSplit, &bars[0]);
+                }
+                const bool landed = inject ? mbar_wait_polls(&bars[0], phaseB, d.status, d.injectWaitPolls)
+                                           : mbar_wait(&bars[0], phaseB, d.status);
+                if (!landed) {
+                    // a copy that was issued is waited for (bounded) before B is reused or
+                    // the CTA exits; then this CTA issues no MMA and releases its waiters
+                    if (!inject) mbar_wait(&bars[0], phaseB, nullptr);
+                    aborted = 1;
+                    mbar_arrive(&bars[1]);
+                } else {
                     tc_fence_after_sync();
                     // pieces (a, b), smallest products first
                     const int pa[6] = {2, 1, 0, 1, 0, 0};
@@ -167,14 +181,17 @@ k_vinv_tc(DescDev d, const double* __restrict__ Ap, const double* __restrict__ A
                             }
                         }
                     }
+                    tc_commit(&bars[1]);
                 }
-                tc_commit(&bars[1]);
             }
             phaseB ^= 1u;
             mbar_wait(&bars[1], phaseM, d.status);  // MMAs done: B is free, accumulators are final
             phaseM ^= 1u;
             tc_fence_after_sync();
+            __syncthreads();  // every thread sees `aborted`
+            if (aborted) break;
         }
+        if (aborted) break;
 
         // ---- drain: row r = 32 (warp % 4) + lane; the four warps of a lane quarter split the column chunks
         {

@@ -180,6 +180,14 @@ def load_library():
     lib.wv_set_vertical_kernel.argtypes = [P, ctypes.c_int]
     lib.wv_get_vertical_kernel.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     lib.wv_get_device_status.argtypes = [P, ctypes.POINTER(ctypes.c_uint)]
+    lib.wv_reset_device_status.argtypes = [P]
+    # test hooks (failure injection for the contract tests)
+    lib.wv_test_fail_allocation_after.argtypes = [ctypes.c_longlong]
+    lib.wv_test_live_device_bytes.argtypes = []
+    lib.wv_test_live_device_bytes.restype = ctypes.c_longlong
+    lib.wv_test_fail_launch_after.argtypes = [P, ctypes.c_longlong]
+    lib.wv_test_hold_busy.argtypes = [P, ctypes.c_int]
+    lib.wv_test_inject_wait_timeout.argtypes = [P, ctypes.c_uint]
     lib.wv_get_stage_times.argtypes = [P, ctypes.POINTER(_StageTimes)]
     for name in ("wv_nonlinear_flux", "wv_evaluate_rhs"):
         getattr(lib, name).argtypes = [P, D, D, P, P, P, P, P, P]
@@ -262,7 +270,9 @@ def exported_symbols():
     """Names of the C entry points this binding expects (declared in include/wvgpu.h)."""
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times",
-            "wv_set_vertical_kernel", "wv_get_vertical_kernel", "wv_get_device_status", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
+            "wv_set_vertical_kernel", "wv_get_vertical_kernel", "wv_get_device_status", "wv_reset_device_status",
+            "wv_test_fail_allocation_after", "wv_test_live_device_bytes", "wv_test_fail_launch_after", "wv_test_hold_busy",
+            "wv_test_inject_wait_timeout", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
             "wv_inverse_device", "wv_rk4_steps_device", "wv_nonlinear_flux_device_noalloc", "wv_flux_vjp_device",
             "wv_inverse_vjp_device", "wv_rk4_step_vjp_device", "wv_rk4_adjoint_device",
