@@ -175,6 +175,11 @@ int wv_get_vertical_kernel(const wv_handle* handle, int* kind);
 int wv_get_device_status(wv_handle* handle, unsigned* status);
 /* Clears the device status word. */
 int wv_reset_device_status(wv_handle* handle);
+/* Per-coefficient absolute error tolerances of the adaptive integrator
+ * (WVWaveVortexCoefficientErrorPolicy::create, PortableRuntime/src/WVForcingEngine.cpp:79-168):
+ * wave[M] for Ap and Am, vortex[M] for A0, [Nj, Nkl] column-major, scaled by
+ * absolute_tolerance_scale.  Host memory; no device work. */
+int wv_error_tolerances(wv_handle* handle, double absolute_tolerance_scale, double* wave, double* vortex);
 int wv_get_stage_times(const wv_handle* handle, wv_stage_times* times);
 
 /* ---- operators (host pointers) ------------------------------------------------------ */

@@ -1659,6 +1659,17 @@ int wv_get_device_status(wv_handle* h, unsigned* status) {
     return finish(h, e, "device status");
 }
 
+int wv_error_tolerances(wv_handle* h, double absolute_tolerance_scale, double* wave, double* vortex) {
+    if (!h) return WV_INVALID_POINTER;
+    if (!wave || !vortex) return fail(h, WV_INVALID_POINTER, "Tolerance outputs must be nonnull.");
+    std::vector<double> w, v;
+    const Status st = wvgpu::adaptive_error_tolerances(h->desc, absolute_tolerance_scale, w, v);
+    if (!st) return fail(h, st.code, st.message);
+    std::memcpy(wave, w.data(), w.size() * sizeof(double));
+    std::memcpy(vortex, v.data(), v.size() * sizeof(double));
+    return WV_SUCCESS;
+}
+
 int wv_reset_device_status(wv_handle* h) {
     if (!h) return WV_INVALID_POINTER;
     cudaSetDevice(h->device);

@@ -181,6 +181,7 @@ def load_library():
     lib.wv_get_vertical_kernel.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     lib.wv_get_device_status.argtypes = [P, ctypes.POINTER(ctypes.c_uint)]
     lib.wv_reset_device_status.argtypes = [P]
+    lib.wv_error_tolerances.argtypes = [P, D, P, P]
     # test hooks (failure injection for the contract tests)
     lib.wv_test_fail_allocation_after.argtypes = [ctypes.c_longlong]
     lib.wv_test_live_device_bytes.argtypes = []
@@ -271,6 +272,7 @@ def exported_symbols():
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times",
             "wv_set_vertical_kernel", "wv_get_vertical_kernel", "wv_get_device_status", "wv_reset_device_status",
+            "wv_error_tolerances",
             "wv_test_fail_allocation_after", "wv_test_live_device_bytes", "wv_test_fail_launch_after", "wv_test_hold_busy",
             "wv_test_inject_wait_timeout", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
