@@ -804,7 +804,7 @@ cudaError_t launch_scalar_advection(wv_handle* h, const double* scalar, const do
     const size_t cb = sizeof(dev::cx<T>);
     const size_t smR2C = (L + p.Nx + 8 * L) * cb + 4 * p.Nx * sizeof(T);
     const size_t smC2R3 = (L + p.Nx + 3 * KX + 8 * L) * cb, smC2R1 = (L + p.Nx + 1 * KX + 8 * L) * cb;
-    const unsigned gridE = static_cast<unsigned>(std::min<size_t>((R + 255) / 256, 152 * 16));
+    const unsigned gridE = static_cast<unsigned>(std::min<size_t>((R + 255) / 256, wvgpu::grid_cap(16)));
     // x r2c, y forward FFT of the scalar (channel 3 of sf), column derivatives (channels 0..2)
     dev::k_xr2c_fields<T><<<dim3(Ny, Nz), 256, smR2C, s>>>(sd, scalar, 1, sp);
     dev::cx<T>* sf3 = sf + (size_t)3 * Nz * P;
@@ -820,7 +820,7 @@ cudaError_t launch_scalar_advection(wv_handle* h, const double* scalar, const do
     if (antialias) {
         dev::k_xr2c_fields<T><<<dim3(Ny, Nz), 256, smR2C, s>>>(sd, rhs, 1, sp);
         dev::k_yfwd<T><<<dim3(cdiv(KX, dev::kYG), Nz, 1), 256, smem_y<T>(p), s>>>(sd, sp, 1, sf);
-        dev::k_scalar_mask<T><<<static_cast<unsigned>(std::min<size_t>((size_t(Nz) * P + 255) / 256, 152 * 16)), 256, 0, s>>>(
+        dev::k_scalar_mask<T><<<static_cast<unsigned>(std::min<size_t>((size_t(Nz) * P + 255) / 256, wvgpu::grid_cap(16))), 256, 0, s>>>(
             sd, sf, h->scalarFlags, hs);
         dev::YInvMap m1{};
         m1.nOut = 1;
@@ -1146,7 +1146,7 @@ cudaError_t rhs_contiguous(wv_handle* h, double t, double t0, const double* y, d
 // contiguous device state h->state.
 cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t s) {
     const size_t n = 6 * h->plan.M * h->dd.members;
-    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, wvgpu::grid_cap(16)));
     const bool dense = h->rk4Dense && h->denseBuf;
     const size_t nb = n * sizeof(double);
     cudaError_t e;
@@ -1177,7 +1177,7 @@ cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t 
 cudaError_t rk4_stages(wv_handle* h, const double* y, double t, double t0, double dt, double* st1, double* st2, double* st3,
                        double* yNext, cudaStream_t s, void* const* ys = nullptr) {
     const size_t n = 6 * h->plan.M;
-    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, wvgpu::grid_cap(16)));
     const size_t M2 = 2 * h->plan.M;
     auto flux = [&](const double* x, double tt, int k) {
         return flux_any(h, tt, t0, x, x + M2, x + 2 * M2, h->kbuf, h->kbuf + M2, h->kbuf + 2 * M2, false, s,
@@ -1207,7 +1207,7 @@ cudaError_t rk4_backward(wv_handle* h, const double* y, const double* st1, const
                          double* ybOut = nullptr) {
     if (!ybOut) ybOut = h->ybacc;
     const size_t n = 6 * h->plan.M;
-    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 16));
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, wvgpu::grid_cap(16)));
     cudaError_t e;
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.0, nullptr, n);
     e = flux_vjp_any(h, t + dt, t0, st3, h->kb, h->sb, s, ys ? ys[3] : nullptr); if (e != cudaSuccess) return e;
@@ -1306,6 +1306,19 @@ size_t static_scratch_layout(const Plan& p, size_t complexBytes, size_t offs[5])
 }  // namespace
 
 namespace wvgpu {
+size_t grid_cap(size_t perSm) {
+    static std::atomic<int> sms[64] = {};
+    int device = 0;
+    cudaGetDevice(&device);
+    if (device < 0 || device >= 64) device = 0;
+    int n = sms[device].load();
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0) n = 1;
+        sms[device].store(n);
+    }
+    return perSm * static_cast<size_t>(n);
+}
+
 const Descriptor& handle_descriptor(const wv_handle* h) { return h->desc; }
 int handle_device(const wv_handle* h) { return h->device; }
 void* handle_stream(const wv_handle* h) { return h->stream; }
@@ -2173,7 +2186,7 @@ int wv_rk4_dense_output_device(wv_handle* h, double time, double* Ap, double* Am
     const double t2 = theta * theta, t3 = t2 * theta, ew = 3 * t2 - 2 * t3, iw = 1 - ew,
                  isw = hstep * (theta - 2 * t2 + t3), esw = hstep * (t3 - t2);
     const size_t n = 6 * h->plan.M, M2 = 2 * h->plan.M;
-    const unsigned grid = static_cast<unsigned>(std::min<size_t>((M2 + 255) / 256, 152 * 16));
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((M2 + 255) / 256, wvgpu::grid_cap(16)));
     const double* b = h->denseBuf;
     dev::k_rk4_dense<<<dim3(grid, 3), 256, 0, static_cast<cudaStream_t>(stream)>>>(b, b + n, b + 2 * n, b + 3 * n, iw, ew, isw,
                                                                                    esw, Ap, Am, A0, M2);

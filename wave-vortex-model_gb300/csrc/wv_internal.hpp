@@ -9,6 +9,10 @@
 
 namespace wvgpu {
 
+// Cap of the grid-stride element-wise launches: perSm blocks per SM of the
+// current device (its multiprocessor count, queried once per device).
+size_t grid_cap(size_t perSm);
+
 const Descriptor& handle_descriptor(const wv_handle* h);
 int handle_device(const wv_handle* h);
 void* handle_stream(const wv_handle* h);  // the stream of the host-pointer entries

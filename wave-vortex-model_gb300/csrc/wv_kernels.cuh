@@ -77,17 +77,43 @@ __device__ __forceinline__ cx<T> twid(const cx<T>* tw, int idx) {
     return INV ? cconj<T>(w) : w;
 }
 
+// Work item `it` of a stage -> (line, j = index within the line's nb butterflies,
+// k = j mod Ns, j / Ns).  Power-of-two lengths (every radix 2 or 4, so nb and Ns
+// are powers of two) use shifts and masks: integer division costs tens of
+// instructions, which the FP32-issue-bound paired-FP32 lines pay per butterfly.
+struct StageIdx {
+    int line, j, k, jq;
+};
+__device__ __forceinline__ StageIdx stage_idx(int it, int nb, int Ns, bool p2, int nbShift, int nsShift) {
+    StageIdx r;
+    if (p2) {
+        r.line = it >> nbShift;
+        r.j = it & (nb - 1);
+        r.k = r.j & (Ns - 1);
+        r.jq = r.j >> nsShift;
+    } else {
+        r.line = it / nb;
+        r.j = it - r.line * nb;
+        r.k = r.j % Ns;
+        r.jq = r.j / Ns;
+    }
+    return r;
+}
+
 template <typename T, bool INV>
 __device__ void fft_stage(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst, int N, int R, int Ns, int lines, int ld,
                           const cx<T>* __restrict__ tw) {
     const int nb = N / R;
     const int tstride = N / (Ns * R);
+    const bool p2 = (N & (N - 1)) == 0;
+    const int nbShift = __ffs(nb) - 1, nsShift = __ffs(Ns) - 1;
     if (R == 4) {
         for (int it = threadIdx.x; it < lines * nb; it += blockDim.x) {
-            const int line = it / nb, j = it - line * nb;
+            const StageIdx ix = stage_idx(it, nb, Ns, p2, nbShift, nsShift);
+            const int line = ix.line, j = ix.j;
             const cx<T>* in = src + line * ld;
             cx<T>* out = dst + line * ld;
-            const int k = j % Ns;
+            const int k = ix.k;
             const int ts = k * tstride;
             cx<T> v0 = in[j], v1 = in[j + nb], v2 = in[j + 2 * nb], v3 = in[j + 3 * nb];
             if (ts) {
@@ -96,7 +122,7 @@ __device__ void fft_stage(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst
                 v3 = cmul<T>(v3, twid<T, INV>(tw, 3 * ts));
             }
             const cx<T> a = cadd<T>(v0, v2), b = csub<T>(v0, v2), c = cadd<T>(v1, v3), d = mul_mi<INV, T>(csub<T>(v1, v3));
-            const int o = (j / Ns) * Ns * 4 + k;
+            const int o = ix.jq * Ns * 4 + k;
             out[o] = cadd<T>(a, c);
             out[o + Ns] = cadd<T>(b, d);
             out[o + 2 * Ns] = csub<T>(a, c);
@@ -104,14 +130,15 @@ __device__ void fft_stage(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst
         }
     } else if (R == 2) {
         for (int it = threadIdx.x; it < lines * nb; it += blockDim.x) {
-            const int line = it / nb, j = it - line * nb;
+            const StageIdx ix = stage_idx(it, nb, Ns, p2, nbShift, nsShift);
+            const int line = ix.line, j = ix.j;
             const cx<T>* in = src + line * ld;
             cx<T>* out = dst + line * ld;
-            const int k = j % Ns;
+            const int k = ix.k;
             const int ts = k * tstride;
             cx<T> v0 = in[j], v1 = in[j + nb];
             if (ts) v1 = cmul<T>(v1, twid<T, INV>(tw, ts));
-            const int o = (j / Ns) * Ns * 2 + k;
+            const int o = ix.jq * Ns * 2 + k;
             out[o] = cadd<T>(v0, v1);
             out[o + Ns] = csub<T>(v0, v1);
         }
@@ -674,8 +701,9 @@ template <typename T>
 __device__ __forceinline__ cx<T> r2c_value(const DescDev& d, const cx<T>* line, int k, const cx<T>* twN) {
     if (d.xEven) {
         const int M = d.Nx >> 1;
-        const cx<T> zk = line[k % M];
-        const cx<T> zn = cconj<T>(line[(M - (k % M)) % M]);
+        const int km = k >= M ? k - M : k;  // k mod M for 0 <= k < 2M
+        const cx<T> zk = line[km];
+        const cx<T> zn = cconj<T>(line[km == 0 ? 0 : M - km]);
         const cx<T> e = mk<T>(T(0.5) * (zk.x + zn.x), T(0.5) * (zk.y + zn.y));
         const cx<T> df = csub<T>(zk, zn);
         const cx<T> o = mk<T>(T(0.5) * df.y, T(-0.5) * df.x);  // (zk - zn) / (2i)
@@ -698,6 +726,8 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
     const int Nx = d.Nx, Ny = d.Ny, KX = d.kxColumns, nt = d.nt, L = d.xLen;
     const int nIn = 4 + 2 * nt;          // U V W N, q_y..., q_z...
     const int nReal = 3 + 3 * nt;        // U V W, then (q_x, q_y, q_z) per target
+    const bool lPow2 = (L & (L - 1)) == 0;
+    const int lShift = __ffs(L) - 1;
     const int y = blockIdx.x, z = blockIdx.y;
     cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);  // [L]
     cx<T>* twN = tw + L;                              // [Nx]
@@ -731,7 +761,7 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
     for (int rb = 0; rb < nReal; rb += 8) {
         const int nr = min(8, nReal - rb);
         for (int i = threadIdx.x; i < nr * L; i += blockDim.x) {
-            const int li = i / L, k = i - li * L;
+            const int li = lPow2 ? i >> lShift : i / L, k = i - li * L;
             int ch; bool useK;
             rowSrc(rb + li, ch, useK);
             bufA[li * L + k] = c2r_line_entry<T>(d, yrow + ch * cstride, k, useK, twN);
@@ -792,7 +822,7 @@ __global__ void __launch_bounds__(256) k_xflux(DescDev d, const cx<T>* __restric
     }
     // forward real transform of each S_q
     for (int i = threadIdx.x; i < nt * L; i += blockDim.x) {
-        const int t = i / L, n = i - t * L;
+        const int t = lPow2 ? i >> lShift : i / L, n = i - t * L;
         bufB[t * L + n] = r2c_line_entry<T>(d, S + t * Nx, n);
     }
     __syncthreads();

@@ -166,7 +166,7 @@ struct DeviceRk23Backend {
 
     size_t packed() const { return 6 * M + nExtra; }
     unsigned components() const { return nExtra ? 4u : 3u; }
-    unsigned grid_for(size_t n) const { return static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 8)); }
+    unsigned grid_for(size_t n) const { return static_cast<unsigned>(std::min<size_t>((n + 255) / 256, wvgpu::grid_cap(8))); }
     int cuda(cudaError_t e, const char* where) {
         if (e == cudaSuccess) return WV_SUCCESS;
         msg = std::string(where) + ": " + cudaGetErrorString(e);

@@ -302,7 +302,7 @@ void release(wv_system* s) {
         if (p) cudaFree(p);
 }
 
-unsigned grid_for(size_t n) { return static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 152 * 8)); }
+unsigned grid_for(size_t n) { return static_cast<unsigned>(std::min<size_t>((n + 255) / 256, wvgpu::grid_cap(8))); }
 
 // evaluateRightHandSide on packed device arrays (no guard; callers hold it).
 int rhs_impl(wv_system* s, double t, double t0, const double* x, double* k, cudaStream_t st) {
