@@ -342,6 +342,8 @@ def _stage_profile(k, dev, t, t0, dt, precision, torch):
     return {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "compute": compute,
             "frac": achieved / peaks["hbm_gbs"], "traffic": traffic_from_profile(dominant, precision),
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch from a committed ncu capture "
+                              "of this kernel on this workload (profiles/ncu_traffic.txt), not from this run",
             "peak_source": peak_kind, "algorithmic_bytes_per_launch": sbytes[dominant],
             "avg_launch_ms": per_launch[dominant], "stage_ms_per_flux": per_launch,
             "flux": {"algorithmic_bytes": b_flux, "ms": flux_ms, "achieved_gbs": b_flux / (flux_ms * 1e-3) / 1e9,
