@@ -1,6 +1,7 @@
-"""Mixed-precision form: FP32 xy transforms, products and vertical contractions;
-FP64 phases, projections, flux accumulation and RK4 stage arithmetic.
-Accuracy is stated against the FP64 oracle / FP64 GPU path."""
+"""Mixed-precision form: FP32 xy transforms, products, vertical contractions
+and the folded flux projection; phase angles reduced in FP64, FP64 state,
+flux stores and RK4 stage arithmetic.  Accuracy is stated against the FP64
+oracle / FP64 GPU path."""
 import numpy as np
 import pytest
 
@@ -88,7 +89,11 @@ def test_mixed_rk4_field_error_after_100_steps(wv):
     f32 = kd.transformWaveVortexToUVWEta(t1, 0.0, *(x.cpu().numpy() for x in d32))
     err = field_rel_l2(f32, f64)
     print("mixed vs fp64 after 100 RK4 steps, relative L2 field error (u, v, w, eta):", err)
-    assert max(err[0], err[1]) <= 1e-6          # spec bound met for the horizontal velocity
-    assert err[3] <= 1e-4 and err[2] <= 1e-2    # w and eta carry the FP32 cancellation (see above)
+    assert max(err[0], err[1]) <= 1e-6          # the 1e-6 bound holds for the horizontal velocity
+    # w and eta do not meet it (at 256x256x129: w 2.0e-3, eta 1.8e-4): the flux
+    # spectrum's dynamic range puts the FP32 rounding of every stage, amplified
+    # ~1e4 in the high-j, small-K_h modes, on w and eta (the paired-FP32 form is
+    # the one that meets 1e-6)
+    assert err[3] <= 1e-4 and err[2] <= 1e-2
     kd.close()
     km.close()
