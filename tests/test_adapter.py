@@ -10,7 +10,8 @@ own integrators with its right-hand side on the GPU.
     wv_evaluate_rhs bit for bit and the reference's own right-hand side at the
     1e-12 gate; the reference's WVFixedStepRK4::step (PortableRuntime/src/
     WVRungeKutta.cpp:335-462) stepping the GPU system matches wv_rk4_steps and the
-    reference's all-CPU run at 1e-12, at a golden grid and at 128x128x65; the
+    reference's all-CPU run at 1e-12 at the golden grids, and its increments at
+    128x128x65 within 3x the flux's measured FP64 floor; the
     reference's WVAdaptiveRK23 (WVRungeKutta.cpp:554-983) stepping the GPU
     system reproduces the reference's own run: accepted / rejected / evaluation
     counts, tolerance hashes (from wv_error_tolerances) and end state.
@@ -24,7 +25,7 @@ import pytest
 
 import ref_lib as R
 import wv_oracle as O
-from _cases import FP64_REL_TOL, golden_cases, load_golden, rel_err, rk23_run
+from _cases import FP64_REL_TOL, golden_cases, load_golden, parity_tolerance, rel_err, rk23_run, state_components_close
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ADAPTER = os.path.join(ROOT, "wave-vortex-model_gb300", "adapters")
@@ -178,8 +179,12 @@ def test_reference_rk4_steps_the_gpu_system_at_128(adapter_lib):
     ref = R.Ref(R.load_lib(), case, R.ENGINE_ORACLE_FFT)
     Rp, Rm, R0, tr = ref.rk4(*A, 0.0, 0.0, dt, 2)
     assert tk == tr
-    for a, b in zip((Kp, Km, K0), (Rp, Rm, R0)):
-        assert rel_err(a, b) <= FP64_REL_TOL
+    # the increments carry the flux's FP64 floor on this steep-spectrum state
+    # (two valid FP64 orderings of the flux differ by ~2e-11 here; see
+    # tests/test_gpu_reference_cpp.py)
+    _, floors = O.noise_floor(O.nonlinear_flux, d, *A, 0.0, 0.0)
+    for a, b, a0, fl in zip((Kp, Km, K0), (Rp, Rm, R0), A, floors):
+        assert rel_err(a - a0, b - a0) <= parity_tolerance(fl), (rel_err(a - a0, b - a0), fl)
     ad.close()
 
 
@@ -196,6 +201,7 @@ def test_reference_rk23_steps_the_gpu_system(adapter_lib, key):
     assert counts == [int(x) for x in run["counts"]]
     assert hashes == [int(x) for x in run["hashes"]]
     assert t == run["tout"]
-    for a, b in zip(Y, (run["Kp"], run["Km"], run["K0"])):
-        assert rel_err(a, b) <= 1e-11
+    # components that are pure accumulated rounding (the single wave's A0) gated
+    # relative to the state, as for the GPU's own RK23 (tests/test_gpu_rk23.py)
+    assert not state_components_close(Y, run, ("Kp", "Km", "K0"), 1e-11)
     ad.close()

@@ -14,8 +14,9 @@ PortableRuntime/tests/TestWVForcingAndRK4.cpp:276-305).
 
 Workload: 16x16x9 and 32x32x17 over 40 km x 40 km x 1 km, N0 5.2e-3, latitude
 45 (the configs[0] domain), seeded spectrum state at 1 m/s rms (strong enough
-that truncation error sits far above paired-FP32 rounding), schedule
-{nonlinear advection, adaptive damping}, t = 0 .. 600 s, checkpoint at 300 s.
+that truncation error sits far above paired-FP32 rounding), t = 0 .. 600 s,
+checkpoint at 300 s; schedule {nonlinear advection, adaptive damping} for the
+segmented / restarted runs, nonlinear advection for the convergence order.
 """
 import numpy as np
 import pytest
@@ -39,13 +40,13 @@ def wv():
     return wvgpu
 
 
-def _setup(wv, N, Nz, precision):
+def _setup(wv, N, Nz, precision, damping=True):
     c = O.Config(Nx=N, Ny=N, Nz=Nz, Nj=O.default_nj(Nz), Lx=40e3, Ly=40e3, Lz=1000.0, N0=5.2e-3, latitude=45.0)
     d = O.build_descriptor(c)
     A = O.spectrum_state(d, seed=7, urms=1.0)
     k = wv.WVTransformConstantStratificationKernel(wv.Configuration(
         Nx=N, Ny=N, Nz=Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, N0=c.N0, latitude=c.latitude), precision=precision)
-    k.set_forcing(nonlinear=True, adaptive_damping=True)
+    k.set_forcing(nonlinear=True, adaptive_damping=damping)
     return c, d, A, k
 
 
@@ -85,7 +86,10 @@ def test_segmented_and_restarted_equal_uninterrupted(wv, grid, precision):
 @pytest.mark.parametrize("precision", ["fp64", "fp32x2"])
 @pytest.mark.parametrize("grid", GRIDS, ids=lambda g: f"{g[0]}x{g[0]}x{g[1]}")
 def test_fixed_step_converges_at_fourth_order(wv, grid, precision):
-    c, d, A, k = _setup(wv, *grid, precision)
+    # nonlinear advection alone: adaptive damping scales the flux by max |u_h|
+    # over the grid, which is only piecewise smooth in the state (its arg max
+    # can move between stages), so with it the observed order falls below four
+    c, d, A, k = _setup(wv, *grid, precision, damping=False)
 
     def err(a, b):
         return max(np.max(np.abs(x - y)) for x, y in zip(a, b)) / max(max(np.max(np.abs(y)) for y in b),
