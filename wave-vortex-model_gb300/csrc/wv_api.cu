@@ -2473,28 +2473,32 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
     for (int i = 0; i < n; ++i) times[i + 1] = times[i] + dt;
     auto slotOf = [&](int seg) { return pipelined ? (seg & 1) : 0; };
     // Stage states (and real rows) of the steps first..last-1 from the state in the
-    // slot's first entry, the state of each next step in the following entry.
-    auto record = [&](int first, int last, int slot, cudaStream_t st) {
+    // slot's first entry, the state of each next step in the following entry;
+    // endOut, when given, receives the state after the last step.
+    auto record = [&](int first, int last, int slot, cudaStream_t st, double* endOut) {
         cudaError_t r = cudaSuccess;
         for (int i = first; i < last && r == cudaSuccess; ++i) {
             double** q = h->segment.data() + 4 * K * slot + 4 * (i - first);
             void* const* ys = keepY ? h->ystore.data() + 4 * K * slot + 4 * (i - first) : nullptr;
-            r = rk4_stages(h, q[0], times[i], t0, dt, q[1], q[2], q[3], i + 1 < last ? q[4] : nullptr, st, ys);
+            r = rk4_stages(h, q[0], times[i], t0, dt, q[1], q[2], q[3], i + 1 < last ? q[4] : endOut, st, ys);
         }
         return r;
     };
-    // forward pass: checkpoints at the start of each segment; the last segment
-    // is recorded directly, so its recomputation is skipped
+    // forward pass: checkpoints at the start of each segment; the segments that
+    // have a slot of their own from the start -- the last one, and with two slots
+    // the one before it -- are recorded directly, so their recomputation is skipped
+    const int directSeg = pipelined && ncp >= 2 ? ncp - 2 : -1;
     e = gather3(h, h->state, Ap, Am, A0, s);
     for (int seg = 0; seg < ncp && e == cudaSuccess; ++seg) {
         const int first = seg * K, last = std::min(n, first + K);
-        if (seg + 1 < ncp) {
+        if (seg + 1 < ncp && seg != directSeg) {
             e = cudaMemcpyAsync(h->checkpoints[seg], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
             for (int i = first; i < last && e == cudaSuccess; ++i) e = rk4_step(h, times[i], t0, dt, s);
         } else {
+            // the same stage arithmetic as rk4_step, so the states are those a recomputation gives
             const int sl = slotOf(seg);
             e = cudaMemcpyAsync(h->segment[4 * K * sl], h->state, stateBytes, cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess) e = record(first, last, sl, s);
+            if (e == cudaSuccess) e = record(first, last, sl, s, seg + 1 < ncp ? h->state : nullptr);
         }
     }
     if (e == cudaSuccess) e = gather3(h, h->ybin, Apb, Amb, A0b, s);
@@ -2514,17 +2518,21 @@ int wv_rk4_adjoint_device(wv_handle* h, const double* Ap, const double* Am, cons
         if (pipelined) {
             if (seg >= 1) {
                 const int ps = slotOf(seg - 1), pf = (seg - 1) * K, pl = std::min(n, pf + K);
-                e = cudaStreamWaitEvent(h->adjStream, h->slotFree[ps], 0);
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync(h->segment[4 * K * ps], h->checkpoints[seg - 1], stateBytes, cudaMemcpyDeviceToDevice,
-                                        h->adjStream);
-                if (e == cudaSuccess) e = record(pf, pl, ps, h->adjStream);
-                if (e == cudaSuccess) e = cudaEventRecord(h->slotReady[ps], h->adjStream);
+                if (seg - 1 == directSeg) {
+                    e = cudaEventRecord(h->slotReady[ps], s);  // recorded by the forward pass on this stream
+                } else {
+                    e = cudaStreamWaitEvent(h->adjStream, h->slotFree[ps], 0);
+                    if (e == cudaSuccess)
+                        e = cudaMemcpyAsync(h->segment[4 * K * ps], h->checkpoints[seg - 1], stateBytes,
+                                            cudaMemcpyDeviceToDevice, h->adjStream);
+                    if (e == cudaSuccess) e = record(pf, pl, ps, h->adjStream, nullptr);
+                    if (e == cudaSuccess) e = cudaEventRecord(h->slotReady[ps], h->adjStream);
+                }
             }
             if (e == cudaSuccess && seg + 1 < ncp) e = cudaStreamWaitEvent(s, h->slotReady[sl], 0);
         } else if (seg + 1 < ncp) {
             e = cudaMemcpyAsync(h->segment[0], h->checkpoints[seg], stateBytes, cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess) e = record(first, last, 0, s);
+            if (e == cudaSuccess) e = record(first, last, 0, s, nullptr);
         }
         for (int i = last - 1; i >= first && e == cudaSuccess; --i) {
             double** q = h->segment.data() + 4 * K * sl + 4 * (i - first);
