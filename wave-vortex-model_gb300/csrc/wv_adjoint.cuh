@@ -165,6 +165,15 @@ __global__ void __launch_bounds__(256) k_vfwd_adj(DescDev d, const double* __res
 
 // physIn, when given, holds the forward real rows [z][nReal][y][Nx] (as
 // k_xflux keeps them); otherwise they are recomputed from yspec.
+//
+// Like k_xflux, the row's forward spectra are read from L2 where the lines are
+// built, and only what the product adjoint needs stays in shared memory: U, V,
+// W and the adjoint rows S_q-bar (3 + nt rows); each derivative row is folded
+// into the velocity gradients as soon as it is available, in row order
+// (g_U -= S_q-bar q_x, g_V -= S_q-bar q_y, g_W -= S_q-bar q_z), and the
+// derivative rows' own gradients (-S_q-bar U, -S_q-bar V, -S_q-bar W) are
+// formed while their r2c lines are built.  About 69 KB of shared memory at
+// Nx = 256 (paired FP32 / FP64), three CTAs per SM.
 template <typename T>
 __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict__ yspec, const cx<T>* __restrict__ yadj,
                                              cx<T>* __restrict__ yout, const T* __restrict__ physIn) {
@@ -175,34 +184,30 @@ __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict
     const int y = blockIdx.x, z = blockIdx.y;
     cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);   // [L]
     cx<T>* twN = tw + L;                               // [Nx]
-    cx<T>* specF = twN + Nx;                           // [nIn][KX]
-    cx<T>* specA = specF + nIn * KX;                   // [nt][KX]
-    cx<T>* bufA = specA + nt * KX;                     // [8][L]
+    cx<T>* specA = twN + Nx;                           // [nt][KX] adjoint spectra, interior kx halved
+    cx<T>* out4 = specA + nt * KX;                     // [4][KX] output channels U, V, W, N
+    cx<T>* bufA = out4 + 4 * KX;                       // [8][L]
     cx<T>* bufB = bufA + 8 * L;
-    T* phys = reinterpret_cast<T*>(bufB + 8 * L);     // [nReal][Nx] forward rows
-    T* sbar = phys + nReal * Nx;                       // [nt][Nx]
-    T* grad = sbar + nt * Nx;                          // [nReal][Nx]
+    T* base = reinterpret_cast<T*>(bufB + 8 * L);     // [3 + nt][Nx]: U, V, W, then S_q-bar per target
+    T* gacc = base + (3 + nt) * Nx;                    // [3][Nx]: gradients of U, V, W
+    const cx<T>* yrow = yspec + ((size_t)z * nIn * Ny + y) * KX;
+    const size_t cstride = (size_t)Ny * KX;
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
     const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
     for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = twg[i];
     for (int i = threadIdx.x; i < Nx; i += blockDim.x) twN[i] = twgN[i];
-    if (physIn) {
-        for (int i = threadIdx.x; i < nReal * Nx; i += blockDim.x) {
-            const int r = i / Nx, x = i - r * Nx;
-            phys[i] = physIn[(((size_t)z * nReal + r) * Ny + y) * Nx + x];
-        }
-    } else {
-        for (int i = threadIdx.x; i < nIn * KX; i += blockDim.x) {
-            const int c = i / KX, k = i - c * KX;
-            specF[i] = yspec[(((size_t)z * nIn + c) * Ny + y) * KX + k];
-        }
-    }
     for (int i = threadIdx.x; i < nt * KX; i += blockDim.x) {
         const int c = i / KX, k = i - c * KX;
         cx<T> v = yadj[(((size_t)z * nt + c) * Ny + y) * KX + k];
         if (k > 0) v = mk<T>(T(0.5) * v.x, T(0.5) * v.y);  // adjoint of r2c: interior kx at weight 1/2 under c2r
         specA[i] = v;
     }
+    for (int i = threadIdx.x; i < 3 * Nx; i += blockDim.x) gacc[i] = T(0);
+    if (physIn)
+        for (int i = threadIdx.x; i < 3 * Nx; i += blockDim.x) {
+            const int r = i / Nx, x = i - r * Nx;
+            base[i] = physIn[(((size_t)z * nReal + r) * Ny + y) * Nx + x];
+        }
     __syncthreads();
     auto rowSrc = [&](int r, int& ch, bool& useK) {
         if (r < 3) { ch = r; useK = false; return; }
@@ -212,85 +217,104 @@ __global__ void __launch_bounds__(256) k_xadj(DescDev d, const cx<T>* __restrict
         else if (kind == 1) { ch = 4 + t; useK = false; }
         else { ch = 4 + nt + t; useK = false; }
     };
-    // c2r: forward rows (nReal, unless kept) then adjoint rows (nt)
-    const int nC2R = nReal + nt;
-    for (int rb = physIn ? nReal : 0; rb < nC2R; rb += 8) {
-        const int nr = min(8, nC2R - rb);
+    // c2r rows, in batches of 8: rows 0..2 U, V, W (unless kept), 3..2+nt the
+    // adjoint rows S_q-bar, then the derivative rows q_x, q_y, q_z of each target
+    // (unless kept), each folded into the gradients of U, V, W as it arrives
+    auto rowOf = [&](int i) { return i < 3 ? i : (i < 3 + nt ? -1 - (i - 3) : i - nt); };  // -1 - t: adjoint row t
+    const int nRows = nReal + nt;
+    for (int rb = physIn ? 3 : 0; rb < nRows; rb += 8) {
+        const int nr = physIn ? min(8, 3 + nt - rb) : min(8, nRows - rb);
+        if (nr <= 0) break;
         for (int i = threadIdx.x; i < nr * L; i += blockDim.x) {
             const int li = i / L, k = i - li * L;
-            const int r = rb + li;
-            if (r < nReal) {
+            const int r = rowOf(rb + li);
+            if (r >= 0) {
                 int ch; bool useK;
                 rowSrc(r, ch, useK);
-                bufA[li * L + k] = c2r_line_entry<T>(d, specF + ch * KX, k, useK, twN);
+                bufA[li * L + k] = c2r_line_entry<T>(d, yrow + ch * cstride, k, useK, twN);
             } else {
-                bufA[li * L + k] = c2r_line_entry<T>(d, specA + (r - nReal) * KX, k, false, twN);
+                bufA[li * L + k] = c2r_line_entry<T>(d, specA + (-1 - r) * KX, k, false, twN);
             }
         }
         __syncthreads();
         cx<T>* res = fft_lines<T, true>(bufA, bufB, d.fx, nr, L, tw);
-        for (int i = threadIdx.x; i < nr * Nx; i += blockDim.x) {
-            const int li = i / Nx, x = i - li * Nx;
-            const int r = rb + li;
-            const T v = c2r_sample<T>(d, res + li * L, x);
-            if (r < nReal) phys[r * Nx + x] = v; else sbar[(r - nReal) * Nx + x] = v;
+        for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+            for (int li = 0; li < nr; ++li) {
+                const int r = rowOf(rb + li);
+                const T v = c2r_sample<T>(d, res + li * L, x);
+                if (r < 0) base[(3 + (-1 - r)) * Nx + x] = v;
+                else if (r < 3) base[r * Nx + x] = v;
+                else {
+                    const int t = (r - 3) / 3, kind = (r - 3) % 3;
+                    gacc[kind * Nx + x] -= base[(3 + t) * Nx + x] * v;
+                }
+            }
         }
         __syncthreads();
     }
-    // product adjoint: S_q = -(U q_x + V q_y + W q_z)
-    for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
-        const T U = phys[0 * Nx + x], V = phys[1 * Nx + x], W = phys[2 * Nx + x];
-        T gu = T(0), gv = T(0), gw = T(0);
-        for (int t = 0; t < nt; ++t) {
-            const T sb = sbar[t * Nx + x];
-            gu -= sb * phys[(3 + 3 * t) * Nx + x];
-            gv -= sb * phys[(4 + 3 * t) * Nx + x];
-            gw -= sb * phys[(5 + 3 * t) * Nx + x];
-            grad[(3 + 3 * t) * Nx + x] = -sb * U;
-            grad[(4 + 3 * t) * Nx + x] = -sb * V;
-            grad[(5 + 3 * t) * Nx + x] = -sb * W;
-        }
-        grad[0 * Nx + x] = gu;
-        grad[1 * Nx + x] = gv;
-        grad[2 * Nx + x] = gw;
+    if (physIn) {
+        // kept derivative rows: folded in row order, as above
+        for (int x = threadIdx.x; x < Nx; x += blockDim.x)
+            for (int r = 3; r < nReal; ++r) {
+                const int t = (r - 3) / 3, kind = (r - 3) % 3;
+                const T v = physIn[(((size_t)z * nReal + r) * Ny + y) * Nx + x];
+                gacc[kind * Nx + x] -= base[(3 + t) * Nx + x] * v;
+            }
+        __syncthreads();
     }
-    __syncthreads();
-    // r2c of the gradient rows (adjoint of c2r: interior kx doubled); results kept in specF (reused)
-    cx<T>* gspec = specF;  // [nReal][KX] (nReal*KX <= nIn*KX + nt*KX: specF and specA are contiguous)
+    // r2c of the gradient rows (adjoint of c2r: interior kx doubled): rows 0..2
+    // the gradients of U, V, W, row 3 + 3 t + kind = -S_q-bar times U, V or W
     for (int rb = 0; rb < nReal; rb += 8) {
         const int nr = min(8, nReal - rb);
         for (int i = threadIdx.x; i < nr * L; i += blockDim.x) {
             const int li = i / L, n = i - li * L;
-            bufA[li * L + n] = r2c_line_entry<T>(d, grad + (rb + li) * Nx, n);
+            const int r = rb + li;
+            cx<T> e;
+            if (r < 3) {
+                e = r2c_line_entry<T>(d, gacc + r * Nx, n);
+            } else {
+                const int t = (r - 3) / 3, kind = (r - 3) % 3;
+                const T* sb = base + (3 + t) * Nx;
+                const T* vel = base + kind * Nx;
+                if (d.xEven) e = mk<T>(-sb[2 * n] * vel[2 * n], -sb[2 * n + 1] * vel[2 * n + 1]);
+                else e = mk<T>(-sb[n] * vel[n], T(0));
+            }
+            bufA[li * L + n] = e;
         }
         __syncthreads();
         cx<T>* res = fft_lines<T, false>(bufA, bufB, d.fx, nr, L, tw);
-        for (int i = threadIdx.x; i < nr * KX; i += blockDim.x) {
-            const int li = i / KX, k = i - li * KX;
-            cx<T> v = r2c_value<T>(d, res + li * L, k, twN);
-            if (k > 0) v = mk<T>(T(2) * v.x, T(2) * v.y);
-            gspec[(rb + li) * KX + k] = v;
+        // one thread per kx walks the batch's rows in order: a channel's own row
+        // (0..2) lands in out4 before its target's x-derivative row adds to it
+        for (int k = threadIdx.x; k < KX; k += blockDim.x) {
+            for (int li = 0; li < nr; ++li) {
+                const int r = rb + li;
+                cx<T> v = r2c_value<T>(d, res + li * L, k, twN);
+                if (k > 0) v = mk<T>(T(2) * v.x, T(2) * v.y);
+                // combine into the forward y-spectrum channel layout
+                if (r < 3) {
+                    out4[r * KX + k] = v;
+                } else {
+                    const int t = (r - 3) / 3, kind = (r - 3) % 3;
+                    if (kind == 0) {  // x-derivative row of target q: (i k)^* = -i k onto channel q
+                        const int c = d.tq[t];
+                        const cx<T> base4 = c < 3 ? out4[c * KX + k] : mk<T>(T(0), T(0));
+                        const T kk = row_k<T>(d)[k];
+                        out4[c * KX + k] = mk<T>(base4.x + kk * v.y, base4.y - kk * v.x);
+                    } else {
+                        const int c = kind == 1 ? 4 + t : 4 + nt + t;
+                        yout[(((size_t)z * nIn + c) * Ny + y) * KX + k] = v;
+                    }
+                }
+            }
         }
         __syncthreads();
     }
-    // combine into the forward y-spectrum channel layout
-    for (int i = threadIdx.x; i < nIn * KX; i += blockDim.x) {
+    for (int i = threadIdx.x; i < 4 * KX; i += blockDim.x) {
         const int c = i / KX, k = i - c * KX;
-        cx<T> v = mk<T>(T(0), T(0));
-        if (c < 4) {
-            if (c < 3) v = gspec[c * KX + k];
-            for (int t = 0; t < nt; ++t) {
-                if (d.tq[t] == c) {  // x-derivative row of target c: (i k)^* = -i k
-                    const cx<T> g = gspec[(3 + 3 * t) * KX + k];
-                    const T kk = row_k<T>(d)[k];
-                    v = mk<T>(v.x + kk * g.y, v.y - kk * g.x);
-                }
-            }
-        } else if (c < 4 + nt) {
-            v = gspec[(4 + 3 * (c - 4)) * KX + k];
-        } else {
-            v = gspec[(5 + 3 * (c - 4 - nt)) * KX + k];
-        }
+        // channels without an x-derivative row (eta in the hydrostatic targets) get their own row or zero
+        bool hasTarget = false;
+        for (int t = 0; t < nt; ++t) hasTarget |= d.tq[t] == c;
+        const cx<T> v = hasTarget || c < 3 ? out4[i] : mk<T>(T(0), T(0));
         yout[(((size_t)z * nIn + c) * Ny + y) * KX + k] = v;
     }
 }

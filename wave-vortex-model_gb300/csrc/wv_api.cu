@@ -926,8 +926,8 @@ template <typename T>
 size_t smem_vfwd_adj(const Plan& p) { return p.targets.count * p.Nj * dev::kVfwdModes * sizeof(dev::cx<T>); }
 template <typename T>
 size_t smem_xadj(const Plan& p) {
-    const size_t nt = p.targets.count, L = x_len(p), nIn = 4 + 2 * nt, nReal = 3 + 3 * nt;
-    return (L + p.Nx + (nIn + nt) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (2 * nReal + nt) * p.Nx * sizeof(T);
+    const size_t nt = p.targets.count, L = x_len(p);
+    return (L + p.Nx + (nt + 4) * p.kxColumns + 16 * L) * sizeof(dev::cx<T>) + (3 + nt + 3) * p.Nx * sizeof(T);
 }
 template <typename T>
 size_t smem_xadj_w(const Plan& p) {
