@@ -20,9 +20,15 @@ struct __align__(8) ff {
     float hi, lo;
     ff() = default;
     __host__ __device__ constexpr ff(float h, float l) : hi(h), lo(l) {}
-    __host__ __device__ ff(double v) : hi(static_cast<float>(v)), lo(static_cast<float>(v - static_cast<double>(static_cast<float>(v)))) {}
-    __host__ __device__ ff(float v) : hi(v), lo(0.0f) {}
-    __host__ __device__ ff(int v) : ff(static_cast<double>(v)) {}
+    // constexpr so that literals (T(0.5), T(2), ...) fold at compile time instead
+    // of running FP64 conversions in device code
+    __host__ __device__ constexpr ff(double v)
+        : hi(static_cast<float>(v)), lo(static_cast<float>(v - static_cast<double>(static_cast<float>(v)))) {}
+    __host__ __device__ constexpr ff(float v) : hi(v), lo(0.0f) {}
+    // integers without FP64: hi = v rounded to FP32, lo = the exact remainder
+    __host__ __device__ constexpr ff(int v)
+        : hi(static_cast<float>(v)),
+          lo(static_cast<float>(static_cast<long long>(v) - static_cast<long long>(static_cast<float>(v)))) {}
     __host__ __device__ explicit operator double() const { return static_cast<double>(hi) + static_cast<double>(lo); }
     __host__ __device__ explicit operator float() const { return hi + lo; }
 };
