@@ -10,10 +10,13 @@ one inverse/forward round trip, 0.1 m/s rms velocity); dt = 0.5 x the CFL limit.
 
   value : device-timed RK4 steps/s, state resident in HBM (CUDA events on the
           launching stream, L2 flushed between steps)
-  e2e   : the same through the host-pointer C ABI (wv_rk4_steps), state copied
-          host->device and back every step, wall-clock timed
-  --impl reference : the CPU oracle restatement of the reference algorithm
-          (numpy/scipy, all host threads), on the same workload
+  e2e   : the same through the host-pointer C ABI (wv_rk4_steps on the caller's
+          pinned arrays), state copied host->device and back every step,
+          wall-clock timed
+  --impl reference : the reference's own C++ step (WVFixedStepRK4 over its
+          CompiledKernel flux, built by oracle/ref_build.sh with the oracle's
+          O(N log N) FFT engine) on every host thread, same workload; the numpy
+          restatement only where the C++ cannot be built
 """
 from __future__ import annotations
 
@@ -600,17 +603,27 @@ def run_ours(args):
     ensemble = _ensemble_timing(wvgpu, stream, torch, np) if rank == 0 and not args.no_ensemble else None
     published = _published_flux_comparison(wvgpu, torch, np) if rank == 0 else None
 
-    # end to end through the host-pointer C ABI, pinned host buffers
+    # end to end through the host-pointer C ABI (wv_rk4_steps, the call the
+    # reference's C++ / MEX callers make): the caller's pinned host arrays are
+    # copied to the device, stepped and copied back in place on every call
     host = [torch.empty(a.shape, dtype=torch.complex128, pin_memory=True).numpy() for a in state]
     for hbuf, a in zip(host, state):
         hbuf[...] = a
-    te = 0.0
-    k.rk4(*host, te, t0, dt, 1)  # warm the host path
+    import ctypes
+    lib = wvgpu.load_library()
+    te = ctypes.c_double(0.0)
+
+    def host_step():
+        rc = lib.wv_rk4_steps(k._h, host[0].ctypes.data, host[1].ctypes.data, host[2].ctypes.data, ctypes.byref(te),
+                              float(t0), float(dt), 1)
+        if rc != 0:
+            raise RuntimeError(lib.wv_last_message(k._h).decode())
+
+    host_step()  # warm the host path
     barrier()
     w0 = time.perf_counter()
     for _ in range(args.steps):
-        Ap, Am, A0, te = k.rk4(*host, te, t0, dt, 1)
-        host[0][...], host[1][...], host[2][...] = Ap, Am, A0
+        host_step()
     e2e_s = max_over_ranks(time.perf_counter() - w0)
     M = k.sizes["M"]
     coeff_bytes = 3 * M * 16
