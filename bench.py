@@ -45,6 +45,12 @@ PUBLISHED_RK4_STEPS_S = 2.20
 PUBLISHED_FLUX_MS = {(256, 65, False): 66.68, (256, 65, True): 57.72, (512, 129, False): 526.66,
                      (512, 129, True): 392.81, (256, 129, False): 134.3}
 UNIT = "RK4 steps/s"
+# how the mixed form's vertical kernels compute (WV_VERTICAL_* names)
+_MIXED_VERTICAL = {
+    "tensor": "as split-BF16 (3 pieces, 6 products) tcgen05 GEMMs with f32 accumulators",
+    "fft": "as f32 FFTs of the even / odd extension over z",
+    "cuda": "as the dense folded f32 contraction on the CUDA cores",
+}
 SEED = 1
 URMS = 0.1
 
@@ -562,25 +568,27 @@ def run_ours(args):
     devm = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in state]
     mixed_ms, tm = _time_steps(km, devm, 0.0, t0, dt, args.steps, args.warmup, stream, barrier, flush, torch)
     mixed_value = world * args.steps / max_over_ranks(mixed_ms / 1e3)
+    vk = km.vertical_kernels()
     mixed = {"value": mixed_value, "unit": UNIT, "ms_per_step": mixed_ms / args.steps,
              "speedup_vs_fp64": mixed_value / value,
-             "dtype": "f32 xy transforms and products; vertical inverse and forward transforms as split-BF16 (3 pieces, "
-                      "6 products) tcgen05 GEMMs with f32 accumulators; f32 projection; f64 phase angles and RK4",
-             "vertical_kernel": "tensor cores (tcgen05.mma)",
+             "dtype": "f32 xy transforms and products; vertical inverse " + _MIXED_VERTICAL[vk[0]] + "; vertical forward "
+                      + _MIXED_VERTICAL[vk[1]] + "; f32 projection; f64 phase angles and RK4",
+             "vertical_kernel": {"inverse": vk[0], "forward": vk[1]},
              "roofline": _stage_profile(km, devm, tm, t0, dt, "mixed", torch)}
     if rank == 0:
         mixed["rel_field_err_vs_fp64_after_100_steps"] = _field_error_after(k, km, state, dt, 100, torch, np)
     mixed["device_status"] = km.device_status()
-    # the same with the vertical inverse transform on the CUDA cores instead of the tensor cores
-    km.set_vertical_kernel("cuda")
-    cc_ms, tm = _time_steps(km, devm, tm, t0, dt, args.steps, args.warmup, stream, barrier, flush, torch)
-    cc_value = world * args.steps / max_over_ranks(cc_ms / 1e3)
-    mixed["cuda_core_vertical"] = {
-        "value": cc_value, "unit": UNIT, "ms_per_step": cc_ms / args.steps, "speedup_vs_fp64": cc_value / value,
-        "stage_ms_per_flux": _stage_profile(km, devm, tm, t0, dt, "mixed", torch)["stage_ms_per_flux"]}
-    if rank == 0:
-        mixed["cuda_core_vertical"]["rel_field_err_vs_fp64_after_100_steps"] = _field_error_after(k, km, state, dt, 100,
-                                                                                                 torch, np)
+    # the same with both vertical transforms on the tensor cores (split-BF16 GEMMs), and
+    # with both as dense contractions on the CUDA cores
+    for name, kind in (("tensor_core_vertical", "tensor"), ("cuda_core_vertical", "cuda")):
+        km.set_vertical_kernel(kind)
+        v_ms, tm = _time_steps(km, devm, tm, t0, dt, args.steps, args.warmup, stream, barrier, flush, torch)
+        v_value = world * args.steps / max_over_ranks(v_ms / 1e3)
+        mixed[name] = {
+            "value": v_value, "unit": UNIT, "ms_per_step": v_ms / args.steps, "speedup_vs_fp64": v_value / value,
+            "stage_ms_per_flux": _stage_profile(km, devm, tm, t0, dt, "mixed", torch)["stage_ms_per_flux"]}
+        if rank == 0:
+            mixed[name]["rel_field_err_vs_fp64_after_100_steps"] = _field_error_after(k, km, state, dt, 100, torch, np)
     km.close()
     # paired-FP32 form (FP32X2): FP64-class accuracy on the FP32 pipe
     kx = wvgpu.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
@@ -641,8 +649,8 @@ def run_ours(args):
                               "M5 Max: 2.20 steps/s (the reference's three-interface record; its run includes an "
                               "observer graph)",
         "dtype": "f64", "data": "synthetic",
-        "precision": "fp64 (plain drop-in); the reduced-precision forms are reported under 'mixed' (f32 + "
-                     "split-BF16 tensor cores) and 'fp32x2' (paired f32)",
+        "precision": "fp64 (plain drop-in); the reduced-precision forms are reported under 'mixed' (f32, the "
+                     "vertical inverse on split-BF16 tensor cores) and 'fp32x2' (paired f32)",
         "vertical_kernel": k.vertical_kernel(),
         "config": {
             "workload": "fixed-step RK4, nonlinear advection, 256x256x129, 800 km x 800 km x 4 km, N0 5.2e-3, lat 33, "
@@ -712,6 +720,7 @@ def _summary(value, mixed, fp32x2, adjoint, ensemble, c2, vs_ref, roofline):
          "fp32x2_max_field_err_100": max(fp32x2.get("rel_field_err_vs_fp64_after_100_steps", [float("nan")])),
          "mixed_speedup_vs_fp64": mixed["speedup_vs_fp64"],
          "mixed_field_err_100": mixed.get("rel_field_err_vs_fp64_after_100_steps"),
+         "mixed_all_tensor_core_vertical_speedup_vs_fp64": mixed.get("tensor_core_vertical", {}).get("speedup_vs_fp64"),
          "flux_hbm_frac_mixed": mixed["roofline"]["flux"]["frac"],
          "flux_hbm_frac_fp64": roofline["flux"]["frac"]}
     if adjoint:
@@ -821,7 +830,9 @@ def _c2_leg(wvgpu, stream, torch, np, steps):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         finals[name] = [x.cpu().numpy() for x in dev]
-        out[name] = {"value": steps / (ms * 1e-3), "ms_per_step": ms / steps, "vertical_kernel": kk.vertical_kernel(),
+        vk = kk.vertical_kernels()
+        out[name] = {"value": steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                     "vertical_kernel": {"inverse": vk[0], "forward": vk[1]},
                      "energy_drift": (_energy(k, finals[name], tT, 0.0, np) - E0) / E0}
         if kk is not k:
             kk.close()

@@ -149,27 +149,35 @@ typedef struct wv_stage_times {
  * the elapsed device time to the handle's stage times (reset on enable). */
 int wv_set_stage_instrumentation(wv_handle* handle, int enabled);
 
-/* Kernels of the flux's vertical transforms in the reduced-precision forms.
- * No counterpart in the reference.  WV_VERTICAL_TENSOR_CORES runs the dense
- * contractions on the tensor cores (tcgen05.mma, FP32 accumulators in tensor
- * memory): on mixed-precision handles (Nz <= 255) both vertical transforms as
- * split-BF16 GEMMs (three BF16 pieces per operand, six cross products), the
- * forward one with the flux projection fused into its drain; on FP32X2 handles
- * (Nj <= 96) the vertical inverse as exact GEMMs of six 8-bit digit slices per
- * operand (paired-FP32 accuracy).  Other handles return
- * WV_UNSUPPORTED_OPERATION.  The default where available when blocks of 32
- * retained columns (one per SM) fill the GPU; WV_VERTICAL_CUDA_CORES otherwise. */
+/* Kernels of the flux's vertical transforms.  No counterpart in the
+ * reference.  WV_VERTICAL_CUDA_CORES: the dense folded contractions on the CUDA
+ * cores.  WV_VERTICAL_TENSOR_CORES: the dense contractions on the tensor cores
+ * (tcgen05.mma, FP32 accumulators in tensor memory): on mixed-precision handles
+ * (Nz <= 255) both vertical transforms as split-BF16 GEMMs (three BF16 pieces
+ * per operand, six cross products), the forward one with the flux projection
+ * fused into its drain; on FP32X2 handles (Nj <= 96) the vertical inverse as
+ * exact GEMMs of six 8-bit digit slices per operand (paired-FP32 accuracy);
+ * other handles return WV_UNSUPPORTED_OPERATION. */
 #define WV_VERTICAL_CUDA_CORES 0
 #define WV_VERTICAL_TENSOR_CORES 1
-/* FP64 and FP32X2 handles (3 <= Nz <= 513; the default there): the flux's
- * vertical inverse and forward transforms as complex FFTs of length 2 (Nz - 1)
- * of the even / odd extension over z, one per pair of a cosine-family and a
- * sine-family channel (the reference's own REDFT00 / RODFT00 route), in the
- * handle's arithmetic. */
+/* Every precision with 3 <= Nz <= 513: the flux's vertical inverse and forward
+ * transforms as complex FFTs of length 2 (Nz - 1) of the even / odd extension
+ * over z, one per pair of a cosine-family and a sine-family channel (the
+ * reference's own REDFT00 / RODFT00 route), in the handle's arithmetic.
+ * wv_set_vertical_kernel sets both directions (the forward transform of a
+ * handle without a tensor-core forward kernel keeps the dense contraction). */
 #define WV_VERTICAL_FFT 2
 int wv_set_vertical_kernel(wv_handle* handle, int kind);
-/* The vertical-transform kernel the handle's flux runs (WV_VERTICAL_*). */
+/* The kernel of the flux's vertical inverse transform (WV_VERTICAL_*). */
 int wv_get_vertical_kernel(const wv_handle* handle, int* kind);
+/* Both directions on their own: the inverse (field spectra -> z grid) and the
+ * forward (products -> flux coefficients) transform, each any kind the handle
+ * has (the tensor-core forward transform: mixed handles with Nz <= 255).  The
+ * defaults: FFTs wherever 3 <= Nz <= 513, except the inverse of a mixed handle,
+ * which runs on the tensor cores where blocks of 32 retained columns fill the
+ * GPU. */
+int wv_set_vertical_kernels(wv_handle* handle, int inverse_kind, int forward_kind);
+int wv_get_vertical_kernels(const wv_handle* handle, int* inverse_kind, int* forward_kind);
 /* Device status word of the handle (synchronous read): bit 0 is set when a
  * bounded wait inside a kernel ran out (the kernel returned without hanging). */
 int wv_get_device_status(wv_handle* handle, unsigned* status);
@@ -358,13 +366,18 @@ int wv_rk4_dense_output_device(wv_handle* handle, double time, double* Ap, doubl
  * has (warp-register or shared-memory Stockham, per axis) and keeps the fastest. */
 typedef struct wv_ensemble wv_ensemble;
 #define WV_ENSEMBLE_MAX_GROUPS 16
+#define WV_ENSEMBLE_MAX_CANDIDATES 12
 typedef struct wv_ensemble_tuning {
     int warp_y_available, warp_x_available;  /* variants the grid has */
     int tensor_vertical_available;
     int stockham_y, stockham_x;              /* chosen: 1 = Stockham, 0 = warp (where available) */
-    int vertical;                            /* chosen vertical-transform kernel (WV_VERTICAL_*) */
-    int candidates;                          /* variants timed */
-    float candidate_ms[8];                   /* flux time of each (vertical, y, x order), ms */
+    int vertical;                            /* chosen kernel of the vertical inverse transform (WV_VERTICAL_*) */
+    int vertical_forward;                    /* ... and of the vertical forward transform */
+    int candidates;                          /* (y, x) variants timed */
+    float candidate_ms[WV_ENSEMBLE_MAX_CANDIDATES]; /* flux time of each (y, x) variant, y outer, ms */
+    float vertical_inverse_ms[3];            /* mixed groups: stage time per flux of each vertical kernel
+                                                (index WV_VERTICAL_*), -1 where the grid has none */
+    float vertical_forward_ms[3];
     float flux_ms;                           /* chosen variant, ms per flux of the whole group */
 } wv_ensemble_tuning;
 typedef struct wv_ensemble_metrics {

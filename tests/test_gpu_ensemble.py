@@ -80,11 +80,16 @@ def test_ensemble_autotune_and_graph_update(wv):
     ens = wv.WVEnsemble([g[0] for g in groups], [g[2].shape[0] for g in groups], precision="mixed", autotune=True)
     tune = ens.tuning()
     print("ensemble autotune:", tune)
-    # the 64 grid has warp and Stockham variants on both axes and both vertical
-    # kernels (8 candidates); 48 has Stockham only (2: the vertical kernels)
-    assert tune[0]["warp_y_available"] and tune[0]["warp_x_available"] and len(tune[0]["candidate_ms"]) == 8
-    assert len(tune[2]["candidate_ms"]) == 2
+    # the 64 grid has warp and Stockham variants on both axes (4 candidates); 48
+    # has Stockham only (1).  Every vertical kernel the grid has is timed per
+    # direction, and the fastest of each direction kept.
+    assert tune[0]["warp_y_available"] and tune[0]["warp_x_available"] and len(tune[0]["candidate_ms"]) == 4
+    assert len(tune[2]["candidate_ms"]) == 1
     assert not tune[2]["warp_y_available"] and not tune[2]["warp_x_available"]
+    for tn in tune:
+        assert set(tn["vertical_inverse_ms"]) == {"cuda", "fft", "tensor"} and set(tn["vertical_forward_ms"]) >= {"cuda", "fft"}
+        assert tn["vertical"] == min(tn["vertical_inverse_ms"], key=tn["vertical_inverse_ms"].get)
+        assert tn["vertical_forward"] == min(tn["vertical_forward_ms"], key=tn["vertical_forward_ms"].get)
     X = [g[2].clone() for g in groups]
     dts = [g[3] for g in groups]
     t = ens.rk4(X, 0.0, 0.0, dts, 2)
@@ -93,7 +98,7 @@ def test_ensemble_autotune_and_graph_update(wv):
     met = ens.metrics()
     assert met["graph_captures"] == 2 and met["graph_instantiations"] == 1 and met["graph_updates"] == 1
     for (cfg, k, X0, dt), Xe, tg, tn in zip(groups, X, t, tune):
-        k.set_vertical_kernel(tn["vertical"])  # the same kernels as the group (FP32 variants differ in rounding)
+        k.set_vertical_kernels(tn["vertical"], tn["vertical_forward"])  # the group's kernels (FP32 variants differ in rounding)
         for m in range(X0.shape[0]):
             s = [X0[m, c].clone() for c in range(3)]
             tt = k.rk4(*s, 0.0, 0.0, dt, 4)[3]

@@ -1,6 +1,6 @@
 """Vertical transforms of the flux as FFTs of the even / odd extension over z
 (WV_VERTICAL_FFT: k_vinv_fft, k_vfwd_fft; the default of FP64 and FP32X2
-handles): every
+handles, selectable on mixed ones): every
 reference golden case at the FP64 (1e-12) and FP32X2 (1e-9) tolerances (RK4
 components that are pure accumulated rounding gated against the state), and
 the flux against the dense folded contraction of the same handle on 0.1 m/s
@@ -118,18 +118,110 @@ def test_fft_vertical_tendencies_at_256(wv, precision, tol):
     k64.close()
 
 
-def test_fft_vertical_is_the_default_for_fp64_and_fp32x2(wv):
+def test_vertical_kernel_defaults(wv):
+    """FP64 and FP32X2: FFTs in both directions wherever 3 <= Nz <= 513.
+    Mixed: the inverse on the tensor cores where 32-column blocks fill the GPU,
+    FFTs from Nz = 129, dense below; the forward FFTs from Nz = 65, dense below.
+    One setter for both directions, one for each, and the rejections."""
     cfg = wv.Configuration(Nx=32, Ny=32, Nz=17, Nj=10, Lx=100e3, Ly=100e3, Lz=4000.0, latitude=33.0)
-    for precision, kind in (("fp64", "fft"), ("fp32x2", "fft"), ("mixed", "cuda")):
+    for precision, kinds in (("fp64", ("fft", "fft")), ("fp32x2", ("fft", "fft")), ("mixed", ("cuda", "cuda"))):
         k = wv.WVTransformConstantStratificationKernel(cfg, precision=precision)
-        assert k.vertical_kernel() == kind, precision
+        assert k.vertical_kernels() == kinds, precision
+        assert k.vertical_kernel() == kinds[0]
         k.close()
-
-
-def test_fft_vertical_rejected_on_mixed(wv):
-    k = wv.WVTransformConstantStratificationKernel(
-        wv.Configuration(Nx=32, Ny=32, Nz=17, Nj=10, Lx=100e3, Ly=100e3, Lz=4000.0, latitude=33.0), precision="mixed")
-    with pytest.raises(wv.WVKernelError) as e:
-        k.set_vertical_kernel("fft")
-    assert e.value.code == 10
+    for (n, nz), kinds in (((128, 65), ("cuda", "fft")), ((256, 129), ("tensor", "fft")), ((64, 257), ("fft", "fft"))):
+        c = wv.Configuration(Nx=n, Ny=n, Nz=nz, Nj=O.default_nj(nz), Lx=3125.0 * n, Ly=3125.0 * n, Lz=4000.0, latitude=33.0)
+        k = wv.WVTransformConstantStratificationKernel(c, precision="mixed")
+        assert k.vertical_kernels() == kinds, (n, nz)
+        k.close()
+    big = wv.Configuration(Nx=256, Ny=256, Nz=129, Nj=O.default_nj(129), Lx=800e3, Ly=800e3, Lz=4000.0, latitude=33.0)
+    k = wv.WVTransformConstantStratificationKernel(big, precision="mixed")
+    k.set_vertical_kernel("cuda")
+    assert k.vertical_kernels() == ("cuda", "cuda")
+    k.set_vertical_kernels("fft", "tensor")
+    assert k.vertical_kernels() == ("fft", "tensor")
     k.close()
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    for inv, fwd in (("tensor", "fft"), ("fft", "tensor")):
+        with pytest.raises(wv.WVKernelError) as e:
+            k.set_vertical_kernels(inv, fwd)
+        assert e.value.code == 10
+    assert k.vertical_kernels() == ("fft", "fft")
+    k.close()
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision="fp32x2")
+    k.set_vertical_kernel("tensor")  # digit-sliced inverse; the forward transform keeps the dense contraction
+    assert k.vertical_kernels() == ("tensor", "cuda")
+    with pytest.raises(wv.WVKernelError):
+        k.set_vertical_kernels("fft", "tensor")
+    k.close()
+
+
+@pytest.mark.parametrize("Nx,Ny,Nz,hydro", [(32, 32, 17, False), (48, 40, 24, False), (64, 64, 33, True),
+                                            (128, 128, 65, False), (256, 256, 129, False), (128, 128, 257, False)])
+def test_fft_vertical_mixed_matches_cuda_cores(wv, Nx, Ny, Nz, hydro):
+    """Mixed handles (FP32 arithmetic): the flux's field tendencies (u, v, w,
+    eta through the FP64 inverse transform) with the FFT vertical transforms
+    against the FP64 flux, within a small factor of the dense CUDA-core
+    contraction's error on the same handle; the switch back to the dense
+    kernels restores their flux bit for bit.  Nz = 257 is past the tensor-core
+    kernels' limit (Nz <= 255)."""
+    import torch
+    cfg = wv.Configuration(Nx=Nx, Ny=Ny, Nz=Nz, Nj=O.default_nj(Nz), Lx=3125.0 * Nx, Ly=3125.0 * Ny, Lz=4000.0,
+                           latitude=33.0, isHydrostatic=hydro)
+    k64 = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision="mixed")
+    A = wv.synthetic_state(k64, seed=21, urms=0.1)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+    exact = k64.transformWaveVortexToUVWEta(0.0, 0.0, *(x.cpu().numpy() for x in k64.nonlinearFlux(777.0, 5.0, *dev)))
+    fields = [0, 1, 3] if hydro else [0, 1, 2, 3]
+
+    def tendency_error(F):
+        f = k64.transformWaveVortexToUVWEta(0.0, 0.0, *(x.cpu().numpy() for x in F))
+        return [float(np.linalg.norm(f[i] - exact[i]) / np.linalg.norm(exact[i])) for i in fields]
+
+    k.set_vertical_kernel("cuda")
+    ref = [x.clone() for x in k.nonlinearFlux(777.0, 5.0, *dev)]
+    e_cuda = tendency_error(ref)
+    k.set_vertical_kernel("fft")
+    assert k.vertical_kernel() == "fft"
+    e_fft = tendency_error(k.nonlinearFlux(777.0, 5.0, *dev))
+    print(f"mixed {Nx}x{Ny}x{Nz} hydro={hydro} flux tendency error vs FP64 (u, v, [w,] eta): "
+          f"dense {e_cuda}, FFT {e_fft}")
+    for a, b in zip(e_fft, e_cuda):
+        assert a <= 3.0 * b + 1e-7
+    k.set_vertical_kernel("cuda")
+    again = [x.cpu().numpy() for x in k.nonlinearFlux(777.0, 5.0, *dev)]
+    for a, b in zip(again, ref):
+        assert np.array_equal(a, b.cpu().numpy())
+    k.close()
+    k64.close()
+
+
+def test_fft_vertical_mixed_vjp_matches_dense(wv):
+    """Mixed handles: the flux VJP with the FFT vertical maps against the FP64
+    VJP (same state and cotangent), within a small factor of the dense adjoint
+    maps' error on the same handle."""
+    import torch
+    c = O.Config(Nx=64, Ny=64, Nz=33, Nj=O.default_nj(33), Lx=200e3, Ly=200e3, Lz=4000.0, latitude=33.0)
+    d = O.build_descriptor(c)
+    rng = np.random.default_rng(9)
+    A = O.spectrum_state(d, seed=3, urms=0.1)
+    Fb = [rng.standard_normal((d.Nkl, c.Nj)) + 1j * rng.standard_normal((d.Nkl, c.Nj)) for _ in range(3)]
+    ins = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (*A, *Fb)]
+    cfg = wv.Configuration(Nx=64, Ny=64, Nz=33, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, latitude=33.0)
+    k64 = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision="mixed")
+    exact = [x.cpu().numpy() for x in k64.flux_vjp(0.0, 0.0, *ins)]
+    errs = {}
+    for kind in ("cuda", "fft"):
+        k.set_vertical_kernel(kind)
+        got = [x.cpu().numpy() for x in k.flux_vjp(0.0, 0.0, *ins)]
+        errs[kind] = [rel_err(g, e) for g, e in zip(got, exact)]
+    print("mixed flux VJP vs FP64 (Apb, Amb, A0b): dense", errs["cuda"], "FFT", errs["fft"])
+    # Each FFT line pairs a cosine-family channel with a sine-family one, so in
+    # FP32 the smaller channel's rounding is relative to the larger one: the
+    # FFT maps' Apb and Amb errors reach the level of the dense maps' A0b error
+    # (both ~6e-5 here), within the mixed VJP's 1e-3 bound against FP64.
+    assert max(errs["fft"]) <= 3.0 * max(errs["cuda"]) + 1e-6
+    k.close()
+    k64.close()

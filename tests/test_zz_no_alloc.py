@@ -42,8 +42,8 @@ def _config(wv, Nx, Ny, Nz):
 
 # (precision, vertical kernel): each precision's default, and the other kernels
 # the handle can be switched to (the entry point follows the handle's choice)
-VARIANTS = [("fp64", None), ("fp64", "cuda"), ("fp32x2", None), ("fp32x2", "tensor"), ("mixed", "tensor"),
-            ("mixed", "cuda")]
+VARIANTS = [("fp64", None), ("fp64", "cuda"), ("fp32x2", None), ("fp32x2", "tensor"), ("mixed", None),
+            ("mixed", "tensor"), ("mixed", "cuda")]
 # 64x64x33, and a rectangular odd grid (radix-3 and radix-5 FFTs, Nz = 25)
 GRIDS = [(64, 64, 33), (60, 45, 25)]
 

@@ -87,11 +87,12 @@ struct wv_handle {
     bool denseValid = false;
     double denseTi = 0.0, denseTf = 0.0;
     bool instrument = false;
-    bool tcAvailable = false;  // tensor-core vertical transform built for this handle
-    bool verticalTC = false;   // ... and selected (default: on where built)
-    bool verticalFFT = false;  // FP64 / FP32X2: vertical inverse as FFTs of the even / odd extension
+    bool tcAvailable = false;  // tensor-core vertical inverse transform built for this handle
+    // kernels of the flux's vertical inverse and forward transforms (WV_VERTICAL_*)
+    int vinvKind = WV_VERTICAL_CUDA_CORES;
+    int vfwdKind = WV_VERTICAL_CUDA_CORES;
     size_t tcSmem = 0;
-    bool tcFwdAvailable = false;  // tensor-core forward vertical transform built (used with verticalTC)
+    bool tcFwdAvailable = false;  // tensor-core forward vertical transform built (mixed handles)
     size_t tcFwdSmem = 0;
     size_t tcxSmem = 0;           // FP32X2: shared memory of the digit-sliced tensor-core inverse
     // F-grid scalar advection (built on first use): full-spectrum descriptor copy,
@@ -412,12 +413,10 @@ cudaError_t set_smem_limits(const Plan& p) {
     WV_SET((dev::k_xr2c_fields<T>), smem_xr2c<T>(p));
     WV_SET((dev::k_vfwd<T, true>), smem_vfwd<T>(p, 4));
     WV_SET((dev::k_vfwd<T, false>), smem_vfwd<T>(p, 4));
-    if constexpr (sizeof(dev::cx<T>) == 16) {
-        if (p.fz.N > 0) {
-            WV_SET((dev::k_vinv_fft<T, true>), dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, dev::VzShape<true>::modes));
-            WV_SET((dev::k_vinv_fft<T, false>), dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, dev::VzShape<false>::modes));
-            WV_SET((dev::k_vfwd_fft<T, true>), dev::smem_vfwd_fft<T>(p.fz.N));
-        }
+    if (p.fz.N > 0) {
+        WV_SET((dev::k_vinv_fft<T, true>), dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, dev::VzShape<T, true>::modes));
+        WV_SET((dev::k_vinv_fft<T, false>), dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, dev::VzShape<T, false>::modes));
+        WV_SET((dev::k_vfwd_fft<T, true>), dev::smem_vfwd_fft<T>(p.fz.N));
     }
 #undef WV_SET
     return cudaSuccess;
@@ -575,7 +574,7 @@ void launch_xr2c(wv_handle* h, const double* fields, int nch, dev::cx<T>* ps, cu
 // The flux's vertical inverse transform with the handle's kernel choice: the
 // tensor-core kernels (mixed: split-BF16; FP32X2: digit slices, with the
 // y-spectra buffer yScratch as its scratch), the FFTs of the even / odd
-// extension (FP64, FP32X2) or the dense folded contraction.
+// extension or the dense folded contraction.
 template <typename T>
 void launch_vinv_flux(wv_handle* h, double elapsed, const double* Ap, const double* Am, const double* A0, dev::cx<T>* z,
                       unsigned long long* speed, dev::cx<T>* yScratch, cudaStream_t s) {
@@ -583,17 +582,20 @@ void launch_vinv_flux(wv_handle* h, double elapsed, const double* Ap, const doub
     const auto& d = h->dd;
     auto* y = yScratch;
     if constexpr (sizeof(T) == 4) {
-        if (h->verticalTC)
+        if (h->vinvKind == WV_VERTICAL_TENSOR_CORES) {
             dev::k_vinv_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcSmem, s>>>(
                 d, Ap, Am, A0, elapsed, reinterpret_cast<float2*>(z), speed);
-        else
-            dev::k_vinv<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvModes), d.members), 256, smem_vinv<T>(p), s>>>(d, Ap, Am, A0, elapsed, z, speed);
-    } else if (std::is_same<T, dev::ff>::value && h->verticalTC) {
-        if constexpr (std::is_same<T, dev::ff>::value)
+            return;
+        }
+    } else if constexpr (std::is_same<T, dev::ff>::value) {
+        if (h->vinvKind == WV_VERTICAL_TENSOR_CORES) {
             dev::k_vinv_tcx<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcxSmem, s>>>(
                 d, Ap, Am, A0, elapsed, z, speed, reinterpret_cast<dev::ff*>(y));
-    } else if (h->verticalFFT) {
-        constexpr int modes = dev::VzShape<true>::modes;
+            return;
+        }
+    }
+    if (h->vinvKind == WV_VERTICAL_FFT) {
+        constexpr int modes = dev::VzShape<T, true>::modes;
         dev::k_vinv_fft<T, true><<<dim3(cdiv(p.Nkl, modes), d.members), 256,
                                     dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, modes), s>>>(d, Ap, Am, A0, elapsed, z, speed);
     } else {
@@ -654,18 +656,16 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
     if (inst) cudaEventRecord(h->ev[4], s);
     bool fwdTC = false;  // forward transform launched by a specialised kernel
     if constexpr (sizeof(T) == 4) {
-        if (h->verticalTC && h->tcFwdAvailable) {
+        if (h->vfwdKind == WV_VERTICAL_TENSOR_CORES) {
             dev::k_vfwd_tc<<<dim3(cdiv(p.Nkl, dev::kTcModes), d.members), dev::kTcThreads, h->tcFwdSmem, s>>>(
                 d, reinterpret_cast<const float2*>(f), elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
             fwdTC = true;
         }
     }
-    if constexpr (sizeof(dev::cx<T>) == 16) {
-        if (!fwdTC && h->verticalFFT) {
-            dev::k_vfwd_fft<T, true><<<dim3(cdiv(p.Nkl, dev::kVfModes), d.members), 256, dev::smem_vfwd_fft<T>(p.fz.N), s>>>(
-                d, f, nt, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
-            fwdTC = true;  // forward transform launched
-        }
+    if (!fwdTC && h->vfwdKind == WV_VERTICAL_FFT) {
+        dev::k_vfwd_fft<T, true><<<dim3(cdiv(p.Nkl, dev::vf_modes<T>()), d.members), 256, dev::smem_vfwd_fft<T>(p.fz.N), s>>>(
+            d, f, nt, elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
+        fwdTC = true;  // forward transform launched
     }
     if (!fwdTC)
         dev::k_vfwd<T, true><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd<T>(p, nt), s>>>(
@@ -970,11 +970,9 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
     WV_SET((dev::k_xr2c_adj<T>), smem_xr2c_adj<T>(p));
     WV_SET((dev::k_vinv_adj<T, true>), smem_vinv_adj<T>(p, true));
     WV_SET((dev::k_vinv_adj<T, false>), smem_vinv_adj<T>(p, false));
-    if constexpr (sizeof(dev::cx<T>) == 16) {
-        if (p.fz.N > 0) {
-            WV_SET((dev::k_vfwd_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
-            WV_SET((dev::k_vinv_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
-        }
+    if (p.fz.N > 0) {
+        WV_SET((dev::k_vfwd_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
+        WV_SET((dev::k_vinv_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
     }
 #undef WV_SET
     return cudaSuccess;
@@ -1047,14 +1045,10 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
     const dev::cx<T>* y = static_cast<const dev::cx<T>*>(h->yspec);
     if (!physIn) launch_flux_fields<T>(h, elapsed, Ap, Am, A0, static_cast<dev::cx<T>*>(h->yspec), s);
     // adjoint of projection and forward vertical transform, then inverse y FFTs
-    bool fftAdj = false;
-    if constexpr (sizeof(dev::cx<T>) == 16) fftAdj = h->verticalFFT;
-    if constexpr (sizeof(dev::cx<T>) == 16) {
-        if (fftAdj)
-            dev::k_vfwd_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::kVfModes), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
-                d, Fpb, Fmb, F0b, elapsed, za);
-    }
-    if (!fftAdj)
+    if (h->vfwdKind == WV_VERTICAL_FFT)
+        dev::k_vfwd_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::vf_modes<T>()), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
+            d, Fpb, Fmb, F0b, elapsed, za);
+    else
         dev::k_vfwd_adj<T><<<dim3(cdiv(p.Nkl, dev::kVfwdModes), d.members), 256, smem_vfwd_adj<T>(p), s>>>(d, Fpb, Fmb, F0b, elapsed, za);
     dev::YInvMap amap{};
     amap.nOut = nt;
@@ -1087,12 +1081,10 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
                                                                                                               nIn, fa);
         }
     }
-    if constexpr (sizeof(dev::cx<T>) == 16) {
-        if (fftAdj)
-            dev::k_vinv_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::kVzLines / 4), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
-                d, fa, elapsed, Apb, Amb, A0b);
-    }
-    if (!fftAdj)
+    if (h->vinvKind == WV_VERTICAL_FFT)
+        dev::k_vinv_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::VzLines<T>::value / 4), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
+            d, fa, elapsed, Apb, Amb, A0b);
+    else
         dev::k_vinv_adj<T, true><<<dim3(cdiv(p.Nkl, dev::kVinvAdjModes), d.members), 256, smem_vinv_adj<T>(p, true), s>>>(d, fa, nIn, elapsed, Apb, Amb, A0b);
     h->metrics.kernel_launches += 5;
     return cudaGetLastError();
@@ -1533,11 +1525,6 @@ static int create_handle(const wv_config* config, int precision, int members, wv
             h->tcSmem = smem;
             if (e == cudaSuccess) e = raise_smem_limit(dev::k_vinv_tc, static_cast<int>(smem));
             h->tcAvailable = e == cudaSuccess;
-            // default where its one-CTA-per-SM blocks of 32 columns fill the GPU (faster
-            // from 256x256x129 up, same accuracy); smaller grids keep the CUDA-core kernel
-            int sms = 0;
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-            h->verticalTC = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
         }
         // forward transform: four accumulators of NF <= 128 output rows over K = zHalf
         const int NF = static_cast<int>(((p.Nj + 1) / 2 + 15) / 16 * 16), KF = static_cast<int>((p.zHalf + 15) / 16 * 16);
@@ -1580,17 +1567,34 @@ static int create_handle(const wv_config* config, int precision, int members, wv
             h->tcxSmem = smem;
             if (e == cudaSuccess) e = raise_smem_limit(dev::k_vinv_tcx, static_cast<int>(smem));
             h->tcAvailable = e == cudaSuccess;
-            int sms = 0;
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-            h->verticalTC = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
         }
     }
-    // FP64 and FP32X2: the vertical transforms of the flux as FFTs by default (the
-    // reference's own route, fewer operations than the dense contraction); the
-    // tensor-core inverse of FP32X2 stays selectable
-    if (precision != WV_PRECISION_MIXED && p.fz.N > 0) {
-        h->verticalFFT = true;
-        h->verticalTC = false;
+    {
+        // Default kernels of the flux's vertical transforms.  FP64 and FP32X2: FFTs
+        // of the even / odd extension (the reference's own route; fewer operations
+        // than the dense contraction, which they beat at every grid) wherever
+        // 3 <= Nz <= 513, else the tensor-core inverse of FP32X2 (digit slices)
+        // where its blocks fill the GPU, else the dense contraction.  Mixed (FP32
+        // lines are cheap, and the dense contraction's cost per output grows only
+        // with Nj): the inverse on the tensor cores where one-CTA-per-SM blocks of
+        // 32 retained columns fill the GPU (0.126 ms against 0.139 for its FFT
+        // at 256x256x129), the FFT from Nz = 129 (1.04 ms against 1.99 dense at
+        // 512x512x257), dense below (0.025 against 0.035 ms FFT at 128x128x65);
+        // the forward transform as FFTs from Nz = 65 (0.092 ms against 0.137 on
+        // the tensor cores at 256x256x129, 0.019 against 0.035 dense at
+        // 128x128x65), dense below.
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+        const bool tcFills = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
+        const bool fft = p.fz.N > 0;
+        if (precision == WV_PRECISION_MIXED) {
+            h->vinvKind = tcFills ? WV_VERTICAL_TENSOR_CORES
+                          : (fft && p.Nz >= 129) ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
+            h->vfwdKind = (fft && p.Nz >= 65) ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
+        } else {
+            h->vinvKind = fft ? WV_VERTICAL_FFT : tcFills ? WV_VERTICAL_TENSOR_CORES : WV_VERTICAL_CUDA_CORES;
+            h->vfwdKind = fft ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
+        }
     }
     const auto ss = scratch_sizes(p);
     const size_t cb = 2 * elem_size(precision);
@@ -1645,23 +1649,42 @@ int wv_get_metrics(const wv_handle* h, wv_metrics* m) {
     return WV_SUCCESS;
 }
 
-int wv_set_vertical_kernel(wv_handle* h, int kind) {
+int wv_set_vertical_kernels(wv_handle* h, int inverse_kind, int forward_kind) {
     if (!h) return WV_INVALID_POINTER;
-    if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES && kind != WV_VERTICAL_FFT)
+    auto known = [](int k) { return k == WV_VERTICAL_CUDA_CORES || k == WV_VERTICAL_TENSOR_CORES || k == WV_VERTICAL_FFT; };
+    if (!known(inverse_kind) || !known(forward_kind))
         return fail(h, WV_INVALID_CONFIGURATION, "Unknown vertical-transform kernel.");
-    if (kind == WV_VERTICAL_FFT && (h->precision == WV_PRECISION_MIXED || h->plan.fz.N == 0))
-        return fail(h, WV_UNSUPPORTED_OPERATION, "The FFT vertical transform needs an FP64 or FP32X2 handle with 3 <= Nz <= 513.");
-    if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
+    if ((inverse_kind == WV_VERTICAL_FFT || forward_kind == WV_VERTICAL_FFT) && h->plan.fz.N == 0)
+        return fail(h, WV_UNSUPPORTED_OPERATION, "The FFT vertical transform needs 3 <= Nz <= 513.");
+    if (inverse_kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
         return fail(h, WV_UNSUPPORTED_OPERATION,
                     "The tensor-core vertical transform needs a mixed-precision (Nz <= 255) or FP32X2 (Nj <= 96) handle.");
-    h->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
-    h->verticalFFT = kind == WV_VERTICAL_FFT;
+    if (forward_kind == WV_VERTICAL_TENSOR_CORES && !h->tcFwdAvailable)
+        return fail(h, WV_UNSUPPORTED_OPERATION,
+                    "The tensor-core forward vertical transform needs a mixed-precision handle with Nz <= 255.");
+    h->vinvKind = inverse_kind;
+    h->vfwdKind = forward_kind;
+    return WV_SUCCESS;
+}
+
+int wv_set_vertical_kernel(wv_handle* h, int kind) {
+    if (!h) return WV_INVALID_POINTER;
+    // where only the inverse has a tensor-core kernel (FP32X2 handles), the forward
+    // transform keeps the dense contraction
+    const int fwd = kind == WV_VERTICAL_TENSOR_CORES && !h->tcFwdAvailable ? WV_VERTICAL_CUDA_CORES : kind;
+    return wv_set_vertical_kernels(h, kind, fwd);
+}
+
+int wv_get_vertical_kernels(const wv_handle* h, int* inverse_kind, int* forward_kind) {
+    if (!h || !inverse_kind || !forward_kind) return WV_INVALID_POINTER;
+    *inverse_kind = h->vinvKind;
+    *forward_kind = h->vfwdKind;
     return WV_SUCCESS;
 }
 
 int wv_get_vertical_kernel(const wv_handle* h, int* kind) {
     if (!h || !kind) return WV_INVALID_POINTER;
-    *kind = h->verticalTC ? WV_VERTICAL_TENSOR_CORES : h->verticalFFT ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
+    *kind = h->vinvKind;
     return WV_SUCCESS;
 }
 
@@ -2642,40 +2665,72 @@ float time_group_flux(wv_handle* h, int reps, cudaStream_t s, cudaError_t& err) 
 }
 
 // Per group, the fastest of the FFT variants that exist for its grid: the
-// register-resident warp FFT or the shared-memory Stockham kernel, per axis.
+// register-resident warp FFT or the shared-memory Stockham kernel, per axis
+// (whole-flux times); then, for mixed groups, the fastest kernel of each
+// vertical transform direction (dense contraction, FFTs, tensor cores: what the
+// grid has), from the stage times of the flux.  FP32X2 and FP64 groups keep the
+// handle's vertical kernels, so that members stay bit-identical to single
+// handles of those precisions.
 cudaError_t autotune_group(wv_handle* h, cudaStream_t s, wv_ensemble_tuning& out) {
     cudaError_t e = cudaMemsetAsync(h->state, 0, 6 * h->plan.M * h->dd.members * sizeof(double), s);
     Plan& p = h->plan;
     const bool fp32 = h->precision == WV_PRECISION_MIXED;  // warp FFT variants exist for FP32 only
     const bool warpY = fp32 && warp_ry<float>(p) != 0, warpX = fp32 && warp_rx<float>(p) != 0;
     float best = -1.0f;
-    bool bestY = false, bestX = false, bestTC = false;
+    bool bestY = false, bestX = false;
     out.candidates = 0;
-    // The tuner chooses the vertical kernel of mixed groups; FP32X2 groups keep the
-    // handle's default, so that members stay bit-identical to single FP32X2 handles.
-    const bool tuneTC = h->tcAvailable && h->precision == WV_PRECISION_MIXED;
-    const bool defaultTC = h->verticalTC;
-    for (int vt = (tuneTC || !defaultTC) ? 0 : 1; vt < (tuneTC || defaultTC ? 2 : 1) && e == cudaSuccess; ++vt) {
-        for (int vy = 0; vy < (warpY ? 2 : 1) && e == cudaSuccess; ++vy) {
-            for (int vx = 0; vx < (warpX ? 2 : 1) && e == cudaSuccess; ++vx) {
-                h->verticalTC = vt == 1;
-                p.stockhamY = vy == 1;
-                p.stockhamX = vx == 1;
-                const float ms = time_group_flux(h, 3, s, e);
-                if (e == cudaSuccess && out.candidates < 8) out.candidate_ms[out.candidates] = ms;
-                out.candidates++;
-                if (e == cudaSuccess && (best < 0.0f || ms < best)) {
-                    best = ms; bestY = p.stockhamY; bestX = p.stockhamX; bestTC = h->verticalTC;
-                }
-            }
+    for (int vy = 0; vy < (warpY ? 2 : 1) && e == cudaSuccess; ++vy) {
+        for (int vx = 0; vx < (warpX ? 2 : 1) && e == cudaSuccess; ++vx) {
+            p.stockhamY = vy == 1;
+            p.stockhamX = vx == 1;
+            const float ms = time_group_flux(h, 3, s, e);
+            if (e == cudaSuccess && out.candidates < WV_ENSEMBLE_MAX_CANDIDATES) out.candidate_ms[out.candidates] = ms;
+            out.candidates++;
+            if (e == cudaSuccess && (best < 0.0f || ms < best)) { best = ms; bestY = p.stockhamY; bestX = p.stockhamX; }
         }
     }
     p.stockhamY = bestY;
     p.stockhamX = bestX;
-    h->verticalTC = bestTC;
+    for (int k = 0; k < 3; ++k) out.vertical_inverse_ms[k] = out.vertical_forward_ms[k] = -1.0f;
+    if (h->precision == WV_PRECISION_MIXED && e == cudaSuccess) {
+        const int kinds[3] = {WV_VERTICAL_CUDA_CORES, WV_VERTICAL_FFT, WV_VERTICAL_TENSOR_CORES};
+        const bool has[3] = {true, p.fz.N > 0, h->tcAvailable};
+        const bool hasFwd[3] = {true, p.fz.N > 0, h->tcFwdAvailable};
+        const size_t M2 = 2 * p.M;
+        const bool inst = h->instrument;
+        const wv_stage_times keep = h->stages;
+        if (wv_set_stage_instrumentation(h, 1) != WV_SUCCESS) e = cudaErrorUnknown;
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+            if (!has[k]) continue;
+            h->vinvKind = kinds[k];
+            h->vfwdKind = hasFwd[k] ? kinds[k] : WV_VERTICAL_CUDA_CORES;
+            e = flux_any(h, 0.0, 0.0, h->state, h->state + M2, h->state + 2 * M2, h->kbuf, h->kbuf + M2, h->kbuf + 2 * M2,
+                         false, s);  // warm-up
+            h->stages = wv_stage_times{};
+            for (int r = 0; r < 3 && e == cudaSuccess; ++r)
+                e = flux_any(h, 0.0, 0.0, h->state, h->state + M2, h->state + 2 * M2, h->kbuf, h->kbuf + M2, h->kbuf + 2 * M2,
+                             false, s);
+            if (e != cudaSuccess) break;
+            const double n = static_cast<double>(h->stages.fluxes > 0 ? h->stages.fluxes : 1);
+            out.vertical_inverse_ms[kinds[k]] = static_cast<float>(h->stages.vertical_inverse_ms / n);
+            if (hasFwd[k]) out.vertical_forward_ms[kinds[k]] = static_cast<float>(h->stages.vertical_forward_ms / n);
+        }
+        h->instrument = inst;
+        h->stages = keep;
+        // fastest of each direction (index WV_VERTICAL_*; the dense kernel always exists)
+        int bi = WV_VERTICAL_CUDA_CORES, bf = WV_VERTICAL_CUDA_CORES;
+        for (int k = 0; k < 3; ++k) {
+            if (out.vertical_inverse_ms[k] >= 0.0f && out.vertical_inverse_ms[k] < out.vertical_inverse_ms[bi]) bi = k;
+            if (out.vertical_forward_ms[k] >= 0.0f && out.vertical_forward_ms[k] < out.vertical_forward_ms[bf]) bf = k;
+        }
+        h->vinvKind = bi;
+        h->vfwdKind = bf;
+        if (e == cudaSuccess) best = time_group_flux(h, 3, s, e);
+    }
     out.stockham_y = bestY ? 1 : 0;
     out.stockham_x = bestX ? 1 : 0;
-    out.vertical = bestTC ? WV_VERTICAL_TENSOR_CORES : h->verticalFFT ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
+    out.vertical = h->vinvKind;
+    out.vertical_forward = h->vfwdKind;
     out.warp_y_available = warpY ? 1 : 0;
     out.warp_x_available = warpX ? 1 : 0;
     out.tensor_vertical_available = h->tcAvailable ? 1 : 0;
@@ -2742,7 +2797,9 @@ int wv_ensemble_create(const wv_config* group_configs, const int* members, int n
             t.warp_y_available = h->precision == WV_PRECISION_MIXED && warp_ry<float>(h->plan) != 0;
             t.warp_x_available = h->precision == WV_PRECISION_MIXED && warp_rx<float>(h->plan) != 0;
             t.tensor_vertical_available = h->tcAvailable ? 1 : 0;
-            t.vertical = h->verticalTC ? WV_VERTICAL_TENSOR_CORES : h->verticalFFT ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
+            t.vertical = h->vinvKind;
+            t.vertical_forward = h->vfwdKind;
+            for (int k = 0; k < 3; ++k) t.vertical_inverse_ms[k] = t.vertical_forward_ms[k] = -1.0f;
             t.flux_ms = -1.0f;
         }
     }
@@ -2779,16 +2836,18 @@ int wv_ensemble_set_vertical_kernel(wv_ensemble* e, int kind) {
     if (kind != WV_VERTICAL_CUDA_CORES && kind != WV_VERTICAL_TENSOR_CORES && kind != WV_VERTICAL_FFT)
         return efail(e, WV_INVALID_CONFIGURATION, "Unknown vertical-transform kernel.");
     for (wv_handle* h : e->groups)
-        if (kind == WV_VERTICAL_FFT && (h->precision == WV_PRECISION_MIXED || h->plan.fz.N == 0))
-            return efail(e, WV_UNSUPPORTED_OPERATION, "The FFT vertical transform needs FP64 or FP32X2 groups with 3 <= Nz <= 513.");
+        if (kind == WV_VERTICAL_FFT && h->plan.fz.N == 0)
+            return efail(e, WV_UNSUPPORTED_OPERATION, "The FFT vertical transform needs groups with 3 <= Nz <= 513.");
     for (wv_handle* h : e->groups)
         if (kind == WV_VERTICAL_TENSOR_CORES && !h->tcAvailable)
             return efail(e, WV_UNSUPPORTED_OPERATION,
                          "The tensor-core vertical transform needs mixed-precision (Nz <= 255) or FP32X2 (Nj <= 96) groups.");
     for (size_t g = 0; g < e->groups.size(); ++g) {
-        e->groups[g]->verticalTC = kind == WV_VERTICAL_TENSOR_CORES;
-        e->groups[g]->verticalFFT = kind == WV_VERTICAL_FFT;
-        e->tuning[g].vertical = kind;
+        wv_handle* h = e->groups[g];
+        h->vinvKind = kind;
+        h->vfwdKind = kind == WV_VERTICAL_TENSOR_CORES && !h->tcFwdAvailable ? WV_VERTICAL_CUDA_CORES : kind;
+        e->tuning[g].vertical = h->vinvKind;
+        e->tuning[g].vertical_forward = h->vfwdKind;
     }
     e->keySteps = -1;  // captured kernels changed: capture anew
     return WV_SUCCESS;

@@ -41,19 +41,24 @@
 namespace wvgpu {
 namespace dev {
 
-constexpr int kVzLines = 4;  // FFT lines per CTA (256 threads: one radix-4 butterfly each at 2L = 256)
+// FFT lines per CTA: 4 (256 threads, one radix-4 butterfly each at 2L = 256)
+// in every precision.  8 lines per CTA in FP32 measured slower at 256x256x129
+// and 512x512x257 (twice the shared memory, fewer CTAs per SM: 0.12 against
+// 0.09 ms for the forward transform at 256, 1.58 against 1.04 ms for the
+// inverse at 512) and only a few percent faster at 128x128x65.
+template <typename T> struct VzLines { static constexpr int value = 4; };
 
-template <bool FLUX>
+template <typename T, bool FLUX>
 struct VzShape {
-    static constexpr int lines = FLUX ? 4 : 2;       // lines per retained column
-    static constexpr int modes = kVzLines / lines;   // retained columns per CTA
+    static constexpr int lines = FLUX ? 4 : 2;                   // lines per retained column
+    static constexpr int modes = VzLines<T>::value / lines;     // retained columns per CTA
 };
 
 // Shared memory of k_vinv_fft: field spectra [4][Nj][modes], two line buffers
-// [kVzLines][2L] and the twiddles [2L].
+// [lines][2L] and the twiddles [2L].
 template <typename T>
 inline size_t smem_vinv_fft(int Nj, int N2, int modes) {
-    return (static_cast<size_t>(4) * Nj * modes + 2 * static_cast<size_t>(kVzLines) * N2 + N2) * sizeof(cx<T>);
+    return (static_cast<size_t>(4) * Nj * modes + 2 * static_cast<size_t>(VzLines<T>::value) * N2 + N2) * sizeof(cx<T>);
 }
 
 template <typename T, bool FLUX>
@@ -61,7 +66,7 @@ __global__ void __launch_bounds__(256) k_vinv_fft(DescDev d, const double* __res
                                                  const double* __restrict__ A0, double elapsed, cx<T>* __restrict__ zspec,
                                                  unsigned long long* __restrict__ maxSpeedBits) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int kLines = VzShape<FLUX>::lines, kModes = VzShape<FLUX>::modes;
+    constexpr int kLines = VzShape<T, FLUX>::lines, kModes = VzShape<T, FLUX>::modes, kVzLines = VzLines<T>::value;
     const int Nj = d.Nj, Nz = d.Nz, P = d.positions, L = Nz - 1, N2 = d.fz.N;
     cx<T>* fld = reinterpret_cast<cx<T>*>(smem_raw);   // [4][Nj][kModes]
     cx<T>* bufA = fld + 4 * Nj * kModes;               // [kVzLines][N2]
@@ -156,13 +161,15 @@ __global__ void __launch_bounds__(256) k_vinv_fft(DescDev d, const double* __res
     }
 }
 
-// Shared memory of k_vfwd_fft: two line buffers [kVzLines][2L] and the twiddles [2L].
+// Shared memory of k_vfwd_fft: two line buffers [lines][2L] and the twiddles [2L].
 template <typename T>
 inline size_t smem_vfwd_fft(int N2) {
-    return (2 * static_cast<size_t>(kVzLines) * N2 + N2) * sizeof(cx<T>);
+    return (2 * static_cast<size_t>(VzLines<T>::value) * N2 + N2) * sizeof(cx<T>);
 }
 
-constexpr int kVfModes = kVzLines / 2;  // retained columns per CTA: lines (u | w) and (v | eta) each
+// retained columns per CTA of k_vfwd_fft / k_vfwd_adj_fft: lines (u | w) and (v | eta) each
+template <typename T>
+__host__ __device__ constexpr int vf_modes() { return VzLines<T>::value / 2; }
 
 template <typename T, bool FLUX>
 __global__ void __launch_bounds__(256) k_vfwd_fft(DescDev d, const cx<T>* __restrict__ fspec, int nch, double elapsed,
@@ -171,6 +178,7 @@ __global__ void __launch_bounds__(256) k_vfwd_fft(DescDev d, const cx<T>* __rest
                                                  int applyDamping, double* __restrict__ Fp, double* __restrict__ Fm,
                                                  double* __restrict__ F0) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kVzLines = VzLines<T>::value, kVfModes = vf_modes<T>();
     const int Nj = d.Nj, Nz = d.Nz, P = d.positions, L = Nz - 1, N2 = d.fz.N;
     cx<T>* bufA = reinterpret_cast<cx<T>*>(smem_raw);  // [kVzLines][N2]
     cx<T>* bufB = bufA + kVzLines * N2;
@@ -251,7 +259,7 @@ __global__ void __launch_bounds__(256) k_vfwd_fft(DescDev d, const cx<T>* __rest
 // Shared memory of the adjoint kernels: two line buffers and the twiddles.
 template <typename T>
 inline size_t smem_vadj_fft(int N2) {
-    return (2 * static_cast<size_t>(kVzLines) * N2 + N2) * sizeof(cx<T>);
+    return (2 * static_cast<size_t>(VzLines<T>::value) * N2 + N2) * sizeof(cx<T>);
 }
 
 // Transpose of the projection + forward vertical transform (k_vfwd_adj) with the
@@ -261,6 +269,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_vfwd_adj_fft(DescDev d, const double* __restrict__ Fpb, const double* __restrict__ Fmb,
                                                      const double* __restrict__ F0b, double elapsed, cx<T>* __restrict__ zadj) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kVzLines = VzLines<T>::value, kVfModes = vf_modes<T>();
     const int Nj = d.Nj, Nz = d.Nz, P = d.positions, nt = d.nt, L = Nz - 1, N2 = d.fz.N;
     cx<T>* bufA = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* bufB = bufA + kVzLines * N2;
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(256) k_vinv_adj_fft(DescDev d, const cx<T>* __
                                                      double* __restrict__ Apb, double* __restrict__ Amb,
                                                      double* __restrict__ A0b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int kLines = 4, kModes = kVzLines / kLines;
+    constexpr int kVzLines = VzLines<T>::value, kLines = 4, kModes = kVzLines / kLines;
     const int Nj = d.Nj, Nz = d.Nz, P = d.positions, nt = d.nt, L = Nz - 1, N2 = d.fz.N;
     cx<T>* bufA = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* bufB = bufA + kVzLines * N2;

@@ -73,11 +73,16 @@ class _StageTimes(ctypes.Structure):
                                                "vertical_forward_ms")] + [("fluxes", ctypes.c_uint64)]
 
 
+_VKIND = {0: "cuda", 1: "tensor", 2: "fft"}  # WV_VERTICAL_*
+_VCODE = {v: k for k, v in _VKIND.items()}
+
+
 class _EnsembleTuning(ctypes.Structure):
     _fields_ = [("warp_y_available", ctypes.c_int), ("warp_x_available", ctypes.c_int),
                 ("tensor_vertical_available", ctypes.c_int), ("stockham_y", ctypes.c_int), ("stockham_x", ctypes.c_int),
-                ("vertical", ctypes.c_int), ("candidates", ctypes.c_int), ("candidate_ms", ctypes.c_float * 8),
-                ("flux_ms", ctypes.c_float)]
+                ("vertical", ctypes.c_int), ("vertical_forward", ctypes.c_int), ("candidates", ctypes.c_int),
+                ("candidate_ms", ctypes.c_float * 12), ("vertical_inverse_ms", ctypes.c_float * 3),
+                ("vertical_forward_ms", ctypes.c_float * 3), ("flux_ms", ctypes.c_float)]
 
 
 class _EnsembleMetrics(ctypes.Structure):
@@ -179,6 +184,8 @@ def load_library():
     lib.wv_set_stage_instrumentation.argtypes = [P, ctypes.c_int]
     lib.wv_set_vertical_kernel.argtypes = [P, ctypes.c_int]
     lib.wv_get_vertical_kernel.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
+    lib.wv_set_vertical_kernels.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    lib.wv_get_vertical_kernels.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     lib.wv_get_device_status.argtypes = [P, ctypes.POINTER(ctypes.c_uint)]
     lib.wv_reset_device_status.argtypes = [P]
     lib.wv_error_tolerances.argtypes = [P, D, P, P]
@@ -271,8 +278,8 @@ def exported_symbols():
     """Names of the C entry points this binding expects (declared in include/wvgpu.h)."""
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times",
-            "wv_set_vertical_kernel", "wv_get_vertical_kernel", "wv_get_device_status", "wv_reset_device_status",
-            "wv_error_tolerances",
+            "wv_set_vertical_kernel", "wv_get_vertical_kernel", "wv_set_vertical_kernels", "wv_get_vertical_kernels",
+            "wv_get_device_status", "wv_reset_device_status", "wv_error_tolerances",
             "wv_test_fail_allocation_after", "wv_test_live_device_bytes", "wv_test_fail_launch_after", "wv_test_hold_busy",
             "wv_test_inject_wait_timeout", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
             "wv_rk4_steps", "wv_nonlinear_flux_device", "wv_evaluate_rhs_device", "wv_forward_device",
@@ -660,14 +667,24 @@ class WVTransformConstantStratificationKernel:
     def set_vertical_kernel(self, kind):
         """'cuda' (CUDA-core dense contractions), 'tensor' (tcgen05 GEMMs: split-BF16 for both vertical
         transforms on mixed handles, exact digit slices for the vertical inverse on FP32X2 handles) or
-        'fft' (FFTs of the even / odd extension over z; FP64 and FP32X2 handles, their default)."""
-        self._check(self._lib.wv_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1, "fft": 2}[kind]))
+        'fft' (FFTs of the even / odd extension over z, 3 <= Nz <= 513; the default of FP64 and FP32X2 handles)."""
+        self._check(self._lib.wv_set_vertical_kernel(self._h, _VCODE[kind]))
 
     def vertical_kernel(self):
-        """The vertical-transform kernel the flux runs: 'cuda', 'tensor' or 'fft'."""
+        """The kernel of the flux's vertical inverse transform: 'cuda', 'tensor' or 'fft'."""
         v = ctypes.c_int(0)
         self._check(self._lib.wv_get_vertical_kernel(self._h, ctypes.byref(v)))
-        return {0: "cuda", 1: "tensor", 2: "fft"}[v.value]
+        return _VKIND[v.value]
+
+    def set_vertical_kernels(self, inverse, forward):
+        """Kernels of the vertical inverse and forward transforms on their own ('cuda', 'tensor', 'fft')."""
+        self._check(self._lib.wv_set_vertical_kernels(self._h, _VCODE[inverse], _VCODE[forward]))
+
+    def vertical_kernels(self):
+        """(inverse, forward) kernels of the flux's vertical transforms."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(self._lib.wv_get_vertical_kernels(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return _VKIND[a.value], _VKIND[b.value]
 
     def device_status(self):
         """Device status word (bit 0: a bounded in-kernel wait ran out)."""
@@ -747,13 +764,16 @@ class WVEnsemble:
                         "tensor_vertical_available": bool(t.tensor_vertical_available),
                         "y": "stockham" if t.stockham_y or not t.warp_y_available else "warp",
                         "x": "stockham" if t.stockham_x or not t.warp_x_available else "warp",
-                        "vertical": {0: "cuda", 1: "tensor", 2: "fft"}[t.vertical],
-                        "candidate_ms": list(t.candidate_ms)[:max(0, min(8, t.candidates))], "flux_ms": t.flux_ms})
+                        "vertical": _VKIND[t.vertical], "vertical_forward": _VKIND[t.vertical_forward],
+                        "candidate_ms": list(t.candidate_ms)[:max(0, min(12, t.candidates))],
+                        "vertical_inverse_ms": {_VKIND[i]: v for i, v in enumerate(t.vertical_inverse_ms) if v >= 0},
+                        "vertical_forward_ms": {_VKIND[i]: v for i, v in enumerate(t.vertical_forward_ms) if v >= 0},
+                        "flux_ms": t.flux_ms})
         return out
 
     def set_vertical_kernel(self, kind):
         """'cuda', 'tensor' or 'fft' for every group (overrides the autotuner's choice)."""
-        self._check(self._lib.wv_ensemble_set_vertical_kernel(self._h, {"cuda": 0, "tensor": 1, "fft": 2}[kind]))
+        self._check(self._lib.wv_ensemble_set_vertical_kernel(self._h, _VCODE[kind]))
 
     def metrics(self):
         m = _EnsembleMetrics()
