@@ -84,6 +84,10 @@ __device__ __forceinline__ void small_dft(cx<T> (&v)[R], const cx<T>* tw, int N)
     }
 }
 
+// The lane butterflies take one form in every lane, with a per-lane sign and
+// twiddle (1 in the top lanes, exactly), instead of evaluating the top and the
+// bottom lane's expressions and selecting: 6 arithmetic instructions per value
+// and stage instead of 10 (fft_P) or 14 (fft_Q), same roundings.
 template <typename T, int R, bool INV>
 __device__ __forceinline__ void fft_P(cx<T> (&v)[R], const cx<T>* tw, int lane) {
     constexpr int N = 32 * R;
@@ -92,12 +96,14 @@ __device__ __forceinline__ void fft_P(cx<T> (&v)[R], const cx<T>* tw, int lane) 
     for (int k = 1; k < R; ++k) v[k] = cmul<T>(v[k], twid<T, INV>(tw, lane * k));
 #pragma unroll
     for (int h = 16; h >= 1; h >>= 1) {
-        const cx<T> w = twid<T, INV>(tw, (lane & (h - 1)) * (N / (2 * h)));
+        // top lane: v + u;  bottom lane: (u - v) w   (u: the partner's value)
         const bool bottom = (lane & h) != 0;
+        const cx<T> w = bottom ? twid<T, INV>(tw, (lane & (h - 1)) * (N / (2 * h))) : mk<T>(T(1), T(0));
+        const T sg = bottom ? T(-1) : T(1);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const cx<T> u = shfl_xor_cx<T>(v[r], h);
-            v[r] = bottom ? cmul<T>(csub<T>(u, v[r]), w) : cadd<T>(v[r], u);
+            v[r] = cmul<T>(mk<T>(sg * v[r].x + u.x, sg * v[r].y + u.y), w);
         }
     }
 }
@@ -107,12 +113,16 @@ __device__ __forceinline__ void fft_Q(cx<T> (&v)[R], const cx<T>* tw, int lane) 
     constexpr int N = 32 * R;
 #pragma unroll
     for (int h = 1; h <= 16; h <<= 1) {
-        const cx<T> w = twid<T, INV>(tw, (lane & (h - 1)) * (N / (2 * h)));
+        // top lane: v + w u;  bottom lane: u - w v   (u: the partner's value): the
+        // bottom lane forms w v before the exchange, the top lane's factor is 1
         const bool bottom = (lane & h) != 0;
+        const cx<T> w = bottom ? twid<T, INV>(tw, (lane & (h - 1)) * (N / (2 * h))) : mk<T>(T(1), T(0));
+        const T sg = bottom ? T(-1) : T(1);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const cx<T> u = shfl_xor_cx<T>(v[r], h);
-            v[r] = bottom ? csub<T>(u, cmul<T>(w, v[r])) : cadd<T>(v[r], cmul<T>(w, u));
+            const cx<T> m = cmul<T>(w, v[r]);
+            const cx<T> u = shfl_xor_cx<T>(m, h);
+            v[r] = mk<T>(sg * m.x + u.x, sg * m.y + u.y);
         }
     }
 #pragma unroll
