@@ -451,7 +451,8 @@ size_t smem_y_w(const Plan& p) { return (p.Ny + p.Ny * dev::kWG) * sizeof(dev::c
 template <typename T>
 size_t smem_xflux_w(const Plan& p) {
     const size_t L = p.Nx / 2;
-    return (3 * L + dev::kWG * L) * sizeof(dev::cx<T>);
+    const size_t stage = 2 * static_cast<size_t>(dev::xstage_len(static_cast<int>(p.kxColumns)));
+    return (3 * L + dev::kWG * (L + stage)) * sizeof(dev::cx<T>);
 }
 template <typename T>
 size_t smem_xc2r_w(const Plan& p, int nch) {

@@ -36,6 +36,21 @@ __device__ __forceinline__ cx<T> shfl_xor_cx(cx<T> v, int m) {
     return mk<T>(shfl_xor_v(v.x, m), shfl_xor_v(v.y, m));
 }
 
+// Asynchronous global -> shared copies of one complex value (cp.async; 8-byte
+// values through L1, 16-byte ones bypassing it), completed by wait_group.
+template <typename T>
+__device__ __forceinline__ void cp_async_cx(cx<T>* dst, const cx<T>* src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    if constexpr (sizeof(cx<T>) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// all but the most recent N committed groups of this thread have landed
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // multiply by exp(sigma * i pi / 2): -i (forward) or +i (inverse)
 template <bool INV, typename T>
 __device__ __forceinline__ cx<T> rot90(cx<T> b) { return INV ? mk<T>(-b.y, b.x) : mk<T>(b.y, -b.x); }
@@ -240,6 +255,18 @@ __device__ __forceinline__ void c2r_row(const DescDev& d, const cx<T>* h, bool u
     fft_P<T, R, true>(v, twL, lane);
 }
 
+// Row i of the x pass (0: U, 1: V, 2: W, then (q_x, q_y, q_z) per target) ->
+// its input channel of the y spectra; q_x is channel q times i k.
+__device__ __forceinline__ int xrow_channel(const DescDev& d, int i) {
+    if (i < 3) return i;
+    const int t = (i - 3) / 3, kind = (i - 3) - 3 * t;
+    return kind == 0 ? d.tq[t] : (kind == 1 ? 4 + t : 4 + d.nt + t);
+}
+
+// Shared-memory stage of one warp's channel rows: two buffers of KX values,
+// padded to an even count (16-byte aligned buffers).
+__host__ __device__ inline int xstage_len(int KX) { return (KX + 1) & ~1; }
+
 // physOut, when given, receives the real rows as complex pairs in register
 // order: [z][nReal][y][L], entry k*32 + lane = register k of lane `lane`.
 // advOut / advIn: the advecting (u, v, w) as doubles [3][z][y][Nx], written out
@@ -261,6 +288,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xflux_w(DescDev
     cx<T>* twL = reinterpret_cast<cx<T>*>(smem_raw);   // [L]
     cx<T>* twN = twL + L;                               // [2L]
     cx<T>* line = twN + 2 * L + warp * L;               // per warp: [L]
+    const int KXs = xstage_len(KX);
+    cx<T>* stage = twN + 2 * L + kWG * L + warp * 2 * KXs;  // per warp: [2][KXs]
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
     const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
     for (int i = threadIdx.x; i < L; i += blockDim.x) twL[i] = twg[i];
@@ -268,14 +297,34 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xflux_w(DescDev
     if (threadIdx.x == 0) warpsDone = 0;
     __syncthreads();
     if (y >= Ny) return;
-    // spectra of this row: channel c at row + c*Ny*KX (read straight from L2/HBM, coalesced)
+    // spectra of this row: channel c at row + c*Ny*KX.  Each channel row is
+    // copied to the warp's stage asynchronously two rows ahead of its use, so
+    // its global-memory latency overlaps the FFTs of the rows before it.
     const cx<T>* row = yspec + (((size_t)z * nIn) * Ny + y) * KX;
     const size_t cstride = (size_t)Ny * KX;
-    cx<T> U[R], V[R], W[R], v[R], S[R];
-    c2r_row<T, R>(d, row + 0 * cstride, false, twL, twN, lane, U);
-    c2r_row<T, R>(d, row + 1 * cstride, false, twL, twN, lane, V);
-    c2r_row<T, R>(d, row + 2 * cstride, false, twL, twN, lane, W);
     const int nReal = 3 + 3 * nt;
+    auto fetch = [&](int i) {
+        if (i < nReal) {
+            const cx<T>* src = row + xrow_channel(d, i) * cstride;
+            cx<T>* dst = stage + (i & 1) * KXs;
+            for (int k = lane; k < KX; k += 32) cp_async_cx<T>(dst + k, src + k);
+        }
+        cp_async_commit();  // an empty group past the last row keeps the count uniform
+    };
+    // row i from its stage buffer; the buffer is refilled with row i + 2 after every lane has read it
+    auto build = [&](int i, bool useK, cx<T> (&out)[R]) {
+        cp_async_wait<1>();
+        __syncwarp();
+        c2r_row<T, R>(d, stage + (i & 1) * KXs, useK, twL, twN, lane, out);
+        __syncwarp();
+        fetch(i + 2);
+    };
+    fetch(0);
+    fetch(1);
+    cx<T> U[R], V[R], W[R], v[R], S[R];
+    build(0, false, U);
+    build(1, false, V);
+    build(2, false, W);
     auto keep = [&](int r, const cx<T> (&x)[R]) {
         cx<T>* o = physOut + (((size_t)z * nReal + r) * Ny + y) * L + lane;
 #pragma unroll
@@ -312,12 +361,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xflux_w(DescDev
     }
 #pragma unroll 1
     for (int t = 0; t < nt; ++t) {
-        const int q = d.tq[t];
         // S_q = -(u q_x + v q_y + w q_z), accumulated in that order
 #pragma unroll 1
         for (int kind = 0; kind < 3; ++kind) {
-            const int ch = kind == 0 ? q : (kind == 1 ? 4 + t : 4 + nt + t);
-            c2r_row<T, R>(d, row + ch * cstride, kind == 0, twL, twN, lane, v);
+            build(3 + 3 * t + kind, kind == 0, v);
             if (physOut) keep(3 + 3 * t + kind, v);
 #pragma unroll
             for (int k = 0; k < R; ++k) {
