@@ -933,7 +933,8 @@ size_t smem_xadj(const Plan& p) {
 template <typename T>
 size_t smem_xadj_w(const Plan& p) {
     const size_t L = p.Nx / 2;
-    return (3 * L + dev::kWG * (L + 4 * p.kxColumns)) * sizeof(dev::cx<T>);
+    const size_t stage = 2 * static_cast<size_t>(dev::xadj_stage_len(static_cast<int>(L), static_cast<int>(p.kxColumns)));
+    return (3 * L + dev::kWG * (L + 4 * p.kxColumns + stage)) * sizeof(dev::cx<T>);
 }
 template <typename T>
 size_t smem_ypair(const Plan& p) { return (p.Ny + 3 * dev::kYG * p.Ny) * sizeof(dev::cx<T>); }

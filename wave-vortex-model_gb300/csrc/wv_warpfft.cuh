@@ -266,6 +266,8 @@ __device__ __forceinline__ int xrow_channel(const DescDev& d, int i) {
 // Shared-memory stage of one warp's channel rows: two buffers of KX values,
 // padded to an even count (16-byte aligned buffers).
 __host__ __device__ inline int xstage_len(int KX) { return (KX + 1) & ~1; }
+// ... of the x-pass adjoint: a spectrum row (KX values) or a kept real row (L values)
+__host__ __device__ inline int xadj_stage_len(int L, int KX) { return L > xstage_len(KX) ? L : xstage_len(KX); }
 
 // physOut, when given, receives the real rows as complex pairs in register
 // order: [z][nReal][y][L], entry k*32 + lane = register k of lane `lane`.
@@ -432,6 +434,8 @@ __global__ void __launch_bounds__(256, 2) k_xadj_w(DescDev d, const cx<T>* __res
     cx<T>* twN = twL + L;                               // [2L]
     cx<T>* line = twN + 2 * L + warp * (L + 4 * KX);    // per warp: [L] line, [4][KX] x-derivative parts
     cx<T>* xpart = line + L;
+    const int SL = xadj_stage_len(L, KX);
+    cx<T>* stage = twN + 2 * L + kWG * (L + 4 * KX) + warp * 2 * SL;  // per warp: [2][SL]
     const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twx);
     const cx<T>* twgN = reinterpret_cast<const cx<T>*>(d.twxN);
     for (int i = threadIdx.x; i < L; i += blockDim.x) twL[i] = twg[i];
@@ -446,19 +450,56 @@ __global__ void __launch_bounds__(256, 2) k_xadj_w(DescDev d, const cx<T>* __res
     __syncwarp();
     cx<T> U[R], V[R], W[R], gu[R], gv[R], gw[R], sb[R], v[R], g[R];
     const int nReal = 3 + 3 * nt;
-    // forward real row r (register order)
-    auto fwdRow = [&](int r, int ch, bool useK, cx<T> (&x)[R]) {
-        if (physIn) {
-            const cx<T>* src = physIn + (((size_t)z * nReal + r) * Ny + y) * L + lane;
+    // Inputs in the order of use: forward rows 0..2 (U, V, W), then per target
+    // its adjoint row and its forward rows q_x, q_y, q_z.  Each is copied to the
+    // warp's stage asynchronously two inputs ahead of its use: a forward row
+    // kept by the forward pass (L values in register order) or a spectrum row
+    // (KX values) for a c2r.
+    const int nItems = 3 + 4 * nt;
+    auto fwdIndex = [&](int i) { return i < 3 ? i : 3 + 3 * ((i - 3) / 4) + ((i - 3) % 4) - 1; };
+    auto fetch = [&](int i) {
+        if (i < nItems) {
+            cx<T>* dst = stage + (i & 1) * SL;
+            const bool adjRow = i >= 3 && (i - 3) % 4 == 0;
+            if (adjRow) {
+                const cx<T>* src = arow + ((i - 3) / 4) * cstride;
+                for (int k = lane; k < KX; k += 32) cp_async_cx<T>(dst + k, src + k);
+            } else if (physIn) {
+                const cx<T>* src = physIn + (((size_t)z * nReal + fwdIndex(i)) * Ny + y) * L;
 #pragma unroll
-            for (int k = 0; k < R; ++k) x[k] = src[32 * k];
-        } else {
-            c2r_row<T, R>(d, row + ch * cstride, useK, twL, twN, lane, x);
+                for (int k = 0; k < R; ++k) cp_async_cx<T>(dst + lane + 32 * k, src + lane + 32 * k);
+            } else {
+                const cx<T>* src = row + xrow_channel(d, fwdIndex(i)) * cstride;
+                for (int k = lane; k < KX; k += 32) cp_async_cx<T>(dst + k, src + k);
+            }
         }
+        cp_async_commit();  // an empty group past the last input keeps the count uniform
     };
-    fwdRow(0, 0, false, U);
-    fwdRow(1, 1, false, V);
-    fwdRow(2, 2, false, W);
+    auto take = [&](int i) -> const cx<T>* {
+        cp_async_wait<1>();
+        __syncwarp();
+        return stage + (i & 1) * SL;
+    };
+    auto release = [&](int i) {  // every lane is done with input i's buffer
+        __syncwarp();
+        fetch(i + 2);
+    };
+    // forward real row of input i (register order)
+    auto fwdRow = [&](int i, bool useK, cx<T> (&x)[R]) {
+        const cx<T>* b = take(i);
+        if (physIn) {
+#pragma unroll
+            for (int k = 0; k < R; ++k) x[k] = b[lane + 32 * k];
+        } else {
+            c2r_row<T, R>(d, b, useK, twL, twN, lane, x);
+        }
+        release(i);
+    };
+    fetch(0);
+    fetch(1);
+    fwdRow(0, false, U);
+    fwdRow(1, false, V);
+    fwdRow(2, false, W);
 #pragma unroll
     for (int k = 0; k < R; ++k) { gu[k] = mk<T>(T(0), T(0)); gv[k] = gu[k]; gw[k] = gu[k]; }
     // half-spectrum r2c of g into output channel ch (or the x-derivative part of value channel q)
@@ -479,14 +520,19 @@ __global__ void __launch_bounds__(256, 2) k_xadj_w(DescDev d, const cx<T>* __res
 #pragma unroll 1
     for (int t = 0; t < nt; ++t) {
         const int q = d.tq[t];
-        c2r_row<T, R>(d, arow + t * cstride, false, twL, twN, lane, sb);
-        const T h0 = arow[t * cstride].x;  // imaginary part dropped by c2r
+        const int ia = 3 + 4 * t;  // input index of the adjoint row
+        {
+            const cx<T>* b = take(ia);
+            c2r_row<T, R>(d, b, false, twL, twN, lane, sb);
+            const T h0 = b[0].x;  // imaginary part dropped by c2r
 #pragma unroll
-        for (int k = 0; k < R; ++k) sb[k] = mk<T>(T(0.5) * sb[k].x + T(0.5) * h0, T(0.5) * sb[k].y + T(0.5) * h0);
+            for (int k = 0; k < R; ++k) sb[k] = mk<T>(T(0.5) * sb[k].x + T(0.5) * h0, T(0.5) * sb[k].y + T(0.5) * h0);
+            release(ia);
+        }
 #pragma unroll 1
         for (int kind = 0; kind < 3; ++kind) {
             const int ch = kind == 0 ? q : (kind == 1 ? 4 + t : 4 + nt + t);
-            fwdRow(3 + 3 * t + kind, ch, kind == 0, v);
+            fwdRow(ia + 1 + kind, kind == 0, v);
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const cx<T> p = mk<T>(sb[k].x * v[k].x, sb[k].y * v[k].y);
