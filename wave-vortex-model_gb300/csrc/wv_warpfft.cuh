@@ -55,6 +55,30 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <bool INV, typename T>
 __device__ __forceinline__ cx<T> rot90(cx<T> b) { return INV ? mk<T>(-b.y, b.x) : mk<T>(b.y, -b.x); }
 
+// One radix-2 layer of span LEN of the in-register DIT DFT, then the next
+// (compile-time recursion, so that every register index is a constant: a
+// runtime loop over the span left 16-point lines in local memory).
+template <typename T, int R, bool INV, int LEN>
+__device__ __forceinline__ void dft_layers(cx<T> (&v)[R], const cx<T>* tw, int N) {
+    if constexpr (LEN <= R) {
+#pragma unroll
+        for (int i = 0; i < R; i += LEN) {
+#pragma unroll
+            for (int j = 0; j < LEN / 2; ++j) {
+                const cx<T> a = v[i + j];
+                cx<T> b = v[i + j + LEN / 2];
+                if (j != 0) {
+                    if (4 * j == LEN) b = rot90<INV, T>(b);
+                    else b = cmul<T>(b, twid<T, INV>(tw, j * (N / LEN)));
+                }
+                v[i + j] = cadd<T>(a, b);
+                v[i + j + LEN / 2] = csub<T>(a, b);
+            }
+        }
+        dft_layers<T, R, INV, 2 * LEN>(v, tw, N);
+    }
+}
+
 // In-register R-point DFT, natural order in and out.  tw: N-entry table of
 // exp(-2 pi i k/N) with R | N.
 template <typename T, int R, bool INV>
@@ -68,23 +92,7 @@ __device__ __forceinline__ void small_dft(cx<T> (&v)[R], const cx<T>* tw, int N)
             const int j = brev_bits(i, LOG);
             if (i < j) { const cx<T> t = v[i]; v[i] = v[j]; v[j] = t; }
         }
-#pragma unroll
-        for (int len = 2; len <= R; len <<= 1) {
-#pragma unroll
-            for (int i = 0; i < R; i += len) {
-#pragma unroll
-                for (int j = 0; j < len / 2; ++j) {
-                    const cx<T> a = v[i + j];
-                    cx<T> b = v[i + j + len / 2];
-                    if (j != 0) {
-                        if (4 * j == len) b = rot90<INV, T>(b);
-                        else b = cmul<T>(b, twid<T, INV>(tw, j * (N / len)));
-                    }
-                    v[i + j] = cadd<T>(a, b);
-                    v[i + j + len / 2] = csub<T>(a, b);
-                }
-            }
-        }
+        dft_layers<T, R, INV, 2>(v, tw, N);
     } else {
         cx<T> out[R];
 #pragma unroll
@@ -274,8 +282,14 @@ __host__ __device__ inline int xadj_stage_len(int L, int KX) { return L > xstage
 // advOut / advIn: the advecting (u, v, w) as doubles [3][z][y][Nx], written out
 // or taken in place of the reconstructed ones (sample pair 2n, 2n+1 of the row
 // sits in register k of lane l with n = k + R brev5(l)).
+// CTAs per SM the x pass is compiled for: FP32 rows of up to 4 registers per
+// lane fit 64 registers without spilling (4 CTAs, 32 warps per SM); longer rows
+// take 2 CTAs (their register tiles would spill at 3)
 template <typename T, int R>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
+__host__ __device__ constexpr int xflux_min_blocks() { return sizeof(T) == 4 && R <= 4 ? 4 : 2; }
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256, xflux_min_blocks<T, R>()) k_xflux_w(DescDev d, const cx<T>* __restrict__ yspec, cx<T>* __restrict__ pspec,
                                                 unsigned long long* __restrict__ maxSpeedBits, cx<T>* __restrict__ physOut,
                                                 double* __restrict__ advOut, const double* __restrict__ advIn) {
     constexpr int L = 32 * R;
