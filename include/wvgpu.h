@@ -178,6 +178,17 @@ int wv_get_vertical_kernel(const wv_handle* handle, int* kind);
  * GPU. */
 int wv_set_vertical_kernels(wv_handle* handle, int inverse_kind, int forward_kind);
 int wv_get_vertical_kernels(const wv_handle* handle, int* inverse_kind, int* forward_kind);
+/* Kernels of the flux's xy FFTs, per axis.  No counterpart in the reference.
+ * WV_FFT_REGISTER: register-resident lines of one warp (32 R points, R values
+ * per lane, five shuffle butterfly stages; mixed and FP32X2 handles, y lines of
+ * 32 R and x rows of 64 R samples for the R each precision has), the default
+ * where the length allows; WV_FFT_STOCKHAM: the shared-memory Stockham kernels
+ * (every length; the only form of FP64 handles).  The get call reports the
+ * kernel that runs. */
+#define WV_FFT_REGISTER 0
+#define WV_FFT_STOCKHAM 1
+int wv_set_fft_variants(wv_handle* handle, int y_variant, int x_variant);
+int wv_get_fft_variants(const wv_handle* handle, int* y_variant, int* x_variant);
 /* Device status word of the handle (synchronous read): bit 0 is set when a
  * bounded wait inside a kernel ran out (the kernel returned without hanging). */
 int wv_get_device_status(wv_handle* handle, unsigned* status);

@@ -326,3 +326,44 @@ def test_adjoint_with_tensor_vertical_matches_cuda_cores(wv, precision, tol):
         assert float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) <= tol
     assert k.device_status() == 0
     k.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32x2", "mixed"])
+@pytest.mark.parametrize("N,Nz", [(64, 33), (128, 65), (256, 129)])
+def test_fft_variants_match_fp64(wv, precision, N, Nz):
+    """Every (y, x) combination of register-line and Stockham FFT kernels
+    (wv_set_fft_variants) on FP32X2 and mixed handles: the flux and the flux VJP
+    against FP64, each within 3x the default variant's error (the kernels differ
+    in rounding order only) and, for FP32X2, within 1e-9 of max |F|; the variant
+    reported back is the one asked for (register lines exist at these lengths)."""
+    import torch
+    import wv_oracle as O
+    c = O.Config(Nx=N, Ny=N, Nz=Nz, Nj=O.default_nj(Nz), Lx=3125.0 * N, Ly=3125.0 * N, Lz=4000.0, latitude=33.0)
+    d = O.build_descriptor(c)
+    A = O.spectrum_state(d, seed=13, urms=0.1)
+    rng = np.random.default_rng(3)
+    Fb = [rng.standard_normal((d.Nkl, c.Nj)) + 1j * rng.standard_normal((d.Nkl, c.Nj)) for _ in range(3)]
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (*A, *Fb)]
+    cfg = wv.Configuration(Nx=N, Ny=N, Nz=Nz, Nj=c.Nj, Lx=c.Lx, Ly=c.Ly, Lz=c.Lz, latitude=33.0)
+    k64 = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    F64 = [x.cpu().numpy() for x in k64.nonlinearFlux(777.0, 5.0, *dev[:3])]
+    V64 = [x.cpu().numpy() for x in k64.flux_vjp(777.0, 5.0, *dev)]
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision=precision)
+    assert k.fft_variants() == ("register", "register")
+    errs = {}
+    for var in (("register", "register"), ("stockham", "stockham"), ("register", "stockham"), ("stockham", "register")):
+        k.set_fft_variants(*var)
+        assert k.fft_variants() == var
+        F = [x.cpu().numpy() for x in k.nonlinearFlux(777.0, 5.0, *dev[:3])]
+        V = [x.cpu().numpy() for x in k.flux_vjp(777.0, 5.0, *dev)]
+        errs[var] = (max(rel_err(a, b) for a, b in zip(F, F64)), max(rel_err(a, b) for a, b in zip(V, V64)))
+        print(f"{precision} {N}x{N}x{Nz} FFT variants {var}: flux {errs[var][0]:.2e}, VJP {errs[var][1]:.2e} against FP64")
+    base = errs[("register", "register")]
+    for var, (ef, ev) in errs.items():
+        assert ef <= 3.0 * base[0] + 1e-13 and ev <= 3.0 * base[1] + 1e-13, var
+        if precision == "fp32x2":
+            assert ef <= FP32X2_TOL and ev <= FP32X2_TOL, var
+    assert k._lib.wv_set_fft_variants(k._h, 0, 7) != 0  # unknown variant rejected
+    assert k.fft_variants() == ("stockham", "register")  # ... and the choice unchanged
+    k.close()
+    k64.close()

@@ -429,19 +429,21 @@ inline unsigned cdiv(size_t a, size_t b) { return static_cast<unsigned>((a + b -
 // FFTs; other lengths use the shared-memory Stockham kernels.
 
 template <typename T>
-inline int warp_ry(const Plan& p) {
+inline int warp_ry(const Plan& p, bool ignoreChoice = false) {
     // FP64 stays on the shared-memory radix-4 Stockham kernels: on the FP64 pipe
     // the radix-2 shuffle stages (64-bit shuffles, the twiddle product evaluated
-    // in every lane) cost more than the smem round trips they replace.
-    // Paired FP32 (8-byte T) also stays on Stockham: its register rows spill or
-    // lose occupancy (measured slower at 256x256x129).
-    if (sizeof(T) == 8 || p.stockhamY || p.Ny % 32 != 0) return 0;
+    // in every lane) cost more than the smem round trips they replace.  Paired
+    // FP32 takes the register lines up to 256 points (8 values per lane; 2.7 %
+    // faster per flux at 256x256x129, 14 % at 128x128x65) and the Stockham
+    // kernel for 512 (16 values per lane: 3 % slower there).
+    if (std::is_same<T, double>::value || (p.stockhamY && !ignoreChoice) || p.Ny % 32 != 0) return 0;
     const int r = static_cast<int>(p.Ny / 32);
-    return (r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8 || r == 16) ? r : 0;
+    const int rmax = sizeof(T) == 8 ? 8 : 16;
+    return ((r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8 || r == 16) && r <= rmax) ? r : 0;
 }
 template <typename T>
-inline int warp_rx(const Plan& p) {
-    if (sizeof(T) == 8 || p.stockhamX || p.Nx % 64 != 0) return 0;
+inline int warp_rx(const Plan& p, bool ignoreChoice = false) {
+    if (std::is_same<T, double>::value || (p.stockhamX && !ignoreChoice) || p.Nx % 64 != 0) return 0;
     const int r = static_cast<int>(p.Nx / 64);
     const int rmax = sizeof(T) == 8 ? 4 : 8;  // register budget of the fused x row
     return ((r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8) && r <= rmax) ? r : 0;
@@ -487,7 +489,7 @@ size_t smem_xr2c_w(const Plan& p) { const size_t L = p.Nx / 2; return (3 * L + d
 template <typename T>
 cudaError_t set_smem_limits_w(const Plan& p) {
     cudaError_t e = cudaSuccess;
-    const int ry = warp_ry<T>(p), rx = warp_rx<T>(p);
+    const int ry = warp_ry<T>(p, true), rx = warp_rx<T>(p, true);
     WV_RSWITCH_Y(ry, {
         e = raise_smem_limit(dev::k_yinv_w<T, RR>, (int)smem_y_w<T>(p));
         if (e == cudaSuccess)
@@ -960,12 +962,12 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
     WV_SET((dev::k_xadj<T>), smem_xadj<T>(p));
     WV_SET((dev::k_yfwd_pair<T>), smem_ypair<T>(p));
     {
-        const int ry = warp_ry<T>(p);
+        const int ry = warp_ry<T>(p, true);  // both variants: the choice can change after set-up
         WV_RSWITCH_Y(ry, e = raise_smem_limit(dev::k_yfwd_pair_w<T, RR>, (int)smem_ypair_w<T>(p)));
         if (e != cudaSuccess) return e;
     }
     {
-        const int rx = warp_rx<T>(p);
+        const int rx = warp_rx<T>(p, true);
         WV_RSWITCH_X(T, rx, e = raise_smem_limit(dev::k_xadj_w<T, RR>, (int)smem_xadj_w<T>(p)));
         if (e != cudaSuccess) return e;
     }
@@ -1687,6 +1689,27 @@ int wv_get_vertical_kernels(const wv_handle* h, int* inverse_kind, int* forward_
 int wv_get_vertical_kernel(const wv_handle* h, int* kind) {
     if (!h || !kind) return WV_INVALID_POINTER;
     *kind = h->vinvKind;
+    return WV_SUCCESS;
+}
+
+int wv_set_fft_variants(wv_handle* h, int y_variant, int x_variant) {
+    if (!h) return WV_INVALID_POINTER;
+    auto known = [](int v) { return v == WV_FFT_REGISTER || v == WV_FFT_STOCKHAM; };
+    if (!known(y_variant) || !known(x_variant)) return fail(h, WV_INVALID_CONFIGURATION, "Unknown FFT variant.");
+    h->plan.stockhamY = y_variant == WV_FFT_STOCKHAM;
+    h->plan.stockhamX = x_variant == WV_FFT_STOCKHAM;
+    return WV_SUCCESS;
+}
+
+int wv_get_fft_variants(const wv_handle* h, int* y_variant, int* x_variant) {
+    if (!h || !y_variant || !x_variant) return WV_INVALID_POINTER;
+    const Plan& p = h->plan;
+    const bool wy = h->precision == WV_PRECISION_FP64 ? false
+                    : h->precision == WV_PRECISION_MIXED ? warp_ry<float>(p) != 0 : warp_ry<dev::ff>(p) != 0;
+    const bool wx = h->precision == WV_PRECISION_FP64 ? false
+                    : h->precision == WV_PRECISION_MIXED ? warp_rx<float>(p) != 0 : warp_rx<dev::ff>(p) != 0;
+    *y_variant = wy ? WV_FFT_REGISTER : WV_FFT_STOCKHAM;
+    *x_variant = wx ? WV_FFT_REGISTER : WV_FFT_STOCKHAM;
     return WV_SUCCESS;
 }
 
@@ -2676,7 +2699,8 @@ float time_group_flux(wv_handle* h, int reps, cudaStream_t s, cudaError_t& err) 
 cudaError_t autotune_group(wv_handle* h, cudaStream_t s, wv_ensemble_tuning& out) {
     cudaError_t e = cudaMemsetAsync(h->state, 0, 6 * h->plan.M * h->dd.members * sizeof(double), s);
     Plan& p = h->plan;
-    const bool fp32 = h->precision == WV_PRECISION_MIXED;  // warp FFT variants exist for FP32 only
+    // FP32X2 and FP64 groups keep the handle's FFT variants (bit-identical members)
+    const bool fp32 = h->precision == WV_PRECISION_MIXED;
     const bool warpY = fp32 && warp_ry<float>(p) != 0, warpX = fp32 && warp_rx<float>(p) != 0;
     float best = -1.0f;
     bool bestY = false, bestX = false;

@@ -185,6 +185,8 @@ def load_library():
     lib.wv_set_vertical_kernel.argtypes = [P, ctypes.c_int]
     lib.wv_get_vertical_kernel.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     lib.wv_set_vertical_kernels.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    lib.wv_set_fft_variants.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    lib.wv_get_fft_variants.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     lib.wv_get_vertical_kernels.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     lib.wv_get_device_status.argtypes = [P, ctypes.POINTER(ctypes.c_uint)]
     lib.wv_reset_device_status.argtypes = [P]
@@ -279,6 +281,7 @@ def exported_symbols():
     return ["wv_describe", "wv_describe_modes", "wv_create", "wv_destroy", "wv_last_message", "wv_get_sizes",
             "wv_get_metrics", "wv_set_forcing", "wv_set_stage_instrumentation", "wv_get_stage_times",
             "wv_set_vertical_kernel", "wv_get_vertical_kernel", "wv_set_vertical_kernels", "wv_get_vertical_kernels",
+            "wv_set_fft_variants", "wv_get_fft_variants",
             "wv_get_device_status", "wv_reset_device_status", "wv_error_tolerances",
             "wv_test_fail_allocation_after", "wv_test_live_device_bytes", "wv_test_fail_launch_after", "wv_test_hold_busy",
             "wv_test_inject_wait_timeout", "wv_nonlinear_flux", "wv_evaluate_rhs", "wv_forward", "wv_inverse",
@@ -679,6 +682,18 @@ class WVTransformConstantStratificationKernel:
     def set_vertical_kernels(self, inverse, forward):
         """Kernels of the vertical inverse and forward transforms on their own ('cuda', 'tensor', 'fft')."""
         self._check(self._lib.wv_set_vertical_kernels(self._h, _VCODE[inverse], _VCODE[forward]))
+
+    def set_fft_variants(self, y, x):
+        """xy FFT kernels per axis: 'register' (warp register lines where the length allows) or 'stockham'."""
+        code = {"register": 0, "stockham": 1}
+        self._check(self._lib.wv_set_fft_variants(self._h, code[y], code[x]))
+
+    def fft_variants(self):
+        """(y, x) FFT kernels the flux runs: 'register' or 'stockham'."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(self._lib.wv_get_fft_variants(self._h, ctypes.byref(a), ctypes.byref(b)))
+        name = {0: "register", 1: "stockham"}
+        return name[a.value], name[b.value]
 
     def vertical_kernels(self):
         """(inverse, forward) kernels of the flux's vertical transforms."""
