@@ -44,6 +44,14 @@ template <typename T> __device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) { 
 template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) { return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 template <typename T> __device__ __forceinline__ cx<T> cconj(cx<T> a) { return mk<T>(a.x, -a.y); }
 template <typename T> __device__ __forceinline__ cx<T> cscale(cx<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+#ifdef __CUDACC__
+// FP32 complex sums on the paired FP32 instructions of sm_100+ (FADD2: both
+// components in one instruction, each rounded as its scalar add)
+template <> __device__ __forceinline__ cx<float> cadd<float>(cx<float> a, cx<float> b) { return __fadd2_rn(a, b); }
+template <> __device__ __forceinline__ cx<float> csub<float>(cx<float> a, cx<float> b) {
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+#endif
 // multiply by +i (INV) or -i (forward) : used by radix-4 butterflies
 template <bool INV, typename T> __device__ __forceinline__ cx<T> mul_mi(cx<T> a) { return INV ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x); }
 

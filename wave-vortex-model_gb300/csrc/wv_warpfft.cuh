@@ -51,6 +51,14 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// s v + u for a lane sign s = +1 or -1 (the lane butterflies' one form); FP32 on
+// one paired FFMA2 per value
+template <typename T>
+__device__ __forceinline__ cx<T> sign_add(T s, cx<T> v, cx<T> u) {
+    if constexpr (std::is_same<T, float>::value) return __ffma2_rn(make_float2(s, s), v, u);
+    else return mk<T>(s * v.x + u.x, s * v.y + u.y);
+}
+
 // multiply by exp(sigma * i pi / 2): -i (forward) or +i (inverse)
 template <bool INV, typename T>
 __device__ __forceinline__ cx<T> rot90(cx<T> b) { return INV ? mk<T>(-b.y, b.x) : mk<T>(b.y, -b.x); }
@@ -126,7 +134,7 @@ __device__ __forceinline__ void fft_P(cx<T> (&v)[R], const cx<T>* tw, int lane) 
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const cx<T> u = shfl_xor_cx<T>(v[r], h);
-            v[r] = cmul<T>(mk<T>(sg * v[r].x + u.x, sg * v[r].y + u.y), w);
+            v[r] = cmul<T>(sign_add<T>(sg, v[r], u), w);
         }
     }
 }
@@ -145,7 +153,7 @@ __device__ __forceinline__ void fft_Q(cx<T> (&v)[R], const cx<T>* tw, int lane) 
         for (int r = 0; r < R; ++r) {
             const cx<T> m = cmul<T>(w, v[r]);
             const cx<T> u = shfl_xor_cx<T>(m, h);
-            v[r] = mk<T>(sg * m.x + u.x, sg * m.y + u.y);
+            v[r] = sign_add<T>(sg, m, u);
         }
     }
 #pragma unroll
