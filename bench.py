@@ -649,8 +649,9 @@ def run_ours(args):
                               "M5 Max: 2.20 steps/s (the reference's three-interface record; its run includes an "
                               "observer graph)",
         "dtype": "f64", "data": "synthetic",
-        "precision": "fp64 (plain drop-in); the reduced-precision forms are reported under 'mixed' (f32, the "
-                     "vertical inverse on split-BF16 tensor cores) and 'fp32x2' (paired f32)",
+        "precision": "fp64 (plain drop-in); the reduced-precision forms are reported under 'mixed' (f32; its "
+                     "split-BF16 tensor-core vertical transforms under mixed.tensor_core_vertical) and 'fp32x2' "
+                     "(paired f32)",
         "vertical_kernel": k.vertical_kernel(),
         "config": {
             "workload": "fixed-step RK4, nonlinear advection, 256x256x129, 800 km x 800 km x 4 km, N0 5.2e-3, lat 33, "

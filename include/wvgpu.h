@@ -173,9 +173,9 @@ int wv_get_vertical_kernel(const wv_handle* handle, int* kind);
 /* Both directions on their own: the inverse (field spectra -> z grid) and the
  * forward (products -> flux coefficients) transform, each any kind the handle
  * has (the tensor-core forward transform: mixed handles with Nz <= 255).  The
- * defaults: FFTs wherever 3 <= Nz <= 513, except the inverse of a mixed handle,
- * which runs on the tensor cores where blocks of 32 retained columns fill the
- * GPU. */
+ * defaults are the measured fastest: FFTs wherever 3 <= Nz <= 513, except on
+ * mixed handles, whose inverse takes the dense contraction below Nz = 97 and
+ * forward transform below Nz = 65. */
 int wv_set_vertical_kernels(wv_handle* handle, int inverse_kind, int forward_kind);
 int wv_get_vertical_kernels(const wv_handle* handle, int* inverse_kind, int* forward_kind);
 /* Kernels of the flux's xy FFTs, per axis.  No counterpart in the reference.

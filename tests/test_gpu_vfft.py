@@ -120,22 +120,25 @@ def test_fft_vertical_tendencies_at_256(wv, precision, tol):
 
 def test_vertical_kernel_defaults(wv):
     """FP64 and FP32X2: FFTs in both directions wherever 3 <= Nz <= 513.
-    Mixed: the inverse on the tensor cores where 32-column blocks fill the GPU,
-    FFTs from Nz = 129, dense below; the forward FFTs from Nz = 65, dense below.
-    One setter for both directions, one for each, and the rejections."""
+    Mixed: the inverse as FFTs from Nz = 97, dense below; the forward as FFTs
+    from Nz = 65, dense below.  One setter for both directions, one for each,
+    and the rejections."""
     cfg = wv.Configuration(Nx=32, Ny=32, Nz=17, Nj=10, Lx=100e3, Ly=100e3, Lz=4000.0, latitude=33.0)
     for precision, kinds in (("fp64", ("fft", "fft")), ("fp32x2", ("fft", "fft")), ("mixed", ("cuda", "cuda"))):
         k = wv.WVTransformConstantStratificationKernel(cfg, precision=precision)
         assert k.vertical_kernels() == kinds, precision
         assert k.vertical_kernel() == kinds[0]
         k.close()
-    for (n, nz), kinds in (((128, 65), ("cuda", "fft")), ((256, 129), ("tensor", "fft")), ((64, 257), ("fft", "fft"))):
+    for (n, nz), kinds in (((128, 65), ("cuda", "fft")), ((192, 97), ("fft", "fft")), ((256, 129), ("fft", "fft")),
+                           ((64, 257), ("fft", "fft"))):
         c = wv.Configuration(Nx=n, Ny=n, Nz=nz, Nj=O.default_nj(nz), Lx=3125.0 * n, Ly=3125.0 * n, Lz=4000.0, latitude=33.0)
         k = wv.WVTransformConstantStratificationKernel(c, precision="mixed")
         assert k.vertical_kernels() == kinds, (n, nz)
         k.close()
     big = wv.Configuration(Nx=256, Ny=256, Nz=129, Nj=O.default_nj(129), Lx=800e3, Ly=800e3, Lz=4000.0, latitude=33.0)
     k = wv.WVTransformConstantStratificationKernel(big, precision="mixed")
+    k.set_vertical_kernel("tensor")
+    assert k.vertical_kernels() == ("tensor", "tensor")
     k.set_vertical_kernel("cuda")
     assert k.vertical_kernels() == ("cuda", "cuda")
     k.set_vertical_kernels("fft", "tensor")

@@ -448,6 +448,16 @@ inline int warp_rx(const Plan& p, bool ignoreChoice = false) {
     const int rmax = sizeof(T) == 8 ? 4 : 8;  // register budget of the fused x row
     return ((r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8) && r <= rmax) ? r : 0;
 }
+// The flux's vertical FFT lines (2 (Nz - 1) = 32 R points) on warp registers:
+// mixed and FP32X2 handles (FP32X2 up to 256 points), otherwise the Stockham
+// kernels of wv_vfft.cuh.
+template <typename T>
+inline int warp_rz(const Plan& p) {
+    if (std::is_same<T, double>::value || p.fz.N == 0 || p.fz.N % 32 != 0) return 0;
+    const int r = p.fz.N / 32;
+    const int rmax = sizeof(T) == 8 ? 8 : 16;
+    return ((r == 1 || r == 2 || r == 3 || r == 4 || r == 6 || r == 8 || r == 16) && r <= rmax) ? r : 0;
+}
 template <typename T>
 size_t smem_y_w(const Plan& p) { return (p.Ny + p.Ny * dev::kWG) * sizeof(dev::cx<T>); }
 template <typename T>
@@ -496,6 +506,14 @@ cudaError_t set_smem_limits_w(const Plan& p) {
             e = raise_smem_limit(dev::k_yfwd_w<T, RR>, (int)smem_y_w<T>(p));
     });
     if (e != cudaSuccess) return e;
+    if constexpr (!std::is_same<T, double>::value) {
+        const int rz = warp_rz<T>(p);
+        WV_RSWITCH_Y(rz, {
+            e = raise_smem_limit(dev::k_vinv_wfft<T, RR>, (int)dev::smem_vinv_wfft<T>(static_cast<int>(p.Nj), p.fz.N));
+            if (e == cudaSuccess) e = raise_smem_limit(dev::k_vfwd_wfft<T, RR>, (int)dev::smem_vfwd_wfft<T>(p.fz.N));
+        });
+        if (e != cudaSuccess) return e;
+    }
     WV_RSWITCH_X(T, rx, {
         e = raise_smem_limit(dev::k_xflux_w<T, RR>, (int)smem_xflux_w<T>(p));
         if (e == cudaSuccess)
@@ -597,7 +615,13 @@ void launch_vinv_flux(wv_handle* h, double elapsed, const double* Ap, const doub
             return;
         }
     }
-    if (h->vinvKind == WV_VERTICAL_FFT) {
+    if (h->vinvKind == WV_VERTICAL_FFT && warp_rz<T>(p)) {
+        if constexpr (!std::is_same<T, double>::value) {
+            const dim3 grid(cdiv(p.Nkl, dev::kVwWarps / 4), d.members);
+            const size_t sm = dev::smem_vinv_wfft<T>(static_cast<int>(p.Nj), p.fz.N);
+            WV_RSWITCH_Y(warp_rz<T>(p), (dev::k_vinv_wfft<T, RR><<<grid, 256, sm, s>>>(d, Ap, Am, A0, elapsed, z, speed)));
+        }
+    } else if (h->vinvKind == WV_VERTICAL_FFT) {
         constexpr int modes = dev::VzShape<T, true>::modes;
         dev::k_vinv_fft<T, true><<<dim3(cdiv(p.Nkl, modes), d.members), 256,
                                     dev::smem_vinv_fft<T>(static_cast<int>(p.Nj), p.fz.N, modes), s>>>(d, Ap, Am, A0, elapsed, z, speed);
@@ -664,6 +688,15 @@ cudaError_t launch_flux(wv_handle* h, double t, double t0, const double* Ap, con
                 d, reinterpret_cast<const float2*>(f), elapsed, Ap, Am, A0, speed, damping ? 1 : 0, Fp, Fm, F0);
             fwdTC = true;
         }
+    }
+    if (!fwdTC && h->vfwdKind == WV_VERTICAL_FFT && warp_rz<T>(p)) {
+        if constexpr (!std::is_same<T, double>::value) {
+            const dim3 grid(cdiv(p.Nkl, dev::kVwWarps / 2), d.members);
+            const size_t sm = dev::smem_vfwd_wfft<T>(p.fz.N);
+            WV_RSWITCH_Y(warp_rz<T>(p), (dev::k_vfwd_wfft<T, RR><<<grid, 256, sm, s>>>(d, f, nt, elapsed, Ap, Am, A0, speed,
+                                                                                          damping ? 1 : 0, Fp, Fm, F0)));
+        }
+        fwdTC = true;
     }
     if (!fwdTC && h->vfwdKind == WV_VERTICAL_FFT) {
         dev::k_vfwd_fft<T, true><<<dim3(cdiv(p.Nkl, dev::vf_modes<T>()), d.members), 256, dev::smem_vfwd_fft<T>(p.fz.N), s>>>(
@@ -1574,26 +1607,25 @@ static int create_handle(const wv_config* config, int precision, int members, wv
         }
     }
     {
-        // Default kernels of the flux's vertical transforms.  FP64 and FP32X2: FFTs
-        // of the even / odd extension (the reference's own route; fewer operations
-        // than the dense contraction, which they beat at every grid) wherever
-        // 3 <= Nz <= 513, else the tensor-core inverse of FP32X2 (digit slices)
-        // where its blocks fill the GPU, else the dense contraction.  Mixed (FP32
-        // lines are cheap, and the dense contraction's cost per output grows only
-        // with Nj): the inverse on the tensor cores where one-CTA-per-SM blocks of
-        // 32 retained columns fill the GPU (0.126 ms against 0.139 for its FFT
-        // at 256x256x129), the FFT from Nz = 129 (1.04 ms against 1.99 dense at
-        // 512x512x257), dense below (0.025 against 0.035 ms FFT at 128x128x65);
-        // the forward transform as FFTs from Nz = 65 (0.092 ms against 0.137 on
-        // the tensor cores at 256x256x129, 0.019 against 0.035 dense at
-        // 128x128x65), dense below.
+        // Default kernels of the flux's vertical transforms, the measured fastest.
+        // FP64 and FP32X2: FFTs of the even / odd extension (the reference's own
+        // route; fewer operations than the dense contraction, which they beat at
+        // every grid) wherever 3 <= Nz <= 513, else the tensor-core inverse of
+        // FP32X2 (digit slices) where its blocks fill the GPU, else the dense
+        // contraction.  Mixed (FP32 lines are cheap, and the dense contraction's
+        // cost per output grows only with Nj): the inverse as FFTs from Nz = 97
+        // (warp-register lines: 0.118 ms against 0.125 on the tensor cores and
+        // 0.143 dense at 256x256x129, 0.058 against 0.067 and 0.078 at
+        // 192x192x97), dense below (0.025 against 0.027 FFT at 128x128x65); the
+        // forward transform as FFTs from Nz = 65 (0.078 ms against 0.135 on the
+        // tensor cores at 256x256x129, 0.018 against 0.034 dense at 128x128x65),
+        // dense below.  The tensor-core kernels stay selectable.
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
         const bool tcFills = h->tcAvailable && static_cast<int>((p.Nkl + dev::kTcModes - 1) / dev::kTcModes) >= sms;
         const bool fft = p.fz.N > 0;
         if (precision == WV_PRECISION_MIXED) {
-            h->vinvKind = tcFills ? WV_VERTICAL_TENSOR_CORES
-                          : (fft && p.Nz >= 129) ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
+            h->vinvKind = (fft && p.Nz >= 97) ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
             h->vfwdKind = (fft && p.Nz >= 65) ? WV_VERTICAL_FFT : WV_VERTICAL_CUDA_CORES;
         } else {
             h->vinvKind = fft ? WV_VERTICAL_FFT : tcFills ? WV_VERTICAL_TENSOR_CORES : WV_VERTICAL_CUDA_CORES;

@@ -37,6 +37,7 @@
 
 #include "wv_adjoint.cuh"
 #include "wv_kernels.cuh"
+#include "wv_warpfft.cuh"
 
 namespace wvgpu {
 namespace dev {
@@ -253,6 +254,222 @@ __global__ void __launch_bounds__(256) k_vfwd_fft(DescDev d, const cx<T>* __rest
             vi[c] = conj ? -v.y : v.y;
         }
         vfwd_project<T, FLUX>(d, w, j, vr, vi, nch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The flux's vertical transforms on register-resident warp lines (mixed and
+// FP32X2 handles, 2L = 32 R points): one line per warp, built in registers
+// from the same entries as k_vinv_fft / k_vfwd_fft, transformed by fft_P (no
+// block barrier inside the FFT; paired FP32 in split form), then parked in a
+// per-warp line buffer for the even / odd split.  Line buffers are padded by
+// one value every 8 so that the lane-bit-reversed stores of fft_P's output
+// meet no bank conflicts.
+
+constexpr int kVwWarps = 8;  // lines per CTA (256 threads)
+__host__ __device__ inline int vw_pad(int i) { return i + (i >> 3); }
+__host__ __device__ inline int vw_line_len(int N2) { return N2 + N2 / 8; }
+
+// k_vinv_wfft: field spectra [4][Nj][2 modes], twiddles [2L], line buffers [8][2L + 2L/8]
+template <typename T>
+inline size_t smem_vinv_wfft(int Nj, int N2) {
+    return (static_cast<size_t>(4) * Nj * (kVwWarps / 4) + N2 + static_cast<size_t>(kVwWarps) * vw_line_len(N2)) *
+           sizeof(cx<T>);
+}
+// k_vfwd_wfft: twiddles [2L], line buffers [8][2L + 2L/8]
+template <typename T>
+inline size_t smem_vfwd_wfft(int N2) {
+    return (N2 + static_cast<size_t>(kVwWarps) * vw_line_len(N2)) * sizeof(cx<T>);
+}
+
+// fft_P output (register k1 of lane t = F[k1 + R brev5(t)]) into a padded line buffer
+template <typename T, int R>
+__device__ __forceinline__ void vw_park(cx<T>* F, const cx<T> (&v)[R], int lane) {
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) F[vw_pad(p_index<R>(k1, lane))] = v[k1];
+    __syncwarp();
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_vinv_wfft(DescDev d, const double* __restrict__ Ap, const double* __restrict__ Am,
+                                                  const double* __restrict__ A0, double elapsed, cx<T>* __restrict__ zspec,
+                                                  unsigned long long* __restrict__ maxSpeedBits) {
+    constexpr int N2 = 32 * R, kModes = kVwWarps / 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, L = Nz - 1;
+    cx<T>* fld = reinterpret_cast<cx<T>*>(smem_raw);  // [4][Nj][kModes]
+    cx<T>* tw = fld + 4 * Nj * kModes;                // [N2]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    cx<T>* F = tw + N2 + warp * vw_line_len(N2);
+    const int m0 = blockIdx.x * kModes;
+    const int nm = min(kModes, d.Nkl - m0);
+    const int member = blockIdx.y;
+    if (member > 0) {
+        const long long o = member * d.memberStride;
+        Ap += o; Am += o; A0 += o;
+        zspec += (size_t)member * Nz * P;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && maxSpeedBits) maxSpeedBits[member] = 0ull;
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it / Nj, j = it - mi * Nj;
+        cx<T> f[4];
+        vinv_field_spectra<T>(d, Ap, Am, A0, elapsed, m0 + mi, j, f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) fld[(q * Nj + j) * kModes + mi] = f[q];
+    }
+    __syncthreads();
+    const int mi = warp >> 2, l = warp & 3;  // mode, line: (u | w), (v | eta), (m w | -m u), (m eta | -m v)
+    if (mi >= nm) return;
+    const T* mz = reinterpret_cast<const T*>(d.tMz);
+    const T half = T(0.5f);
+    // line entries y[k], k = lane + 32 r: y[0] = C_0 / 2, y[L] = C_L,
+    // y[j] = (C_j + i D_j) / 2, y[2L-j] = (C_j - i D_j) / 2
+    cx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int k = lane + 32 * r;
+        const int j = k <= L ? k : N2 - k;
+        cx<T> val = mk<T>(T(0), T(0));
+        if (j < Nj) {
+            const cx<T> U = fld[(0 * Nj + j) * kModes + mi], V = fld[(1 * Nj + j) * kModes + mi];
+            const cx<T> W = fld[(2 * Nj + j) * kModes + mi], E = fld[(3 * Nj + j) * kModes + mi];
+            cx<T> C, D;
+            if (l == 0) { C = U; D = W; }
+            else if (l == 1) { C = V; D = E; }
+            else {
+                const T m = mz[j];
+                if (l == 2) { C = mk<T>(m * W.x, m * W.y); D = mk<T>(-(m * U.x), -(m * U.y)); }
+                else { C = mk<T>(m * E.x, m * E.y); D = mk<T>(-(m * V.x), -(m * V.y)); }
+            }
+            if (k == 0) {
+                val = mk<T>(C.x * half, C.y * half);
+            } else if (k == L) {
+                val = C;
+            } else {
+                const cx<T> c = mk<T>(C.x * half, C.y * half);
+                const cx<T> id = mk<T>(-(D.y * half), D.x * half);
+                val = k < L ? cadd<T>(c, id) : csub<T>(c, id);
+            }
+        }
+        v[r] = val;
+    }
+    fft_P<T, R, false>(v, tw, lane);
+    vw_park<T, R>(F, v, lane);
+    // even part -> cosine channel, odd part -> sine channel, n = 0 .. L
+    int derivChan[4] = {-1, -1, -1, -1};
+    for (int t = 0; t < d.nt; ++t) derivChan[d.tq[t]] = 4 + t;
+    int chC, chS;
+    if (l == 0) { chC = 0; chS = 2; }
+    else if (l == 1) { chC = 1; chS = 3; }
+    else if (l == 2) { chC = derivChan[2]; chS = derivChan[0]; }
+    else { chC = derivChan[3]; chS = derivChan[1]; }
+    const int mode = m0 + mi;
+    const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
+    for (int n = lane; n <= L; n += 32) {
+        const cx<T> a = F[vw_pad(n)];
+        cx<T> ev = a, od = mk<T>(T(0), T(0));
+        if (n != 0 && n != L) {
+            const cx<T> b = F[vw_pad(N2 - n)];
+            ev = mk<T>((a.x + b.x) * half, (a.y + b.y) * half);
+            od = mk<T>((a.x - b.x) * half, (a.y - b.y) * half);
+        }
+        if (chC >= 0) {
+            cx<T>* base = zspec + (size_t)chC * d.zTotal * P + (size_t)n * P;
+            base[pos] = ev;
+            if (cpos >= 0) base[cpos] = cconj<T>(ev);
+        }
+        if (chS >= 0) {
+            cx<T>* base = zspec + (size_t)chS * d.zTotal * P + (size_t)n * P;
+            base[pos] = od;
+            if (cpos >= 0) base[cpos] = cconj<T>(od);
+        }
+    }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_vfwd_wfft(DescDev d, const cx<T>* __restrict__ fspec, int nch, double elapsed,
+                                                  const double* __restrict__ Ap, const double* __restrict__ Am,
+                                                  const double* __restrict__ A0, const unsigned long long* __restrict__ maxSpeedBits,
+                                                  int applyDamping, double* __restrict__ Fp, double* __restrict__ Fm,
+                                                  double* __restrict__ F0) {
+    constexpr int N2 = 32 * R, kModes = kVwWarps / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, L = Nz - 1;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);  // [N2]
+    cx<T>* lines = tw + N2;                           // [8][N2 + N2/8]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m0 = blockIdx.x * kModes;
+    const int nm = min(kModes, d.Nkl - m0);
+    const int member = blockIdx.y;
+    if (member > 0) {
+        const long long o = member * d.memberStride;
+        if (Ap) { Ap += o; Am += o; A0 += o; }
+        Fp += o; Fm += o; F0 += o;
+        fspec += (size_t)member * Nz * P;
+        if (maxSpeedBits) maxSpeedBits += member;
+    }
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    // channel holding each field slot q (0 u, 1 v: cosine family; 2 w, 3 eta: sine family)
+    int chanOfQ[4] = {-1, -1, -1, -1};
+    for (int c = 0; c < nch; ++c) chanOfQ[d.tq[c]] = c;
+    __syncthreads();
+    const int mi = warp >> 1, l = warp & 1;  // mode, line: (u | w), (v | eta)
+    if (mi < nm) {
+        const int pos = d.modePos[m0 + mi];
+        const int cc = l == 0 ? chanOfQ[0] : chanOfQ[1], cs = l == 0 ? chanOfQ[2] : chanOfQ[3];
+        auto at = [&](int ch, int z) {
+            return ch >= 0 ? fspec[(size_t)ch * d.zTotal * P + (size_t)z * P + pos] : mk<T>(T(0), T(0));
+        };
+        // y[0] = c_0, y[L] = c_L, y[z] = c_z + s_z, y[2L-z] = c_z - s_z
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int k = lane + 32 * r;
+            const int z = k <= L ? k : N2 - k;
+            const cx<T> cv = at(cc, z);
+            v[r] = (k == 0 || k == L) ? cv : (k < L ? cadd<T>(cv, at(cs, z)) : csub<T>(cv, at(cs, z)));
+        }
+        fft_P<T, R, false>(v, tw, lane);
+        vw_park<T, R>(lines + warp * vw_line_len(N2), v, lane);
+    }
+    __syncthreads();  // both lines of every mode parked
+    double maxSpeed = 0.0;
+    if (applyDamping) maxSpeed = __longlong_as_double((long long)*maxSpeedBits);
+    const T sc = T(1.0 / (static_cast<double>(L) * static_cast<double>(d.Nx) * static_cast<double>(d.Ny)));
+    const T half = T(0.5f);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int m = it % nm, j = it / nm;
+        const int mode = m0 + m;
+        const int w = d.modeWV[mode];
+        const bool conj = d.modeFlags[mode] & 1;
+        cx<T> X[4];
+#pragma unroll
+        for (int ll = 0; ll < 2; ++ll) {
+            const cx<T>* row = lines + (m * 2 + ll) * vw_line_len(N2);
+            const cx<T> a = row[vw_pad(j)];
+            cx<T> ev = a, od = mk<T>(T(0), T(0));
+            if (j != 0 && j != L) {
+                const cx<T> b = row[vw_pad(N2 - j)];
+                ev = mk<T>((a.x + b.x) * half, (a.y + b.y) * half);
+                od = mk<T>((a.x - b.x) * half, (a.y - b.y) * half);
+            }
+            const T scC = j == L ? sc * half : sc;
+            X[ll] = mk<T>(ev.x * scC, ev.y * scC);
+            X[2 + ll] = mk<T>(-(od.y * sc), od.x * sc);  // i * odd part
+        }
+        T vr[4] = {T(0), T(0), T(0), T(0)}, vi[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c >= nch) break;
+            const int q = d.tq[c];
+            const cx<T> v = q == 0 ? X[0] : q == 1 ? X[1] : q == 2 ? X[2] : X[3];
+            vr[c] = v.x;
+            vi[c] = conj ? -v.y : v.y;
+        }
+        vfwd_project<T, true>(d, w, j, vr, vi, nch, elapsed, maxSpeed, applyDamping, Ap, Am, A0, Fp, Fm, F0);
     }
 }
 
