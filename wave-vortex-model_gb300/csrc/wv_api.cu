@@ -1010,6 +1010,13 @@ cudaError_t set_smem_limits_adj(const Plan& p) {
     if (p.fz.N > 0) {
         WV_SET((dev::k_vfwd_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
         WV_SET((dev::k_vinv_adj_fft<T>), dev::smem_vadj_fft<T>(p.fz.N));
+        if constexpr (!std::is_same<T, double>::value) {
+            WV_RSWITCH_Y(warp_rz<T>(p), {
+                e = raise_smem_limit(dev::k_vfwd_adj_wfft<T, RR>, (int)dev::smem_vfwd_adj_wfft<T>(static_cast<int>(p.Nj), p.fz.N));
+                if (e == cudaSuccess) e = raise_smem_limit(dev::k_vinv_adj_wfft<T, RR>, (int)dev::smem_vinv_adj_wfft<T>(p.fz.N));
+            });
+            if (e != cudaSuccess) return e;
+        }
     }
 #undef WV_SET
     return cudaSuccess;
@@ -1082,7 +1089,17 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
     const dev::cx<T>* y = static_cast<const dev::cx<T>*>(h->yspec);
     if (!physIn) launch_flux_fields<T>(h, elapsed, Ap, Am, A0, static_cast<dev::cx<T>*>(h->yspec), s);
     // adjoint of projection and forward vertical transform, then inverse y FFTs
-    if (h->vfwdKind == WV_VERTICAL_FFT)
+    bool done = false;  // the vertical forward map launched on warp lines
+    if constexpr (!std::is_same<T, double>::value) {
+        if (h->vfwdKind == WV_VERTICAL_FFT && warp_rz<T>(p)) {
+            const dim3 grid(cdiv(p.Nkl, dev::kVwWarps / 2), d.members);
+            const size_t sm = dev::smem_vfwd_adj_wfft<T>(static_cast<int>(p.Nj), p.fz.N);
+            WV_RSWITCH_Y(warp_rz<T>(p), (dev::k_vfwd_adj_wfft<T, RR><<<grid, 256, sm, s>>>(d, Fpb, Fmb, F0b, elapsed, za)));
+            done = true;
+        }
+    }
+    if (done) {
+    } else if (h->vfwdKind == WV_VERTICAL_FFT)
         dev::k_vfwd_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::vf_modes<T>()), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
             d, Fpb, Fmb, F0b, elapsed, za);
     else
@@ -1118,7 +1135,17 @@ cudaError_t launch_flux_vjp(wv_handle* h, double t, double t0, const double* Ap,
                                                                                                               nIn, fa);
         }
     }
-    if (h->vinvKind == WV_VERTICAL_FFT)
+    bool vdone = false;  // the vertical inverse map launched on warp lines
+    if constexpr (!std::is_same<T, double>::value) {
+        if (h->vinvKind == WV_VERTICAL_FFT && warp_rz<T>(p)) {
+            const dim3 grid(cdiv(p.Nkl, dev::kVwWarps / 4), d.members);
+            const size_t sm = dev::smem_vinv_adj_wfft<T>(p.fz.N);
+            WV_RSWITCH_Y(warp_rz<T>(p), (dev::k_vinv_adj_wfft<T, RR><<<grid, 256, sm, s>>>(d, fa, elapsed, Apb, Amb, A0b)));
+            vdone = true;
+        }
+    }
+    if (vdone) {
+    } else if (h->vinvKind == WV_VERTICAL_FFT)
         dev::k_vinv_adj_fft<T><<<dim3(cdiv(p.Nkl, dev::VzLines<T>::value / 4), d.members), 256, dev::smem_vadj_fft<T>(p.fz.N), s>>>(
             d, fa, elapsed, Apb, Amb, A0b);
     else

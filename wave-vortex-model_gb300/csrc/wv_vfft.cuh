@@ -473,6 +473,189 @@ __global__ void __launch_bounds__(256) k_vfwd_wfft(DescDev d, const cx<T>* __res
     }
 }
 
+// The flux VJP's vertical maps on warp-register lines (mixed and FP32X2,
+// 2L = 32 R): the lines of k_vfwd_adj_fft / k_vinv_adj_fft, one per warp.
+
+// k_vfwd_adj_wfft: cotangent targets [4][Nj][4 modes], twiddles, line buffers
+template <typename T>
+inline size_t smem_vfwd_adj_wfft(int Nj, int N2) {
+    return (static_cast<size_t>(4) * Nj * (kVwWarps / 2) + N2 + static_cast<size_t>(kVwWarps) * vw_line_len(N2)) *
+           sizeof(cx<T>);
+}
+// k_vinv_adj_wfft: twiddles, line buffers
+template <typename T>
+inline size_t smem_vinv_adj_wfft(int N2) {
+    return (N2 + static_cast<size_t>(kVwWarps) * vw_line_len(N2)) * sizeof(cx<T>);
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_vfwd_adj_wfft(DescDev d, const double* __restrict__ Fpb, const double* __restrict__ Fmb,
+                                                      const double* __restrict__ F0b, double elapsed, cx<T>* __restrict__ zadj) {
+    constexpr int N2 = 32 * R, kModes = kVwWarps / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, nt = d.nt, L = Nz - 1;
+    cx<T>* tv = reinterpret_cast<cx<T>*>(smem_raw);  // [4][Nj][kModes]: target cotangents per slot q
+    cx<T>* tw = tv + 4 * Nj * kModes;                // [N2]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    cx<T>* F = tw + N2 + warp * vw_line_len(N2);
+    const int m0 = blockIdx.x * kModes;
+    const int nm = min(kModes, d.Nkl - m0);
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    int tOfQ[4] = {-1, -1, -1, -1};
+    for (int t = 0; t < nt; ++t) tOfQ[d.tq[t]] = t;
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int mi = it % nm, j = it / nm;
+        cx<T> vt[4];
+        vfwd_adj_values<T>(d, Fpb, Fmb, F0b, elapsed, d.modeWV[m0 + mi], j, vt);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int t = tOfQ[q];
+            tv[(q * Nj + j) * kModes + mi] = t < 0 ? mk<T>(T(0), T(0)) : (t == 0 ? vt[0] : t == 1 ? vt[1] : t == 2 ? vt[2] : vt[3]);
+        }
+    }
+    __syncthreads();
+    const int mi = warp >> 1, l = warp & 1;  // mode, line: (u | w), (v | eta)
+    if (mi >= nm) return;
+    const T half = T(0.5f);
+    // y[0] = X_0, y[L] = X_L / 2, y[j] = (X_j + i Y_j) / 2, y[2L-j] = (X_j - i Y_j) / 2
+    cx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int k = lane + 32 * r;
+        const int j = k <= L ? k : N2 - k;
+        cx<T> val = mk<T>(T(0), T(0));
+        if (j < Nj) {
+            const cx<T> C = tv[(l * Nj + j) * kModes + mi], D = tv[((2 + l) * Nj + j) * kModes + mi];
+            if (k == 0) {
+                val = C;
+            } else if (k == L) {
+                val = mk<T>(C.x * half, C.y * half);
+            } else {
+                const cx<T> c = mk<T>(C.x * half, C.y * half);
+                const cx<T> id = mk<T>(-(D.y * half), D.x * half);
+                val = k < L ? cadd<T>(c, id) : csub<T>(c, id);
+            }
+        }
+        v[r] = val;
+    }
+    fft_P<T, R, false>(v, tw, lane);
+    vw_park<T, R>(F, v, lane);
+    const T sc = T(1.0 / (static_cast<double>(L) * static_cast<double>(d.Nx) * static_cast<double>(d.Ny)));
+    const T sc2 = sc + sc;
+    const int mode = m0 + mi;
+    const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
+    const bool conj = d.modeFlags[mode] & 1;
+    const int tc = l == 0 ? tOfQ[0] : tOfQ[1], ts = l == 0 ? tOfQ[2] : tOfQ[3];
+    for (int z = lane; z <= L; z += 32) {
+        const cx<T> a = F[vw_pad(z)];
+        cx<T> vc, vs;
+        if (z == 0 || z == L) {
+            vc = mk<T>(a.x * sc, a.y * sc);
+            vs = mk<T>(T(0), T(0));
+        } else {
+            const cx<T> b = F[vw_pad(N2 - z)];
+            vc = mk<T>((a.x + b.x) * sc, (a.y + b.y) * sc);  // w_z (F[z] + F[2L-z]) / 2 with w_z = 2
+            vs = mk<T>((a.x - b.x) * half * sc2, (a.y - b.y) * half * sc2);
+        }
+        if (tc >= 0) {
+            cx<T>* base = zadj + (size_t)tc * Nz * P + (size_t)z * P;
+            base[pos] = conj ? cconj<T>(vc) : vc;
+            if (cpos >= 0) base[cpos] = mk<T>(T(0), T(0));
+        }
+        if (ts >= 0) {
+            cx<T>* base = zadj + (size_t)ts * Nz * P + (size_t)z * P;
+            base[pos] = conj ? cconj<T>(vs) : vs;
+            if (cpos >= 0) base[cpos] = mk<T>(T(0), T(0));
+        }
+    }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_vinv_adj_wfft(DescDev d, const cx<T>* __restrict__ fadj, double elapsed,
+                                                      double* __restrict__ Apb, double* __restrict__ Amb,
+                                                      double* __restrict__ A0b) {
+    constexpr int N2 = 32 * R, kModes = kVwWarps / 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Nj = d.Nj, Nz = d.Nz, P = d.positions, nt = d.nt, L = Nz - 1;
+    cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);  // [N2]
+    cx<T>* lines = tw + N2;                           // [8][N2 + N2/8]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m0 = blockIdx.x * kModes;
+    const int nm = min(kModes, d.Nkl - m0);
+    const cx<T>* twg = reinterpret_cast<const cx<T>*>(d.twz);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) tw[i] = twg[i];
+    int derivChan[4] = {-1, -1, -1, -1};
+    for (int t = 0; t < nt; ++t) derivChan[d.tq[t]] = 4 + t;
+    const T half = T(0.5f);
+    __syncthreads();
+    const int mi = warp >> 2, l = warp & 3;
+    if (mi < nm) {
+        const int mode = m0 + mi;
+        const int pos = d.modePos[mode], cpos = d.modeCompPos[mode];
+        const unsigned char flags = d.modeFlags[mode];
+        int chC, chS;
+        if (l == 0) { chC = 0; chS = 2; }
+        else if (l == 1) { chC = 1; chS = 3; }
+        else if (l == 2) { chC = derivChan[2]; chS = derivChan[0]; }
+        else { chC = derivChan[3]; chS = derivChan[1]; }
+        // stored row + conjugated completion row, frame of k_vinv (as k_vinv_adj's gather)
+        auto colval = [&](int ch, int z) -> cx<T> {
+            if (ch < 0) return mk<T>(T(0), T(0));
+            const cx<T>* r = fadj + ((size_t)ch * Nz + z) * P;
+            cx<T> v = r[pos];
+            if (cpos >= 0) { const cx<T> c = r[cpos]; v = mk<T>(v.x + c.x, v.y - c.y); }
+            if (flags & 2) v.y = T(0);
+            if (flags & 1) v.y = -v.y;
+            return v;
+        };
+        // y[0] = o_0, y[L] = o_L, y[z] = (o_z + i s_z) / 2, y[2L-z] = (o_z - i s_z) / 2
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int k = lane + 32 * r;
+            const int z = k <= L ? k : N2 - k;
+            const cx<T> o = colval(chC, z);
+            if (k == 0 || k == L) {
+                v[r] = o;
+            } else {
+                const cx<T> sv = colval(chS, z);
+                const cx<T> c = mk<T>(o.x * half, o.y * half);
+                const cx<T> id = mk<T>(-(sv.y * half), sv.x * half);
+                v[r] = k < L ? cadd<T>(c, id) : csub<T>(c, id);
+            }
+        }
+        fft_P<T, R, false>(v, tw, lane);
+        vw_park<T, R>(lines + warp * vw_line_len(N2), v, lane);
+    }
+    __syncthreads();  // the four lines of every mode parked
+    const T* mz = reinterpret_cast<const T*>(d.tMz);
+    for (int it = threadIdx.x; it < nm * Nj; it += blockDim.x) {
+        const int m = it % nm, j = it / nm;
+        const int w = d.modeWV[m0 + m];
+        cx<T> Ev[4], Od[4];
+#pragma unroll
+        for (int ll = 0; ll < 4; ++ll) {
+            const cx<T>* row = lines + (m * 4 + ll) * vw_line_len(N2);
+            const cx<T> a = row[vw_pad(j)];
+            if (j == 0 || j == L) {
+                Ev[ll] = j == 0 ? mk<T>(a.x * half, a.y * half) : a;  // Ccos's 1/2 at j = 0
+                Od[ll] = mk<T>(T(0), T(0));
+            } else {
+                const cx<T> b = row[vw_pad(N2 - j)];
+                Ev[ll] = mk<T>((a.x + b.x) * half, (a.y + b.y) * half);
+                Od[ll] = mk<T>((a.x - b.x) * half, (a.y - b.y) * half);
+            }
+        }
+        const T mj = mz[j];
+        const cx<T> ubT = mk<T>(Ev[0].x - mj * Od[2].x, Ev[0].y - mj * Od[2].y);
+        const cx<T> wbT = mk<T>(Od[0].x + mj * Ev[2].x, Od[0].y + mj * Ev[2].y);
+        const cx<T> vbT = mk<T>(Ev[1].x - mj * Od[3].x, Ev[1].y - mj * Od[3].y);
+        const cx<T> nbT = mk<T>(Od[1].x + mj * Ev[3].x, Od[1].y + mj * Ev[3].y);
+        vinv_adj_store<T>(d, j + Nj * w, elapsed, ubT, vbT, wbT, nbT, Apb, Amb, A0b);
+    }
+}
+
 // Shared memory of the adjoint kernels: two line buffers and the twiddles.
 template <typename T>
 inline size_t smem_vadj_fft(int N2) {
