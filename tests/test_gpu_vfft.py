@@ -1,6 +1,7 @@
 """Vertical transforms of the flux as FFTs of the even / odd extension over z
-(WV_VERTICAL_FFT: k_vinv_fft, k_vfwd_fft; the default of FP64 and FP32X2
-handles, selectable on mixed ones): every
+(WV_VERTICAL_FFT: the shared-memory k_vinv_fft, k_vfwd_fft, and on mixed and
+FP32X2 handles with 2 (Nz - 1) = 32 R the warp-register k_vinv_wfft,
+k_vfwd_wfft and the VJP's k_vfwd_adj_wfft, k_vinv_adj_wfft): every
 reference golden case at the FP64 (1e-12) and FP32X2 (1e-9) tolerances (RK4
 components that are pure accumulated rounding gated against the state), and
 the flux against the dense folded contraction of the same handle on 0.1 m/s

@@ -1,5 +1,5 @@
-// Vertical transforms as FFTs of the even / odd extension over z (FP64 and
-// FP32X2 handles), the way the reference computes them (FFTW REDFT00 /
+// Vertical transforms as FFTs of the even / odd extension over z (every
+// precision), the way the reference computes them (FFTW REDFT00 /
 // RODFT00, WVNativeFFTWEngine.cpp:154; exact definitions
 // WVReferenceFFTEngine.cpp:88-107), instead of the dense folded contraction.
 //
