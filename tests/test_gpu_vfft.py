@@ -229,3 +229,40 @@ def test_fft_vertical_mixed_vjp_matches_dense(wv):
     assert max(errs["fft"]) <= 3.0 * max(errs["cuda"]) + 1e-6
     k.close()
     k64.close()
+
+@pytest.mark.parametrize("inv,fwd", [("tensor", "fft"), ("fft", "tensor"), ("cuda", "fft"), ("fft", "cuda"), ("tensor", "cuda")])
+def test_mixed_vertical_kernel_per_direction(wv, inv, fwd):
+    """Mixed handles, each vertical direction on its own kernel
+    (wv_set_vertical_kernels): the flux's field tendencies against the FP64 flux
+    within a small factor of the dense contraction's error, the device status
+    word clear (the tensor-core kernels' bounded waits), and the VJP following
+    the chosen maps within the mixed VJP's bound."""
+    import torch
+    cfg = wv.Configuration(Nx=128, Ny=128, Nz=65, Nj=O.default_nj(65), Lx=400e3, Ly=400e3, Lz=4000.0, latitude=33.0)
+    k64 = wv.WVTransformConstantStratificationKernel(cfg, precision="fp64")
+    k = wv.WVTransformConstantStratificationKernel(cfg, precision="mixed")
+    A = wv.synthetic_state(k64, seed=31, urms=0.1)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in A]
+    exact = k64.transformWaveVortexToUVWEta(0.0, 0.0, *(x.cpu().numpy() for x in k64.nonlinearFlux(777.0, 5.0, *dev)))
+
+    def tendency_error():
+        F = k.nonlinearFlux(777.0, 5.0, *dev)
+        f = k64.transformWaveVortexToUVWEta(0.0, 0.0, *(x.cpu().numpy() for x in F))
+        return [float(np.linalg.norm(f[i] - exact[i]) / np.linalg.norm(exact[i])) for i in range(4)]
+
+    k.set_vertical_kernel("cuda")
+    base = tendency_error()
+    k.set_vertical_kernels(inv, fwd)
+    assert k.vertical_kernels() == (inv, fwd)
+    err = tendency_error()
+    assert k.device_status() == 0
+    print(f"mixed 128x128x65 vertical ({inv}, {fwd}): tendency errors {err}, dense {base}")
+    for a, b in zip(err, base):
+        assert a <= 3.0 * b + 1e-7
+    rng = np.random.default_rng(4)
+    Fb = [torch.from_numpy(rng.standard_normal(x.shape) + 1j * rng.standard_normal(x.shape)).cuda() for x in dev]
+    exact_vjp = [x.cpu().numpy() for x in k64.flux_vjp(777.0, 5.0, *dev, *Fb)]
+    got = [x.cpu().numpy() for x in k.flux_vjp(777.0, 5.0, *dev, *Fb)]
+    assert max(rel_err(g, e) for g, e in zip(got, exact_vjp)) <= 1e-3
+    k.close()
+    k64.close()
