@@ -329,7 +329,7 @@ def test_adjoint_with_tensor_vertical_matches_cuda_cores(wv, precision, tol):
 
 
 @pytest.mark.parametrize("precision", ["fp32x2", "mixed"])
-@pytest.mark.parametrize("N,Nz", [(64, 33), (128, 65), (256, 129)])
+@pytest.mark.parametrize("N,Nz", [(64, 33), (128, 65), (192, 97), (256, 129)])
 def test_fft_variants_match_fp64(wv, precision, N, Nz):
     """Every (y, x) combination of register-line and Stockham FFT kernels
     (wv_set_fft_variants) on FP32X2 and mixed handles: the flux and the flux VJP
@@ -338,7 +338,8 @@ def test_fft_variants_match_fp64(wv, precision, N, Nz):
     and the VJP within 1e-8 (single coefficients of high j and small K_h are
     ill-conditioned: FP64's own floor is 3e-10 at 256x256x129, FP32X2 measures
     1e-8 there); the variant reported back is the one asked for (register lines
-    exist at these lengths)."""
+    exist at these lengths; 192 takes the radix-3 x rows and the 2 x 3 y and
+    vertical lines)."""
     import torch
     import wv_oracle as O
     c = O.Config(Nx=N, Ny=N, Nz=Nz, Nj=O.default_nj(Nz), Lx=3125.0 * N, Ly=3125.0 * N, Lz=4000.0, latitude=33.0)
@@ -361,9 +362,12 @@ def test_fft_variants_match_fp64(wv, precision, N, Nz):
         V = [x.cpu().numpy() for x in k.flux_vjp(777.0, 5.0, *dev)]
         errs[var] = (max(rel_err(a, b) for a, b in zip(F, F64)), max(rel_err(a, b) for a, b in zip(V, V64)))
         print(f"{precision} {N}x{N}x{Nz} FFT variants {var}: flux {errs[var][0]:.2e}, VJP {errs[var][1]:.2e} against FP64")
-    base = errs[("register", "register")]
+    # every variant within 3x of every other (the register lines against the
+    # Stockham kernels both ways)
+    lo_f = min(e[0] for e in errs.values())
+    lo_v = min(e[1] for e in errs.values())
     for var, (ef, ev) in errs.items():
-        assert ef <= 3.0 * base[0] + 1e-13 and ev <= 3.0 * base[1] + 1e-13, var
+        assert ef <= 3.0 * lo_f + 1e-13 and ev <= 3.0 * lo_v + 1e-13, var
         if precision == "fp32x2":
             assert ef <= 1e-7 and ev <= 1e-8, var
     assert k._lib.wv_set_fft_variants(k._h, 0, 7) != 0  # unknown variant rejected

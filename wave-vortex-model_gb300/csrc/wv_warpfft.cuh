@@ -87,12 +87,39 @@ __device__ __forceinline__ void dft_layers(cx<T> (&v)[R], const cx<T>* tw, int N
     }
 }
 
+// 3-point DFT in place: t1 = v1 + v2, t2 = v0 - t1 / 2, t3 = i s (v1 - v2) with
+// s = -sqrt(3)/2 (forward) or +sqrt(3)/2 (inverse); out = v0 + t1, t2 + t3, t2 - t3.
+template <typename T, bool INV>
+__device__ __forceinline__ void dft3(cx<T>& v0, cx<T>& v1, cx<T>& v2) {
+    const T s3 = INV ? T(0.86602540378443864676) : T(-0.86602540378443864676);
+    const cx<T> t1 = cadd<T>(v1, v2);
+    const cx<T> t2 = mk<T>(v0.x - T(0.5) * t1.x, v0.y - T(0.5) * t1.y);
+    const cx<T> dl = csub<T>(v1, v2);
+    const cx<T> t3 = mk<T>(-(s3 * dl.y), s3 * dl.x);
+    v0 = cadd<T>(v0, t1);
+    v1 = cadd<T>(t2, t3);
+    v2 = csub<T>(t2, t3);
+}
+
 // In-register R-point DFT, natural order in and out.  tw: N-entry table of
-// exp(-2 pi i k/N) with R | N.
+// exp(-2 pi i k/N) with R | N.  Radix 3 directly, 6 as 2 x 3 (the DFTs of the
+// even and the odd samples, one twiddled radix-2 layer), other odd radices by
+// the O(R^2) sum.
 template <typename T, int R, bool INV>
 __device__ __forceinline__ void small_dft(cx<T> (&v)[R], const cx<T>* tw, int N) {
     if constexpr (R == 1) {
         return;
+    } else if constexpr (R == 3) {
+        dft3<T, INV>(v[0], v[1], v[2]);
+    } else if constexpr (R == 6) {
+        cx<T> e0 = v[0], e1 = v[2], e2 = v[4], o0 = v[1], o1 = v[3], o2 = v[5];
+        dft3<T, INV>(e0, e1, e2);
+        dft3<T, INV>(o0, o1, o2);
+        o1 = cmul<T>(o1, twid<T, INV>(tw, N / 6));
+        o2 = cmul<T>(o2, twid<T, INV>(tw, 2 * (N / 6)));
+        v[0] = cadd<T>(e0, o0); v[3] = csub<T>(e0, o0);
+        v[1] = cadd<T>(e1, o1); v[4] = csub<T>(e1, o1);
+        v[2] = cadd<T>(e2, o2); v[5] = csub<T>(e2, o2);
     } else if constexpr ((R & (R - 1)) == 0) {
         constexpr int LOG = ilog2c(R);
 #pragma unroll
@@ -138,10 +165,35 @@ __device__ __forceinline__ void s_dft_layers(ffs (&v)[R], const ff2* tw, int N) 
     }
 }
 
+// dft3 in split form (the scalar form's operations per component)
+template <bool INV>
+__device__ __forceinline__ void s_dft3(ffs& v0, ffs& v1, ffs& v2) {
+    const ff s3 = INV ? ff(0.86602540378443864676) : ff(-0.86602540378443864676);
+    const ffs t1 = s_add(v1, v2);
+    const ffs t2 = s_sub(v0, s_mul({f2(0.5f, 0.5f), f2(0.0f, 0.0f)}, t1));
+    const ffs dl = s_sub(v1, v2);
+    // (-(s3 dl.im), s3 dl.re)
+    const ffs t3 = s_mul({f2(-s3.hi, s3.hi), f2(-s3.lo, s3.lo)}, {f2(dl.h.y, dl.h.x), f2(dl.l.y, dl.l.x)});
+    v0 = s_add(v0, t1);
+    v1 = s_add(t2, t3);
+    v2 = s_sub(t2, t3);
+}
+
 template <int R, bool INV>
 __device__ __forceinline__ void s_small_dft(ffs (&v)[R], const ff2* tw, int N) {
     if constexpr (R == 1) {
         return;
+    } else if constexpr (R == 3) {
+        s_dft3<INV>(v[0], v[1], v[2]);
+    } else if constexpr (R == 6) {
+        ffs e0 = v[0], e1 = v[2], e2 = v[4], o0 = v[1], o1 = v[3], o2 = v[5];
+        s_dft3<INV>(e0, e1, e2);
+        s_dft3<INV>(o0, o1, o2);
+        o1 = s_cmul(o1, s_twiddle<INV>(tw, N / 6));
+        o2 = s_cmul(o2, s_twiddle<INV>(tw, 2 * (N / 6)));
+        v[0] = s_add(e0, o0); v[3] = s_sub(e0, o0);
+        v[1] = s_add(e1, o1); v[4] = s_sub(e1, o1);
+        v[2] = s_add(e2, o2); v[5] = s_sub(e2, o2);
     } else if constexpr ((R & (R - 1)) == 0) {
         constexpr int LOG = ilog2c(R);
 #pragma unroll
