@@ -1216,10 +1216,9 @@ cudaError_t rk4_step(wv_handle* h, double t, double t0, double dt, cudaStream_t 
     dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 2.0, h->state, dt, h->stage, 0, n);
     e = rhs_contiguous(h, t + dt, t0, h->stage, h->kbuf, s); if (e != cudaSuccess) return e;
     if (dense) { e = cudaMemcpyAsync(h->denseBuf + 3 * n, h->kbuf, nb, cudaMemcpyDeviceToDevice, s); if (e != cudaSuccess) return e; }
-    dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, nullptr, 0.0, nullptr, 0, n);
-    dev::k_affine<<<grid, 256, 0, s>>>(h->state, h->acc, dt / 6.0, h->state, n);
+    dev::k_rk4_finish<<<grid, 256, 0, s>>>(h->acc, h->kbuf, h->state, dt / 6.0, h->state, n);
     if (dense) { e = cudaMemcpyAsync(h->denseBuf + n, h->state, nb, cudaMemcpyDeviceToDevice, s); if (e != cudaSuccess) return e; }
-    h->metrics.kernel_launches += 5;
+    h->metrics.kernel_launches += 4;
     h->metrics.rk4_steps += 1;
     h->metrics.rhs_evaluations += 4;
     return cudaGetLastError();
@@ -1249,9 +1248,8 @@ cudaError_t rk4_stages(wv_handle* h, const double* y, double t, double t0, doubl
     if (!yNext && ys) { e = flux(st3, t + dt, 3); if (e != cudaSuccess) return e; }
     if (yNext) {
         e = flux(st3, t + dt, 3); if (e != cudaSuccess) return e;
-        dev::k_accumulate_and_stage<<<grid, 256, 0, s>>>(h->acc, h->kbuf, 1.0, nullptr, 0.0, nullptr, 0, n);
-        dev::k_affine<<<grid, 256, 0, s>>>(y, h->acc, dt / 6.0, yNext, n);
-        h->metrics.kernel_launches += 2;
+        dev::k_rk4_finish<<<grid, 256, 0, s>>>(h->acc, h->kbuf, y, dt / 6.0, yNext, n);
+        h->metrics.kernel_launches += 1;
     }
     return cudaGetLastError();
 }

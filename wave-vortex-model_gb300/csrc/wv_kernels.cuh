@@ -1239,11 +1239,6 @@ __global__ void __launch_bounds__(256, VertOcc<T>::value) k_vfwd(DescDev d, cons
 // contraction like IntegrationBuffer::setAffine / addScaled
 // (PortableRuntime/src/WVRungeKutta.cpp:140-176).
 
-// out = base + scale * inc
-__global__ void k_affine(const double* __restrict__ base, const double* __restrict__ inc, double scale, double* __restrict__ out, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        out[i] = __dadd_rn(base[i], __dmul_rn(scale, inc[i]));
-}
 // acc = acc + scale * inc ; stage = base + cs * inc   (both from the same k)
 __global__ void k_accumulate_and_stage(double* __restrict__ acc, const double* __restrict__ inc, double scale,
                                        const double* __restrict__ base, double cs, double* __restrict__ stage, int first, size_t n) {
@@ -1251,6 +1246,17 @@ __global__ void k_accumulate_and_stage(double* __restrict__ acc, const double* _
         const double k = inc[i];
         acc[i] = first ? k : __dadd_rn(acc[i], __dmul_rn(scale, k));
         if (stage) stage[i] = __dadd_rn(base[i], __dmul_rn(cs, k));
+    }
+}
+
+// The step's end: out = base + scale * (acc + k), with the arithmetic of
+// k_accumulate_and_stage at weight 1 followed by base + scale * acc, in one
+// pass (the final weighted sum is consumed here and not stored).
+__global__ void k_rk4_finish(const double* __restrict__ acc, const double* __restrict__ inc, const double* base, double scale,
+                             double* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double a = __dadd_rn(acc[i], __dmul_rn(1.0, inc[i]));
+        out[i] = __dadd_rn(base[i], __dmul_rn(scale, a));
     }
 }
 
