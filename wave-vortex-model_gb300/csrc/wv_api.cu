@@ -1265,17 +1265,14 @@ cudaError_t rk4_backward(wv_handle* h, const double* y, const double* st1, const
     cudaError_t e;
     dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.0, nullptr, n);
     e = flux_vjp_any(h, t + dt, t0, st3, h->kb, h->sb, s, ys ? ys[3] : nullptr); if (e != cudaSuccess) return e;
-    dev::k_lincomb<<<grid, 256, 0, s>>>(ybOut, 1.0, yb, 1.0, h->sb, n);
-    dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, dt, h->sb, n);
+    dev::k_adj_stage<<<grid, 256, 0, s>>>(ybOut, true, h->kb, dt / 3.0, yb, dt, h->sb, n);
     e = flux_vjp_any(h, t + 0.5 * dt, t0, st2, h->kb, h->sb, s, ys ? ys[2] : nullptr); if (e != cudaSuccess) return e;
-    dev::k_accumulate<<<grid, 256, 0, s>>>(ybOut, h->sb, n);
-    dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 3.0, yb, 0.5 * dt, h->sb, n);
+    dev::k_adj_stage<<<grid, 256, 0, s>>>(ybOut, false, h->kb, dt / 3.0, yb, 0.5 * dt, h->sb, n);
     e = flux_vjp_any(h, t + 0.5 * dt, t0, st1, h->kb, h->sb, s, ys ? ys[1] : nullptr); if (e != cudaSuccess) return e;
-    dev::k_accumulate<<<grid, 256, 0, s>>>(ybOut, h->sb, n);
-    dev::k_lincomb<<<grid, 256, 0, s>>>(h->kb, dt / 6.0, yb, 0.5 * dt, h->sb, n);
+    dev::k_adj_stage<<<grid, 256, 0, s>>>(ybOut, false, h->kb, dt / 6.0, yb, 0.5 * dt, h->sb, n);
     e = flux_vjp_any(h, t, t0, y, h->kb, h->sb, s, ys ? ys[0] : nullptr); if (e != cudaSuccess) return e;
     dev::k_accumulate<<<grid, 256, 0, s>>>(ybOut, h->sb, n);
-    h->metrics.kernel_launches += 8;
+    h->metrics.kernel_launches += 5;
     return cudaGetLastError();
 }
 

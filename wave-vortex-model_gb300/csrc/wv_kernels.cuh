@@ -1269,7 +1269,18 @@ namespace dev {
 __global__ void k_lincomb(double* __restrict__ out, double a, const double* __restrict__ x, double b,
                           const double* __restrict__ y, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        out[i] = y ? a * x[i] + b * y[i] : a * x[i];
+        out[i] = y ? __fma_rn(a, x[i], __dmul_rn(b, y[i])) : __dmul_rn(a, x[i]);
+}
+// One stage of the RK4 backward sweep after a flux VJP s: the step's
+// cotangent acc = x + s (first stage) or acc += s, and the next stage's flux
+// cotangent kb = a x + b s, with k_lincomb's rounding.
+__global__ void k_adj_stage(double* __restrict__ acc, bool first, double* __restrict__ kb, double a,
+                            const double* __restrict__ x, double b, const double* __restrict__ s, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double xi = x[i], si = s[i];
+        acc[i] = first ? __fma_rn(1.0, xi, __dmul_rn(1.0, si)) : __dadd_rn(acc[i], si);
+        kb[i] = __fma_rn(a, xi, __dmul_rn(b, si));
+    }
 }
 // out += x
 __global__ void k_accumulate(double* __restrict__ out, const double* __restrict__ x, size_t n) {
