@@ -71,9 +71,9 @@ def parse():
                     help="with --profile-flux: one checkpointed RK4 adjoint of 20 steps, checkpoints every 10, instead")
     ap.add_argument("--profile-size", type=int, default=256,
                     help="with --profile-flux: grid N x N x (N/2+1) over 3.125 km x N (256: the benchmark workload)")
-    ap.add_argument("--workload", choices=["c1", "c2"], default="c1",
-                    help="c2: only the 512x512x257 leg (mixed and paired FP32 vs FP64 over --c2-steps RK4 steps)")
-    ap.add_argument("--c2-steps", type=int, default=200,
+    ap.add_argument("--workload", choices=["256", "512"], default="256",
+                    help="512: only the 512x512x257 leg (mixed and paired FP32 vs FP64 over --steps-512 RK4 steps)")
+    ap.add_argument("--steps-512", type=int, default=200,
                     help="RK4 steps of the 512x512x257 leg (part of the default run; 0 skips it)")
     return ap.parse_args()
 
@@ -636,7 +636,7 @@ def run_ours(args):
     e2e_s = max_over_ranks(time.perf_counter() - w0)
     M = k.sizes["M"]
     coeff_bytes = 3 * M * 16
-    c2 = _c2_leg(wvgpu, stream, torch, np, args.c2_steps) if rank == 0 and args.c2_steps > 0 else None
+    g512 = _leg_512(wvgpu, stream, torch, np, args.steps_512) if rank == 0 and args.steps_512 > 0 else None
     cpu, vs_ref = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, final = cpu_baseline(state, dt)
@@ -668,14 +668,14 @@ def run_ours(args):
         "adjoint": adjoint,
         "ensemble": ensemble,
         "published_flux_comparison": published,
-        "c2_512x512x257": c2,
+        "grid_512x512x257": g512,
         "error_vs_reference_cpp": vs_ref,
         "clocks": clocks.summary(),
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
     if rank == 0:
-        out["summary"] = _summary(value, mixed, fp32x2, adjoint, ensemble, c2, vs_ref, roofline)
+        out["summary"] = _summary(value, mixed, fp32x2, adjoint, ensemble, g512, vs_ref, roofline)
         print(json.dumps(out), flush=True)
     k.close()
     if world > 1:
@@ -710,7 +710,7 @@ def _error_vs_reference_cpp(wvgpu, cfg, k64, state, dt, final, torch, np):
     return out
 
 
-def _summary(value, mixed, fp32x2, adjoint, ensemble, c2, vs_ref, roofline):
+def _summary(value, mixed, fp32x2, adjoint, ensemble, g512, vs_ref, roofline):
     """The metric's own figures as flat scalars, last on the line."""
     ok = [(f, d) for f, d in (("fp32x2", fp32x2), ("mixed", mixed))
           if d and max(d.get("rel_field_err_vs_fp64_after_100_steps", [1.0])) <= 1e-6]
@@ -730,11 +730,11 @@ def _summary(value, mixed, fp32x2, adjoint, ensemble, c2, vs_ref, roofline):
             s[f"adjoint_over_forward_{p}"] = a["adjoint_over_forward"]
     if ensemble:
         s["ensemble_speedup_vs_one_at_a_time"] = ensemble["speedup_vs_one_at_a_time"]
-    if c2:
-        s["c2_fp64_steps_s"] = c2["fp64"]["value"]
+    if g512:
+        s["g512_fp64_steps_s"] = g512["fp64"]["value"]
         for p in ("fp32x2", "mixed"):
-            s[f"c2_{p}_speedup_vs_fp64"] = c2[p]["speedup_vs_fp64"]
-            s[f"c2_{p}_max_field_err_{c2['steps']}"] = max(c2[p]["rel_field_err_vs_fp64"])
+            s[f"g512_{p}_speedup_vs_fp64"] = g512[p]["speedup_vs_fp64"]
+            s[f"g512_{p}_max_field_err_{g512['steps']}"] = max(g512[p]["rel_field_err_vs_fp64"])
     if vs_ref:
         for p in ("fp64", "fp32x2", "mixed"):
             s[f"{p}_max_field_err_vs_reference_cpp_{vs_ref['steps']}_steps"] = max(vs_ref[p]["rel_field_err"])
@@ -807,7 +807,7 @@ def _energy(k, state, t, t0, np):
     return 0.5 * float(np.sum(e * wz[:, None, None]) / (np.sum(wz) * f.shape[2] * f.shape[3]))
 
 
-def _c2_leg(wvgpu, stream, torch, np, steps):
+def _leg_512(wvgpu, stream, torch, np, steps):
     """512x512x257 over the 800 km x 800 km x 4 km domain of the 256 workload, seeded
     spectrum state at 0.1 m/s (seed 2), dt = 0.5 CFL: RK4 steps/s of the FP64, mixed
     and paired-FP32 forms over `steps` steps, per-field relative L2 error of the
@@ -849,14 +849,14 @@ def _c2_leg(wvgpu, stream, torch, np, steps):
     return out
 
 
-def run_workload_c2(args):
-    """The 512x512x257 leg alone (see _c2_leg)."""
+def run_workload_512(args):
+    """The 512x512x257 leg alone (see _leg_512)."""
     import numpy as np
     import torch
     import wvgpu
     from wvgpu import build
     build.build()
-    print(json.dumps(_c2_leg(wvgpu, torch.cuda.current_stream(), torch, np, args.c2_steps)), flush=True)
+    print(json.dumps(_leg_512(wvgpu, torch.cuda.current_stream(), torch, np, args.steps_512)), flush=True)
 
 
 def run_profile_case(args):
@@ -897,8 +897,8 @@ def main():
     args = parse()
     if args.profile_flux:
         run_profile_case(args)
-    elif args.workload == "c2":
-        run_workload_c2(args)
+    elif args.workload == "512":
+        run_workload_512(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

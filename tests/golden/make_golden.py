@@ -30,7 +30,7 @@ CASES = {
     # 40 km x 40 km x 1 km, 16x16x9, lat 45: single internal wave + adaptive damping
     "c0_16x16x9": dict(Nx=16, Ny=16, Nz=9, Nj=5, Lx=40e3, Ly=40e3, Lz=1000.0, latitude=45.0,
                        isHydrostatic=False, shouldAntialias=True, damping=True, dt=10.0, steps=3),
-    # odd grid (the survey's 15x13x9 parity case)
+    # odd grid: 15x13x9 (odd Nx, odd Ny)
     "odd_15x13x9": dict(Nx=15, Ny=13, Nz=9, Nj=5, Lx=15e3, Ly=12e3, Lz=1300.0, latitude=33.0,
                         isHydrostatic=False, shouldAntialias=True, damping=False, dt=20.0, steps=2),
     # the reference's own RK4 test grid (TestWVForcingAndRK4.cpp:66-74), both physics

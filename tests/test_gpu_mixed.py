@@ -72,7 +72,7 @@ def test_mixed_inverse_forward(wv):
 
 def test_mixed_rk4_field_error_after_100_steps(wv):
     """Relative field error of the mixed form against the FP64 GPU path after
-    100 RK4 steps at dt = 0.5 x CFL (spec criterion: <= 1e-6)."""
+    100 RK4 steps at dt = 0.5 x CFL (the accuracy target of the reduced forms: <= 1e-6)."""
     import torch
     c = _case(64, 64, 33)
     kd = wv.WVTransformConstantStratificationKernel(_wv_config(wv, c), precision="fp64")

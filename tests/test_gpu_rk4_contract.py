@@ -13,7 +13,7 @@ PortableRuntime/tests/TestWVForcingAndRK4.cpp:276-305).
     fine error).
 
 Workload: 16x16x9 and 32x32x17 over 40 km x 40 km x 1 km, N0 5.2e-3, latitude
-45 (the configs[0] domain), seeded spectrum state at 1 m/s rms (strong enough
+45 (the single-wave 16x16x9 domain), seeded spectrum state at 1 m/s rms (strong enough
 that truncation error sits far above paired-FP32 rounding), t = 0 .. 600 s,
 checkpoint at 300 s; schedule {nonlinear advection, adaptive damping} for the
 segmented / restarted runs, nonlinear advection for the convergence order.

@@ -6,7 +6,7 @@ import pytest
 
 import wv_oracle as O
 
-CONFIGS = [
+ADJ_CASES = [
     O.Config(Nx=16, Ny=16, Nz=9, Nj=5, Lx=40e3, Ly=40e3, Lz=1000.0, latitude=45.0),
     O.Config(Nx=15, Ny=13, Nz=9, Nj=5, Lx=15e3, Ly=12e3, Lz=1300.0, latitude=33.0),
     O.Config(Nx=8, Ny=6, Nz=7, Nj=4, Lx=15e3, Ly=12e3, Lz=1300.0, latitude=33.0, isHydrostatic=True),
@@ -21,7 +21,7 @@ def inner(a, b):
     return sum(float(np.real(np.vdot(x, y))) for x, y in zip(a, b))
 
 
-@pytest.mark.parametrize("c", CONFIGS, ids=lambda c: f"{c.Nx}x{c.Ny}x{c.Nz}{'h' if c.isHydrostatic else ''}")
+@pytest.mark.parametrize("c", ADJ_CASES, ids=lambda c: f"{c.Nx}x{c.Ny}x{c.Nz}{'h' if c.isHydrostatic else ''}")
 def test_flux_and_inverse_dot_product(c):
     rng = np.random.default_rng(1)
     d = O.build_descriptor(c)
@@ -43,7 +43,7 @@ def test_flux_and_inverse_dot_product(c):
 
 
 def test_rk4_step_adjoint_matches_central_differences():
-    c = CONFIGS[0]
+    c = ADJ_CASES[0]
     rng = np.random.default_rng(2)
     d = O.build_descriptor(c)
     sh = (d.Nkl, c.Nj)
