@@ -68,7 +68,7 @@ def parity_tolerance(floor):
 
 
 # Adaptive RK23 fixture runs (tests/golden/rk23.npz) and the golden case each uses.
-RK23_RUNS = {"odd": "odd_15x13x9", "c0": "c0_16x16x9", "hd": "hydro_damp_12x10x11"}
+RK23_RUNS = {"odd": "odd_15x13x9", "wave": "wave_16x16x9", "hd": "hydro_damp_12x10x11"}
 
 
 def rk23_run(key):

@@ -28,7 +28,7 @@ from ref_lib import BASE, Ref, load_lib  # noqa: E402
 
 CASES = {
     # 40 km x 40 km x 1 km, 16x16x9, lat 45: single internal wave + adaptive damping
-    "c0_16x16x9": dict(Nx=16, Ny=16, Nz=9, Nj=5, Lx=40e3, Ly=40e3, Lz=1000.0, latitude=45.0,
+    "wave_16x16x9": dict(Nx=16, Ny=16, Nz=9, Nj=5, Lx=40e3, Ly=40e3, Lz=1000.0, latitude=45.0,
                        isHydrostatic=False, shouldAntialias=True, damping=True, dt=10.0, steps=3),
     # odd grid: 15x13x9 (odd Nx, odd Ny)
     "odd_15x13x9": dict(Nx=15, Ny=13, Nz=9, Nj=5, Lx=15e3, Ly=12e3, Lz=1300.0, latitude=33.0,
@@ -75,8 +75,8 @@ def main():
         fields = rng.standard_normal((nch, case["Nz"], case["Ny"], case["Nx"])) * 0.05
         Bp, Bm, B0 = r.forward(fields, t, t0)
         inv = r.inverse(Ap, Am, A0, t, t0)
-        # single internal wave state (kMode 1, lMode 0, j 1) for the c0 case
-        if name.startswith("c0"):
+        # single internal wave state (kMode 1, lMode 0, j 1) for the wave case
+        if name.startswith("wave"):
             Sp = np.zeros(shape, np.complex128)
             Sm = np.zeros(shape, np.complex128)
             S0 = np.zeros(shape, np.complex128)
@@ -123,7 +123,7 @@ def main():
         json.dump(manifest, fh, indent=1, sort_keys=True)
     # 16x16x9 end to end: the single internal wave (kMode=1, lMode=0, j=1, u = 0.05 m/s)
     # under {nonlinear advection, adaptive damping}, 60 RK4 steps of dt = 10 s to t = 600 s
-    case = CASES["c0_16x16x9"]
+    case = CASES["wave_16x16x9"]
     r = Ref(lib, case)
     shape = (r.Nkl, case["Nj"])
     desc = r.descriptor()
@@ -133,20 +133,20 @@ def main():
     zero = np.zeros(shape, np.complex128)
     Kp, Km, K0, tK = r.rk4(Sp, zero, zero, 0.0, 0.0, 10.0, 60)
     fields = r.inverse(Kp, Km, K0, tK, 0.0)
-    np.savez_compressed(os.path.join(HERE, "c0_t600.npz"), Ap=Sp, Am=zero, A0=zero, dt=10.0, steps=60,
+    np.savez_compressed(os.path.join(HERE, "wave_16x16x9_t600.npz"), Ap=Sp, Am=zero, A0=zero, dt=10.0, steps=60,
                         Kp=Kp, Km=Km, K0=K0, t=tK, fields=fields)
     lib.wvref_destroy(r.h)
-    print(f"c0_t600: t = {tK}")
+    print(f"wave_16x16x9_t600: t = {tK}")
 
 
 # Adaptive RK23 runs through the reference integrator (WVAdaptiveRK23):
 #   odd:  seeded state, default options, t 100 -> 200 from a 5 s initial step
-#   c0:   the single internal wave under {advection, damping} to t = 600 s
+#   wave: the single internal wave under {advection, damping} to t = 600 s
 #   hd:   hydrostatic with damping, every option away from its default
 RK23_RUNS = {
     "odd": dict(case="odd_15x13x9", scale=1e-3, t=100.0, t0=0.0, final=200.0, initial=5.0,
                 opts=(1e-3, 1e-6, 0.8, 0.5, 5.0, float("inf"))),
-    "c0": dict(case="c0_16x16x9", scale=None, t=0.0, t0=0.0, final=600.0, initial=10.0,
+    "wave": dict(case="wave_16x16x9", scale=None, t=0.0, t0=0.0, final=600.0, initial=10.0,
                opts=(1e-3, 1e-6, 0.8, 0.5, 5.0, float("inf"))),
     "hd": dict(case="hydro_damp_12x10x11", scale=3e-3, t=50.0, t0=-3.0, final=56.0, initial=40.0,
                opts=(1e-5, 1e-7, 0.9, 0.3, 2.0, 15.0)),

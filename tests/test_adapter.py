@@ -133,7 +133,7 @@ def _wv_config(wv, case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["c0_16x16x9", "hydro_damp_12x10x11", "odd_15x13x9"])
+@pytest.mark.parametrize("name", ["wave_16x16x9", "hydro_damp_12x10x11", "odd_15x13x9"])
 def test_reference_rk4_steps_the_gpu_system(adapter_lib, name):
     import wvgpu
     case = dict(golden_cases()[name])
@@ -189,7 +189,7 @@ def test_reference_rk4_steps_the_gpu_system_at_128(adapter_lib):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("key", ["odd", "c0", "hd"])
+@pytest.mark.parametrize("key", ["odd", "wave", "hd"])
 def test_reference_rk23_steps_the_gpu_system(adapter_lib, key):
     """WVAdaptiveRK23 of the reference over the GPU system: the same counts and
     tolerance hashes as the reference's own run (tests/golden/rk23.npz)."""

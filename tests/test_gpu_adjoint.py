@@ -45,7 +45,7 @@ def cplx(rng, shape):
     return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
 
 
-@pytest.mark.parametrize("name", ["c0_16x16x9", "odd_15x13x9", "hydro_8x6x7", "noalias_16x16x9"])
+@pytest.mark.parametrize("name", ["wave_16x16x9", "odd_15x13x9", "hydro_8x6x7", "noalias_16x16x9"])
 def test_flux_vjp_matches_oracle_adjoint(wv, name):
     cf = golden_cases()[name]
     c = config_from_case(cf)
@@ -90,7 +90,7 @@ def test_flux_vjp_dot_product_on_gpu(wv, shape, hydro):
     k.close()
 
 
-@pytest.mark.parametrize("name", ["c0_16x16x9", "odd_15x13x9"])
+@pytest.mark.parametrize("name", ["wave_16x16x9", "odd_15x13x9"])
 def test_inverse_vjp_matches_oracle(wv, name):
     import torch
     c = config_from_case(golden_cases()[name])
@@ -106,7 +106,7 @@ def test_inverse_vjp_matches_oracle(wv, name):
 
 
 def test_rk4_step_vjp_matches_oracle(wv):
-    c = config_from_case(golden_cases()["c0_16x16x9"])
+    c = config_from_case(golden_cases()["wave_16x16x9"])
     d = O.build_descriptor(c)
     rng = np.random.default_rng(6)
     A = [1e-2 * cplx(rng, (d.Nkl, c.Nj)) for _ in range(3)]

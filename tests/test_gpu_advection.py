@@ -76,9 +76,9 @@ def test_using_own_advection_fields_equals_flux(wv, shape, precision):
 
 def test_advection_fields_overlap_rejected(wv):
     import torch
-    c = config_from_case(golden_cases()["c0_16x16x9"])
+    c = config_from_case(golden_cases()["wave_16x16x9"])
     k = wv.WVTransformConstantStratificationKernel(to_wv(wv, c))
-    g = load_golden("c0_16x16x9")
+    g = load_golden("wave_16x16x9")
     buf = torch.zeros(3 * c.Nx * c.Ny * c.Nz * 2, dtype=torch.float64, device="cuda")
     A = [torch.from_numpy(np.ascontiguousarray(g[n])).cuda() for n in ("Ap", "Am", "A0")]
     # a flux output inside the fields buffer

@@ -78,12 +78,12 @@ def test_fp32x2_flux_rhs_transforms_and_rk4_match_reference(wv, name):
     k.close()
 
 
-def test_fp32x2_configs0_to_t600(wv):
+def test_fp32x2_single_wave_to_t600(wv):
     """The 16x16x9 single internal wave with adaptive damping, 60 RK4 steps to t = 600 s,
     against the reference's own run."""
     import os
-    c = config_from_case(CASES["c0_16x16x9"])
-    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "c0_t600.npz"))
+    c = config_from_case(CASES["wave_16x16x9"])
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "wave_16x16x9_t600.npz"))
     k = wv.WVTransformConstantStratificationKernel(_conf(wv, c), precision="fp32x2")
     k.set_forcing(nonlinear=True, adaptive_damping=True)
     Ap, Am, A0, t = k.rk4(g["Ap"], g["Am"], g["A0"], 0.0, 0.0, float(g["dt"]), int(g["steps"]))

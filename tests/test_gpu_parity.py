@@ -219,14 +219,14 @@ def test_stage_instrumentation(wv):
     k.close()
 
 
-def test_configs0_single_wave_to_t600_matches_reference(wv):
+def test_single_wave_16x16x9_to_t600_matches_reference(wv):
     """16x16x9 end to end: single internal wave (kMode=1, lMode=0, j=1,
     u = 0.05 m/s) under {nonlinear advection, adaptive damping}, 60 RK4 steps of
     10 s to t = 600 s, field by field against the reference FP64 path (its own
-    run, tests/golden/c0_t600.npz)."""
+    run, tests/golden/wave_16x16x9_t600.npz)."""
     import os
-    c = config_from_case(golden_cases()["c0_16x16x9"])
-    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "c0_t600.npz"))
+    c = config_from_case(golden_cases()["wave_16x16x9"])
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "wave_16x16x9_t600.npz"))
     k = wv.WVTransformConstantStratificationKernel(to_wv(wv, c))
     k.set_forcing(nonlinear=True, adaptive_damping=True)
     Ap, Am, A0, t = k.rk4(g["Ap"], g["Am"], g["A0"], 0.0, 0.0, float(g["dt"]), int(g["steps"]))

@@ -141,12 +141,12 @@ def test_oracle_family_derivatives(name):
     assert rel_err(O.family_derivatives(d, g["Apm"], g["A0"], False), g["gall"]) <= 1e-12
 
 
-def test_oracle_configs0_to_t600():
+def test_oracle_single_wave_to_t600():
     """16x16x9: single internal wave under {nonlinear advection, adaptive damping},
     60 RK4 steps of 10 s, against the reference's own run (coefficients and fields)."""
-    c = config_from_case(golden_cases()["c0_16x16x9"])
+    c = config_from_case(golden_cases()["wave_16x16x9"])
     d = O.build_descriptor(c)
-    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "c0_t600.npz"))
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "wave_16x16x9_t600.npz"))
     damp = O.adaptive_damping_operator(d)
     Ap, Am, A0, t = O.rk4(d, g["Ap"], g["Am"], g["A0"], 0.0, 0.0, float(g["dt"]), int(g["steps"]), damping=damp)
     assert t == float(g["t"])
